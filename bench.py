@@ -1,0 +1,336 @@
+"""Benchmark: plain GB300 delta tracker on the neural-radiance-cache scene.
+
+Workload (one step = one progressive pass, 1 camera sample per pixel):
+  1024x512x1024 fBm cloud (8 octaves), FP16 8^3 bricks with FP32 per-brick
+  scale and majorant, sigma_t = 32 * density, 1920x1080, albedo 0.99,
+  HG g = 0.857, <= 64 scatter events, ratio-tracking sun NEE, DDA majorant
+  traversal, persistent warp-refilled wavefront kernel.
+  The grid (1 GiB of FP16 texels) is larger than L2 (129 MB), so no L2
+  flush is needed between timed passes.
+
+value  : camera samples per second over the timed passes (Msamples/s),
+         device-timed with CUDA events on the launching stream.
+e2e    : the same metric through the C-ABI with host buffers: the grid is
+         uploaded from pinned host memory once inside the timed region, and
+         every pass reads its FP32 mean image back to the host.
+roofline: the wavefront kernel's algorithmic bytes (8 texels x 2 B per
+         density lookup) per launch / its launch time, against the measured
+         HBM copy bandwidth.
+--impl reference: the CPU restatement of the reference's tracker (the
+         oracle) on all host cores, on a bounded sample of the same passes.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "cloudrendering-vulkan_gb300")
+for p in (ROOT, PKG):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+METRIC = "time-to-1% relRMSE & Msamples/s: NN-cached vs plain tracker on 1 GB300"
+UNIT = "Msamples/s"
+BYTES_PER_LOOKUP = {0: 32, 1: 16, 2: 16}  # 8 texels x element size
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index: int):
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+        os.makedirs(os.path.dirname(self.path), exist_ok=True)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={index}", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if not self.p:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def traffic_per_lookup():
+    """DRAM bytes per density lookup of the wavefront kernel from the
+    committed ncu summary (profiles/pt_wavefront_c5.json), or None."""
+    path = os.path.join(ROOT, "profiles", "pt_wavefront_c5.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return json.load(f).get("dram_bytes_per_lookup")
+    return None
+
+
+def run_vcr(args):
+    import torch
+    import vcr
+    from vcr import configs
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    sc = configs.C5_NRC
+    W, H = sc.width, sc.height
+    prec = sc.precision
+    stream = torch.cuda.Stream()
+    sh = stream.cuda_stream
+
+    def barrier():
+        torch.cuda.synchronize()
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    with vcr.Context(local) as ctx:
+        configs.setup_context(ctx, sc, tracker=vcr.TRACKER_DDA)
+        ctx.synchronize()
+        seed = 1000 + rank
+        for k in range(args.warmup):
+            ctx.pt_pass(seed=seed, pass_index=k, stream=sh)
+        barrier()
+        clk = Clocks(local)
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        barrier()
+        ev0.record(stream)
+        for k in range(args.steps):
+            ctx.pt_pass(seed=seed, pass_index=args.warmup + k, stream=sh)
+        ev1.record(stream)
+        barrier()
+        clocks = clk.stop()
+        ms_total = ev0.elapsed_time(ev1)
+        # per-launch kernel durations and lookups (for the roofline)
+        durs, looks, events, paths = [], [], [], []
+        for k in range(min(args.steps, 3)):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            ctx.pt_pass(seed=seed + 7, pass_index=k, stream=sh)
+            b.record(stream)
+            b.synchronize()
+            durs.append(a.elapsed_time(b))
+            c = ctx.counters()
+            paths.append(c[0]); looks.append(c[1]); events.append(c[2])
+        img = ctx.image_mean()
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms_total], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_total = float(t.item())
+
+    samples_per_step = W * H
+    value = ws * samples_per_step * args.steps / (ms_total / 1e3) / 1e6
+    peak, peak_kind = measured_peaks()
+    bpl = BYTES_PER_LOOKUP[prec]
+    lookups = float(np.mean(looks))
+    dur_ms = float(np.mean(durs))
+    achieved = lookups * bpl / (dur_ms / 1e3) / 1e9
+    tpl = traffic_per_lookup()
+
+    # e2e through the C-ABI with host buffers
+    e2e = run_e2e(args, sc, local, sh) if rank == 0 else None
+
+    if rank != 0:
+        return
+    cpu = cpu_baseline(sc, args) if ws == 1 and not args.no_cpu else None
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_total / args.steps, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (fp16 texels, fp64 accumulation)",
+        "data": "synthetic: seeded 8-octave Perlin fBm cloud generated on the device",
+        "config": {"workload": sc.name, "grid": list(sc.size), "precision": "fp16-bricks", "sigma_t_scale": 32,
+                   "image": [W, H], "spp_per_step": 1, "max_events": sc.max_events, "tracker": "dda-wavefront",
+                   "l2": "inputs larger than L2 (1 GiB FP16 grid), no flush",
+                   "parallelism": f"replicas{ws}"},
+        "gpu_launches": args.steps,
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                     "traffic": (round(tpl * lookups) if tpl else None),
+                     "kernel": "pt_wavefront_kernel", "bytes_per_lookup": bpl,
+                     "lookups_per_launch": int(lookups), "launch_ms": round(dur_ms, 4),
+                     "lookups_per_s": round(lookups / (dur_ms / 1e3), 1)},
+        "clocks": clocks,
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+        "stats": {"events_per_path": round(float(np.sum(events)) / max(1, float(np.sum(paths))), 3),
+                  "lookups_per_path": round(lookups / samples_per_step, 2), "image_mean": float(img.mean())},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_e2e(args, sc, device, sh):
+    """Grid upload from pinned host memory + per-pass mean-image read back,
+    all through the C-ABI, wall-clock timed."""
+    import torch
+    import vcr
+
+    dense = vcr.fbm_fill_host(sc.size, sc.fbm())  # the library's host generator (threaded)
+    pinned = torch.from_numpy(dense).pin_memory()
+    img_bytes = sc.width * sc.height * 3 * 4
+    with vcr.Context(device) as ctx:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        import ctypes as C
+        check = vcr.check
+        check(vcr.lib().vcr_grid_upload(ctx.h, C.byref(sc.grid_desc()), C.c_void_p(pinned.data_ptr()),
+                                        sc.precision), ctx.h)
+        ctx.set_cloud(sc.cloud())
+        ctx.set_camera(sc.camera())
+        ctx.set_params(sc.params(vcr.TRACKER_DDA))
+        ctx.set_frame(sc.width, sc.height)
+        for k in range(args.steps):
+            ctx.pt_pass(seed=5, pass_index=k, stream=sh)
+            img = ctx.image_mean()
+        t1 = time.perf_counter()
+    grid_bytes = dense.nbytes
+    return {"value": round(sc.width * sc.height * args.steps / (t1 - t0) / 1e6, 3), "unit": UNIT,
+            "h2d_bytes_per_step": int(grid_bytes // args.steps), "d2h_bytes_per_step": img_bytes,
+            "note": "grid (FP32, pinned) uploaded once per run; mean image read back every pass"}
+
+
+class OracleScene:
+    """The oracle (a CPU port of the reference's tracker) set up on the
+    benchmark scene, generated by the oracle's own fBm on all host cores."""
+
+    def __init__(self, sc, threads=None):
+        import vcr
+        from oracle import oracle as orc
+
+        self.sc = sc
+        self.threads = threads or os.cpu_count() or 1
+        t0 = time.perf_counter()
+        dense = orc.fbm_fill(sc.size, seed=sc.seed, octaves=sc.octaves, threads=self.threads)
+        self.g = orc.Grid(dense, sc.precision)
+        del dense
+        self.setup_s = time.perf_counter() - t0
+        self.cloud = sc.cloud()
+        self.cloud.max_extinction = max(self.g.max_density(), 0.01)
+        self.cam, self.prm = sc.camera(), sc.params(vcr.TRACKER_DDA)
+
+    def pass_rows(self, rows, pass_index):
+        """One pass over a full-width band of `rows` image rows through the
+        image centre; returns (paths, seconds)."""
+        W, H = self.sc.width, self.sc.height
+        y0 = max(0, H // 2 - rows // 2)
+        t0 = time.perf_counter()
+        self.g.pt_pass(self.cloud, self.cam, self.prm, W, H, seed=3, pass_index=pass_index, crop=(0, y0, W, rows),
+                       threads=self.threads)
+        return W * rows, time.perf_counter() - t0
+
+    def rows_for(self, seconds):
+        paths, dt = self.pass_rows(2, 0)
+        per_row = dt / 2
+        return int(max(1, min(self.sc.height, seconds / max(per_row, 1e-6))))
+
+
+def cpu_baseline(sc, args, budget_s=15.0):
+    os_ = OracleScene(sc)
+    rows = os_.rows_for(budget_s / 4)
+    done = t = 0.0
+    for k in range(4):
+        p, dt = os_.pass_rows(rows, k + 1)
+        done += p
+        t += dt
+    return {"value": round(done / t / 1e6, 4), "unit": UNIT, "cores": os_.threads, "kind": "port",
+            "sample": f"4 passes x {rows} full-width rows through the image centre = {int(done)} camera paths, "
+                      f"{t:.1f} s of CPU time (grid setup {os_.setup_s:.1f} s not counted)"}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from vcr import configs
+    sc = configs.C5_NRC
+    os_ = OracleScene(sc)
+    rows = os_.rows_for(6.0)  # each step: one pass over a ~6 s band of rows
+    for k in range(args.warmup):
+        os_.pass_rows(max(1, rows // 4), k + 1)
+    done = t = 0.0
+    for k in range(args.steps):
+        p, dt = os_.pass_rows(rows, args.warmup + k + 1)
+        done += p
+        t += dt
+    v = round(done / t / 1e6, 4)
+    cpu = {"cores": os_.threads,
+           "sample": f"{args.steps} passes x {rows} full-width rows = {int(done)} camera paths, {t:.1f} s"}
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 (fp16 texels decoded, fp64 accumulation)", "data": "synthetic",
+            "config": {"workload": sc.name, "grid": list(sc.size), "image": [sc.width, sc.height],
+                       "tracker": "dda (CPU port)"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cpu["cores"], "kind": "port",
+                             "sample": cpu["sample"]},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="vcr", choices=["vcr", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        import __graft_entry__ as ge
+        ge.build()
+        run_vcr(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,214 @@
+// Density grid: fBm generation, bricking (FP32 / FP16 / BF16 with a per-brick
+// FP32 scale), brick majorants, trilinear sampling and the DDA trace.
+//
+// Replaces the reference's dense R32F 3D image upload (main.cpp:266-335) and
+// its single global majorant (Grid3D::GetMajorant, Grid3D.h:180-192;
+// main.cpp:152).
+#include "vcr_internal.h"
+#include "vcr_fbm.cuh"
+
+namespace vcr {
+
+__constant__ FbmConst c_fbm;
+
+__global__ void fbm_kernel(float* __restrict__ out, uint64_t total) {
+  uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t nx = c_fbm.n[0], ny = c_fbm.n[1];
+  for (; idx < total; idx += stride) {
+    uint32_t i = (uint32_t)(idx % nx);
+    uint64_t r = idx / nx;
+    uint32_t j = (uint32_t)(r % ny);
+    uint32_t k = (uint32_t)(r / ny);
+    out[idx] = fbm_density(c_fbm, i, j, k);
+  }
+}
+
+// One CTA per brick, one thread per texel: brick maximum -> scale, encode.
+template <int P>
+__global__ void __launch_bounds__(512) brick_kernel(const float* __restrict__ dense, void* __restrict__ bricks,
+                                                    float* __restrict__ scales, int nx, int ny, int nz,
+                                                    int bx, int by) {
+  __shared__ float red[16];
+  uint32_t b = blockIdx.x;
+  int ib = (int)(b % (uint32_t)bx), jb = (int)((b / (uint32_t)bx) % (uint32_t)by), kb = (int)(b / ((uint32_t)bx * (uint32_t)by));
+  int t = threadIdx.x;
+  int i = ib * kBrick + (t & 7), j = jb * kBrick + ((t >> 3) & 7), k = kb * kBrick + (t >> 6);
+  float v = 0.0f;
+  if (i < nx && j < ny && k < nz) v = dense[(size_t)i + (size_t)nx * ((size_t)j + (size_t)ny * (size_t)k)];
+  size_t off = ((size_t)b << 9) + (size_t)t;
+  if (P == 0) {
+    reinterpret_cast<float*>(bricks)[off] = v;
+    return;
+  }
+  float m = v;
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((t & 31) == 0) red[t >> 5] = m;
+  __syncthreads();
+  if (t < 32) {
+    m = t < 16 ? red[t] : 0.0f;
+    for (int o = 8; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (t == 0) red[0] = m;
+  }
+  __syncthreads();
+  float s = red[0];
+  float q = s > 0.0f ? v / s : 0.0f;
+  if (P == 1) reinterpret_cast<__half*>(bricks)[off] = __float2half_rn(q);
+  else reinterpret_cast<__nv_bfloat16*>(bricks)[off] = __float2bfloat16_rn(q);
+  if (t == 0) scales[b] = s;
+}
+
+// Brick majorant: max decoded texel over [8b-1, 8b+8] per axis (clamped),
+// which bounds every trilinear sample whose position lies in the brick's
+// cell (a sample at texel coordinate u reads floor(u - 1/2) and the next).
+__global__ void __launch_bounds__(256) majorant_kernel(GridView g, float* __restrict__ maj,
+                                                       unsigned int* __restrict__ gmax) {
+  __shared__ float red[8];
+  uint32_t b = blockIdx.x;
+  int ib = (int)(b % (uint32_t)g.nb[0]), jb = (int)((b / (uint32_t)g.nb[0]) % (uint32_t)g.nb[1]);
+  int kb = (int)(b / ((uint32_t)g.nb[0] * (uint32_t)g.nb[1]));
+  float m = 0.0f;
+  for (int t = threadIdx.x; t < 1000; t += blockDim.x) {
+    int di = t % 10, dj = (t / 10) % 10, dk = t / 100;
+    int i = min(max(ib * kBrick - 1 + di, 0), g.n[0] - 1);
+    int j = min(max(jb * kBrick - 1 + dj, 0), g.n[1] - 1);
+    int k = min(max(kb * kBrick - 1 + dk, 0), g.n[2] - 1);
+    m = fmaxf(m, texel(g, i, j, k));
+  }
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = fmaxf(m, red[w]);
+    m = fmaxf(m, red[0]);
+    maj[b] = m;
+    atomicMax(gmax, __float_as_uint(m));  // non-negative floats order as integers
+  }
+}
+
+__global__ void sample_kernel(GridView g, SceneView s, const float* __restrict__ pos, float* __restrict__ out,
+                              uint32_t n) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  f3 p = mk(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]);
+  out[i] = density_at(g, s, p);
+}
+
+__global__ void dda_trace_kernel(SceneView s, int nc0, int nc1, int nc2, const float* __restrict__ o,
+                                 const float* __restrict__ d, uint32_t n, uint32_t max_cells,
+                                 uint32_t* __restrict__ cells, float* __restrict__ tt,
+                                 uint32_t* __restrict__ count) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int nc[3] = {nc0, nc1, nc2};
+  f3 org = mk(o[3 * i], o[3 * i + 1], o[3 * i + 2]);
+  f3 dir = mk(d[3 * i], d[3 * i + 1], d[3 * i + 2]);
+  float tmin, tmax;
+  uint32_t k = 0;
+  if (slab(org, dir, s.b0, s.b1, tmin, tmax) && tmax >= 0.0f) {
+    if (tmin > 0.0f) {
+      org = along(org, dir, tmin);
+      slab(org, dir, s.b0, s.b1, tmin, tmax);
+    }
+    Dda dd;
+    dda_init(dd, org, dir, s.b0, s.cell, nc);
+    float t = 0.0f;
+    while (k < max_cells) {
+      float e = dda_cell_exit(dd);
+      float se = fminf(e, tmax);
+      size_t at = (size_t)i * max_cells + k;
+      cells[at] = dda_linear(dd, nc);
+      tt[2 * at] = t;
+      tt[2 * at + 1] = se;
+      ++k;
+      if (e >= tmax) break;
+      if (!dda_advance(dd, nc)) break;
+      t = se;
+    }
+  }
+  count[i] = k;
+}
+
+void fbm_permutation(uint64_t seed, uint8_t perm[256]) { fbm_make_perm(seed, perm); }
+
+vcr_status grid_fbm_device(vcr_ctx* ctx, float* d_dense, const vcr_grid_desc* desc, const vcr_fbm_desc* fbm,
+                           cudaStream_t s) {
+  FbmConst c{};
+  fbm_make_perm(fbm->seed, c.perm);
+  for (int a = 0; a < 3; ++a) c.n[a] = desc->size[a];
+  c.octaves = fbm->octaves;
+  c.lacunarity = fbm->lacunarity;
+  c.gain = fbm->gain;
+  c.f0 = fbm->base_frequency;
+  VCR_CUDA(ctx, cudaMemcpyToSymbolAsync(c_fbm, &c, sizeof(c), 0, cudaMemcpyHostToDevice, s));
+  uint64_t total = (uint64_t)desc->size[0] * desc->size[1] * desc->size[2];
+  int blocks = ctx->sm_count * 8;
+  fbm_kernel<<<blocks, 256, 0, s>>>(d_dense, total);
+  VCR_CUDA(ctx, cudaGetLastError());
+  return VCR_OK;
+}
+
+vcr_status grid_build(vcr_ctx* ctx, const float* d_dense, const vcr_grid_desc* desc, int precision,
+                      cudaStream_t s) {
+  int n[3] = {(int)desc->size[0], (int)desc->size[1], (int)desc->size[2]};
+  int nb[3];
+  for (int a = 0; a < 3; ++a) nb[a] = (n[a] + kBrick - 1) / kBrick;
+  uint64_t nbricks = (uint64_t)nb[0] * nb[1] * nb[2];
+  if (nbricks > (1ull << 22)) return fail(ctx, VCR_ERR_UNSUPPORTED, "grid too large: %llu bricks (max 2^22)",
+                                          (unsigned long long)nbricks);
+  size_t esz = precision == 0 ? 4 : 2;
+  // release the previous grid
+  cudaFree(ctx->d_bricks);
+  cudaFree(ctx->d_scales);
+  cudaFree(ctx->d_majorants);
+  ctx->d_bricks = nullptr;
+  ctx->d_scales = nullptr;
+  ctx->d_majorants = nullptr;
+  ctx->has_grid = false;
+  VCR_CUDA(ctx, cudaMalloc(&ctx->d_bricks, nbricks * kBrickVoxels * esz));
+  VCR_CUDA(ctx, cudaMalloc(&ctx->d_scales, nbricks * sizeof(float)));
+  VCR_CUDA(ctx, cudaMalloc(&ctx->d_majorants, nbricks * sizeof(float)));
+  VCR_CUDA(ctx, cudaMemsetAsync(ctx->d_scales, 0, nbricks * sizeof(float), s));
+  if (precision == 0)
+    brick_kernel<0><<<(unsigned)nbricks, 512, 0, s>>>(d_dense, ctx->d_bricks, ctx->d_scales, n[0], n[1], n[2], nb[0], nb[1]);
+  else if (precision == 1)
+    brick_kernel<1><<<(unsigned)nbricks, 512, 0, s>>>(d_dense, ctx->d_bricks, ctx->d_scales, n[0], n[1], n[2], nb[0], nb[1]);
+  else
+    brick_kernel<2><<<(unsigned)nbricks, 512, 0, s>>>(d_dense, ctx->d_bricks, ctx->d_scales, n[0], n[1], n[2], nb[0], nb[1]);
+  VCR_CUDA(ctx, cudaGetLastError());
+  ctx->gdesc = *desc;
+  ctx->precision = precision;
+  for (int a = 0; a < 3; ++a) ctx->nb[a] = nb[a];
+  unsigned int* d_gmax = reinterpret_cast<unsigned int*>(ctx->d_counters + 5);
+  VCR_CUDA(ctx, cudaMemsetAsync(d_gmax, 0, sizeof(unsigned int), s));
+  GridView g = grid_view(ctx);
+  majorant_kernel<<<(unsigned)nbricks, 256, 0, s>>>(g, ctx->d_majorants, d_gmax);
+  VCR_CUDA(ctx, cudaGetLastError());
+  unsigned int gm = 0;
+  VCR_CUDA(ctx, cudaMemcpyAsync(&gm, d_gmax, sizeof(gm), cudaMemcpyDeviceToHost, s));
+  VCR_CUDA(ctx, cudaStreamSynchronize(s));
+  float f;
+  memcpy(&f, &gm, sizeof(f));
+  if (!(f <= 3.0e38f)) return fail(ctx, VCR_ERR_INVALID, "grid holds non-finite densities");
+  ctx->max_density = f;
+  ctx->has_grid = true;
+  return VCR_OK;
+}
+
+vcr_status grid_sample_launch(vcr_ctx* ctx, const float* d_pos, float* d_out, uint32_t n, cudaStream_t s) {
+  if (n == 0) return VCR_OK;
+  sample_kernel<<<(n + 255) / 256, 256, 0, s>>>(grid_view(ctx), scene_view(ctx), d_pos, d_out, n);
+  VCR_CUDA(ctx, cudaGetLastError());
+  return VCR_OK;
+}
+
+vcr_status dda_trace_launch(vcr_ctx* ctx, const float* d_o, const float* d_d, uint32_t n, uint32_t max_cells,
+                            uint32_t* d_cells, float* d_t, uint32_t* d_count, cudaStream_t s) {
+  if (n == 0) return VCR_OK;
+  dda_trace_kernel<<<(n + 127) / 128, 128, 0, s>>>(scene_view(ctx), ctx->nb[0], ctx->nb[1], ctx->nb[2], d_o, d_d, n,
+                                                   max_cells, d_cells, d_t, d_count);
+  VCR_CUDA(ctx, cudaGetLastError());
+  return VCR_OK;
+}
+
+}  // namespace vcr

@@ -1,0 +1,175 @@
+// Device views of the scene and the tracking primitives every tracker uses:
+// brick-layout texel fetch, software trilinear filter, majorant-grid DDA,
+// delta / ratio tracking steps.
+#pragma once
+
+#include <cuda_fp16.h>
+#include <cuda_bf16.h>
+
+#include "vcr_math.cuh"
+
+namespace vcr {
+
+constexpr int kBrickLog2 = 3;  // 8^3 texels per brick
+constexpr int kBrick = 1 << kBrickLog2;
+constexpr int kBrickVoxels = kBrick * kBrick * kBrick;
+
+// Density grid in brick layout.  Texel (i,j,k) lives in brick
+// b = (i>>3) + B.x*((j>>3) + B.y*(k>>3)) at offset (i&7) + 8(j&7) + 64(k&7);
+// reduced-precision bricks store v / scale[b] and decode as float(h) * scale[b].
+struct GridView {
+  const void* bricks;
+  const float* scales;     // per brick (FP16/BF16 only)
+  const float* majorants;  // per brick: max decoded texel over the brick + 1-texel halo
+  int n[3];                // voxel counts
+  int nb[3];               // brick counts
+  int precision;           // vcr_precision
+};
+
+// Scene constants of one pass (CloudProperties + Parameters + light).
+struct SceneView {
+  f3 b0, b1;        // cloud AABB (CloudProperties.bounds)
+  float max_ext;    // global density majorant (CloudProperties.maxExtinction)
+  float ds, bs;     // CloudProperties.densityScaling, baseScaling
+  float k_sigma;    // ds / bs: sigma_t = k_sigma * density
+  f3 cell;          // world size of one majorant cell (8 voxels per axis)
+  Phase ph;
+  float albedo;
+  float light;      // sun irradiance
+  f3 sun;           // unit direction the sunlight travels
+  f3 sky;
+  int sky_mode, rng_mode, nee_mode, tracker;
+  uint32_t max_events;
+};
+
+#if defined(__CUDACC__)
+
+__device__ __forceinline__ float texel(const GridView& g, int i, int j, int k) {
+  uint32_t b = (uint32_t)(i >> kBrickLog2) +
+               (uint32_t)g.nb[0] * ((uint32_t)(j >> kBrickLog2) + (uint32_t)g.nb[1] * (uint32_t)(k >> kBrickLog2));
+  uint32_t off = (b << 9) + (uint32_t)(i & 7) + ((uint32_t)(j & 7) << 3) + ((uint32_t)(k & 7) << 6);
+  if (g.precision == 0) return __ldg(reinterpret_cast<const float*>(g.bricks) + off);
+  float s = __ldg(g.scales + b);
+  if (g.precision == 1) {
+    __half h = __ldg(reinterpret_cast<const __half*>(g.bricks) + off);
+    return __half2float(h) * s;
+  }
+  __nv_bfloat16 h = __ldg(reinterpret_cast<const __nv_bfloat16*>(g.bricks) + off);
+  return __bfloat162float(h) * s;
+}
+
+// Software trilinear filter with clamp-to-edge and texel centres at
+// (i + 1/2)/N in normalised coordinates (the reference's sampler,
+// Initializers.cpp:408-418, sampleCloud PathTracer.comp:115-119).  Lerps are
+// fma(t, b - a, a), x then y then z.
+__device__ __forceinline__ float trilinear(const GridView& g, f3 nrm) {
+  float ux = nrm.x * (float)g.n[0] - 0.5f;
+  float uy = nrm.y * (float)g.n[1] - 0.5f;
+  float uz = nrm.z * (float)g.n[2] - 0.5f;
+  float fx0 = floorf(ux), fy0 = floorf(uy), fz0 = floorf(uz);
+  float tx = ux - fx0, ty = uy - fy0, tz = uz - fz0;
+  int x0 = (int)fx0, y0 = (int)fy0, z0 = (int)fz0;
+  int x1 = min(max(x0 + 1, 0), g.n[0] - 1);
+  int y1 = min(max(y0 + 1, 0), g.n[1] - 1);
+  int z1 = min(max(z0 + 1, 0), g.n[2] - 1);
+  x0 = min(max(x0, 0), g.n[0] - 1);
+  y0 = min(max(y0, 0), g.n[1] - 1);
+  z0 = min(max(z0, 0), g.n[2] - 1);
+  float v000 = texel(g, x0, y0, z0), v100 = texel(g, x1, y0, z0);
+  float v010 = texel(g, x0, y1, z0), v110 = texel(g, x1, y1, z0);
+  float v001 = texel(g, x0, y0, z1), v101 = texel(g, x1, y0, z1);
+  float v011 = texel(g, x0, y1, z1), v111 = texel(g, x1, y1, z1);
+  float c00 = fmaf(tx, v100 - v000, v000);
+  float c10 = fmaf(tx, v110 - v010, v010);
+  float c01 = fmaf(tx, v101 - v001, v001);
+  float c11 = fmaf(tx, v111 - v011, v011);
+  float c0 = fmaf(ty, c10 - c00, c00);
+  float c1 = fmaf(ty, c11 - c01, c01);
+  return fmaf(tz, c1 - c0, c0);
+}
+
+__device__ __forceinline__ float density_at(const GridView& g, const SceneView& s, f3 p) {
+  f3 ext = s.b1 - s.b0;
+  return trilinear(g, div(p - s.b0, ext));
+}
+
+#endif  // __CUDACC__
+
+// ---------------------------------------------------------------------------
+// Majorant-grid DDA (Amanatides & Woo 1987) over 8^3-voxel cells.
+// Ties between axes advance x before y before z.
+// ---------------------------------------------------------------------------
+struct Dda {
+  int c[3];      // current cell
+  int step[3];
+  float tmax[3];  // ray t of the next boundary per axis
+  float tdel[3];
+};
+
+VCR_HD void dda_axis_init(float o, float d, float b0, float cs, int c, int& step, float& tmax,
+                          float& tdel) {
+  if (d > 0.0f) {
+    step = 1;
+    tmax = ((b0 + (float)(c + 1) * cs) - o) / d;
+    tdel = cs / d;
+  } else if (d < 0.0f) {
+    step = -1;
+    tmax = ((b0 + (float)c * cs) - o) / d;
+    tdel = -cs / d;
+  } else {
+    step = 0;
+    tmax = INFINITY;
+    tdel = INFINITY;
+  }
+}
+
+VCR_HD int cell_of(float o, float b0, float cs, int nc) {
+  int c = (int)floorf((o - b0) / cs);
+  return c < 0 ? 0 : (c > nc - 1 ? nc - 1 : c);
+}
+
+VCR_HD void dda_init(Dda& d, f3 o, f3 dir, f3 b0, f3 cs, const int nc[3]) {
+  d.c[0] = cell_of(o.x, b0.x, cs.x, nc[0]);
+  d.c[1] = cell_of(o.y, b0.y, cs.y, nc[1]);
+  d.c[2] = cell_of(o.z, b0.z, cs.z, nc[2]);
+  dda_axis_init(o.x, dir.x, b0.x, cs.x, d.c[0], d.step[0], d.tmax[0], d.tdel[0]);
+  dda_axis_init(o.y, dir.y, b0.y, cs.y, d.c[1], d.step[1], d.tmax[1], d.tdel[1]);
+  dda_axis_init(o.z, dir.z, b0.z, cs.z, d.c[2], d.step[2], d.tmax[2], d.tdel[2]);
+}
+
+VCR_HD float dda_cell_exit(const Dda& d) { return fminf(fminf(d.tmax[0], d.tmax[1]), d.tmax[2]); }
+
+// Advance to the next cell; false when it leaves the grid.
+// (Each axis is spelled out so the state stays in registers.)
+VCR_HD bool dda_advance(Dda& d, const int nc[3]) {
+  if (d.tmax[0] <= d.tmax[1] && d.tmax[0] <= d.tmax[2]) {
+    d.c[0] += d.step[0];
+    d.tmax[0] = d.tmax[0] + d.tdel[0];
+    return d.c[0] >= 0 && d.c[0] < nc[0];
+  }
+  if (d.tmax[1] <= d.tmax[2]) {
+    d.c[1] += d.step[1];
+    d.tmax[1] = d.tmax[1] + d.tdel[1];
+    return d.c[1] >= 0 && d.c[1] < nc[1];
+  }
+  d.c[2] += d.step[2];
+  d.tmax[2] = d.tmax[2] + d.tdel[2];
+  return d.c[2] >= 0 && d.c[2] < nc[2];
+}
+
+VCR_HD uint32_t dda_linear(const Dda& d, const int nc[3]) {
+  return (uint32_t)d.c[0] + (uint32_t)nc[0] * ((uint32_t)d.c[1] + (uint32_t)nc[1] * (uint32_t)d.c[2]);
+}
+
+// One free-flight sample against piecewise-constant majorants: consume the
+// optical depth tau = -ln(u) cell by cell.  Returns true with t at a
+// tentative collision inside the current cell (majorant *m, density units),
+// false when the segment [t, t_end] is used up.
+//   per cell: e = min(tmax), s = min(e, t_end), dtau = (m*k)*(s - t);
+//   if dtau > tau: t = t + tau/(m*k), stop; else tau -= dtau, t = s, advance.
+struct TrackState {
+  Dda dda;
+  float t, t_end, m;
+};
+
+}  // namespace vcr

@@ -1,0 +1,96 @@
+// Host-side context of the vcr C-ABI and the launch helpers each kernel file
+// exports to the ABI layer.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/vcr/abi.h"
+#include "vcr_device.cuh"
+
+struct vcr_ctx {
+  int device = 0;
+  int sm_count = 0;
+  std::string err;
+
+  // density grid (bricks) + majorants
+  vcr_grid_desc gdesc{};
+  bool has_grid = false;
+  int precision = 0;
+  void* d_bricks = nullptr;
+  float* d_scales = nullptr;
+  float* d_majorants = nullptr;
+  float max_density = 0.0f;
+  int nb[3] = {0, 0, 0};
+
+  vcr_cloud cloud{};
+  bool has_cloud = false;
+  vcr_camera cam{};
+  bool has_cam = false;
+  vcr_params params{};
+  bool has_params = false;
+
+  // frame target: FP64 RGB sums
+  uint32_t width = 0, height = 0;
+  double* d_sum = nullptr;
+  uint32_t* d_stats = nullptr;
+  uint32_t passes = 0;
+  uint64_t samples = 0;  // camera samples per pixel summed over passes
+  // recorded on the stream of every queued pass; synchronous reads wait on
+  // it (a caller's non-blocking stream does not synchronise with stream 0)
+  cudaEvent_t work_done = nullptr;
+
+  // device counters: [0] paths [1] lookups [2] events [3] dda cells [4] work cursor
+  unsigned long long* d_counters = nullptr;
+  int* d_error = nullptr;  // device error word (bounded waits, index checks)
+
+  // shadow volume
+  float* d_sv = nullptr;
+  vcr_shadow_volume sv{};
+  bool has_sv = false;
+
+  // reusable scratch
+  void* d_scratch = nullptr;
+  size_t scratch_bytes = 0;
+};
+
+namespace vcr {
+
+// Error helpers: record a message on the context and return a status.
+vcr_status fail(vcr_ctx* ctx, vcr_status st, const char* fmt, ...);
+vcr_status cuda_fail(vcr_ctx* ctx, cudaError_t e, const char* what);
+
+#define VCR_CUDA(ctx, call)                                        \
+  do {                                                             \
+    cudaError_t e_ = (call);                                       \
+    if (e_ != cudaSuccess) return ::vcr::cuda_fail((ctx), e_, #call); \
+  } while (0)
+
+// Scratch buffer owned by the context (grown, never shrunk).
+vcr_status ensure_scratch(vcr_ctx* ctx, size_t bytes);
+
+GridView grid_view(const vcr_ctx* ctx);
+SceneView scene_view(const vcr_ctx* ctx);
+
+// grid.cu
+vcr_status grid_build(vcr_ctx* ctx, const float* d_dense, const vcr_grid_desc* desc, int precision,
+                      cudaStream_t s);
+vcr_status grid_fbm_device(vcr_ctx* ctx, float* d_dense, const vcr_grid_desc* desc,
+                           const vcr_fbm_desc* fbm, cudaStream_t s);
+void fbm_permutation(uint64_t seed, uint8_t perm[256]);
+vcr_status grid_sample_launch(vcr_ctx* ctx, const float* d_pos, float* d_out, uint32_t n,
+                              cudaStream_t s);
+vcr_status dda_trace_launch(vcr_ctx* ctx, const float* d_o, const float* d_d, uint32_t n,
+                            uint32_t max_cells, uint32_t* d_cells, float* d_t, uint32_t* d_count,
+                            cudaStream_t s);
+
+// pt.cu
+vcr_status pt_pass_launch(vcr_ctx* ctx, const vcr_pass_desc* pass, cudaStream_t s);
+
+// sv.cu
+vcr_status sv_build_launch(vcr_ctx* ctx, const vcr_shadow_volume* sv, cudaStream_t s);
+
+}  // namespace vcr

@@ -1,0 +1,197 @@
+"""Python view of the vcr C-ABI (libvcr.so), used by the tests and bench.py.
+
+The product is the C-ABI library and its C++ RenderTechnique classes; this
+module only wraps the C entry points with numpy buffers for convenience.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _abi
+from ._abi import *  # noqa: F401,F403  (struct and enum names)
+from ._abi import check, lib
+
+
+def _ptr(a: np.ndarray) -> C.c_void_p:
+    assert a.flags["C_CONTIGUOUS"], "buffers must be C-contiguous"
+    return C.c_void_p(a.ctypes.data)
+
+
+def grid_desc(size, voxel_size) -> _abi.GridDesc:
+    d = _abi.GridDesc()
+    for a in range(3):
+        d.size[a] = int(size[a])
+        d.voxel_size[a] = float(voxel_size[a])
+    return d
+
+
+def fbm_desc(seed=1, octaves=6, lacunarity=2.0, gain=0.5, base_frequency=4.0) -> _abi.FbmDesc:
+    f = _abi.FbmDesc()
+    f.seed, f.octaves, f.lacunarity, f.gain, f.base_frequency = seed, octaves, lacunarity, gain, base_frequency
+    return f
+
+
+def fbm_fill_host(size, fbm: _abi.FbmDesc) -> np.ndarray:
+    """The generator on the host (same float arithmetic as the device kernel)."""
+    out = np.empty((size[2], size[1], size[0]), np.float32)
+    check(lib().vcr_fbm_fill_host(C.byref(grid_desc(size, (1, 1, 1))), C.byref(fbm), _ptr(out)))
+    return out
+
+
+def params_set_phase_g(p: _abi.Params, g: float) -> None:
+    check(lib().vcr_params_set_phase_g(C.byref(p), g))
+
+
+def cloud_from_grid(desc: _abi.GridDesc, base_scaling: float, density_scaling: float) -> _abi.Cloud:
+    c = _abi.Cloud()
+    check(lib().vcr_cloud_from_grid(C.byref(desc), base_scaling, density_scaling, C.byref(c)))
+    return c
+
+
+def camera_look(position, forward, fov_y_deg, near_plane, width, height) -> _abi.Camera:
+    cam = _abi.Camera()
+    check(lib().vcr_camera_look(C.byref(cam), _abi.F3(*position), _abi.F3(*forward), fov_y_deg, near_plane,
+                                int(width), int(height)))
+    return cam
+
+
+def shadow_volume_setup(light_dir, bmin, bmax, n) -> _abi.ShadowVolume:
+    sv = _abi.ShadowVolume()
+    check(lib().vcr_shadow_volume_setup(C.byref(sv), _abi.F3(*light_dir), _abi.F3(*bmin), _abi.F3(*bmax), n))
+    return sv
+
+
+def xyz_write(path: str, desc: _abi.GridDesc, data: np.ndarray) -> None:
+    data = np.ascontiguousarray(data, np.float32)
+    check(lib().vcr_xyz_write(path.encode(), C.byref(desc), _ptr(data)))
+
+
+def xyz_read(path: str):
+    desc = _abi.GridDesc()
+    check(lib().vcr_xyz_read(path.encode(), C.byref(desc), None, 0))
+    out = np.empty((desc.size[2], desc.size[1], desc.size[0]), np.float32)
+    check(lib().vcr_xyz_read(path.encode(), C.byref(desc), _ptr(out), out.size))
+    return desc, out
+
+
+class Context:
+    """One vcr_ctx: owns the device grid, frame sums and scratch."""
+
+    def __init__(self, device: int = 0):
+        L = lib()
+        h = C.c_void_p()
+        d = _abi.DeviceDesc(device, 0)
+        check(L.vcr_create(C.byref(h), C.byref(d)))
+        self.h = h
+        self.width = self.height = 0
+
+    def close(self):
+        if self.h:
+            lib().vcr_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _ck(self, st):
+        check(st, self.h)
+
+    # grid -------------------------------------------------------------------
+    def grid_upload(self, desc, dense: np.ndarray, precision=_abi.PREC_FP32):
+        dense = np.ascontiguousarray(dense, np.float32)
+        self._ck(lib().vcr_grid_upload(self.h, C.byref(desc), _ptr(dense), precision))
+
+    def grid_generate(self, desc, fbm, precision=_abi.PREC_FP32):
+        self._ck(lib().vcr_grid_generate(self.h, C.byref(desc), C.byref(fbm), precision))
+
+    def grid_info(self):
+        m = C.c_float()
+        nb = (C.c_uint32 * 3)()
+        self._ck(lib().vcr_grid_info(self.h, C.byref(m), nb))
+        return m.value, tuple(nb)
+
+    def majorants(self) -> np.ndarray:
+        _, nb = self.grid_info()
+        out = np.empty(nb[0] * nb[1] * nb[2], np.float32)
+        self._ck(lib().vcr_grid_read_majorants(self.h, _ptr(out), out.size))
+        return out
+
+    def grid_sample(self, d_pos: int, d_out: int, n: int, stream: int = 0):
+        self._ck(lib().vcr_grid_sample(self.h, C.c_void_p(d_pos), C.c_void_p(d_out), n, C.c_void_p(stream)))
+
+    # scene ------------------------------------------------------------------
+    def set_cloud(self, cloud):
+        self._ck(lib().vcr_set_cloud(self.h, C.byref(cloud)))
+
+    def set_camera(self, cam):
+        self._ck(lib().vcr_set_camera(self.h, C.byref(cam)))
+
+    def set_params(self, p):
+        self._ck(lib().vcr_set_params(self.h, C.byref(p)))
+
+    def set_frame(self, w, h):
+        self._ck(lib().vcr_set_frame(self.h, w, h))
+        self.width, self.height = w, h
+
+    def reset(self):
+        self._ck(lib().vcr_reset_accumulation(self.h))
+
+    def shadow_volume_build(self, sv, stream=0):
+        self._ck(lib().vcr_shadow_volume_build(self.h, C.byref(sv), C.c_void_p(stream)))
+
+    # passes -----------------------------------------------------------------
+    def pt_pass(self, seed=0, pass_index=0, spp=1, crop=(0, 0, 0, 0), flags=0, stream=0):
+        p = _abi.PassDesc()
+        p.seed, p.pass_index, p.spp, p.flags = seed, pass_index, spp, flags
+        for i in range(4):
+            p.crop[i] = crop[i]
+        self._ck(lib().vcr_pt_pass(self.h, C.byref(p), C.c_void_p(stream)))
+
+    def counters(self):
+        out = (C.c_uint64 * 4)()
+        self._ck(lib().vcr_pt_counters(self.h, out))
+        return tuple(out)
+
+    def dda_trace(self, d_o, d_d, n, max_cells, d_cells, d_t, d_count, stream=0):
+        self._ck(lib().vcr_dda_trace(self.h, C.c_void_p(d_o), C.c_void_p(d_d), n, max_cells, C.c_void_p(d_cells),
+                                     C.c_void_p(d_t), C.c_void_p(d_count), C.c_void_p(stream)))
+
+    def synchronize(self):
+        self._ck(lib().vcr_synchronize(self.h))
+
+    # read back --------------------------------------------------------------
+    def image_mean(self) -> np.ndarray:
+        out = np.empty((self.height, self.width, 3), np.float32)
+        self._ck(lib().vcr_readback(self.h, _abi.BUF_IMAGE_MEAN, _ptr(out), out.nbytes))
+        return out
+
+    def image_sum(self) -> np.ndarray:
+        out = np.empty((self.height, self.width, 3), np.float64)
+        self._ck(lib().vcr_readback(self.h, _abi.BUF_IMAGE_SUM, _ptr(out), out.nbytes))
+        return out
+
+    def path_stats(self) -> np.ndarray:
+        out = np.empty((self.height, self.width, 4), np.uint32)
+        self._ck(lib().vcr_readback(self.h, _abi.BUF_PATH_STATS, _ptr(out), out.nbytes))
+        return out
+
+    def shadow_volume(self, n) -> np.ndarray:
+        out = np.empty((n, n, n), np.float32)
+        self._ck(lib().vcr_readback(self.h, _abi.BUF_SHADOW_VOLUME, _ptr(out), out.nbytes))
+        return out
+
+    def pass_count(self) -> int:
+        v = C.c_uint32()
+        self._ck(lib().vcr_pass_count(self.h, C.byref(v)))
+        return v.value

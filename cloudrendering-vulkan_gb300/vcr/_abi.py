@@ -1,0 +1,136 @@
+"""ctypes mirror of include/vcr/abi.h.
+
+The shared library is loaded from the package directory; there is no
+fallback: if libvcr.so is missing, loading raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(PKG_DIR, "libvcr.so")
+
+# status codes
+OK, ERR_INVALID, ERR_CUDA, ERR_OOM, ERR_TIMEOUT, ERR_STATE, ERR_IO, ERR_UNSUPPORTED, ERR_CAPACITY = range(9)
+STATUS_NAMES = ["OK", "INVALID", "CUDA", "OOM", "TIMEOUT", "STATE", "IO", "UNSUPPORTED", "CAPACITY"]
+
+PREC_FP32, PREC_FP16, PREC_BF16 = 0, 1, 2
+RNG_PCG, RNG_XORSHIFT = 0, 1
+NEE_RATIO, NEE_SHADOW_VOLUME = 0, 1
+SKY_CONSTANT, SKY_GRADIENT = 0, 1
+TRACKER_GLOBAL, TRACKER_DDA = 0, 1
+BUF_IMAGE_MEAN, BUF_IMAGE_SUM, BUF_PATH_STATS, BUF_PPM_STATS, BUF_SHADOW_VOLUME = range(5)
+PASS_RECORD_STATS, PASS_NO_ACCUMULATE = 1, 2
+
+F3 = C.c_float * 3
+
+
+class DeviceDesc(C.Structure):
+    _fields_ = [("device", C.c_int32), ("flags", C.c_uint32)]
+
+
+class GridDesc(C.Structure):
+    _fields_ = [("size", C.c_uint32 * 3), ("_pad", C.c_uint32), ("voxel_size", C.c_double * 3)]
+
+
+class Cloud(C.Structure):
+    _fields_ = [("bounds_min", F3), ("bounds_max", F3), ("max_extinction", C.c_float),
+                ("base_scaling", C.c_float), ("density_scaling", C.c_float)]
+
+
+class Camera(C.Structure):
+    _fields_ = [("position", F3), ("forward", F3), ("right", F3), ("up", F3), ("near_plane", C.c_float),
+                ("pixel_size_x", C.c_float), ("pixel_size_y", C.c_float), ("half_width", C.c_int32),
+                ("half_height", C.c_int32)]
+
+
+class Params(C.Structure):
+    _fields_ = [("max_events", C.c_uint32), ("light_intensity", C.c_float), ("phase_g", C.c_float),
+                ("phase_one_plus_g2", C.c_float), ("phase_one_minus_g2", C.c_float),
+                ("phase_one_over_2g", C.c_float), ("isotropic", C.c_int32), ("albedo", C.c_float),
+                ("sun_dir", F3), ("sky", F3), ("sky_mode", C.c_uint32), ("rng_mode", C.c_uint32),
+                ("nee_mode", C.c_uint32), ("tracker", C.c_uint32), ("nrc_events", C.c_uint32)]
+
+
+class ShadowVolume(C.Structure):
+    _fields_ = [("bounds_min", F3), ("bounds_max", F3), ("light_dir", F3), ("right", F3), ("up", F3),
+                ("basis_change", C.c_float * 9), ("voxel_axis_count", C.c_uint32), ("voxel_size", C.c_float)]
+
+
+class PassDesc(C.Structure):
+    _fields_ = [("seed", C.c_uint32), ("pass_index", C.c_uint32), ("spp", C.c_uint32),
+                ("crop", C.c_uint32 * 4), ("flags", C.c_uint32)]
+
+
+class FbmDesc(C.Structure):
+    _fields_ = [("seed", C.c_uint64), ("octaves", C.c_uint32), ("lacunarity", C.c_float), ("gain", C.c_float),
+                ("base_frequency", C.c_float)]
+
+
+_P = C.c_void_p
+_S = C.c_int  # vcr_status
+_u32, _u64, _f, _sz = C.c_uint32, C.c_uint64, C.c_float, C.c_size_t
+
+# name -> (restype, argtypes).  The list is also the set of symbols the
+# header declares; tests check that every one is exported.
+SIGNATURES = {
+    "vcr_create": (_S, [C.POINTER(_P), C.POINTER(DeviceDesc)]),
+    "vcr_destroy": (_S, [_P]),
+    "vcr_last_error": (C.c_char_p, [_P]),
+    "vcr_version": (_u32, []),
+    "vcr_synchronize": (_S, [_P]),
+    "vcr_params_set_phase_g": (_S, [C.POINTER(Params), _f]),
+    "vcr_cloud_from_grid": (_S, [C.POINTER(GridDesc), _f, _f, C.POINTER(Cloud)]),
+    "vcr_camera_look": (_S, [C.POINTER(Camera), F3, F3, _f, _f, C.c_int32, C.c_int32]),
+    "vcr_shadow_volume_setup": (_S, [C.POINTER(ShadowVolume), F3, F3, F3, _u32]),
+    "vcr_grid_upload": (_S, [_P, C.POINTER(GridDesc), _P, C.c_int]),
+    "vcr_grid_generate": (_S, [_P, C.POINTER(GridDesc), C.POINTER(FbmDesc), C.c_int]),
+    "vcr_grid_info": (_S, [_P, C.POINTER(_f), C.POINTER(_u32)]),
+    "vcr_grid_read_majorants": (_S, [_P, _P, _sz]),
+    "vcr_grid_sample": (_S, [_P, _P, _P, _u32, _P]),
+    "vcr_xyz_read": (_S, [C.c_char_p, C.POINTER(GridDesc), _P, _sz]),
+    "vcr_xyz_write": (_S, [C.c_char_p, C.POINTER(GridDesc), _P]),
+    "vcr_fbm_fill_host": (_S, [C.POINTER(GridDesc), C.POINTER(FbmDesc), _P]),
+    "vcr_set_cloud": (_S, [_P, C.POINTER(Cloud)]),
+    "vcr_set_camera": (_S, [_P, C.POINTER(Camera)]),
+    "vcr_set_params": (_S, [_P, C.POINTER(Params)]),
+    "vcr_set_frame": (_S, [_P, _u32, _u32]),
+    "vcr_reset_accumulation": (_S, [_P]),
+    "vcr_shadow_volume_build": (_S, [_P, C.POINTER(ShadowVolume), _P]),
+    "vcr_pt_pass": (_S, [_P, C.POINTER(PassDesc), _P]),
+    "vcr_pt_counters": (_S, [_P, C.POINTER(_u64)]),
+    "vcr_dda_trace": (_S, [_P, _P, _P, _u32, _u32, _P, _P, _P, _P]),
+    "vcr_readback": (_S, [_P, C.c_int, _P, _sz]),
+    "vcr_pass_count": (_S, [_P, C.POINTER(_u32)]),
+}
+
+_lib = None
+
+
+def lib():
+    """Load libvcr.so once; raise if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: run __graft_entry__.build() first")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+class VcrError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        self.status = status
+        name = STATUS_NAMES[status] if 0 <= status < len(STATUS_NAMES) else str(status)
+        super().__init__(f"vcr status {name}: {msg}")
+
+
+def check(status: int, ctx=None) -> None:
+    if status != OK:
+        msg = lib().vcr_last_error(ctx)
+        raise VcrError(status, msg.decode() if msg else "")

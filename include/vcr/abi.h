@@ -1,0 +1,313 @@
+/*
+ * vcr — GB300-native volumetric cloud light-transport core: the C-ABI.
+ *
+ * Every entry point is `extern "C"`, takes plain pointers, sizes and POD
+ * structs, and returns a vcr_status.  No exception crosses this boundary and
+ * no CUDA or C++ type appears in a signature: streams are passed as `void*`
+ * (a cudaStream_t, 0 = the legacy default stream).
+ *
+ * Conventions
+ *  - A vcr_ctx owns all device memory it allocates (grid bricks, accumulation
+ *    images, photon maps, beams, BVH nodes, network weights, scratch).
+ *  - Host structs are copied at the call; the caller keeps ownership.
+ *  - Calls are stream-ordered and asynchronous unless documented otherwise;
+ *    calls on one context must come from one host thread at a time (the
+ *    reference also records and submits from a single thread, main.cpp:603-712).
+ *  - Device-side waits are bounded; a wait that runs out reports
+ *    VCR_ERR_TIMEOUT instead of hanging.
+ *  - vcr_last_error(ctx) returns a human-readable message for the last
+ *    failing call on that context (NULL ctx: the last creation failure).
+ *
+ * The reference drives its GLSL compute shaders through the RenderTechnique
+ * interface (CloudRendering-Vulkan/RenderTechnique.h:15-67); each group of
+ * entry points below names the reference call it replaces.
+ */
+#ifndef VCR_ABI_H
+#define VCR_ABI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define VCR_API __declspec(dllexport)
+#else
+#define VCR_API __attribute__((visibility("default")))
+#endif
+
+/* ------------------------------------------------------------------------ */
+/* Status codes                                                             */
+/* ------------------------------------------------------------------------ */
+typedef enum vcr_status {
+  VCR_OK = 0,
+  VCR_ERR_INVALID = 1,     /* bad argument (null pointer, size, enum)        */
+  VCR_ERR_CUDA = 2,        /* a CUDA runtime call failed                     */
+  VCR_ERR_OOM = 3,         /* device allocation failed                      */
+  VCR_ERR_TIMEOUT = 4,     /* a bounded device-side wait ran out             */
+  VCR_ERR_STATE = 5,       /* call out of order (e.g. pass before a grid)    */
+  VCR_ERR_IO = 6,          /* file could not be read or written              */
+  VCR_ERR_UNSUPPORTED = 7, /* feature or size not supported                  */
+  VCR_ERR_CAPACITY = 8     /* an output buffer was too small (data dropped)  */
+} vcr_status;
+
+typedef struct vcr_ctx vcr_ctx;
+
+/* ------------------------------------------------------------------------ */
+/* Enums                                                                    */
+/* ------------------------------------------------------------------------ */
+typedef enum vcr_precision {
+  VCR_PREC_FP32 = 0,
+  VCR_PREC_FP16 = 1, /* FP16 texels, FP32 scale per 8^3 brick */
+  VCR_PREC_BF16 = 2  /* BF16 texels, FP32 scale per 8^3 brick */
+} vcr_precision;
+
+typedef enum vcr_rng_mode {
+  VCR_RNG_PCG = 0,     /* counter-keyed PCG stream per (seed, path, pass)    */
+  VCR_RNG_XORSHIFT = 1 /* the shaders' xorshift32 (PathTracer.comp:220-241)  */
+} vcr_rng_mode;
+
+typedef enum vcr_nee_mode {
+  VCR_NEE_RATIO = 0,       /* unbiased ratio tracking toward the sun          */
+  VCR_NEE_SHADOW_VOLUME = 1 /* shadow-volume lookup (PathTracer.comp:406-411) */
+} vcr_nee_mode;
+
+typedef enum vcr_sky_mode {
+  VCR_SKY_CONSTANT = 0, /* constant radiance vcr_params.sky                 */
+  VCR_SKY_GRADIENT = 1  /* five-stop gradient (PathTracer.comp:104-113)      */
+} vcr_sky_mode;
+
+typedef enum vcr_tracker {
+  VCR_TRACKER_GLOBAL = 0, /* one global majorant (PathTracer.comp:318-361)    */
+  VCR_TRACKER_DDA = 1     /* per-brick majorants walked by a 3D DDA           */
+} vcr_tracker;
+
+typedef enum vcr_buffer_id {
+  VCR_BUF_IMAGE_MEAN = 0,   /* float32 RGB, W*H*3: accumulated mean          */
+  VCR_BUF_IMAGE_SUM = 1,    /* float64 RGB, W*H*3: raw FP64 sums             */
+  VCR_BUF_PATH_STATS = 2,   /* uint32 x4 per pixel of the last pass          */
+  VCR_BUF_PPM_STATS = 3,    /* float64 x4 per pixel: N, R, flux(luminance)   */
+  VCR_BUF_SHADOW_VOLUME = 4 /* float32 n^3 shadow-volume texels              */
+} vcr_buffer_id;
+
+/* ------------------------------------------------------------------------ */
+/* POD restatements of the reference's uniform blocks                       */
+/* ------------------------------------------------------------------------ */
+
+/* Device selection (the reference picks one Vulkan queue,
+ * VulkanPhysicalDevice.cpp:102-104). */
+typedef struct vcr_device_desc {
+  int32_t device;  /* CUDA device ordinal */
+  uint32_t flags;  /* reserved, 0 */
+} vcr_device_desc;
+
+/* Grid3D<float> header (Grid3D.h:9-41): voxel counts and voxel size. */
+typedef struct vcr_grid_desc {
+  uint32_t size[3];
+  uint32_t _pad;
+  double voxel_size[3];
+} vcr_grid_desc;
+
+/* CloudProperties (UniformBuffers.h:71-78).  max_extinction is the
+ * density majorant; vcr_grid_upload/vcr_grid_generate set it to
+ * max(grid max, 0.01) as SetCloudProperties does (main.cpp:152). */
+typedef struct vcr_cloud {
+  float bounds_min[3];
+  float bounds_max[3];
+  float max_extinction;
+  float base_scaling;
+  float density_scaling;
+} vcr_cloud;
+
+/* CameraProperties (UniformBuffers.h:15-69).  Image width = 2*half_width. */
+typedef struct vcr_camera {
+  float position[3];
+  float forward[3];
+  float right[3];
+  float up[3];
+  float near_plane;
+  float pixel_size_x;
+  float pixel_size_y;
+  int32_t half_width;
+  int32_t half_height;
+} vcr_camera;
+
+/* Parameters (UniformBuffers.h:80-112) plus the light and the semantic
+ * switches.  The phase_* terms follow Parameters::SetPhaseG; use
+ * vcr_params_set_phase_g to fill them. */
+typedef struct vcr_params {
+  uint32_t max_events;     /* scatter events per path; 0 = until escape      */
+  float light_intensity;   /* sun irradiance (Parameters.lightIntensity)     */
+  float phase_g;
+  float phase_one_plus_g2;
+  float phase_one_minus_g2;
+  float phase_one_over_2g;
+  int32_t isotropic;
+  float albedo;            /* single-scattering albedo (1 = reference PT)    */
+  float sun_dir[3];        /* unit direction the sunlight travels            */
+  float sky[3];            /* constant sky radiance (VCR_SKY_CONSTANT)       */
+  uint32_t sky_mode;       /* vcr_sky_mode                                   */
+  uint32_t rng_mode;       /* vcr_rng_mode                                   */
+  uint32_t nee_mode;       /* vcr_nee_mode                                   */
+  uint32_t tracker;        /* vcr_tracker                                    */
+  uint32_t nrc_events;     /* >0: terminate into the radiance cache after    */
+                           /*     this many events (vcr_nrc_*)               */
+} vcr_params;
+
+/* ShadowVolumeProperties (UniformBuffers.h:114-167), derived state included
+ * (bounds, basis, voxel size); vcr_shadow_volume_setup fills it. */
+typedef struct vcr_shadow_volume {
+  float bounds_min[3];
+  float bounds_max[3];
+  float light_dir[3];
+  float right[3];
+  float up[3];
+  float basis_change[9]; /* row-major 3x3 world -> (right, up, light) */
+  uint32_t voxel_axis_count;
+  float voxel_size;
+} vcr_shadow_volume;
+
+/* PushConstants (UniformBuffers.h:6-13) for one progressive pass. */
+typedef struct vcr_pass_desc {
+  uint32_t seed;       /* render seed                                         */
+  uint32_t pass_index; /* 0-based pass; the RNG key and the running mean use it */
+  uint32_t spp;        /* camera samples per pixel in this pass (>=1)          */
+  uint32_t crop[4];    /* x0, y0, w, h; w == 0 renders the whole frame         */
+  uint32_t flags;      /* VCR_PASS_* */
+} vcr_pass_desc;
+
+#define VCR_PASS_RECORD_STATS 1u /* write VCR_BUF_PATH_STATS for this pass    */
+#define VCR_PASS_NO_ACCUMULATE 2u /* overwrite instead of adding to the sums  */
+
+/* Seeded Perlin-fBm density generator (the synthetic stand-in for the
+ * reference's cloud files, models/mycloud.xyz). */
+typedef struct vcr_fbm_desc {
+  uint64_t seed;
+  uint32_t octaves;
+  float lacunarity;
+  float gain;
+  float base_frequency; /* noise frequency over the longest grid axis */
+} vcr_fbm_desc;
+
+/* ------------------------------------------------------------------------ */
+/* Context lifecycle                                                        */
+/* Replaces: RenderTechnique construction + VulkanDevice (main.cpp:765-840) */
+/* ------------------------------------------------------------------------ */
+VCR_API vcr_status vcr_create(vcr_ctx** out, const vcr_device_desc* desc);
+VCR_API vcr_status vcr_destroy(vcr_ctx* ctx);
+VCR_API const char* vcr_last_error(const vcr_ctx* ctx);
+VCR_API uint32_t vcr_version(void);
+/* Blocks until all work the context queued has finished (vkDeviceWaitIdle,
+ * main.cpp:269); also reports any device-side error word. */
+VCR_API vcr_status vcr_synchronize(vcr_ctx* ctx);
+
+/* ------------------------------------------------------------------------ */
+/* Host-side helpers for the reference's parameter structs                 */
+/* ------------------------------------------------------------------------ */
+/* Parameters::SetPhaseG (UniformBuffers.h:93-106): clamps g to +-0.95. */
+VCR_API vcr_status vcr_params_set_phase_g(vcr_params* p, float g);
+/* SetCloudProperties (main.cpp:145-163): bounds from voxel size x count x
+ * base scaling, x/y centred, z from 0. */
+VCR_API vcr_status vcr_cloud_from_grid(const vcr_grid_desc* grid, float base_scaling,
+                                       float density_scaling, vcr_cloud* out);
+/* CameraProperties defaults + SetResolution/SetFOV (UniformBuffers.h:15-58). */
+VCR_API vcr_status vcr_camera_look(vcr_camera* cam, const float position[3],
+                                   const float forward[3], float fov_y_deg,
+                                   float near_plane, int32_t width, int32_t height);
+/* ShadowVolumeProperties::SetLightDirection + SetOrigin
+ * (UniformBuffers.h:131-166) for a cloud AABB. */
+VCR_API vcr_status vcr_shadow_volume_setup(vcr_shadow_volume* sv, const float light_dir[3],
+                                           const float bounds_min[3], const float bounds_max[3],
+                                           uint32_t voxel_axis_count);
+
+/* ------------------------------------------------------------------------ */
+/* Density grid                                                             */
+/* Replaces: Grid3D<float> load + UpdateCloudData upload (main.cpp:266-335)
+ *           + QueueUpdateCloudData/QueueUpdateCloudDataSampler             */
+/* ------------------------------------------------------------------------ */
+/* Upload an x-fastest float grid (Grid3D memory order, Grid3D.h:116) from
+ * host memory, brick it at `precision`, build the brick majorant grid.
+ * Synchronous with respect to the host buffer (it may be reused on return). */
+VCR_API vcr_status vcr_grid_upload(vcr_ctx* ctx, const vcr_grid_desc* desc,
+                                   const float* host_density, vcr_precision precision);
+/* Same, generating the density on the device from a seeded fBm. */
+VCR_API vcr_status vcr_grid_generate(vcr_ctx* ctx, const vcr_grid_desc* desc,
+                                     const vcr_fbm_desc* fbm, vcr_precision precision);
+/* Global density maximum of the stored grid (Grid3D::GetMajorant,
+ * Grid3D.h:180-192) and brick-grid dimensions. */
+VCR_API vcr_status vcr_grid_info(vcr_ctx* ctx, float* out_max_density,
+                                 uint32_t out_bricks[3]);
+/* Read the brick majorant grid (float per 8^3 brick, x-fastest). */
+VCR_API vcr_status vcr_grid_read_majorants(vcr_ctx* ctx, float* host_out, size_t count);
+/* Densities at n world positions (device pointers; float3 in, float out),
+ * through the same trilinear fetch the trackers use. */
+VCR_API vcr_status vcr_grid_sample(vcr_ctx* ctx, const float* d_pos, float* d_out,
+                                   uint32_t n, void* stream);
+
+/* .xyz file I/O (Grid3D::Load Grid3D.h:44-90, GridData::save GridData.h:14-25).
+ * The file stores z fastest; memory is x fastest.  Pass a NULL data pointer
+ * to vcr_xyz_read to query the header only. */
+VCR_API vcr_status vcr_xyz_read(const char* path, vcr_grid_desc* desc, float* host_out,
+                                size_t capacity);
+VCR_API vcr_status vcr_xyz_write(const char* path, const vcr_grid_desc* desc,
+                                 const float* host_data);
+/* The fBm generator on the host (same float arithmetic as the device one). */
+VCR_API vcr_status vcr_fbm_fill_host(const vcr_grid_desc* desc, const vcr_fbm_desc* fbm,
+                                     float* host_out);
+
+/* ------------------------------------------------------------------------ */
+/* Scene state (QueueUpdateCameraProperties / QueueUpdateParameters /       */
+/* QueueUpdateShadowVolume + UpdateDescriptorSets)                          */
+/* ------------------------------------------------------------------------ */
+VCR_API vcr_status vcr_set_cloud(vcr_ctx* ctx, const vcr_cloud* cloud);
+VCR_API vcr_status vcr_set_camera(vcr_ctx* ctx, const vcr_camera* cam);
+VCR_API vcr_status vcr_set_params(vcr_ctx* ctx, const vcr_params* params);
+/* SetFrameReferences (RenderTechniquePT.cpp:63-80): a headless FP64 RGB
+ * accumulation target of width x height; clears the running sums. */
+VCR_API vcr_status vcr_set_frame(vcr_ctx* ctx, uint32_t width, uint32_t height);
+/* Zero the running sums (frameCount = 1 reset, main.cpp:262). */
+VCR_API vcr_status vcr_reset_accumulation(vcr_ctx* ctx);
+
+/* ------------------------------------------------------------------------ */
+/* Shadow volume (RenderTechniqueSV::RecordDrawCommands,                    */
+/* RenderTechniqueSV.cpp:102-113 + ShadowVolume.comp:77-93)                  */
+/* ------------------------------------------------------------------------ */
+VCR_API vcr_status vcr_shadow_volume_build(vcr_ctx* ctx, const vcr_shadow_volume* sv,
+                                           void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* Path tracing (RenderTechniquePT::RecordDrawCommands,                     */
+/* RenderTechniquePT.cpp:129-168 + PathTracer.comp:366-425)                  */
+/* ------------------------------------------------------------------------ */
+/* One progressive pass: `spp` camera paths per pixel of the crop, added to
+ * the FP64 sums.  vcr_params.tracker selects the reference per-pixel
+ * global-majorant tracker or the persistent DDA wavefront tracker. */
+VCR_API vcr_status vcr_pt_pass(vcr_ctx* ctx, const vcr_pass_desc* pass, void* stream);
+/* Counters of the last vcr_pt_pass: [0] paths, [1] density lookups,
+ * [2] scatter events, [3] DDA cell visits. */
+VCR_API vcr_status vcr_pt_counters(vcr_ctx* ctx, uint64_t out[4]);
+
+/* Trace the majorant-grid DDA of n rays (device float3 origins and unit
+ * directions, already inside or entering the cloud box).  For ray i, up to
+ * max_cells visits are written at out_cells[i*max_cells ..] as (linear cell
+ * index) and out_t[2*(i*max_cells+k) ..] as (t_enter, t_exit); out_count[i]
+ * gets the number of visits.  Bit-exact against the CPU oracle. */
+VCR_API vcr_status vcr_dda_trace(vcr_ctx* ctx, const float* d_origin, const float* d_dir,
+                                 uint32_t n, uint32_t max_cells, uint32_t* d_out_cells,
+                                 float* d_out_t, uint32_t* d_out_count, void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* Read back                                                                */
+/* ------------------------------------------------------------------------ */
+/* Synchronous copy of a context buffer to host memory (bytes must match). */
+VCR_API vcr_status vcr_readback(vcr_ctx* ctx, vcr_buffer_id id, void* host_out, size_t bytes);
+/* Number of passes accumulated into the sums so far. */
+VCR_API vcr_status vcr_pass_count(vcr_ctx* ctx, uint32_t* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VCR_ABI_H */

@@ -1,0 +1,150 @@
+"""ctypes binding of the CPU oracle (liboracle.so) — test infrastructure.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use
+this module, and only as the checker or the timed CPU reference.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+sys.path.insert(0, os.path.join(ROOT, "cloudrendering-vulkan_gb300"))
+from vcr import _abi  # noqa: E402  (struct layouts only)
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        from . import build as _b  # type: ignore
+        path = _b.build()
+        L = C.CDLL(path)
+        P = C.c_void_p
+        u32, f = C.c_uint32, C.c_float
+        sig = {
+            "oracle_grid_new": (P, [P, P, C.c_int]),
+            "oracle_grid_free": (None, [P]),
+            "oracle_grid_max": (f, [P]),
+            "oracle_grid_majorants": (None, [P, P]),
+            "oracle_grid_decoded": (None, [P, P]),
+            "oracle_grid_sample": (None, [P, C.POINTER(_abi.Cloud), P, u32, P]),
+            "oracle_dda_trace": (None, [P, C.POINTER(_abi.Cloud), P, P, u32, u32, P, P, P]),
+            "oracle_pt_pass": (C.c_int, [P, C.POINTER(_abi.Cloud), C.POINTER(_abi.Camera), C.POINTER(_abi.Params),
+                                         C.POINTER(_abi.ShadowVolume), P, u32, u32, C.POINTER(_abi.PassDesc), P, P,
+                                         C.c_int]),
+            "oracle_sv_build": (None, [P, C.POINTER(_abi.Cloud), C.POINTER(_abi.ShadowVolume), P]),
+            "oracle_fbm_fill": (None, [P, C.c_uint64, u32, f, f, f, P, C.c_int]),
+            "oracle_log": (f, [f]),
+            "oracle_exp": (f, [f]),
+            "oracle_sincos2pi": (None, [f, C.POINTER(f), C.POINTER(f)]),
+            "oracle_pcg_hash": (u32, [u32]),
+            "oracle_f32_to_f16": (C.c_uint16, [f]),
+            "oracle_f32_to_bf16": (C.c_uint16, [f]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _p(a: np.ndarray):
+    assert a.flags["C_CONTIGUOUS"]
+    return C.c_void_p(a.ctypes.data)
+
+
+def fbm_fill(size, seed=1, octaves=6, lacunarity=2.0, gain=0.5, f0=4.0, threads=0) -> np.ndarray:
+    out = np.empty((size[2], size[1], size[0]), np.float32)
+    n = (C.c_uint32 * 3)(*size)
+    lib().oracle_fbm_fill(C.cast(n, C.c_void_p), seed, octaves, lacunarity, gain, f0, _p(out),
+                          threads or os.cpu_count() or 1)
+    return out
+
+
+class Grid:
+    """Oracle grid: decoded texels of the requested precision + majorants."""
+
+    def __init__(self, dense: np.ndarray, precision: int = 0):
+        dense = np.ascontiguousarray(dense, np.float32)
+        nz, ny, nx = dense.shape
+        self.size = (nx, ny, nz)
+        n = (C.c_uint32 * 3)(nx, ny, nz)
+        self.h = lib().oracle_grid_new(C.cast(n, C.c_void_p), _p(dense), precision)
+        self.nb = tuple((s + 7) // 8 for s in self.size)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().oracle_grid_free(self.h)
+            self.h = None
+
+    def max_density(self) -> float:
+        return lib().oracle_grid_max(self.h)
+
+    def majorants(self) -> np.ndarray:
+        out = np.empty(self.nb[0] * self.nb[1] * self.nb[2], np.float32)
+        lib().oracle_grid_majorants(self.h, _p(out))
+        return out
+
+    def decoded(self) -> np.ndarray:
+        out = np.empty(self.size[::-1], np.float32)
+        lib().oracle_grid_decoded(self.h, _p(out))
+        return out
+
+    def sample(self, cloud, pos: np.ndarray) -> np.ndarray:
+        pos = np.ascontiguousarray(pos, np.float32)
+        out = np.empty(pos.shape[0], np.float32)
+        lib().oracle_grid_sample(self.h, C.byref(cloud), _p(pos), pos.shape[0], _p(out))
+        return out
+
+    def dda_trace(self, cloud, o: np.ndarray, d: np.ndarray, max_cells: int):
+        o = np.ascontiguousarray(o, np.float32)
+        d = np.ascontiguousarray(d, np.float32)
+        n = o.shape[0]
+        cells = np.zeros((n, max_cells), np.uint32)
+        tt = np.zeros((n, max_cells, 2), np.float32)
+        cnt = np.zeros(n, np.uint32)
+        lib().oracle_dda_trace(self.h, C.byref(cloud), _p(o), _p(d), n, max_cells, _p(cells), _p(tt), _p(cnt))
+        return cells, tt, cnt
+
+    def pt_pass(self, cloud, cam, params, width, height, seed=0, pass_index=0, spp=1, crop=(0, 0, 0, 0), flags=0,
+                sum_img=None, stats=None, sv=None, sv_tex=None, threads=0):
+        if sum_img is None:
+            sum_img = np.zeros((height, width, 3), np.float64)
+        if stats is None:
+            stats = np.zeros((height, width, 4), np.uint32)
+        p = _abi.PassDesc()
+        p.seed, p.pass_index, p.spp, p.flags = seed, pass_index, spp, flags
+        for i in range(4):
+            p.crop[i] = crop[i]
+        svp = C.byref(sv) if sv is not None else None
+        svt = _p(np.ascontiguousarray(sv_tex, np.float32)) if sv_tex is not None else None
+        lib().oracle_pt_pass(self.h, C.byref(cloud), C.byref(cam), C.byref(params), svp, svt, width, height,
+                             C.byref(p), _p(sum_img), _p(stats), threads or os.cpu_count() or 1)
+        return sum_img, stats
+
+    def sv_build(self, cloud, sv) -> np.ndarray:
+        n = sv.voxel_axis_count
+        out = np.empty((n, n, n), np.float32)
+        lib().oracle_sv_build(self.h, C.byref(cloud), C.byref(sv), _p(out))
+        return out
+
+
+def olog(x: float) -> float:
+    return lib().oracle_log(x)
+
+
+def oexp(x: float) -> float:
+    return lib().oracle_exp(x)
+
+
+def sincos2pi(u: float):
+    s, c = C.c_float(), C.c_float()
+    lib().oracle_sincos2pi(u, C.byref(s), C.byref(c))
+    return s.value, c.value
