@@ -1,0 +1,312 @@
+// Stable LSD radix sort of (uint32 key, uint32 value) pairs with 4-bit
+// digits, and the Morton codes the photon-beam pipeline sorts.
+//
+// Reference design: PPB_RadixSort_LocalSort.comp (block-local 4-bit sort by
+// four 1-bit split passes with a Blelloch scan + 16-bin histogram),
+// PPB_RadixSort_PrefixSum.comp and PPB_RadixSort_GlobalSort.comp (scan of
+// the histograms, scatter), driven from RenderTechniquePPB.cpp:465-491; keys
+// from expandBits/getMortonCode (PPB_PT.comp:317-333).
+//
+// GB300 design: one histogram kernel computes the digit counts of every
+// pass at once; each digit pass is then ONE kernel over 2048-key tiles:
+// stable in-tile ranking with warp match_any, a decoupled look-back across
+// tiles (tile ids taken in launch order from an atomic counter, so every
+// tile waits only on tiles already running), shared-memory staging and a
+// coalesced scatter.  Each pass reads and writes every pair once (16 B/key
+// per pass).  Spins are bounded: a wait that runs out sets the context's
+// error word instead of hanging.
+#include "vcr_internal.h"
+
+namespace vcr {
+
+constexpr int kSortThreads = 256;
+constexpr int kSortItems = 8;
+constexpr int kSortTile = kSortThreads * kSortItems;  // 2048 keys
+constexpr uint32_t kFlagA = 1u << 30;                 // tile aggregate published
+constexpr uint32_t kFlagP = 2u << 30;                 // inclusive prefix published
+constexpr uint32_t kCountMask = (1u << 30) - 1u;
+constexpr uint32_t kSpinLimit = 1u << 22;
+
+struct SortScratch {
+  uint32_t* hist;     // [8][16] digit counts per pass
+  uint32_t* tiles;    // [8] tile counters
+  uint32_t* desc;     // [8][ntiles][16] look-back words
+  uint32_t* keys_tmp; // n
+  uint32_t* vals_tmp; // n
+};
+
+size_t sort_scratch_bytes(uint32_t n) {
+  size_t ntiles = ((size_t)n + kSortTile - 1) / kSortTile;
+  size_t small = (8 * 16 + 8 + 8 * ntiles * 16) * sizeof(uint32_t);
+  small = (small + 255) & ~(size_t)255;
+  return small + 2 * (((size_t)n * 4 + 255) & ~(size_t)255);
+}
+
+static SortScratch carve(void* base, uint32_t n) {
+  size_t ntiles = ((size_t)n + kSortTile - 1) / kSortTile;
+  uint32_t* p = reinterpret_cast<uint32_t*>(base);
+  SortScratch s;
+  s.hist = p;
+  s.tiles = p + 8 * 16;
+  s.desc = p + 8 * 16 + 8;
+  size_t small = (8 * 16 + 8 + 8 * ntiles * 16) * sizeof(uint32_t);
+  small = (small + 255) & ~(size_t)255;
+  uint8_t* b = reinterpret_cast<uint8_t*>(base) + small;
+  s.keys_tmp = reinterpret_cast<uint32_t*>(b);
+  s.vals_tmp = reinterpret_cast<uint32_t*>(b + (((size_t)n * 4 + 255) & ~(size_t)255));
+  return s;
+}
+
+size_t sort_scratch_header_bytes(uint32_t n) {
+  size_t ntiles = ((size_t)n + kSortTile - 1) / kSortTile;
+  return (8 * 16 + 8 + 8 * ntiles * 16) * sizeof(uint32_t);
+}
+
+// Digit counts of all passes in one read of the keys.
+__global__ void __launch_bounds__(256) sort_hist_kernel(const uint32_t* __restrict__ keys, uint32_t n,
+                                                        uint32_t begin_bit, uint32_t passes,
+                                                        uint32_t* __restrict__ hist) {
+  __shared__ uint32_t h[8][16];
+  for (int i = threadIdx.x; i < 8 * 16; i += blockDim.x) (&h[0][0])[i] = 0;
+  __syncthreads();
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    uint32_t k = keys[i];
+    for (uint32_t p = 0; p < passes; ++p) atomicAdd(&h[p][(k >> (begin_bit + 4 * p)) & 15u], 1u);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < (int)(passes * 16); i += blockDim.x) {
+    uint32_t v = (&h[0][0])[i];
+    if (v) atomicAdd(hist + i, v);
+  }
+}
+
+__global__ void __launch_bounds__(kSortThreads) sort_pass_kernel(const uint32_t* __restrict__ kin,
+                                                                 const uint32_t* __restrict__ vin,
+                                                                 uint32_t* __restrict__ kout,
+                                                                 uint32_t* __restrict__ vout, uint32_t n,
+                                                                 uint32_t shift, uint32_t pass,
+                                                                 SortScratch sc, int* __restrict__ err) {
+  __shared__ uint32_t s_tile;
+  __shared__ uint32_t s_cnt[kSortThreads / 32][16];
+  __shared__ uint32_t s_tile_start[16];  // digit start inside the tile
+  __shared__ uint32_t s_base[16];        // global output offset of the digit's run
+  __shared__ uint32_t s_keys[kSortTile];
+  __shared__ uint32_t s_vals[kSortTile];
+
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+  const uint32_t lt = (1u << lane) - 1u;
+  if (threadIdx.x == 0) s_tile = atomicAdd(sc.tiles + pass, 1u);
+  if (threadIdx.x < 16 * (kSortThreads / 32)) (&s_cnt[0][0])[threadIdx.x] = 0;
+  __syncthreads();
+  const uint32_t tile = s_tile;
+  const uint32_t tile0 = tile * kSortTile;
+  const uint32_t count = min((uint32_t)kSortTile, n - tile0);
+
+  uint32_t key[kSortItems], val[kSortItems], rank[kSortItems];
+#pragma unroll
+  for (int j = 0; j < kSortItems; ++j) {
+    uint32_t local = warp * (32 * kSortItems) + j * 32 + lane;
+    uint32_t idx = tile0 + local;
+    bool ok = local < count;
+    key[j] = ok ? kin[idx] : 0u;
+    val[j] = ok ? (vin ? vin[idx] : idx) : 0u;
+    uint32_t valid = __ballot_sync(0xffffffffu, ok);
+    uint32_t d = (key[j] >> shift) & 15u;
+    uint32_t peers = __match_any_sync(0xffffffffu, ok ? d : 16u) & valid;
+    uint32_t base = ok ? s_cnt[warp][d] : 0u;
+    __syncwarp();
+    if (ok && (peers & lt) == 0u) s_cnt[warp][d] = base + __popc(peers);
+    __syncwarp();
+    rank[j] = base + __popc(peers & lt);
+  }
+  __syncthreads();
+  if (threadIdx.x < 16) {
+    const uint32_t d = threadIdx.x;
+    uint32_t run = 0;
+    for (int w = 0; w < kSortThreads / 32; ++w) {
+      uint32_t c = s_cnt[w][d];
+      s_cnt[w][d] = run;  // exclusive prefix over warps
+      run += c;
+    }
+    // digit start inside the tile: exclusive scan over digits (16 lanes)
+    uint32_t incl = run;
+    for (int o = 1; o < 16; o <<= 1) {
+      uint32_t v = __shfl_up_sync(0x0000ffffu, incl, o, 16);
+      if (d >= (uint32_t)o) incl += v;
+    }
+    s_tile_start[d] = incl - run;
+    // exclusive global offset of digit d in this pass
+    uint32_t g = 0;
+    for (uint32_t e = 0; e < d; ++e) g += sc.hist[pass * 16 + e];
+    // decoupled look-back
+    volatile uint32_t* desc = sc.desc + (size_t)pass * ((size_t)gridDim.x * 16);
+    if (tile == 0) {
+      desc[d] = kFlagP | run;
+      s_base[d] = g;
+    } else {
+      desc[(size_t)tile * 16 + d] = kFlagA | run;
+      __threadfence();
+      uint32_t excl = 0;
+      int t = (int)tile - 1;
+      uint32_t spins = 0;
+      while (t >= 0) {
+        uint32_t w = desc[(size_t)t * 16 + d];
+        uint32_t flag = w & ~kCountMask;
+        if (flag == 0u) {
+          if (++spins > kSpinLimit) {
+            atomicExch(err, 2);  // look-back wait ran out
+            break;
+          }
+          continue;
+        }
+        excl += w & kCountMask;
+        if (flag == kFlagP) break;
+        --t;
+      }
+      desc[(size_t)tile * 16 + d] = kFlagP | (excl + run);
+      s_base[d] = g + excl;
+    }
+  }
+  __syncthreads();
+  // stage in tile order
+#pragma unroll
+  for (int j = 0; j < kSortItems; ++j) {
+    uint32_t local = warp * (32 * kSortItems) + j * 32 + lane;
+    if (local < count) {
+      uint32_t d = (key[j] >> shift) & 15u;
+      uint32_t pos = s_tile_start[d] + s_cnt[warp][d] + rank[j];
+      s_keys[pos] = key[j];
+      s_vals[pos] = val[j];
+    }
+  }
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < count; i += kSortThreads) {
+    uint32_t k = s_keys[i];
+    uint32_t d = (k >> shift) & 15u;
+    uint32_t o = s_base[d] + (i - s_tile_start[d]);
+    if (o < n) {  // always true unless a look-back wait ran out (error word set)
+      kout[o] = k;
+      vout[o] = s_vals[i];
+    }
+  }
+}
+
+// Runs the passes for bits [begin_bit, end_bit) in 4-bit digits.  The pass
+// chain ping-pongs between `out` and the scratch copy so the last pass
+// lands in `out`; in-place calls (in == out) with an odd pass count start
+// from a copy.
+vcr_status sort_pairs_run(vcr_ctx* ctx, int* d_err, void* scratch, const uint32_t* kin, const uint32_t* vin,
+                          uint32_t* kout, uint32_t* vout, uint32_t n, uint32_t begin_bit, uint32_t end_bit,
+                          cudaStream_t st) {
+  if (n == 0) return VCR_OK;
+  uint32_t passes = (end_bit - begin_bit + 3) / 4;
+  SortScratch sc = carve(scratch, n);
+  uint32_t ntiles = (n + kSortTile - 1) / kSortTile;
+  VCR_CUDA(ctx, cudaMemsetAsync(scratch, 0, sort_scratch_header_bytes(n), st));
+  int hb = (int)std::min<uint32_t>((n + 255) / 256, (uint32_t)ctx->sm_count * 4);
+  sort_hist_kernel<<<hb, 256, 0, st>>>(kin, n, begin_bit, passes, sc.hist);
+  VCR_CUDA(ctx, cudaGetLastError());
+  const uint32_t* ck = kin;
+  const uint32_t* cv = vin;
+  // Destinations alternate; the first one is `out` when that makes the last
+  // pass land in `out` (odd count) unless the input aliases `out`, in which
+  // case the chain starts in scratch and ends with one copy.
+  bool alias = (kin == kout) || (vin && vin == vout);
+  bool first_to_out = (passes % 2u == 1u) && !alias;
+  for (uint32_t p = 0; p < passes; ++p) {
+    bool to_out = ((p % 2u) == 0u) == first_to_out;
+    uint32_t* nk = to_out ? kout : sc.keys_tmp;
+    uint32_t* nv = to_out ? vout : sc.vals_tmp;
+    sort_pass_kernel<<<ntiles, kSortThreads, 0, st>>>(ck, cv, nk, nv, n, begin_bit + 4 * p, p, sc, d_err);
+    VCR_CUDA(ctx, cudaGetLastError());
+    ck = nk;
+    cv = nv;
+  }
+  if (ck != kout) {
+    VCR_CUDA(ctx, cudaMemcpyAsync(kout, ck, (size_t)n * 4, cudaMemcpyDeviceToDevice, st));
+    VCR_CUDA(ctx, cudaMemcpyAsync(vout, cv, (size_t)n * 4, cudaMemcpyDeviceToDevice, st));
+  }
+  return VCR_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Morton codes
+// ---------------------------------------------------------------------------
+// Spread the low 10 bits of v so two zeros separate each (Karras 2012; the
+// reference's 8-bit expandBits is PPB_PT.comp:319-325).
+__device__ __forceinline__ uint32_t expand10(uint32_t v) {
+  v = (v * 0x00010001u) & 0xFF0000FFu;
+  v = (v * 0x00000101u) & 0x0F00F00Fu;
+  v = (v * 0x00000011u) & 0xC30C30C3u;
+  v = (v * 0x00000005u) & 0x49249249u;
+  return v;
+}
+
+__device__ __forceinline__ uint32_t quant(float p, float b0, float ext, float cells) {
+  float q = ((p - b0) / ext) * cells;
+  q = fminf(fmaxf(q, 0.0f), cells - 1.0f);
+  return (uint32_t)q;
+}
+
+// bits == 30: 10 bits per axis over the box [b0, b1] (x << 2 | y << 1 | z);
+// bits == 24: the reference's getMortonCode (PPB_PT.comp:327-333), relative
+// position / 256 clamped to [0, 255] per axis.
+__global__ void morton_kernel(const float* __restrict__ pts, uint32_t n, f3 b0, f3 b1, int bits,
+                              uint32_t* __restrict__ codes) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  f3 p = mk(pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]);
+  if (bits == 24) {
+    f3 r = p - b0;
+    uint32_t x = (uint32_t)fminf(fmaxf(r.x / 256.0f, 0.0f), 255.0f);
+    uint32_t y = (uint32_t)fminf(fmaxf(r.y / 256.0f, 0.0f), 255.0f);
+    uint32_t z = (uint32_t)fminf(fmaxf(r.z / 256.0f, 0.0f), 255.0f);
+    codes[i] = (expand10(x) << 2) + (expand10(y) << 1) + expand10(z);
+    return;
+  }
+  f3 e = b1 - b0;
+  uint32_t x = quant(p.x, b0.x, e.x, 1024.0f), y = quant(p.y, b0.y, e.y, 1024.0f), z = quant(p.z, b0.z, e.z, 1024.0f);
+  codes[i] = (expand10(x) << 2) | (expand10(y) << 1) | expand10(z);
+}
+
+vcr_status morton_launch(vcr_ctx* ctx, const float* d_pts, uint32_t n, const float b0[3], const float b1[3],
+                         int bits, uint32_t* d_codes, cudaStream_t st) {
+  if (n == 0) return VCR_OK;
+  morton_kernel<<<(n + 255) / 256, 256, 0, st>>>(d_pts, n, mk(b0[0], b0[1], b0[2]), mk(b1[0], b1[1], b1[2]), bits,
+                                                 d_codes);
+  VCR_CUDA(ctx, cudaGetLastError());
+  return VCR_OK;
+}
+
+}  // namespace vcr
+
+using namespace vcr;
+
+extern "C" VCR_API vcr_status vcr_radix_sort_pairs(vcr_ctx* ctx, const uint32_t* d_keys_in, const uint32_t* d_vals_in,
+                                                   uint32_t* d_keys_out, uint32_t* d_vals_out, uint32_t n,
+                                                   uint32_t begin_bit, uint32_t end_bit, void* stream) {
+  if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  if (n && (!d_keys_in || !d_keys_out || !d_vals_out)) return fail(ctx, VCR_ERR_INVALID, "null sort buffer");
+  if (begin_bit >= end_bit || end_bit > 32) return fail(ctx, VCR_ERR_INVALID, "bit range [%u, %u)", begin_bit, end_bit);
+  if (n > (1u << 30) - 1u) return fail(ctx, VCR_ERR_UNSUPPORTED, "sort of %u keys (max 2^30 - 1)", n);
+  if (d_vals_in == d_vals_out && d_keys_in != d_keys_out)
+    return fail(ctx, VCR_ERR_INVALID, "values may alias only together with keys");
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
+  vcr_status st = ensure_scratch(ctx, sort_scratch_bytes(n));
+  if (st) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  st = sort_pairs_run(ctx, ctx->d_error, ctx->d_scratch, d_keys_in, d_vals_in, d_keys_out, d_vals_out, n, begin_bit,
+                      end_bit, s);
+  if (st) return st;
+  VCR_CUDA(ctx, cudaEventRecord(ctx->work_done, s));
+  return VCR_OK;
+}
+
+extern "C" VCR_API vcr_status vcr_morton_codes(vcr_ctx* ctx, const float* d_points, uint32_t n,
+                                               const float bounds_min[3], const float bounds_max[3],
+                                               uint32_t bits, uint32_t* d_codes, void* stream) {
+  if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  if (n && (!d_points || !d_codes || !bounds_min || !bounds_max)) return fail(ctx, VCR_ERR_INVALID, "null argument");
+  if (bits != 30 && bits != 24) return fail(ctx, VCR_ERR_INVALID, "Morton bits must be 30 or 24");
+  return morton_launch(ctx, d_points, n, bounds_min, bounds_max, (int)bits, d_codes, (cudaStream_t)stream);
+}

@@ -170,6 +170,16 @@ class Context:
     def synchronize(self):
         self._ck(lib().vcr_synchronize(self.h))
 
+    # beam ordering primitives (device pointers) -----------------------------
+    def radix_sort_pairs(self, d_kin, d_vin, d_kout, d_vout, n, begin_bit=0, end_bit=32, stream=0):
+        self._ck(lib().vcr_radix_sort_pairs(self.h, C.c_void_p(d_kin), C.c_void_p(d_vin or 0) if d_vin else None,
+                                            C.c_void_p(d_kout), C.c_void_p(d_vout), n, begin_bit, end_bit,
+                                            C.c_void_p(stream)))
+
+    def morton_codes(self, d_pts, n, bmin, bmax, bits, d_codes, stream=0):
+        self._ck(lib().vcr_morton_codes(self.h, C.c_void_p(d_pts), n, _abi.F3(*bmin), _abi.F3(*bmax), bits,
+                                        C.c_void_p(d_codes), C.c_void_p(stream)))
+
     # read back --------------------------------------------------------------
     def image_mean(self) -> np.ndarray:
         out = np.empty((self.height, self.width, 3), np.float32)

@@ -299,6 +299,27 @@ VCR_API vcr_status vcr_dda_trace(vcr_ctx* ctx, const float* d_origin, const floa
                                  float* d_out_t, uint32_t* d_out_count, void* stream);
 
 /* ------------------------------------------------------------------------ */
+/* Photon-beam ordering primitives                                          */
+/* ------------------------------------------------------------------------ */
+/* Stable LSD radix sort of (uint32 key, uint32 value) pairs over key bits
+ * [begin_bit, end_bit) in 4-bit digits; device pointers, n <= 2^30 - 1.
+ * d_vals_in == NULL sorts the indices 0..n-1 as values (a permutation).
+ * Keys (and values) may be sorted in place.  Scratch comes from the
+ * context (about 8 bytes per key).
+ * Replaces: PPB_RadixSort_LocalSort.comp (:154-252) + PPB_RadixSort_PrefixSum
+ * .comp (:28-37) + PPB_RadixSort_GlobalSort.comp (:54-106), dispatched by
+ * RenderTechniquePPB::RecordDrawCommands (RenderTechniquePPB.cpp:465-491). */
+VCR_API vcr_status vcr_radix_sort_pairs(vcr_ctx* ctx, const uint32_t* d_keys_in, const uint32_t* d_vals_in,
+                                        uint32_t* d_keys_out, uint32_t* d_vals_out, uint32_t n,
+                                        uint32_t begin_bit, uint32_t end_bit, void* stream);
+/* Morton codes of n points (device float3): bits == 30 quantises each axis
+ * to 1024 cells of [bounds_min, bounds_max] and interleaves x<<2|y<<1|z;
+ * bits == 24 is the reference's getMortonCode (PPB_PT.comp:317-333:
+ * (p - bounds_min)/256 clamped to [0,255] per axis). */
+VCR_API vcr_status vcr_morton_codes(vcr_ctx* ctx, const float* d_points, uint32_t n, const float bounds_min[3],
+                                    const float bounds_max[3], uint32_t bits, uint32_t* d_codes, void* stream);
+
+/* ------------------------------------------------------------------------ */
 /* Read back                                                                */
 /* ------------------------------------------------------------------------ */
 /* Synchronous copy of a context buffer to host memory (bytes must match). */

@@ -46,6 +46,10 @@ def lib():
             "oracle_pcg_hash": (u32, [u32]),
             "oracle_f32_to_f16": (C.c_uint16, [f]),
             "oracle_f32_to_bf16": (C.c_uint16, [f]),
+            "oracle_sort_fixture_keys": (None, [P]),
+            "oracle_split_sort": (None, [P, u32, u32, u32]),
+            "oracle_lsd_sort_pairs": (None, [P, P, u32, u32, u32, P, P]),
+            "oracle_morton": (None, [P, u32, P, P, u32, P]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -148,3 +152,33 @@ def sincos2pi(u: float):
     s, c = C.c_float(), C.c_float()
     lib().oracle_sincos2pi(u, C.byref(s), C.byref(c))
     return s.value, c.value
+
+
+def sort_fixture_keys() -> np.ndarray:
+    out = np.empty(176, np.uint32)
+    lib().oracle_sort_fixture_keys(_p(out))
+    return out
+
+
+def split_sort(keys: np.ndarray, first_bit: int, nbits: int) -> np.ndarray:
+    k = np.ascontiguousarray(keys, np.uint32).copy()
+    lib().oracle_split_sort(_p(k), len(k), first_bit, nbits)
+    return k
+
+
+def lsd_sort_pairs(keys: np.ndarray, vals=None, begin=0, end=32):
+    keys = np.ascontiguousarray(keys, np.uint32)
+    n = len(keys)
+    ko, vo = np.empty(n, np.uint32), np.empty(n, np.uint32)
+    vp = _p(np.ascontiguousarray(vals, np.uint32)) if vals is not None else None
+    lib().oracle_lsd_sort_pairs(_p(keys), vp, n, begin, end, _p(ko), _p(vo))
+    return ko, vo
+
+
+def morton(points: np.ndarray, bmin, bmax, bits: int) -> np.ndarray:
+    pts = np.ascontiguousarray(points, np.float32)
+    out = np.empty(len(pts), np.uint32)
+    b0 = np.ascontiguousarray(bmin, np.float32)
+    b1 = np.ascontiguousarray(bmax, np.float32)
+    lib().oracle_morton(_p(pts), len(pts), _p(b0), _p(b1), bits, _p(out))
+    return out
