@@ -16,6 +16,7 @@
 // per pass).  Spins are bounded: a wait that runs out sets the context's
 // error word instead of hanging.
 #include "vcr_internal.h"
+#include "sort.cuh"
 
 namespace vcr {
 
@@ -35,31 +36,18 @@ struct SortScratch {
   uint32_t* vals_tmp; // n
 };
 
-size_t sort_scratch_bytes(uint32_t n) {
-  size_t ntiles = ((size_t)n + kSortTile - 1) / kSortTile;
-  size_t small = (8 * 16 + 8 + 8 * ntiles * 16) * sizeof(uint32_t);
-  small = (small + 255) & ~(size_t)255;
-  return small + 2 * (((size_t)n * 4 + 255) & ~(size_t)255);
-}
+static_assert(kSortTile == (int)kSortTileKeys, "tile size");
 
 static SortScratch carve(void* base, uint32_t n) {
-  size_t ntiles = ((size_t)n + kSortTile - 1) / kSortTile;
   uint32_t* p = reinterpret_cast<uint32_t*>(base);
   SortScratch s;
   s.hist = p;
   s.tiles = p + 8 * 16;
   s.desc = p + 8 * 16 + 8;
-  size_t small = (8 * 16 + 8 + 8 * ntiles * 16) * sizeof(uint32_t);
-  small = (small + 255) & ~(size_t)255;
-  uint8_t* b = reinterpret_cast<uint8_t*>(base) + small;
+  uint8_t* b = reinterpret_cast<uint8_t*>(base) + sort_round256(sort_scratch_header_bytes(n));
   s.keys_tmp = reinterpret_cast<uint32_t*>(b);
-  s.vals_tmp = reinterpret_cast<uint32_t*>(b + (((size_t)n * 4 + 255) & ~(size_t)255));
+  s.vals_tmp = reinterpret_cast<uint32_t*>(b + sort_round256((size_t)n * 4));
   return s;
-}
-
-size_t sort_scratch_header_bytes(uint32_t n) {
-  size_t ntiles = ((size_t)n + kSortTile - 1) / kSortTile;
-  return (8 * 16 + 8 + 8 * ntiles * 16) * sizeof(uint32_t);
 }
 
 // Digit counts of all passes in one read of the keys.
@@ -195,17 +183,18 @@ __global__ void __launch_bounds__(kSortThreads) sort_pass_kernel(const uint32_t*
 // chain ping-pongs between `out` and the scratch copy so the last pass
 // lands in `out`; in-place calls (in == out) with an odd pass count start
 // from a copy.
-vcr_status sort_pairs_run(vcr_ctx* ctx, int* d_err, void* scratch, const uint32_t* kin, const uint32_t* vin,
-                          uint32_t* kout, uint32_t* vout, uint32_t n, uint32_t begin_bit, uint32_t end_bit,
-                          cudaStream_t st) {
-  if (n == 0) return VCR_OK;
+cudaError_t sort_pairs_enqueue(int sm_count, int* d_err, void* scratch, const uint32_t* kin, const uint32_t* vin,
+                               uint32_t* kout, uint32_t* vout, uint32_t n, uint32_t begin_bit, uint32_t end_bit,
+                               cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
   uint32_t passes = (end_bit - begin_bit + 3) / 4;
   SortScratch sc = carve(scratch, n);
   uint32_t ntiles = (n + kSortTile - 1) / kSortTile;
-  VCR_CUDA(ctx, cudaMemsetAsync(scratch, 0, sort_scratch_header_bytes(n), st));
-  int hb = (int)std::min<uint32_t>((n + 255) / 256, (uint32_t)ctx->sm_count * 4);
+  cudaError_t e = cudaMemsetAsync(scratch, 0, sort_scratch_header_bytes(n), st);
+  if (e != cudaSuccess) return e;
+  int hb = (int)std::min<uint32_t>((n + 255) / 256, (uint32_t)std::max(sm_count, 1) * 4);
   sort_hist_kernel<<<hb, 256, 0, st>>>(kin, n, begin_bit, passes, sc.hist);
-  VCR_CUDA(ctx, cudaGetLastError());
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
   const uint32_t* ck = kin;
   const uint32_t* cv = vin;
   // Destinations alternate; the first one is `out` when that makes the last
@@ -218,15 +207,15 @@ vcr_status sort_pairs_run(vcr_ctx* ctx, int* d_err, void* scratch, const uint32_
     uint32_t* nk = to_out ? kout : sc.keys_tmp;
     uint32_t* nv = to_out ? vout : sc.vals_tmp;
     sort_pass_kernel<<<ntiles, kSortThreads, 0, st>>>(ck, cv, nk, nv, n, begin_bit + 4 * p, p, sc, d_err);
-    VCR_CUDA(ctx, cudaGetLastError());
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
     ck = nk;
     cv = nv;
   }
   if (ck != kout) {
-    VCR_CUDA(ctx, cudaMemcpyAsync(kout, ck, (size_t)n * 4, cudaMemcpyDeviceToDevice, st));
-    VCR_CUDA(ctx, cudaMemcpyAsync(vout, cv, (size_t)n * 4, cudaMemcpyDeviceToDevice, st));
+    if ((e = cudaMemcpyAsync(kout, ck, (size_t)n * 4, cudaMemcpyDeviceToDevice, st)) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(vout, cv, (size_t)n * 4, cudaMemcpyDeviceToDevice, st)) != cudaSuccess) return e;
   }
-  return VCR_OK;
+  return cudaSuccess;
 }
 
 // ---------------------------------------------------------------------------
@@ -295,9 +284,8 @@ extern "C" VCR_API vcr_status vcr_radix_sort_pairs(vcr_ctx* ctx, const uint32_t*
   vcr_status st = ensure_scratch(ctx, sort_scratch_bytes(n));
   if (st) return st;
   cudaStream_t s = (cudaStream_t)stream;
-  st = sort_pairs_run(ctx, ctx->d_error, ctx->d_scratch, d_keys_in, d_vals_in, d_keys_out, d_vals_out, n, begin_bit,
-                      end_bit, s);
-  if (st) return st;
+  VCR_CUDA(ctx, sort_pairs_enqueue(ctx->sm_count, ctx->d_error, ctx->d_scratch, d_keys_in, d_vals_in, d_keys_out,
+                                   d_vals_out, n, begin_bit, end_bit, s));
   VCR_CUDA(ctx, cudaEventRecord(ctx->work_done, s));
   return VCR_OK;
 }

@@ -102,6 +102,7 @@ SIGNATURES = {
     "vcr_pt_counters": (_S, [_P, C.POINTER(_u64)]),
     "vcr_dda_trace": (_S, [_P, _P, _P, _u32, _u32, _P, _P, _P, _P]),
     "vcr_radix_sort_pairs": (_S, [_P, _P, _P, _P, _P, _u32, _u32, _u32, _P]),
+    "vcr_radix_sort_pairs_noalloc": (_S, [_P, _P, _P, _P, _u32, _u32, _u32, _P]),
     "vcr_morton_codes": (_S, [_P, _P, _u32, F3, F3, _u32, _P, _P]),
     "vcr_readback": (_S, [_P, C.c_int, _P, _sz]),
     "vcr_pass_count": (_S, [_P, C.POINTER(_u32)]),

@@ -312,6 +312,21 @@ VCR_API vcr_status vcr_dda_trace(vcr_ctx* ctx, const float* d_origin, const floa
 VCR_API vcr_status vcr_radix_sort_pairs(vcr_ctx* ctx, const uint32_t* d_keys_in, const uint32_t* d_vals_in,
                                         uint32_t* d_keys_out, uint32_t* d_vals_out, uint32_t n,
                                         uint32_t begin_bit, uint32_t end_bit, void* stream);
+/* The same sort for callers that cannot allocate device memory (a host
+ * application that owns all device memory through its own pool, a render
+ * loop that must not allocate after start-up, a plug-in handed buffers but
+ * no allocator).  No counterpart in the reference.  It takes no context and
+ * allocates nothing: its working memory is one fixed device array (about
+ * 8.3 MB) inside this library, held by every GPU that loads it until the
+ * process exits.  At most VCR_SORT_NOALLOC_MAX_KEYS pairs per call (larger
+ * n returns VCR_ERR_CAPACITY).  Calls share that array: calls that overlap
+ * on the GPU race, so serialise them.  The first call on each device looks
+ * up the array's address with that device current; make it before any
+ * stream capture.  Errors are reported through vcr_last_error(NULL). */
+#define VCR_SORT_NOALLOC_MAX_KEYS (1u << 20)
+VCR_API vcr_status vcr_radix_sort_pairs_noalloc(const uint32_t* d_keys_in, const uint32_t* d_vals_in,
+                                                uint32_t* d_keys_out, uint32_t* d_vals_out, uint32_t n,
+                                                uint32_t begin_bit, uint32_t end_bit, void* stream);
 /* Morton codes of n points (device float3): bits == 30 quantises each axis
  * to 1024 cells of [bounds_min, bounds_max] and interleaves x<<2|y<<1|z;
  * bits == 24 is the reference's getMortonCode (PPB_PT.comp:317-333:
