@@ -135,6 +135,7 @@ def run_vcr(args):
     with vcr.Context(local) as ctx:
         configs.setup_context(ctx, sc, tracker=vcr.TRACKER_DDA)
         ctx.synchronize()
+        tuning = ctx.autotune(seed=999, stream=sh)  # picks majorant level / DDA steps / CTA size
         seed = 1000 + rank
         for k in range(args.warmup):
             ctx.pt_pass(seed=seed, pass_index=k, stream=sh)
@@ -189,6 +190,7 @@ def run_vcr(args):
         "data": "synthetic: seeded 8-octave Perlin fBm cloud generated on the device",
         "config": {"workload": sc.name, "grid": list(sc.size), "precision": "fp16-bricks", "sigma_t_scale": 32,
                    "image": [W, H], "spp_per_step": 1, "max_events": sc.max_events, "tracker": "dda-wavefront",
+                   "tuning": tuning,
                    "l2": "inputs larger than L2 (1 GiB FP16 grid), no flush",
                    "parallelism": f"replicas{ws}"},
         "gpu_launches": args.steps,

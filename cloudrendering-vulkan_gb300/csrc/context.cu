@@ -44,10 +44,13 @@ GridView grid_view(const vcr_ctx* ctx) {
   GridView g;
   g.bricks = ctx->d_bricks;
   g.scales = ctx->d_scales;
-  g.majorants = ctx->d_majorants;
+  int lv = (int)ctx->tuning.majorant_level;
+  g.majorants = ctx->d_majorants ? ctx->d_majorants + ctx->moff[lv] : nullptr;
+  g.level = lv;
   for (int a = 0; a < 3; ++a) {
     g.n[a] = (int)ctx->gdesc.size[a];
     g.nb[a] = ctx->nb[a];
+    g.mnb[a] = ctx->mnb[lv][a];
   }
   g.precision = ctx->precision;
   return g;
@@ -63,9 +66,10 @@ SceneView scene_view(const vcr_ctx* ctx) {
   s.bs = c.base_scaling;
   s.k_sigma = c.density_scaling / c.base_scaling;
   f3 ext = s.b1 - s.b0;
-  s.cell.x = (ext.x / (float)ctx->gdesc.size[0]) * (float)kBrick;
-  s.cell.y = (ext.y / (float)ctx->gdesc.size[1]) * (float)kBrick;
-  s.cell.z = (ext.z / (float)ctx->gdesc.size[2]) * (float)kBrick;
+  const float cv = (float)(kBrick << ctx->tuning.majorant_level);  // voxels per majorant cell
+  s.cell.x = (ext.x / (float)ctx->gdesc.size[0]) * cv;
+  s.cell.y = (ext.y / (float)ctx->gdesc.size[1]) * cv;
+  s.cell.z = (ext.z / (float)ctx->gdesc.size[2]) * cv;
   const vcr_params& p = ctx->params;
   s.ph.g = p.phase_g;
   s.ph.opg2 = p.phase_one_plus_g2;
@@ -328,12 +332,29 @@ extern "C" VCR_API vcr_status vcr_grid_info(vcr_ctx* ctx, float* out_max, uint32
   return VCR_OK;
 }
 
-extern "C" VCR_API vcr_status vcr_grid_read_majorants(vcr_ctx* ctx, float* host, size_t count) {
+extern "C" VCR_API vcr_status vcr_grid_read_majorants(vcr_ctx* ctx, uint32_t level, float* host, size_t count) {
   if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
   if (!ctx->has_grid) return fail(ctx, VCR_ERR_STATE, "no grid");
-  size_t nb = (size_t)ctx->nb[0] * ctx->nb[1] * ctx->nb[2];
+  if (level > 3) return fail(ctx, VCR_ERR_INVALID, "majorant level %u (0..3)", level);
+  const int* m = ctx->mnb[level];
+  size_t nb = (size_t)m[0] * m[1] * m[2];
   if (!host || count != nb) return fail(ctx, VCR_ERR_INVALID, "majorant count %zu != %zu", count, nb);
-  VCR_CUDA(ctx, cudaMemcpy(host, ctx->d_majorants, nb * sizeof(float), cudaMemcpyDeviceToHost));
+  VCR_CUDA(ctx, cudaMemcpy(host, ctx->d_majorants + ctx->moff[level], nb * sizeof(float), cudaMemcpyDeviceToHost));
+  return VCR_OK;
+}
+
+extern "C" VCR_API vcr_status vcr_set_tuning(vcr_ctx* ctx, const vcr_tuning* t) {
+  if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  if (!t || t->majorant_level > 3 || t->dda_steps == 0 || t->dda_steps > 4096 ||
+      (t->block_threads != 128 && t->block_threads != 256))
+    return fail(ctx, VCR_ERR_INVALID, "tuning: level 0..3, dda_steps 1..4096, block_threads 128 or 256");
+  ctx->tuning = *t;
+  return VCR_OK;
+}
+
+extern "C" VCR_API vcr_status vcr_get_tuning(vcr_ctx* ctx, vcr_tuning* out) {
+  if (!ctx || !out) return fail(ctx, VCR_ERR_INVALID, "null argument");
+  *out = ctx->tuning;
   return VCR_OK;
 }
 

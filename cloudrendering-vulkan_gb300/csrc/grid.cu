@@ -86,6 +86,23 @@ __global__ void __launch_bounds__(256) majorant_kernel(GridView g, float* __rest
   }
 }
 
+// Level l+1 of the majorant pyramid: max over the (up to) 2x2x2 cells of
+// level l it covers.
+__global__ void majorant_reduce_kernel(const float* __restrict__ src, int sx, int sy, int sz,
+                                       float* __restrict__ dst, int dx, int dy, int dz) {
+  uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= (uint32_t)(dx * dy * dz)) return;
+  int i = (int)(c % (uint32_t)dx), j = (int)((c / (uint32_t)dx) % (uint32_t)dy), k = (int)(c / ((uint32_t)dx * dy));
+  float m = 0.0f;
+  for (int dk = 0; dk < 2; ++dk)
+    for (int dj = 0; dj < 2; ++dj)
+      for (int di = 0; di < 2; ++di) {
+        int a = 2 * i + di, b = 2 * j + dj, e = 2 * k + dk;
+        if (a < sx && b < sy && e < sz) m = fmaxf(m, src[(size_t)a + (size_t)sx * ((size_t)b + (size_t)sy * e)]);
+      }
+  dst[c] = m;
+}
+
 __global__ void sample_kernel(GridView g, SceneView s, const float* __restrict__ pos, float* __restrict__ out,
                               uint32_t n) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -167,7 +184,17 @@ vcr_status grid_build(vcr_ctx* ctx, const float* d_dense, const vcr_grid_desc* d
   ctx->has_grid = false;
   VCR_CUDA(ctx, cudaMalloc(&ctx->d_bricks, nbricks * kBrickVoxels * esz));
   VCR_CUDA(ctx, cudaMalloc(&ctx->d_scales, nbricks * sizeof(float)));
-  VCR_CUDA(ctx, cudaMalloc(&ctx->d_majorants, nbricks * sizeof(float)));
+  // majorant pyramid: level l has ceil(nb / 2^l) cells per axis; each level
+  // starts on a 16-byte boundary (bulk copies into shared memory need it)
+  size_t mtotal = 0;
+  for (int l = 0; l < 4; ++l) {
+    for (int a = 0; a < 3; ++a) ctx->mnb[l][a] = l == 0 ? nb[a] : (ctx->mnb[l - 1][a] + 1) / 2;
+    ctx->moff[l] = mtotal;
+    size_t cnt = (size_t)ctx->mnb[l][0] * ctx->mnb[l][1] * ctx->mnb[l][2];
+    mtotal += (cnt + 3) & ~(size_t)3;
+  }
+  VCR_CUDA(ctx, cudaMalloc(&ctx->d_majorants, mtotal * sizeof(float)));
+  VCR_CUDA(ctx, cudaMemsetAsync(ctx->d_majorants, 0, mtotal * sizeof(float), s));
   VCR_CUDA(ctx, cudaMemsetAsync(ctx->d_scales, 0, nbricks * sizeof(float), s));
   if (precision == 0)
     brick_kernel<0><<<(unsigned)nbricks, 512, 0, s>>>(d_dense, ctx->d_bricks, ctx->d_scales, n[0], n[1], n[2], nb[0], nb[1]);
@@ -184,6 +211,15 @@ vcr_status grid_build(vcr_ctx* ctx, const float* d_dense, const vcr_grid_desc* d
   GridView g = grid_view(ctx);
   majorant_kernel<<<(unsigned)nbricks, 256, 0, s>>>(g, ctx->d_majorants, d_gmax);
   VCR_CUDA(ctx, cudaGetLastError());
+  for (int l = 1; l < 4; ++l) {
+    const int* sdim = ctx->mnb[l - 1];
+    const int* ddim = ctx->mnb[l];
+    uint32_t cnt = (uint32_t)(ddim[0] * ddim[1] * ddim[2]);
+    majorant_reduce_kernel<<<(cnt + 255) / 256, 256, 0, s>>>(ctx->d_majorants + ctx->moff[l - 1], sdim[0], sdim[1],
+                                                              sdim[2], ctx->d_majorants + ctx->moff[l], ddim[0],
+                                                              ddim[1], ddim[2]);
+    VCR_CUDA(ctx, cudaGetLastError());
+  }
   unsigned int gm = 0;
   VCR_CUDA(ctx, cudaMemcpyAsync(&gm, d_gmax, sizeof(gm), cudaMemcpyDeviceToHost, s));
   VCR_CUDA(ctx, cudaStreamSynchronize(s));
@@ -205,8 +241,9 @@ vcr_status grid_sample_launch(vcr_ctx* ctx, const float* d_pos, float* d_out, ui
 vcr_status dda_trace_launch(vcr_ctx* ctx, const float* d_o, const float* d_d, uint32_t n, uint32_t max_cells,
                             uint32_t* d_cells, float* d_t, uint32_t* d_count, cudaStream_t s) {
   if (n == 0) return VCR_OK;
-  dda_trace_kernel<<<(n + 127) / 128, 128, 0, s>>>(scene_view(ctx), ctx->nb[0], ctx->nb[1], ctx->nb[2], d_o, d_d, n,
-                                                   max_cells, d_cells, d_t, d_count);
+  const int* m = ctx->mnb[ctx->tuning.majorant_level];
+  dda_trace_kernel<<<(n + 127) / 128, 128, 0, s>>>(scene_view(ctx), m[0], m[1], m[2], d_o, d_d, n, max_cells, d_cells,
+                                                   d_t, d_count);
   VCR_CUDA(ctx, cudaGetLastError());
   return VCR_OK;
 }

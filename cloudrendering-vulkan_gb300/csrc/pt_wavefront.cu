@@ -1,0 +1,363 @@
+// Persistent DDA wavefront path tracer.
+//
+// Same light transport as the per-pixel tracker (PathTracer.comp:366-425)
+// with two changes of method the target asks for: free flights walk a
+// pyramid level of per-cell majorants with a 3D DDA (instead of one global
+// majorant, PathTracer.comp:338), and sun NEE is unbiased ratio tracking
+// (instead of the shadow-volume lookup, PathTracer.comp:406-411).
+//
+// Schedule: persistent CTAs; every lane owns one path at a time and refills
+// itself from a global cursor with one atomic per warp (ballot + popc), so
+// lanes never idle while paths remain.  A wavefront step is one bounded DDA
+// walk (at most `dda_steps` majorant cells, resumable: the optical depth
+// left over is kept) followed by at most one density lookup, so a lane
+// crossing many empty cells cannot hold its warp for a whole flight.  When
+// the selected majorant level fits, one thread stages it into shared memory
+// with a TMA bulk copy (cp.async.bulk + mbarrier) at CTA start and every
+// DDA cell visit reads shared memory.  The arithmetic per path is identical
+// to the oracle's sequential loop, so results are bit-exact with it.
+#include "pt_common.cuh"
+
+namespace vcr {
+
+constexpr uint32_t kMbarSpin = 1u << 24;  // bounded mbarrier wait
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t phase) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(phase)
+      : "memory");
+  return ok != 0u;
+}
+
+// Copy `bytes` (multiple of 16, 16-byte aligned both sides) from global to
+// this CTA's shared memory with one bulk copy; every thread waits (bounded).
+// Returns false (error word set) if the copy did not complete in time.
+__device__ bool stage_to_smem(void* dst, const void* src, uint32_t bytes, uint64_t* bar, int* err) {
+  const uint32_t b = smem_u32(bar);
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(bytes) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(b)
+                 : "memory");
+  }
+  bool ok = false;
+  for (uint32_t i = 0; i < kMbarSpin; ++i) {
+    if (mbar_try_wait(b, 0u)) {
+      ok = true;
+      break;
+    }
+  }
+  if (!ok) {
+    atomicExch(err, 3);  // staging wait ran out; wait (bounded) once more for the copy in flight
+    for (uint32_t i = 0; i < kMbarSpin; ++i)
+      if (mbar_try_wait(b, 0u)) break;
+  }
+  return __syncthreads_and(ok ? 1 : 0) != 0;
+}
+
+struct Track {
+  Dda dda;
+  float t, t_end, m;
+};
+
+__device__ __forceinline__ void track_init(Track& tr, const GridView& g, const SceneView& s, const float* maj, f3 o,
+                                           f3 d, uint32_t& cells) {
+  float tmin, tmax;
+  if (!slab(o, d, s.b0, s.b1, tmin, tmax) || !finite_pos(tmax)) tmax = 0.0f;
+  tr.t = 0.0f;
+  tr.t_end = tmax;
+  dda_init(tr.dda, o, d, s.b0, s.cell, g.mnb);
+  tr.m = maj[dda_linear(tr.dda, g.mnb)];
+  ++cells;
+}
+
+enum : int { kPending = 0, kCandidate = 1, kExit = 2 };
+
+// Up to `steps` cells of one free flight: consume the optical depth `tau`
+// cell by cell (dtau = (m k)(min(exit, t_end) - t)); a tentative collision
+// lands at t + tau/(m k) inside the cell where tau runs out.
+__device__ __forceinline__ int track_walk(Track& tr, const GridView& g, const float* maj, float k, float& tau,
+                                          uint32_t& cells, uint32_t steps) {
+  for (uint32_t i = 0; i < steps; ++i) {
+    float e = dda_cell_exit(tr.dda);
+    float se = fminf(e, tr.t_end);
+    float sig = tr.m * k;
+    float dtau = sig * (se - tr.t);
+    if (dtau > tau) {
+      tr.t = tr.t + tau / sig;
+      return kCandidate;
+    }
+    tau = tau - dtau;
+    tr.t = se;
+    if (e >= tr.t_end) return kExit;
+    if (!dda_advance(tr.dda, g.mnb)) return kExit;
+    tr.m = maj[dda_linear(tr.dda, g.mnb)];
+    ++cells;
+  }
+  return kPending;
+}
+
+enum : uint32_t { kIdle = 0, kScatter = 1, kNee = 2 };
+
+// Rarely-taken bodies live out of line: the persistent loop then stays small
+// enough for the instruction cache (a fully inlined loop stalled on
+// instruction fetch more than on memory).
+__device__ __noinline__ f3 sample_direction(const Phase& ph, f3 dir, Rng& rng) { return hg_sample(ph, dir, rng, true); }
+
+__device__ __noinline__ f3 escape_radiance(const SceneView& s, f3 dir) { return sky(s, dir); }
+
+// Camera ray of a path; returns false (L = sky) if it misses the cloud.
+__device__ __noinline__ bool start_path(const CamView& cam, const SceneView& s, int x, int y, f3& pos, f3& dir,
+                                        f3& L) {
+  camera_ray(cam, x, y, pos, dir);
+  float tmin, tmax;
+  if (!slab(pos, dir, s.b0, s.b1, tmin, tmax) || tmax < 0.0f || !(s.ds > 0.0f)) {
+    L = sky(s, dir);
+    return false;
+  }
+  pos = along(pos, dir, tmax < tmin ? tmax : tmin);
+  return true;
+}
+
+// 4 x 256 threads per SM: 64 registers a thread (a few spill to L1), which
+// measured ~7% faster than 3 CTAs at 77 registers on the 1024x512x1024 scene.
+template <int kThreads, bool kStage>
+__global__ void __launch_bounds__(kThreads, 1024 / kThreads)
+    pt_wavefront_kernel(GridView g, SceneView s, CamView cam, PassView pv, double* __restrict__ sum,
+                        uint32_t* __restrict__ stats, Counters cnt, uint32_t total, uint32_t dda_steps,
+                        uint32_t maj_bytes, int* __restrict__ err) {
+  extern __shared__ __align__(16) float s_maj[];
+  __shared__ __align__(8) uint64_t s_bar;
+  const float* maj = g.majorants;
+  if (kStage) {
+    if (stage_to_smem(s_maj, g.majorants, maj_bytes, &s_bar, err)) maj = s_maj;
+  }
+  const uint32_t lane = threadIdx.x & 31u;
+  const float k = s.k_sigma;
+  const f3 lsun = -s.sun;
+  uint32_t mode = kIdle;
+  bool exhausted = false, flying = false, need_init = false;
+  float tau = 0.0f;
+  uint32_t pid = 0, pix = 0, events = 0, lookups = 0, cells = 0;
+  unsigned long long n_paths = 0, n_look = 0, n_ev = 0, n_cells = 0;
+  Rng rng{0u, 0u};
+  f3 pos = mk(0.f, 0.f, 0.f), dir = pos, L = pos, idir = pos;
+  float beta = 1.0f, T = 1.0f, phase = 0.0f;
+  Track tr;
+  const bool atomic = pv.spp > 1;
+
+  while (true) {
+    // ---- warp-aggregated refill of idle lanes ---------------------------
+    bool need = (mode == kIdle) && !exhausted;
+    uint32_t mask = __ballot_sync(0xffffffffu, need);
+    if (mask) {
+      uint32_t leader = __ffs(mask) - 1;
+      uint32_t base = 0;
+      if (lane == leader) base = (uint32_t)atomicAdd(cnt.c + 4, (unsigned long long)__popc(mask));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (need) {
+        uint32_t id = base + __popc(mask & ((1u << lane) - 1u));
+        if (id >= total) {
+          exhausted = true;
+        } else {
+          pid = id;
+          uint32_t per_row = pv.cw * pv.spp;
+          uint32_t cy = id / per_row, rem = id - cy * per_row;
+          uint32_t cx = rem / pv.spp, sp = rem - cx * pv.spp;
+          int x = (int)(pv.x0 + cx), y = (int)(pv.y0 + cy);
+          pix = (uint32_t)y * pv.width + (uint32_t)x;
+          rng = rng_pcg(pv.seed, pix * pv.spp + sp, pv.pass);
+          L = mk(0.f, 0.f, 0.f);
+          beta = 1.0f;
+          events = lookups = cells = 0;
+          ++n_paths;
+          if (start_path(cam, s, x, y, pos, dir, L)) {
+            mode = kScatter;
+            idir = dir;
+            need_init = true;
+          } else {
+            write_result(pv, sum, pix, L, atomic);
+            if (stats && sp == 0) {
+              uint32_t* st = stats + 4 * (size_t)pix;
+              st[0] = 0; st[1] = 0; st[2] = pv.pass; st[3] = 0;
+            }
+          }
+        }
+      }
+    }
+    if (__all_sync(0xffffffffu, exhausted && mode == kIdle)) break;
+
+    // ---- one bounded walk + at most one lookup ----------------------------
+    if (mode != kIdle && !need_init) {
+      if (!flying) {
+        tau = -vlog(rng_next(rng));
+        flying = true;
+      }
+      int r = track_walk(tr, g, maj, k, tau, cells, dda_steps);
+      if (r != kPending) {
+        flying = false;
+        bool nee_done = false, finish = false;
+        if (r == kCandidate) {
+          f3 rd = mode == kScatter ? dir : lsun;
+          f3 p = along(pos, rd, tr.t);
+          float rho = density_at(g, s, p);
+          ++lookups;
+          if (mode == kScatter) {
+            float xi = rng_next(rng);
+            if (xi < rho / tr.m) {  // real collision: start the NEE ray
+              pos = p;
+              ++events;
+              beta = beta * s.albedo;
+              phase = hg_pdf(s.ph, dot(-dir, s.sun));
+              T = 1.0f;
+              mode = kNee;
+              idir = lsun;
+              need_init = true;
+            }
+          } else {
+            T = T * (1.0f - rho / tr.m);
+            if (T < 0.05f) {
+              if (rng_next(rng) >= 0.5f) {
+                T = 0.0f;
+                nee_done = true;
+              } else {
+                T = T * 2.0f;
+              }
+            }
+          }
+        } else if (mode == kScatter) {
+          L = L + escape_radiance(s, dir) * beta;
+          finish = true;
+        } else {
+          nee_done = true;
+        }
+        if (nee_done) {
+          float c = ((s.light * phase) * T) * beta;
+          L = L + mk(c, c, c);
+          if (s.max_events && events >= s.max_events) {
+            finish = true;
+          } else {
+            dir = sample_direction(s.ph, dir, rng);
+            mode = kScatter;
+            idir = dir;
+            need_init = true;
+          }
+        }
+        if (lookups + cells > kPathWorkCap) finish = true;  // runaway guard (non-finite input)
+        if (finish) {
+          write_result(pv, sum, pix, L, atomic);
+          if (stats && (pid % pv.spp) == 0) {
+            uint32_t* st = stats + 4 * (size_t)pix;
+            st[0] = events; st[1] = lookups; st[2] = pv.pass; st[3] = cells;
+          }
+          n_look += lookups;
+          n_ev += events;
+          n_cells += cells;
+          mode = kIdle;
+          need_init = false;
+        }
+      }
+    }
+    // ---- the one DDA set-up site (camera ray, NEE ray, scattered ray) ------
+    if (need_init) {
+      track_init(tr, g, s, maj, pos, idir, cells);
+      need_init = false;
+    }
+  }
+  flush_counters(cnt, n_paths, n_look, n_ev, n_cells);
+}
+
+constexpr uint32_t kMaxStagedBytes = 96u * 1024u;
+
+template <int kThreads, bool kStage>
+static vcr_status launch_t(vcr_ctx* ctx, const GridView& g, const SceneView& s, const CamView& cam,
+                           const PassView& pv, uint32_t* stats, Counters cnt, uint32_t total, uint32_t maj_bytes,
+                           cudaStream_t st) {
+  auto kern = pt_wavefront_kernel<kThreads, kStage>;
+  size_t smem = kStage ? maj_bytes : 0;
+  if (kStage)  // the attribute is per device, so it is set on every launch (a host-side call)
+    VCR_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxStagedBytes));
+  int per_sm = 0;
+  VCR_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem));
+  if (per_sm < 1) per_sm = 1;
+  uint32_t blocks = (uint32_t)(ctx->sm_count * per_sm);
+  uint32_t need = (total + kThreads - 1) / kThreads;
+  if (blocks > need) blocks = need;
+  kern<<<blocks, kThreads, smem, st>>>(g, s, cam, pv, ctx->d_sum, stats, cnt, total, ctx->tuning.dda_steps,
+                                       maj_bytes, ctx->d_error);
+  VCR_CUDA(ctx, cudaGetLastError());
+  return VCR_OK;
+}
+
+vcr_status wavefront_launch(vcr_ctx* ctx, const GridView& g, const SceneView& s, const CamView& cam,
+                            const PassView& pv, uint32_t* stats, Counters cnt, uint32_t total, cudaStream_t st) {
+  const vcr_tuning& t = ctx->tuning;
+  size_t cells = (size_t)g.mnb[0] * g.mnb[1] * g.mnb[2];
+  uint32_t bytes = (uint32_t)(((cells + 3) & ~(size_t)3) * sizeof(float));  // padded level: 16-byte multiple
+  bool stage = t.stage_majorants && bytes <= kMaxStagedBytes;
+  if (t.block_threads == 128)
+    return stage ? launch_t<128, true>(ctx, g, s, cam, pv, stats, cnt, total, bytes, st)
+                 : launch_t<128, false>(ctx, g, s, cam, pv, stats, cnt, total, bytes, st);
+  return stage ? launch_t<256, true>(ctx, g, s, cam, pv, stats, cnt, total, bytes, st)
+               : launch_t<256, false>(ctx, g, s, cam, pv, stats, cnt, total, bytes, st);
+}
+
+}  // namespace vcr
+
+using namespace vcr;
+
+// Times one pass per candidate tuning and keeps the fastest.  The passes
+// render into the sums, which are reset afterwards.
+extern "C" VCR_API vcr_status vcr_autotune_pt(vcr_ctx* ctx, const vcr_pass_desc* pass, vcr_tuning* out,
+                                              void* stream) {
+  if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  if (!pass) return fail(ctx, VCR_ERR_INVALID, "null pass");
+  if (ctx->params.tracker != VCR_TRACKER_DDA) return fail(ctx, VCR_ERR_STATE, "autotune applies to the DDA tracker");
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaEvent_t a, b;
+  VCR_CUDA(ctx, cudaEventCreate(&a));
+  VCR_CUDA(ctx, cudaEventCreate(&b));
+  vcr_tuning saved = ctx->tuning, best = saved;
+  float best_ms = 1e30f;
+  const uint32_t levels[] = {0, 1, 2, 3};
+  const uint32_t steps[] = {2, 8};
+  const uint32_t threads[] = {128, 256};
+  vcr_status status = VCR_OK;
+  for (uint32_t lv : levels)
+    for (uint32_t sp : steps)
+      for (uint32_t th : threads) {
+        ctx->tuning = vcr_tuning{lv, sp, 1u, th};
+        for (int rep = 0; rep < 2 && !status; ++rep) {  // first run warms up
+          cudaEventRecord(a, st);
+          status = pt_pass_launch(ctx, pass, st);
+          cudaEventRecord(b, st);
+        }
+        if (status) break;
+        cudaEventSynchronize(b);
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, a, b);
+        if (ms < best_ms) {
+          best_ms = ms;
+          best = ctx->tuning;
+        }
+      }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  ctx->tuning = status ? saved : best;
+  if (status) return status;
+  vcr_status r = vcr_reset_accumulation(ctx);
+  if (r) return r;
+  if (out) *out = best;
+  return VCR_OK;
+}

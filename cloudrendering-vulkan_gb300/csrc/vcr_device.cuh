@@ -20,9 +20,11 @@ constexpr int kBrickVoxels = kBrick * kBrick * kBrick;
 struct GridView {
   const void* bricks;
   const float* scales;     // per brick (FP16/BF16 only)
-  const float* majorants;  // per brick: max decoded texel over the brick + 1-texel halo
+  const float* majorants;  // the selected pyramid level (max over the cell + halo)
   int n[3];                // voxel counts
   int nb[3];               // brick counts
+  int mnb[3];              // cells per axis of the selected majorant level
+  int level;               // selected majorant level: cells of 8 << level voxels
   int precision;           // vcr_precision
 };
 

@@ -22,9 +22,12 @@ struct vcr_ctx {
   int precision = 0;
   void* d_bricks = nullptr;
   float* d_scales = nullptr;
-  float* d_majorants = nullptr;
+  float* d_majorants = nullptr;  // pyramid levels 0..3, each 16-byte aligned
   float max_density = 0.0f;
   int nb[3] = {0, 0, 0};
+  int mnb[4][3] = {};            // cells per axis of each majorant level
+  size_t moff[4] = {};           // float offset of each level in d_majorants
+  vcr_tuning tuning{2u, 4u, 1u, 256u};
 
   vcr_cloud cloud{};
   bool has_cloud = false;

@@ -121,11 +121,30 @@ class Context:
         self._ck(lib().vcr_grid_info(self.h, C.byref(m), nb))
         return m.value, tuple(nb)
 
-    def majorants(self) -> np.ndarray:
+    def majorants(self, level: int = 0) -> np.ndarray:
         _, nb = self.grid_info()
-        out = np.empty(nb[0] * nb[1] * nb[2], np.float32)
-        self._ck(lib().vcr_grid_read_majorants(self.h, _ptr(out), out.size))
+        d = list(nb)
+        for _ in range(level):
+            d = [(x + 1) // 2 for x in d]
+        out = np.empty(d[0] * d[1] * d[2], np.float32)
+        self._ck(lib().vcr_grid_read_majorants(self.h, level, _ptr(out), out.size))
         return out
+
+    def set_tuning(self, majorant_level=2, dda_steps=4, stage_majorants=1, block_threads=256):
+        t = _abi.Tuning(majorant_level, dda_steps, stage_majorants, block_threads)
+        self._ck(lib().vcr_set_tuning(self.h, C.byref(t)))
+
+    def get_tuning(self) -> dict:
+        t = _abi.Tuning()
+        self._ck(lib().vcr_get_tuning(self.h, C.byref(t)))
+        return {f: getattr(t, f) for f, _ in _abi.Tuning._fields_}
+
+    def autotune(self, seed=0, pass_index=0, spp=1, stream=0) -> dict:
+        p = _abi.PassDesc()
+        p.seed, p.pass_index, p.spp = seed, pass_index, spp
+        t = _abi.Tuning()
+        self._ck(lib().vcr_autotune_pt(self.h, C.byref(p), C.byref(t), C.c_void_p(stream)))
+        return {f: getattr(t, f) for f, _ in _abi.Tuning._fields_}
 
     def grid_sample(self, d_pos: int, d_out: int, n: int, stream: int = 0):
         self._ck(lib().vcr_grid_sample(self.h, C.c_void_p(d_pos), C.c_void_p(d_out), n, C.c_void_p(stream)))

@@ -58,6 +58,11 @@ class ShadowVolume(C.Structure):
                 ("basis_change", C.c_float * 9), ("voxel_axis_count", C.c_uint32), ("voxel_size", C.c_float)]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("majorant_level", C.c_uint32), ("dda_steps", C.c_uint32), ("stage_majorants", C.c_uint32),
+                ("block_threads", C.c_uint32)]
+
+
 class PassDesc(C.Structure):
     _fields_ = [("seed", C.c_uint32), ("pass_index", C.c_uint32), ("spp", C.c_uint32),
                 ("crop", C.c_uint32 * 4), ("flags", C.c_uint32)]
@@ -87,7 +92,10 @@ SIGNATURES = {
     "vcr_grid_upload": (_S, [_P, C.POINTER(GridDesc), _P, C.c_int]),
     "vcr_grid_generate": (_S, [_P, C.POINTER(GridDesc), C.POINTER(FbmDesc), C.c_int]),
     "vcr_grid_info": (_S, [_P, C.POINTER(_f), C.POINTER(_u32)]),
-    "vcr_grid_read_majorants": (_S, [_P, _P, _sz]),
+    "vcr_grid_read_majorants": (_S, [_P, _u32, _P, _sz]),
+    "vcr_set_tuning": (_S, [_P, C.POINTER(Tuning)]),
+    "vcr_get_tuning": (_S, [_P, C.POINTER(Tuning)]),
+    "vcr_autotune_pt": (_S, [_P, C.POINTER(PassDesc), C.POINTER(Tuning), _P]),
     "vcr_grid_sample": (_S, [_P, _P, _P, _u32, _P]),
     "vcr_xyz_read": (_S, [C.c_char_p, C.POINTER(GridDesc), _P, _sz]),
     "vcr_xyz_write": (_S, [C.c_char_p, C.POINTER(GridDesc), _P]),

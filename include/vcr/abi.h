@@ -169,6 +169,19 @@ typedef struct vcr_shadow_volume {
   float voxel_size;
 } vcr_shadow_volume;
 
+/* Performance knobs of the DDA wavefront tracker (no reference counterpart;
+ * the reference uses one global majorant, PathTracer.comp:338).
+ * majorant_level selects DDA cells of (8 << level) voxels per axis, 0..3;
+ * it changes how random numbers are consumed (not the expected image), so
+ * it is part of a render's determinism key.  The other fields change only
+ * the schedule, never a result bit. */
+typedef struct vcr_tuning {
+  uint32_t majorant_level;  /* 0..3 */
+  uint32_t dda_steps;       /* majorant cells a lane may walk per wavefront step, >= 1 */
+  uint32_t stage_majorants; /* 1: stage the level's majorants in shared memory (TMA bulk copy) when they fit */
+  uint32_t block_threads;   /* wavefront CTA size: 128 or 256 */
+} vcr_tuning;
+
 /* PushConstants (UniformBuffers.h:6-13) for one progressive pass. */
 typedef struct vcr_pass_desc {
   uint32_t seed;       /* render seed                                         */
@@ -239,8 +252,11 @@ VCR_API vcr_status vcr_grid_generate(vcr_ctx* ctx, const vcr_grid_desc* desc,
  * Grid3D.h:180-192) and brick-grid dimensions. */
 VCR_API vcr_status vcr_grid_info(vcr_ctx* ctx, float* out_max_density,
                                  uint32_t out_bricks[3]);
-/* Read the brick majorant grid (float per 8^3 brick, x-fastest). */
-VCR_API vcr_status vcr_grid_read_majorants(vcr_ctx* ctx, float* host_out, size_t count);
+/* Read one level of the majorant pyramid (float per cell, x-fastest).
+ * Level 0 has one cell per 8^3 brick: the max decoded texel over the brick
+ * plus a one-texel halo; level l+1 takes the max over 2x2x2 cells of level
+ * l; level l has ceil(bricks / 2^l) cells per axis. */
+VCR_API vcr_status vcr_grid_read_majorants(vcr_ctx* ctx, uint32_t level, float* host_out, size_t count);
 /* Densities at n world positions (device pointers; float3 in, float out),
  * through the same trilinear fetch the trackers use. */
 VCR_API vcr_status vcr_grid_sample(vcr_ctx* ctx, const float* d_pos, float* d_out,
@@ -285,6 +301,13 @@ VCR_API vcr_status vcr_shadow_volume_build(vcr_ctx* ctx, const vcr_shadow_volume
  * the FP64 sums.  vcr_params.tracker selects the reference per-pixel
  * global-majorant tracker or the persistent DDA wavefront tracker. */
 VCR_API vcr_status vcr_pt_pass(vcr_ctx* ctx, const vcr_pass_desc* pass, void* stream);
+/* Tracker tuning (vcr_tuning).  Defaults: level 2, 4 steps, staging on,
+ * 256 threads.  vcr_autotune_pt times one pass of `pass` per candidate on
+ * `stream` (the passes are rendered into the sums and then reset), keeps
+ * the fastest and returns it. */
+VCR_API vcr_status vcr_set_tuning(vcr_ctx* ctx, const vcr_tuning* t);
+VCR_API vcr_status vcr_get_tuning(vcr_ctx* ctx, vcr_tuning* out);
+VCR_API vcr_status vcr_autotune_pt(vcr_ctx* ctx, const vcr_pass_desc* pass, vcr_tuning* out, void* stream);
 /* Counters of the last vcr_pt_pass: [0] paths, [1] density lookups,
  * [2] scatter events, [3] DDA cell visits. */
 VCR_API vcr_status vcr_pt_counters(vcr_ctx* ctx, uint64_t out[4]);

@@ -31,11 +31,12 @@ def lib():
             "oracle_grid_new": (P, [P, P, C.c_int]),
             "oracle_grid_free": (None, [P]),
             "oracle_grid_max": (f, [P]),
-            "oracle_grid_majorants": (None, [P, P]),
+            "oracle_grid_majorants": (None, [P, C.c_int, P]),
             "oracle_grid_decoded": (None, [P, P]),
             "oracle_grid_sample": (None, [P, C.POINTER(_abi.Cloud), P, u32, P]),
-            "oracle_dda_trace": (None, [P, C.POINTER(_abi.Cloud), P, P, u32, u32, P, P, P]),
-            "oracle_pt_pass": (C.c_int, [P, C.POINTER(_abi.Cloud), C.POINTER(_abi.Camera), C.POINTER(_abi.Params),
+            "oracle_dda_trace": (None, [P, C.POINTER(_abi.Cloud), C.c_int, P, P, u32, u32, P, P, P]),
+            "oracle_pt_pass": (C.c_int, [P, C.c_int, C.POINTER(_abi.Cloud), C.POINTER(_abi.Camera),
+                                         C.POINTER(_abi.Params),
                                          C.POINTER(_abi.ShadowVolume), P, u32, u32, C.POINTER(_abi.PassDesc), P, P,
                                          C.c_int]),
             "oracle_sv_build": (None, [P, C.POINTER(_abi.Cloud), C.POINTER(_abi.ShadowVolume), P]),
@@ -91,9 +92,16 @@ class Grid:
     def max_density(self) -> float:
         return lib().oracle_grid_max(self.h)
 
-    def majorants(self) -> np.ndarray:
-        out = np.empty(self.nb[0] * self.nb[1] * self.nb[2], np.float32)
-        lib().oracle_grid_majorants(self.h, _p(out))
+    def level_dims(self, level: int):
+        d = list(self.nb)
+        for _ in range(level):
+            d = [(x + 1) // 2 for x in d]
+        return tuple(d)
+
+    def majorants(self, level: int = 0) -> np.ndarray:
+        d = self.level_dims(level)
+        out = np.empty(d[0] * d[1] * d[2], np.float32)
+        lib().oracle_grid_majorants(self.h, level, _p(out))
         return out
 
     def decoded(self) -> np.ndarray:
@@ -107,18 +115,18 @@ class Grid:
         lib().oracle_grid_sample(self.h, C.byref(cloud), _p(pos), pos.shape[0], _p(out))
         return out
 
-    def dda_trace(self, cloud, o: np.ndarray, d: np.ndarray, max_cells: int):
+    def dda_trace(self, cloud, o: np.ndarray, d: np.ndarray, max_cells: int, level: int = 0):
         o = np.ascontiguousarray(o, np.float32)
         d = np.ascontiguousarray(d, np.float32)
         n = o.shape[0]
         cells = np.zeros((n, max_cells), np.uint32)
         tt = np.zeros((n, max_cells, 2), np.float32)
         cnt = np.zeros(n, np.uint32)
-        lib().oracle_dda_trace(self.h, C.byref(cloud), _p(o), _p(d), n, max_cells, _p(cells), _p(tt), _p(cnt))
+        lib().oracle_dda_trace(self.h, C.byref(cloud), level, _p(o), _p(d), n, max_cells, _p(cells), _p(tt), _p(cnt))
         return cells, tt, cnt
 
     def pt_pass(self, cloud, cam, params, width, height, seed=0, pass_index=0, spp=1, crop=(0, 0, 0, 0), flags=0,
-                sum_img=None, stats=None, sv=None, sv_tex=None, threads=0):
+                sum_img=None, stats=None, sv=None, sv_tex=None, threads=0, level=2):
         if sum_img is None:
             sum_img = np.zeros((height, width, 3), np.float64)
         if stats is None:
@@ -129,7 +137,7 @@ class Grid:
             p.crop[i] = crop[i]
         svp = C.byref(sv) if sv is not None else None
         svt = _p(np.ascontiguousarray(sv_tex, np.float32)) if sv_tex is not None else None
-        lib().oracle_pt_pass(self.h, C.byref(cloud), C.byref(cam), C.byref(params), svp, svt, width, height,
+        lib().oracle_pt_pass(self.h, level, C.byref(cloud), C.byref(cam), C.byref(params), svp, svt, width, height,
                              C.byref(p), _p(sum_img), _p(stats), threads or os.cpu_count() or 1)
         return sum_img, stats
 

@@ -24,7 +24,9 @@ struct Grid {
   int n[3];
   int nb[3];
   std::vector<float> tex;  // decoded, x fastest
-  std::vector<float> maj;  // per 8^3 brick, halo included
+  std::vector<float> maj;  // per 8^3 brick, halo included (pyramid level 0)
+  std::vector<float> lv[4];  // pyramid: level l+1 = max over 2x2x2 cells of level l
+  int lnb[4][3];
   float max_density = 0.0f;
 
   float at(int i, int j, int k) const { return tex[(size_t)i + (size_t)n[0] * ((size_t)j + (size_t)n[1] * k)]; }
@@ -76,6 +78,25 @@ Grid* grid_new(const uint32_t size[3], const float* dense, int precision) {
         g->maj[(size_t)ib + (size_t)g->nb[0] * ((size_t)jb + (size_t)g->nb[1] * kb)] = m;
       }
   for (float m : g->maj) g->max_density = std::fmax(g->max_density, m);
+  g->lv[0] = g->maj;
+  for (int a = 0; a < 3; ++a) g->lnb[0][a] = g->nb[a];
+  for (int l = 1; l < 4; ++l) {
+    const int* sd = g->lnb[l - 1];
+    int* dd = g->lnb[l];
+    for (int a = 0; a < 3; ++a) dd[a] = (sd[a] + 1) / 2;
+    g->lv[l].assign((size_t)dd[0] * dd[1] * dd[2], 0.0f);
+    for (int k = 0; k < dd[2]; ++k)
+      for (int j = 0; j < dd[1]; ++j)
+        for (int i = 0; i < dd[0]; ++i) {
+          float m = 0.0f;
+          for (int c = 0; c < 8; ++c) {
+            int a = 2 * i + (c & 1), b = 2 * j + ((c >> 1) & 1), e = 2 * k + (c >> 2);
+            if (a < sd[0] && b < sd[1] && e < sd[2])
+              m = std::fmax(m, g->lv[l - 1][(size_t)a + (size_t)sd[0] * ((size_t)b + (size_t)sd[1] * e)]);
+          }
+          g->lv[l][(size_t)i + (size_t)dd[0] * ((size_t)j + (size_t)dd[1] * k)] = m;
+        }
+  }
   return g;
 }
 
@@ -102,6 +123,8 @@ float trilinear(const float* tex, const int n[3], V3 nrm) {
 
 struct Scene {
   const Grid* g;
+  const float* maj;  // majorants of the selected pyramid level
+  int mnb[3];
   V3 b0, b1;
   float max_ext, ds, bs, k;
   V3 cell;
@@ -351,8 +374,8 @@ void track_init(const Scene& s, Track& tr, V3 o, V3 d, Counts& c) {
   if (!slab(o, d, s.b0, s.b1, tmin, tmax) || !finite_pos(tmax)) tmax = 0.0f;
   tr.t = 0.0f;
   tr.t_end = tmax;
-  dda_init(tr.dda, o, d, s.b0, s.cell, s.g->nb);
-  tr.m = s.g->maj[dda_linear(tr.dda, s.g->nb)];
+  dda_init(tr.dda, o, d, s.b0, s.cell, s.mnb);
+  tr.m = s.maj[dda_linear(tr.dda, s.mnb)];
   ++c.cells;
 }
 
@@ -371,8 +394,8 @@ bool track_step(const Scene& s, Track& tr, float u, Counts& c) {
     tau = tau - dtau;
     tr.t = se;
     if (e >= tr.t_end) return false;
-    if (!dda_advance(tr.dda, s.g->nb)) return false;
-    tr.m = s.g->maj[dda_linear(tr.dda, s.g->nb)];
+    if (!dda_advance(tr.dda, s.mnb)) return false;
+    tr.m = s.maj[dda_linear(tr.dda, s.mnb)];
     ++c.cells;
   }
 }
@@ -458,7 +481,7 @@ V3 trace_path(const Scene& s, const vcr_camera& cam, int x, int y, Rng& rng, Cou
   return L;
 }
 
-Scene make_scene(const Grid* g, const vcr_cloud& cl, const vcr_params& p, const vcr_shadow_volume* sv,
+Scene make_scene(const Grid* g, const vcr_cloud& cl, const vcr_params& p, const vcr_shadow_volume* sv, int level,
                  const float* sv_tex) {
   Scene s{};
   s.g = g;
@@ -469,7 +492,10 @@ Scene make_scene(const Grid* g, const vcr_cloud& cl, const vcr_params& p, const 
   s.bs = cl.base_scaling;
   s.k = cl.density_scaling / cl.base_scaling;
   V3 ext = sub(s.b1, s.b0);
-  s.cell = v3((ext.x / (float)g->n[0]) * 8.0f, (ext.y / (float)g->n[1]) * 8.0f, (ext.z / (float)g->n[2]) * 8.0f);
+  const float cv = (float)(8 << level);  // voxels per majorant cell
+  s.cell = v3((ext.x / (float)g->n[0]) * cv, (ext.y / (float)g->n[1]) * cv, (ext.z / (float)g->n[2]) * cv);
+  s.maj = g->lv[level].data();
+  for (int a = 0; a < 3; ++a) s.mnb[a] = g->lnb[level][a];
   s.g_ = p.phase_g;
   s.opg2 = p.phase_one_plus_g2;
   s.omg2 = p.phase_one_minus_g2;
@@ -573,9 +599,9 @@ void* oracle_grid_new(const uint32_t size[3], const float* dense, int precision)
 }
 void oracle_grid_free(void* h) { delete static_cast<Grid*>(h); }
 float oracle_grid_max(void* h) { return static_cast<Grid*>(h)->max_density; }
-void oracle_grid_majorants(void* h, float* out) {
+void oracle_grid_majorants(void* h, int level, float* out) {
   Grid* g = static_cast<Grid*>(h);
-  std::copy(g->maj.begin(), g->maj.end(), out);
+  std::copy(g->lv[level].begin(), g->lv[level].end(), out);
 }
 void oracle_grid_decoded(void* h, float* out) {
   Grid* g = static_cast<Grid*>(h);
@@ -584,15 +610,15 @@ void oracle_grid_decoded(void* h, float* out) {
 
 void oracle_grid_sample(void* h, const vcr_cloud* cl, const float* pos, uint32_t n, float* out) {
   vcr_params p{};
-  Scene s = make_scene(static_cast<Grid*>(h), *cl, p, nullptr, nullptr);
+  Scene s = make_scene(static_cast<Grid*>(h), *cl, p, nullptr, 0, nullptr);
   for (uint32_t i = 0; i < n; ++i) out[i] = density(s, v3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]));
 }
 
-void oracle_dda_trace(void* h, const vcr_cloud* cl, const float* o, const float* d, uint32_t n, uint32_t max_cells,
+void oracle_dda_trace(void* h, const vcr_cloud* cl, int level, const float* o, const float* d, uint32_t n, uint32_t max_cells,
                       uint32_t* cells, float* tt, uint32_t* count) {
   vcr_params p{};
-  Scene s = make_scene(static_cast<Grid*>(h), *cl, p, nullptr, nullptr);
-  const int* nc = s.g->nb;
+  Scene s = make_scene(static_cast<Grid*>(h), *cl, p, nullptr, level, nullptr);
+  const int* nc = s.mnb;
   for (uint32_t i = 0; i < n; ++i) {
     V3 org = v3(o[3 * i], o[3 * i + 1], o[3 * i + 2]);
     V3 dir = v3(d[3 * i], d[3 * i + 1], d[3 * i + 2]);
@@ -625,10 +651,10 @@ void oracle_dda_trace(void* h, const vcr_cloud* cl, const float* o, const float*
 
 // One progressive pass over the crop: adds spp paths per pixel into sum
 // (float64 RGB, W*H*3) and writes stats (uint32 x4: events, lookups, pass, cells).
-int oracle_pt_pass(void* h, const vcr_cloud* cl, const vcr_camera* cam, const vcr_params* prm,
+int oracle_pt_pass(void* h, int level, const vcr_cloud* cl, const vcr_camera* cam, const vcr_params* prm,
                    const vcr_shadow_volume* sv, const float* sv_tex, uint32_t width, uint32_t height,
                    const vcr_pass_desc* pass, double* sum, uint32_t* stats, int threads) {
-  Scene s = make_scene(static_cast<Grid*>(h), *cl, *prm, sv, sv_tex);
+  Scene s = make_scene(static_cast<Grid*>(h), *cl, *prm, sv, level, sv_tex);
   uint32_t x0 = pass->crop[0], y0 = pass->crop[1];
   uint32_t cw = pass->crop[2] ? pass->crop[2] : width, ch = pass->crop[2] ? pass->crop[3] : height;
   uint32_t spp = pass->spp ? pass->spp : 1;
@@ -674,7 +700,7 @@ int oracle_pt_pass(void* h, const vcr_cloud* cl, const vcr_camera* cam, const vc
 // ShadowVolume.comp:77-93: one column per (x, y), z marching along the light.
 void oracle_sv_build(void* h, const vcr_cloud* cl, const vcr_shadow_volume* sv, float* out) {
   vcr_params p{};
-  Scene s = make_scene(static_cast<Grid*>(h), *cl, p, nullptr, nullptr);
+  Scene s = make_scene(static_cast<Grid*>(h), *cl, p, nullptr, 0, nullptr);
   uint32_t n = sv->voxel_axis_count;
   V3 b0 = v3(sv->bounds_min[0], sv->bounds_min[1], sv->bounds_min[2]);
   V3 R = v3(sv->right[0], sv->right[1], sv->right[2]), U = v3(sv->up[0], sv->up[1], sv->up[2]),

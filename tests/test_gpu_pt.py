@@ -45,7 +45,8 @@ def test_generated_grid_bricks_and_majorants_bit_exact(cuda, small, prec):
             mx, nb = ctx.grid_info()
             assert nb == og.nb
             assert mx == og.max_density()
-            np.testing.assert_array_equal(ctx.majorants(), og.majorants())
+            for level in range(4):
+                np.testing.assert_array_equal(ctx.majorants(level), og.majorants(level))
             b0, b1 = np.array(cloud.bounds_min), np.array(cloud.bounds_max)
             pts = (b0 + (b1 - b0) * np.random.default_rng(prec).random((100000, 3)) * 1.1 - 0.05 * (b1 - b0))
             pts = pts.astype(np.float32)
@@ -56,7 +57,8 @@ def test_generated_grid_bricks_and_majorants_bit_exact(cuda, small, prec):
             np.testing.assert_array_equal(d_out.cpu().numpy(), og.sample(cloud, pts))
 
 
-def test_dda_cell_sequence_bit_exact(cuda, small):
+@pytest.mark.parametrize("level", [0, 1, 2, 3])
+def test_dda_cell_sequence_bit_exact(cuda, small, level):
     import torch
     size, dense = small
     desc = vcr.grid_desc(size, (1 / 48,) * 3)
@@ -73,15 +75,16 @@ def test_dda_cell_sequence_bit_exact(cuda, small):
     with vcr.Context() as ctx:
         ctx.grid_upload(desc, dense)
         ctx.set_cloud(cloud)
+        ctx.set_tuning(majorant_level=level)
         d_o, d_d = _dev(o, cuda), _dev(d, cuda)
         cells = torch.zeros((n, mc), dtype=torch.int32, device=cuda)
         tt = torch.zeros((n, mc, 2), dtype=torch.float32, device=cuda)
         cnt = torch.zeros(n, dtype=torch.int32, device=cuda)
         ctx.dda_trace(d_o.data_ptr(), d_d.data_ptr(), n, mc, cells.data_ptr(), tt.data_ptr(), cnt.data_ptr())
         torch.cuda.synchronize()
-    oc, ot, on = og.dda_trace(cloud, o, d, mc)
+    oc, ot, on = og.dda_trace(cloud, o, d, mc, level)
     np.testing.assert_array_equal(cnt.cpu().numpy().view(np.uint32), on)
-    assert on.max() > 4 and (on == 0).sum() > 10
+    assert on.max() > (4 >> level) and (on == 0).sum() > 10
     mask = np.arange(mc)[None, :] < on[:, None]
     np.testing.assert_array_equal(cells.cpu().numpy().view(np.uint32)[mask], oc[mask])
     np.testing.assert_array_equal(tt.cpu().numpy()[mask], ot[mask])
@@ -167,6 +170,47 @@ def test_c1_pass_matches_oracle_on_64x64_crop(cuda, tracker):
     frac, exact = _compare_pass(*out, crop)
     assert paths == 64 * 64 and lookups > 64 * 64 and events > 64 * 64
     assert out[1][crop[1]:crop[1] + 64, crop[0]:crop[0] + 64, 0].sum() == events
+
+
+@pytest.mark.parametrize("tuning", [dict(majorant_level=0, dda_steps=1, stage_majorants=0, block_threads=128),
+                                    dict(majorant_level=1, dda_steps=64, stage_majorants=1, block_threads=256),
+                                    dict(majorant_level=3, dda_steps=3, stage_majorants=1, block_threads=128),
+                                    dict(majorant_level=2, dda_steps=2, stage_majorants=0, block_threads=256)])
+def test_dda_tuning_knobs_keep_oracle_parity(cuda, tuning):
+    """The level selects the estimator (the oracle mirrors it); the step
+    count, shared-memory staging and CTA size are schedule-only."""
+    sc = configs.C1_PT
+    dense = orc.fbm_fill(sc.size, seed=sc.seed, octaves=sc.octaves)
+    og = orc.Grid(dense, 0)
+    crop = (160, 200, 96, 64)
+    with vcr.Context() as ctx:
+        ctx.grid_upload(sc.grid_desc(), dense, vcr.PREC_FP32)
+        ctx.set_tuning(**tuning)
+        cloud = sc.cloud()
+        cloud.max_extinction = max(og.max_density(), 0.01)
+        ctx.set_cloud(cloud)
+        ctx.set_camera(sc.camera())
+        ctx.set_params(sc.params(vcr.TRACKER_DDA))
+        ctx.set_frame(sc.width, sc.height)
+        ctx.pt_pass(seed=9, pass_index=1, crop=crop, flags=vcr.PASS_RECORD_STATS)
+        ctx.synchronize()
+        g_sum, g_st = ctx.image_sum(), ctx.path_stats()
+    o_sum, o_st = og.pt_pass(cloud, sc.camera(), sc.params(vcr.TRACKER_DDA), sc.width, sc.height, seed=9,
+                             pass_index=1, crop=crop, flags=vcr.PASS_RECORD_STATS, level=tuning["majorant_level"])
+    _compare_pass(g_sum, g_st, o_sum, o_st, crop)
+    np.testing.assert_array_equal(g_st[..., 3], o_st[..., 3])  # DDA cell visits
+
+
+def test_autotune_picks_a_valid_tuning(cuda):
+    sc = configs.C1_PT
+    with vcr.Context() as ctx:
+        configs.setup_context(ctx, sc, width=128, height=128)
+        best = ctx.autotune(seed=1)
+        assert best["majorant_level"] in range(4) and best["block_threads"] in (128, 256)
+        assert ctx.get_tuning() == best
+        assert ctx.pass_count() == 0  # autotune passes are not accumulated
+        ctx.pt_pass(seed=1)
+        ctx.synchronize()
 
 
 @pytest.mark.parametrize("prec", [vcr.PREC_FP16, vcr.PREC_BF16])
