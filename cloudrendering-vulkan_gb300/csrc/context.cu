@@ -144,6 +144,9 @@ extern "C" VCR_API vcr_status vcr_destroy(vcr_ctx* ctx) {
   void* ptrs[] = {ctx->d_bricks, ctx->d_scales, ctx->d_majorants, ctx->d_sum, ctx->d_stats,
                   ctx->d_counters, ctx->d_error, ctx->d_sv, ctx->d_scratch};
   for (void* p : ptrs) cudaFree(p);
+  ppb_free(ctx);
+  ppm_free(ctx);
+  nrc_free(ctx);
   if (ctx->work_done) cudaEventDestroy(ctx->work_done);
   delete ctx;
   return VCR_OK;

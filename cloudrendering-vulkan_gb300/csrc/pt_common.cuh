@@ -141,6 +141,27 @@ inline CamView cam_view(const vcr_camera& c) {
   return v;
 }
 
+// Pass constants from a vcr_pass_desc (crop defaults to the whole frame).
+inline vcr_status make_pass_view(vcr_ctx* ctx, const vcr_pass_desc* pass, PassView& pv) {
+  pv.seed = pass->seed;
+  pv.pass = pass->pass_index;
+  pv.spp = pass->spp ? pass->spp : 1;
+  pv.flags = pass->flags;
+  pv.width = ctx->width;
+  pv.height = ctx->height;
+  pv.padded_w = 32u * (ctx->width / 32u + 1u);
+  pv.x0 = pass->crop[0];
+  pv.y0 = pass->crop[1];
+  pv.cw = pass->crop[2] ? pass->crop[2] : ctx->width;
+  pv.ch = pass->crop[2] ? pass->crop[3] : ctx->height;
+  if ((uint64_t)pv.x0 + pv.cw > ctx->width || (uint64_t)pv.y0 + pv.ch > ctx->height || pv.ch == 0 || pv.cw == 0)
+    return fail(ctx, VCR_ERR_INVALID, "crop %u,%u %ux%u outside the %ux%u frame", pv.x0, pv.y0, pv.cw, pv.ch,
+                ctx->width, ctx->height);
+  if ((pv.flags & VCR_PASS_NO_ACCUMULATE) && pv.spp != 1)
+    return fail(ctx, VCR_ERR_INVALID, "VCR_PASS_NO_ACCUMULATE needs spp == 1");
+  return VCR_OK;
+}
+
 // DDA wavefront tracker launch (pt_wavefront.cu).
 vcr_status wavefront_launch(vcr_ctx* ctx, const GridView& g, const SceneView& s, const CamView& cam,
                             const PassView& pv, uint32_t* stats, Counters cnt, uint32_t total, cudaStream_t st);

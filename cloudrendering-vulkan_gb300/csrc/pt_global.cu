@@ -126,22 +126,8 @@ vcr_status pt_pass_launch(vcr_ctx* ctx, const vcr_pass_desc* pass, cudaStream_t 
   if (!ctx->has_grid || !ctx->has_cloud || !ctx->has_cam || !ctx->has_params || !ctx->d_sum)
     return fail(ctx, VCR_ERR_STATE, "vcr_pt_pass needs a grid, cloud, camera, params and frame");
   PassView pv;
-  pv.seed = pass->seed;
-  pv.pass = pass->pass_index;
-  pv.spp = pass->spp ? pass->spp : 1;
-  pv.flags = pass->flags;
-  pv.width = ctx->width;
-  pv.height = ctx->height;
-  pv.padded_w = 32u * (ctx->width / 32u + 1u);
-  pv.x0 = pass->crop[0];
-  pv.y0 = pass->crop[1];
-  pv.cw = pass->crop[2] ? pass->crop[2] : ctx->width;
-  pv.ch = pass->crop[2] ? pass->crop[3] : ctx->height;
-  if (pv.x0 + pv.cw > ctx->width || pv.y0 + pv.ch > ctx->height || pv.ch == 0)
-    return fail(ctx, VCR_ERR_INVALID, "crop %u,%u %ux%u outside the %ux%u frame", pv.x0, pv.y0, pv.cw, pv.ch,
-                ctx->width, ctx->height);
-  if ((pv.flags & VCR_PASS_NO_ACCUMULATE) && pv.spp != 1)
-    return fail(ctx, VCR_ERR_INVALID, "VCR_PASS_NO_ACCUMULATE needs spp == 1");
+  vcr_status vs = make_pass_view(ctx, pass, pv);
+  if (vs) return vs;
   const vcr_params& P = ctx->params;
   if (P.rng_mode == VCR_RNG_XORSHIFT && pv.spp != 1)
     return fail(ctx, VCR_ERR_UNSUPPORTED, "the xorshift parity mode renders 1 spp per pass");

@@ -16,7 +16,7 @@
 // with a TMA bulk copy (cp.async.bulk + mbarrier) at CTA start and every
 // DDA cell visit reads shared memory.  The arithmetic per path is identical
 // to the oracle's sequential loop, so results are bit-exact with it.
-#include "pt_common.cuh"
+#include "track.cuh"
 
 namespace vcr {
 
@@ -64,48 +64,6 @@ __device__ bool stage_to_smem(void* dst, const void* src, uint32_t bytes, uint64
       if (mbar_try_wait(b, 0u)) break;
   }
   return __syncthreads_and(ok ? 1 : 0) != 0;
-}
-
-struct Track {
-  Dda dda;
-  float t, t_end, m;
-};
-
-__device__ __forceinline__ void track_init(Track& tr, const GridView& g, const SceneView& s, const float* maj, f3 o,
-                                           f3 d, uint32_t& cells) {
-  float tmin, tmax;
-  if (!slab(o, d, s.b0, s.b1, tmin, tmax) || !finite_pos(tmax)) tmax = 0.0f;
-  tr.t = 0.0f;
-  tr.t_end = tmax;
-  dda_init(tr.dda, o, d, s.b0, s.cell, g.mnb);
-  tr.m = maj[dda_linear(tr.dda, g.mnb)];
-  ++cells;
-}
-
-enum : int { kPending = 0, kCandidate = 1, kExit = 2 };
-
-// Up to `steps` cells of one free flight: consume the optical depth `tau`
-// cell by cell (dtau = (m k)(min(exit, t_end) - t)); a tentative collision
-// lands at t + tau/(m k) inside the cell where tau runs out.
-__device__ __forceinline__ int track_walk(Track& tr, const GridView& g, const float* maj, float k, float& tau,
-                                          uint32_t& cells, uint32_t steps) {
-  for (uint32_t i = 0; i < steps; ++i) {
-    float e = dda_cell_exit(tr.dda);
-    float se = fminf(e, tr.t_end);
-    float sig = tr.m * k;
-    float dtau = sig * (se - tr.t);
-    if (dtau > tau) {
-      tr.t = tr.t + tau / sig;
-      return kCandidate;
-    }
-    tau = tau - dtau;
-    tr.t = se;
-    if (e >= tr.t_end) return kExit;
-    if (!dda_advance(tr.dda, g.mnb)) return kExit;
-    tr.m = maj[dda_linear(tr.dda, g.mnb)];
-    ++cells;
-  }
-  return kPending;
 }
 
 enum : uint32_t { kIdle = 0, kScatter = 1, kNee = 2 };

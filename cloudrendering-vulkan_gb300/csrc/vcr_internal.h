@@ -11,6 +11,12 @@
 #include "../../include/vcr/abi.h"
 #include "vcr_device.cuh"
 
+namespace vcr {
+struct PpbState;
+struct PpmState;
+struct NrcState;
+}  // namespace vcr
+
 struct vcr_ctx {
   int device = 0;
   int sm_count = 0;
@@ -58,6 +64,11 @@ struct vcr_ctx {
   // reusable scratch
   void* d_scratch = nullptr;
   size_t scratch_bytes = 0;
+
+  // technique state (allocated by the technique's setup call)
+  vcr::PpbState* ppb = nullptr;
+  vcr::PpmState* ppm = nullptr;
+  vcr::NrcState* nrc = nullptr;
 };
 
 namespace vcr {
@@ -90,8 +101,13 @@ vcr_status dda_trace_launch(vcr_ctx* ctx, const float* d_o, const float* d_d, ui
                             uint32_t max_cells, uint32_t* d_cells, float* d_t, uint32_t* d_count,
                             cudaStream_t s);
 
-// pt.cu
+// pt_global.cu
 vcr_status pt_pass_launch(vcr_ctx* ctx, const vcr_pass_desc* pass, cudaStream_t s);
+
+// ppb.cu / ppm.cu / nrc.cu: release technique state (vcr_destroy)
+void ppb_free(vcr_ctx* ctx);
+void ppm_free(vcr_ctx* ctx);
+void nrc_free(vcr_ctx* ctx);
 
 // sv.cu
 vcr_status sv_build_launch(vcr_ctx* ctx, const vcr_shadow_volume* sv, cudaStream_t s);

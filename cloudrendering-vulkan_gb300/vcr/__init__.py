@@ -189,6 +189,46 @@ class Context:
     def synchronize(self):
         self._ck(lib().vcr_synchronize(self.h))
 
+    # photon beams -----------------------------------------------------------
+    def ppb_setup(self, photons, capacity, radius, alpha=0.8):
+        p = _abi.PpbParams(photons, capacity, radius, alpha)
+        self._ck(lib().vcr_ppb_setup(self.h, C.byref(p)))
+
+    def ppb_free(self):
+        self._ck(lib().vcr_ppb_free(self.h))
+
+    def ppb_pass(self, seed=0, pass_index=0, crop=(0, 0, 0, 0), flags=0, stream=0):
+        p = _abi.PassDesc()
+        p.seed, p.pass_index, p.spp, p.flags = seed, pass_index, 1, flags
+        for i in range(4):
+            p.crop[i] = crop[i]
+        self._ck(lib().vcr_ppb_pass(self.h, C.byref(p), C.c_void_p(stream)))
+
+    def ppb_info(self) -> dict:
+        i = _abi.PpbInfo()
+        self._ck(lib().vcr_ppb_info(self.h, C.byref(i)))
+        return {f: getattr(i, f) for f, _ in _abi.PpbInfo._fields_}
+
+    def ppb_read(self, name, photons=None) -> np.ndarray:
+        info = self.ppb_info()
+        n, K = info["segments"], info["beam_slots"]
+        shapes = {"slots": ((photons or 0) * K, 28), "nbeams": (photons or 0,), "seg_a": (n, 4), "seg_b": (n, 4),
+                  "seg_beam": (n,), "codes": (n,), "order": (n,), "left": (max(n - 1, 0),),
+                  "right": (max(n - 1, 0),), "node_lo": (max(n - 1, 0), 4), "node_hi": (max(n - 1, 0), 4),
+                  "leaf_lo": (n, 4), "leaf_hi": (n, 4)}
+        dt = np.float32 if name in ("slots", "seg_a", "seg_b", "node_lo", "node_hi", "leaf_lo", "leaf_hi") \
+            else np.uint32
+        out = np.empty(shapes[name], dt)
+        self._ck(lib().vcr_ppb_read(self.h, _abi.PPB_BUFFERS[name], _ptr(out) if out.size else C.c_void_p(1),
+                                    out.nbytes))
+        return out
+
+    def lbvh_build(self, d_codes, d_order, d_seg_a, d_seg_b, n, d_left, d_right, d_nlo, d_nhi, d_llo, d_lhi,
+                   stream=0):
+        v = C.c_void_p
+        self._ck(lib().vcr_lbvh_build(self.h, v(d_codes), v(d_order), v(d_seg_a), v(d_seg_b), n, v(d_left),
+                                      v(d_right), v(d_nlo), v(d_nhi), v(d_llo), v(d_lhi), v(stream)))
+
     # beam ordering primitives (device pointers) -----------------------------
     def radix_sort_pairs(self, d_kin, d_vin, d_kout, d_vout, n, begin_bit=0, end_bit=32, stream=0):
         self._ck(lib().vcr_radix_sort_pairs(self.h, C.c_void_p(d_kin), C.c_void_p(d_vin or 0) if d_vin else None,

@@ -63,6 +63,18 @@ class Tuning(C.Structure):
                 ("block_threads", C.c_uint32)]
 
 
+class PpbParams(C.Structure):
+    _fields_ = [("photons", C.c_uint32), ("capacity", C.c_uint32), ("radius", C.c_float), ("alpha", C.c_float)]
+
+
+class PpbInfo(C.Structure):
+    _fields_ = [("segments", C.c_uint32), ("dropped", C.c_uint32), ("radius", C.c_float), ("beam_slots", C.c_uint32)]
+
+
+PPB_BUFFERS = {"slots": 0, "nbeams": 1, "seg_a": 2, "seg_b": 3, "seg_beam": 4, "codes": 5, "order": 6, "left": 7,
+               "right": 8, "node_lo": 9, "node_hi": 10, "leaf_lo": 11, "leaf_hi": 12}
+
+
 class PassDesc(C.Structure):
     _fields_ = [("seed", C.c_uint32), ("pass_index", C.c_uint32), ("spp", C.c_uint32),
                 ("crop", C.c_uint32 * 4), ("flags", C.c_uint32)]
@@ -109,6 +121,12 @@ SIGNATURES = {
     "vcr_pt_pass": (_S, [_P, C.POINTER(PassDesc), _P]),
     "vcr_pt_counters": (_S, [_P, C.POINTER(_u64)]),
     "vcr_dda_trace": (_S, [_P, _P, _P, _u32, _u32, _P, _P, _P, _P]),
+    "vcr_ppb_setup": (_S, [_P, C.POINTER(PpbParams)]),
+    "vcr_ppb_free": (_S, [_P]),
+    "vcr_ppb_pass": (_S, [_P, C.POINTER(PassDesc), _P]),
+    "vcr_ppb_info": (_S, [_P, C.POINTER(PpbInfo)]),
+    "vcr_ppb_read": (_S, [_P, C.c_int, _P, _sz]),
+    "vcr_lbvh_build": (_S, [_P, _P, _P, _P, _P, _u32, _P, _P, _P, _P, _P, _P, _P]),
     "vcr_radix_sort_pairs": (_S, [_P, _P, _P, _P, _P, _u32, _u32, _u32, _P]),
     "vcr_radix_sort_pairs_noalloc": (_S, [_P, _P, _P, _P, _u32, _u32, _u32, _P]),
     "vcr_morton_codes": (_S, [_P, _P, _u32, F3, F3, _u32, _P, _P]),

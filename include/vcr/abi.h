@@ -322,6 +322,66 @@ VCR_API vcr_status vcr_dda_trace(vcr_ctx* ctx, const float* d_origin, const floa
                                  float* d_out_t, uint32_t* d_out_count, void* stream);
 
 /* ------------------------------------------------------------------------ */
+/* Progressive photon beams (RenderTechniquePPB, RenderTechniquePPB.cpp)    */
+/* ------------------------------------------------------------------------ */
+typedef struct vcr_ppb_params {
+  uint32_t photons;  /* photons emitted per pass (m_beamsPerPass, RenderTechniquePPB.h:117-120) */
+  uint32_t capacity; /* beam segments per pass (BVH leaves; m_maxBeamCount :116); extra are dropped */
+  float radius;      /* initial beam radius r0, world units (initialRadius, main.cpp:814) */
+  float alpha;       /* radius reduction (m_alpha, RenderTechniquePPB.h:114) */
+} vcr_ppb_params;
+
+typedef struct vcr_ppb_info_t {
+  uint32_t segments;   /* beam segments (BVH leaves) of the last pass */
+  uint32_t dropped;    /* segments beyond the capacity in the last pass */
+  float radius;        /* radius used by the last pass */
+  uint32_t beam_slots; /* beams a photon can deposit (events + 1) */
+} vcr_ppb_info_t;
+
+typedef enum vcr_ppb_buffer {
+  VCR_PPB_SLOTS = 0,    /* float x28 per (photon, beam): start, dir, length, power, 16 distances */
+  VCR_PPB_NBEAMS = 1,   /* uint32 per photon */
+  VCR_PPB_SEG_A = 2,    /* float4 per segment: start, radius */
+  VCR_PPB_SEG_B = 3,    /* float4 per segment: end, offset along its beam */
+  VCR_PPB_SEG_BEAM = 4, /* uint32 per segment: beam slot */
+  VCR_PPB_CODES = 5,    /* uint32 per segment: 30-bit Morton code (unsorted) */
+  VCR_PPB_ORDER = 6,    /* uint32 per leaf: segment of each sorted leaf */
+  VCR_PPB_LEFT = 7,     /* uint32 per internal node (bit 31 = leaf) */
+  VCR_PPB_RIGHT = 8,
+  VCR_PPB_NODE_LO = 9,  /* float4 per internal node */
+  VCR_PPB_NODE_HI = 10,
+  VCR_PPB_LEAF_LO = 11, /* float4 per leaf */
+  VCR_PPB_LEAF_HI = 12
+} vcr_ppb_buffer;
+
+/* Allocate the beam buffers (RenderTechniquePPB::AllocateResources,
+ * RenderTechniquePPB.cpp:282-355); beams hold max_events + 1 slots per
+ * photon, so call after vcr_set_params. */
+VCR_API vcr_status vcr_ppb_setup(vcr_ctx* ctx, const vcr_ppb_params* p);
+/* FreeResources (RenderTechniquePPB.cpp:282-355). */
+VCR_API vcr_status vcr_ppb_free(vcr_ctx* ctx);
+/* One progressive pass (RecordDrawCommands, RenderTechniquePPB.cpp:436-519):
+ * photon emission with beam deposit (PPB_PT.comp), segmenting + 30-bit
+ * Morton keys, radix sort, LBVH build (PPB_GenerateHierarchy.comp), AABB
+ * refit (PPB_CalculateAABB.comp), per-pixel beam gather (PPB_PE.comp); the
+ * radius of pass k is r0 prod_{i=1..k} (i + alpha)/(i + 1) (UpdateRadius,
+ * :530-546).  One estimate per pixel is added to the FP64 sums. */
+VCR_API vcr_status vcr_ppb_pass(vcr_ctx* ctx, const vcr_pass_desc* pass, void* stream);
+VCR_API vcr_status vcr_ppb_info(vcr_ctx* ctx, vcr_ppb_info_t* out);
+/* Synchronous copy of one of the last pass's beam buffers. */
+VCR_API vcr_status vcr_ppb_read(vcr_ctx* ctx, vcr_ppb_buffer which, void* host_out, size_t bytes);
+/* LBVH over n Morton-sorted segments (device buffers): Karras build with
+ * index-augmented prefixes for equal keys, then capped-cylinder leaf boxes
+ * and the bottom-up refit.  d_order[i] = segment of sorted leaf i;
+ * segments are float4 (start, radius) and float4 (end, any).  Internal node
+ * children carry bit 31 for leaves.  Replaces PPB_GenerateHierarchy.comp
+ * (:122-168) + PPB_CalculateAABB.comp (:100-120). */
+VCR_API vcr_status vcr_lbvh_build(vcr_ctx* ctx, const uint32_t* d_sorted_codes, const uint32_t* d_order,
+                                  const float* d_seg_a, const float* d_seg_b, uint32_t n, uint32_t* d_left,
+                                  uint32_t* d_right, float* d_node_lo, float* d_node_hi, float* d_leaf_lo,
+                                  float* d_leaf_hi, void* stream);
+
+/* ------------------------------------------------------------------------ */
 /* Photon-beam ordering primitives                                          */
 /* ------------------------------------------------------------------------ */
 /* Stable LSD radix sort of (uint32 key, uint32 value) pairs over key bits

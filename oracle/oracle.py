@@ -190,3 +190,83 @@ def morton(points: np.ndarray, bmin, bmax, bits: int) -> np.ndarray:
     b1 = np.ascontiguousarray(bmax, np.float32)
     lib().oracle_morton(_p(pts), len(pts), _p(b0), _p(b1), bits, _p(out))
     return out
+
+
+class _PpbOut(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n in ("n", "slots", "nbeams", "seg_a", "seg_b", "seg_beam", "codes", "order",
+                                         "left", "right", "node_lo", "node_hi", "leaf_lo", "leaf_hi")] + \
+               [("capacity_out", C.c_uint32)]
+
+
+def _ppb_lib():
+    L = lib()
+    if not getattr(L, "_ppb_bound", False):
+        P, u32, f = C.c_void_p, C.c_uint32, C.c_float
+        L.oracle_ppb_radius.restype = f
+        L.oracle_ppb_radius.argtypes = [f, f, u32]
+        L.oracle_ppb_pass.restype = C.c_int
+        L.oracle_ppb_pass.argtypes = [P, C.c_int, C.POINTER(_abi.Cloud), C.POINTER(_abi.Camera),
+                                      C.POINTER(_abi.Params), u32, u32, f, f, u32, u32, C.POINTER(_abi.PassDesc), P,
+                                      C.POINTER(_PpbOut), C.c_int]
+        L.oracle_lbvh.restype = None
+        L.oracle_lbvh.argtypes = [P, P, P, P, u32, P, P, P, P, P, P]
+        L._ppb_bound = True
+    return L
+
+
+def ppb_radius(r0, alpha, k) -> float:
+    return _ppb_lib().oracle_ppb_radius(r0, alpha, k)
+
+
+def lbvh(sorted_codes, order, seg_a, seg_b):
+    n = len(sorted_codes)
+    sc = np.ascontiguousarray(sorted_codes, np.uint32)
+    od = np.ascontiguousarray(order, np.uint32)
+    a = np.ascontiguousarray(seg_a, np.float32)
+    b = np.ascontiguousarray(seg_b, np.float32)
+    m = max(n - 1, 1)
+    left, right = np.zeros(m, np.uint32), np.zeros(m, np.uint32)
+    nlo, nhi = np.zeros((m, 4), np.float32), np.zeros((m, 4), np.float32)
+    llo, lhi = np.zeros((n, 4), np.float32), np.zeros((n, 4), np.float32)
+    _ppb_lib().oracle_lbvh(_p(sc), _p(od), _p(a), _p(b), n, _p(left), _p(right), _p(nlo), _p(nhi), _p(llo), _p(lhi))
+    k = max(n - 1, 0)
+    return dict(left=left[:k], right=right[:k], node_lo=nlo[:k], node_hi=nhi[:k], leaf_lo=llo, leaf_hi=lhi)
+
+
+def ppb_pass(grid, cloud, cam, params, photons, capacity, r0, alpha, width, height, seed=0, pass_index=0,
+             crop=(0, 0, 0, 0), flags=0, sum_img=None, level=2, threads=0, want_buffers=True):
+    """One oracle photon-beam pass; returns (sum image, dict of buffers)."""
+    L = _ppb_lib()
+    if sum_img is None:
+        sum_img = np.zeros((height, width, 3), np.float64)
+    p = _abi.PassDesc()
+    p.seed, p.pass_index, p.spp, p.flags = seed, pass_index, 1, flags
+    for i in range(4):
+        p.crop[i] = crop[i]
+    K = min(params.max_events + 1, 65) if params.max_events else 65
+    bufs = {}
+    out = _PpbOut()
+    nn = np.zeros(2, np.uint32)
+    out.n = nn.ctypes.data
+    out.capacity_out = capacity if want_buffers else 0
+    if want_buffers:
+        m = max(capacity - 1, 1)
+        bufs = dict(slots=np.zeros((photons * K, 28), np.float32), nbeams=np.zeros(photons, np.uint32),
+                    seg_a=np.zeros((capacity, 4), np.float32), seg_b=np.zeros((capacity, 4), np.float32),
+                    seg_beam=np.zeros(capacity, np.uint32), codes=np.zeros(capacity, np.uint32),
+                    order=np.zeros(capacity, np.uint32), left=np.zeros(m, np.uint32), right=np.zeros(m, np.uint32),
+                    node_lo=np.zeros((m, 4), np.float32), node_hi=np.zeros((m, 4), np.float32),
+                    leaf_lo=np.zeros((capacity, 4), np.float32), leaf_hi=np.zeros((capacity, 4), np.float32))
+        for k, v in bufs.items():
+            setattr(out, k, v.ctypes.data)
+    L.oracle_ppb_pass(grid.h, level, C.byref(cloud), C.byref(cam), C.byref(params), photons, capacity, r0, alpha,
+                      width, height, C.byref(p), _p(sum_img), C.byref(out), threads or os.cpu_count() or 1)
+    n = int(nn[0])
+    info = dict(segments=n, dropped=int(nn[1]))
+    if want_buffers:
+        for k in ("seg_a", "seg_b", "seg_beam", "codes", "order", "leaf_lo", "leaf_hi"):
+            bufs[k] = bufs[k][:n]
+        for k in ("left", "right", "node_lo", "node_hi"):
+            bufs[k] = bufs[k][:max(n - 1, 0)]
+    bufs["info"] = info
+    return sum_img, bufs

@@ -12,26 +12,13 @@
 #include <algorithm>
 #include <vector>
 
-#include "../include/vcr/abi.h"
-#include "oracle_math.h"
+#include "oracle_scene.h"
 
 namespace oracle {
 
 // ---------------------------------------------------------------------------
 // grid: decoded texels (what the GPU reads back from its bricks) + majorants
 // ---------------------------------------------------------------------------
-struct Grid {
-  int n[3];
-  int nb[3];
-  std::vector<float> tex;  // decoded, x fastest
-  std::vector<float> maj;  // per 8^3 brick, halo included (pyramid level 0)
-  std::vector<float> lv[4];  // pyramid: level l+1 = max over 2x2x2 cells of level l
-  int lnb[4][3];
-  float max_density = 0.0f;
-
-  float at(int i, int j, int k) const { return tex[(size_t)i + (size_t)n[0] * ((size_t)j + (size_t)n[1] * k)]; }
-};
-
 Grid* grid_new(const uint32_t size[3], const float* dense, int precision) {
   Grid* g = new Grid();
   for (int a = 0; a < 3; ++a) {
@@ -120,26 +107,6 @@ float trilinear(const float* tex, const int n[3], V3 nrm) {
   float c1 = std::fma(ty, c11 - c01, c01);
   return std::fma(tz, c1 - c0, c0);
 }
-
-struct Scene {
-  const Grid* g;
-  const float* maj;  // majorants of the selected pyramid level
-  int mnb[3];
-  V3 b0, b1;
-  float max_ext, ds, bs, k;
-  V3 cell;
-  // Parameters
-  float g_, opg2, omg2, o2g;
-  bool iso;
-  float albedo, light;
-  V3 sun, sky;
-  uint32_t sky_mode, rng_mode, nee_mode, tracker, max_events;
-  // shadow volume (reference-parity NEE)
-  const float* sv_tex = nullptr;
-  int sv_n = 0;
-  V3 sv_b0, sv_ext;
-  float B[9];
-};
 
 // sampleCloud (PathTracer.comp:115-119)
 float density(const Scene& s, V3 p) { return trilinear(s.g->tex.data(), s.g->n, vdiv(sub(p, s.b0), sub(s.b1, s.b0))); }
@@ -259,15 +226,6 @@ float sv_lookup(const Scene& s, V3 p) {
 // ---------------------------------------------------------------------------
 // global-majorant tracking (reference semantics)
 // ---------------------------------------------------------------------------
-struct Counts {
-  uint32_t events = 0, lookups = 0, cells = 0;
-};
-
-// Loop guards, identical to the kernels': a non-finite exit distance counts
-// as an immediate exit and step counts are capped.
-const uint32_t kStepCap = 1u << 24;
-const uint32_t kPathWorkCap = 1u << 26;
-inline bool finite_pos(float v) { return v >= 0.0f && v <= 3.0e38f; }
 
 // findScatterPoint (PathTracer.comp:318-361)
 bool find_scatter_global(const Scene& s, float sigma_bar, V3& pos, V3 dir, Rng& rng, Counts& c) {
@@ -316,10 +274,6 @@ float ratio_global(const Scene& s, float sigma_bar, V3 pos, V3 ldir, Rng& rng, C
 // ---------------------------------------------------------------------------
 // DDA over 8^3-voxel majorant cells (Amanatides & Woo); ties x < y < z
 // ---------------------------------------------------------------------------
-struct Dda {
-  int c[3], step[3];
-  float tmax[3], tdel[3];
-};
 
 static void dda_axis(float o, float d, float b0, float cs, int c, int& step, float& tmax, float& tdel) {
   if (d > 0.0f) {
@@ -364,10 +318,6 @@ uint32_t dda_linear(const Dda& d, const int nc[3]) {
   return (uint32_t)d.c[0] + (uint32_t)nc[0] * ((uint32_t)d.c[1] + (uint32_t)nc[1] * (uint32_t)d.c[2]);
 }
 
-struct Track {
-  Dda dda;
-  float t, t_end, m;
-};
 
 void track_init(const Scene& s, Track& tr, V3 o, V3 d, Counts& c) {
   float tmin, tmax;
