@@ -189,6 +189,36 @@ class Context:
     def synchronize(self):
         self._ck(lib().vcr_synchronize(self.h))
 
+    # photon mapping ---------------------------------------------------------
+    def ppm_setup(self, photons, capacity, radius, alpha=0.7):
+        p = _abi.PpmParams(photons, capacity, radius, alpha)
+        self._ck(lib().vcr_ppm_setup(self.h, C.byref(p)))
+
+    def ppm_free(self):
+        self._ck(lib().vcr_ppm_free(self.h))
+
+    def ppm_pass(self, seed=0, pass_index=0, crop=(0, 0, 0, 0), stream=0):
+        p = _abi.PassDesc()
+        p.seed, p.pass_index, p.spp = seed, pass_index, 1
+        for i in range(4):
+            p.crop[i] = crop[i]
+        self._ck(lib().vcr_ppm_pass(self.h, C.byref(p), C.c_void_p(stream)))
+
+    def ppm_info(self) -> dict:
+        i = _abi.PpmInfo()
+        self._ck(lib().vcr_ppm_info(self.h, C.byref(i)))
+        return {f: getattr(i, f) for f, _ in _abi.PpmInfo._fields_}
+
+    def ppm_read(self, name) -> np.ndarray:
+        n = self.ppm_info()["photons_stored"]
+        shapes = {"stats": (self.height, self.width, 8), "pos": (n, 4), "power": (n, 4), "dir": (n, 4),
+                  "uid": (n,), "order": (n,), "left": (max(n - 1, 0),), "right": (max(n - 1, 0),)}
+        dt = {"stats": np.float64, "pos": np.float32, "power": np.float32, "dir": np.float32}.get(name, np.uint32)
+        out = np.empty(shapes[name], dt)
+        self._ck(lib().vcr_ppm_read(self.h, _abi.PPM_BUFFERS[name], _ptr(out) if out.size else C.c_void_p(1),
+                                    out.nbytes))
+        return out
+
     # photon beams -----------------------------------------------------------
     def ppb_setup(self, photons, capacity, radius, alpha=0.8):
         p = _abi.PpbParams(photons, capacity, radius, alpha)

@@ -63,6 +63,17 @@ class Tuning(C.Structure):
                 ("block_threads", C.c_uint32)]
 
 
+class PpmParams(C.Structure):
+    _fields_ = [("photons", C.c_uint32), ("capacity", C.c_uint32), ("radius", C.c_float), ("alpha", C.c_float)]
+
+
+class PpmInfo(C.Structure):
+    _fields_ = [("photons_stored", C.c_uint32), ("dropped", C.c_uint32)]
+
+
+PPM_BUFFERS = {"stats": 0, "pos": 1, "power": 2, "dir": 3, "uid": 4, "order": 5, "left": 6, "right": 7}
+
+
 class PpbParams(C.Structure):
     _fields_ = [("photons", C.c_uint32), ("capacity", C.c_uint32), ("radius", C.c_float), ("alpha", C.c_float)]
 
@@ -121,6 +132,11 @@ SIGNATURES = {
     "vcr_pt_pass": (_S, [_P, C.POINTER(PassDesc), _P]),
     "vcr_pt_counters": (_S, [_P, C.POINTER(_u64)]),
     "vcr_dda_trace": (_S, [_P, _P, _P, _u32, _u32, _P, _P, _P, _P]),
+    "vcr_ppm_setup": (_S, [_P, C.POINTER(PpmParams)]),
+    "vcr_ppm_free": (_S, [_P]),
+    "vcr_ppm_pass": (_S, [_P, C.POINTER(PassDesc), _P]),
+    "vcr_ppm_info": (_S, [_P, C.POINTER(PpmInfo)]),
+    "vcr_ppm_read": (_S, [_P, C.c_int, _P, _sz]),
     "vcr_ppb_setup": (_S, [_P, C.POINTER(PpbParams)]),
     "vcr_ppb_free": (_S, [_P]),
     "vcr_ppb_pass": (_S, [_P, C.POINTER(PassDesc), _P]),

@@ -322,6 +322,47 @@ VCR_API vcr_status vcr_dda_trace(vcr_ctx* ctx, const float* d_origin, const floa
                                  float* d_out_t, uint32_t* d_out_count, void* stream);
 
 /* ------------------------------------------------------------------------ */
+/* Volumetric progressive photon mapping (RenderTechniquePPM)               */
+/* ------------------------------------------------------------------------ */
+typedef struct vcr_ppm_params {
+  uint32_t photons;  /* photons emitted per pass (200 x 64 in RenderTechniquePPM.cpp:253) */
+  uint32_t capacity; /* photons stored per pass (every real collision); extra are dropped */
+  float radius;      /* initial per-pixel gather radius R0, world units (initialRadius) */
+  float alpha;       /* radius reduction (m_alpha, RenderTechniquePPM.h:66) */
+} vcr_ppm_params;
+
+typedef struct vcr_ppm_info_t {
+  uint32_t photons_stored; /* photons in the last pass's tree */
+  uint32_t dropped;        /* photons beyond the capacity in the last pass */
+} vcr_ppm_info_t;
+
+typedef enum vcr_ppm_buffer {
+  VCR_PPM_STATS = 0, /* float64 x8 per pixel: N, R, tau rgb, background-sum rgb */
+  VCR_PPM_POS = 1,   /* float4 per stored photon (append order) */
+  VCR_PPM_POWER = 2, /* float4 per stored photon: arriving power rgb */
+  VCR_PPM_DIR = 3,   /* float4 per stored photon: travel direction */
+  VCR_PPM_UID = 4,   /* uint32 per stored photon: photon * 64 + event */
+  VCR_PPM_ORDER = 5, /* uint32 per tree leaf: stored photon of the leaf */
+  VCR_PPM_LEFT = 6,  /* uint32 per internal node (bit 31 = leaf) */
+  VCR_PPM_RIGHT = 7
+} vcr_ppm_buffer;
+
+/* Allocate photon buffers and per-pixel statistics for the current frame;
+ * resets the sums (RenderTechniquePPM::AllocateResources, :115-156). */
+VCR_API vcr_status vcr_ppm_setup(vcr_ctx* ctx, const vcr_ppm_params* p);
+VCR_API vcr_status vcr_ppm_free(vcr_ctx* ctx);
+/* One pass (RecordDrawCommands, RenderTechniquePPM.cpp:229-300): photon
+ * emission with a deposit at every real collision (PPM_PT.comp), photon
+ * tree over the Morton-sorted photons (the KDTree the reference stubs,
+ * KDTree.cpp:6-79), per-pixel measurement point + radius query
+ * (samplePhotonMap, PPM_PE.comp:304-375) and the FP64 N/R/flux update
+ * (in place of the global UpdateRadius, :302-312).  The sums then hold the
+ * current estimate times the pass count. */
+VCR_API vcr_status vcr_ppm_pass(vcr_ctx* ctx, const vcr_pass_desc* pass, void* stream);
+VCR_API vcr_status vcr_ppm_info(vcr_ctx* ctx, vcr_ppm_info_t* out);
+VCR_API vcr_status vcr_ppm_read(vcr_ctx* ctx, vcr_ppm_buffer which, void* host_out, size_t bytes);
+
+/* ------------------------------------------------------------------------ */
 /* Progressive photon beams (RenderTechniquePPB, RenderTechniquePPB.cpp)    */
 /* ------------------------------------------------------------------------ */
 typedef struct vcr_ppb_params {

@@ -19,6 +19,7 @@
 #include <numeric>
 #include <vector>
 
+#include "oracle_lbvh.h"
 #include "oracle_scene.h"
 
 namespace oracle {
@@ -27,13 +28,8 @@ const int kBeamDists = 16;
 const int kSlotFloats = 28;
 const uint32_t kMaxBeamsPerPhoton = 65;
 const uint32_t kMaxSegPerBeam = 4096;
-const uint32_t kLeafBit = 0x80000000u;
 const uint32_t kEmitSalt = 0x85EBCA6Bu;
 const uint32_t kGatherSalt = 0xC2B2AE35u;
-
-struct F4 {
-  float x, y, z, w;
-};
 
 static uint32_t segments_of(float len, float r) {
   float q = len / r;
@@ -52,7 +48,7 @@ static float box_entry(const Scene& s, V3 d, Rng& rng, V3& o) {
   return at;
 }
 
-static uint32_t expand10(uint32_t v) {
+uint32_t expand10(uint32_t v) {
   v = (v * 0x00010001u) & 0xFF0000FFu;
   v = (v * 0x00000101u) & 0x0F00F00Fu;
   v = (v * 0x00000011u) & 0xC30C30C3u;
@@ -69,7 +65,7 @@ static int lbvh_delta(const uint32_t* keys, int n, int i, int j) {
   return clz32(a ^ b);
 }
 
-static void lbvh_build(const uint32_t* keys, int n, uint32_t* left, uint32_t* right) {
+void lbvh_build(const uint32_t* keys, int n, uint32_t* left, uint32_t* right) {
   for (int i = 0; i < n - 1; ++i) {
     int d = lbvh_delta(keys, n, i, i + 1) - lbvh_delta(keys, n, i, i - 1) > 0 ? 1 : -1;
     int dmin = lbvh_delta(keys, n, i, i - d);
@@ -92,7 +88,7 @@ static void lbvh_build(const uint32_t* keys, int n, uint32_t* left, uint32_t* ri
   }
 }
 
-static void segment_box(F4 A, F4 B, F4& lo, F4& hi) {
+void segment_box(F4 A, F4 B, F4& lo, F4& hi) {
   V3 pa = v3(A.x, A.y, A.z), pb = v3(B.x, B.y, B.z);
   float r = A.w;
   V3 a = sub(pb, pa);
@@ -110,8 +106,8 @@ static void segment_box(F4 A, F4 B, F4& lo, F4& hi) {
 }
 
 // Boxes of the whole tree, recursively (same min/max as the GPU refit).
-static void refit(uint32_t node, const uint32_t* left, const uint32_t* right, const std::vector<F4>& llo,
-                  const std::vector<F4>& lhi, std::vector<F4>& nlo, std::vector<F4>& nhi) {
+void refit(uint32_t node, const uint32_t* left, const uint32_t* right, const std::vector<F4>& llo,
+           const std::vector<F4>& lhi, std::vector<F4>& nlo, std::vector<F4>& nhi) {
   uint32_t c[2] = {left[node], right[node]};
   F4 lo[2], hi[2];
   for (int k = 0; k < 2; ++k) {

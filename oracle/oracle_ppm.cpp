@@ -1,0 +1,267 @@
+// ORACLE — test infrastructure only (see oracle_math.h).  CPU restatement of
+// volumetric progressive photon mapping:
+//   emission : PPM_PT.comp main (:452-489) / interactWithMedium (:393-447) /
+//              depositPhoton (:304-321), with a deposit at every real
+//              collision carrying the power arriving there
+//   tree     : photons in (photon, event) order, stable Morton order, binary
+//              radix tree with point leaves (see oracle_ppb.cpp)
+//   gather   : samplePhotonMap (PPM_PE.comp:304-375) at one delta-tracked
+//              measurement point per pixel, with the pixel's radius
+//   update   : stochastic progressive photon mapping per pixel in FP64
+//              (instead of the global UpdateRadius, RenderTechniquePPM.cpp
+//              :302-312)
+// The float and double operations follow the CUDA kernels in order.
+#include <algorithm>
+#include <cmath>
+#include <numeric>
+#include <vector>
+
+#include "oracle_lbvh.h"
+#include "oracle_scene.h"
+
+namespace oracle {
+
+const uint32_t kPpmMaxEvents = 64;
+const uint32_t kPpmEmitSalt = 0x27D4EB2Fu;
+const uint32_t kPpmGatherSalt = 0x165667B1u;
+
+struct Photon {
+  F4 pos, pw, dir;
+  uint32_t uid;
+};
+
+static float box_entry(const Scene& s, V3 d, Rng& rng, V3& o) {
+  V3 e = sub(s.b1, s.b0);
+  float ax = std::fabs(d.x) * (e.y * e.z), ay = std::fabs(d.y) * (e.x * e.z), az = std::fabs(d.z) * (e.x * e.y);
+  float at = (ax + ay) + az;
+  float sel = rng.next() * at;
+  float u = rng.next(), v = rng.next();
+  if (sel < ax) o = v3(d.x > 0.0f ? s.b0.x : s.b1.x, s.b0.y + u * e.y, s.b0.z + v * e.z);
+  else if (sel < ax + ay) o = v3(s.b0.x + u * e.x, d.y > 0.0f ? s.b0.y : s.b1.y, s.b0.z + v * e.z);
+  else o = v3(s.b0.x + u * e.x, s.b0.y + v * e.y, d.z > 0.0f ? s.b0.z : s.b1.z);
+  return at;
+}
+
+static double cbrt_ratio(double r) {
+  double y = 1.0;
+  for (int i = 0; i < 6; ++i) y = y - (y * y * y - r) / (3.0 * y * y);
+  return y;
+}
+
+static float box_dist2(V3 x, F4 lo, F4 hi) {
+  float dx = std::fmax(std::fmax(lo.x - x.x, 0.0f), x.x - hi.x);
+  float dy = std::fmax(std::fmax(lo.y - x.y, 0.0f), x.y - hi.y);
+  float dz = std::fmax(std::fmax(lo.z - x.z, 0.0f), x.z - hi.z);
+  return (dx * dx + dy * dy) + dz * dz;
+}
+
+struct PhotonTree {
+  std::vector<Photon> ph;  // (photon, event) order
+  uint32_t dropped = 0;
+  std::vector<uint32_t> order, left, right;
+  std::vector<F4> leaf_lo, leaf_hi, node_lo, node_hi;
+};
+
+static void emit(const Scene& s, uint32_t P, uint32_t cap, uint32_t seed, uint32_t pass, PhotonTree& T,
+                 int threads) {
+  std::vector<std::vector<Photon>> per(P);
+#pragma omp parallel for schedule(dynamic, 256) num_threads(threads > 0 ? threads : 1)
+  for (int64_t pi = 0; pi < (int64_t)P; ++pi) {
+    uint32_t p = (uint32_t)pi;
+    Counts c;
+    Rng rng = rng_pcg(seed ^ kPpmEmitSalt, p, pass);
+    const float inv = 1.0f / ((float)P * 0.5f);
+    V3 d, o, power;
+    bool sun = rng.next() < 0.5f;
+    if (sun) {
+      d = s.sun;
+    } else {
+      float z = 1.0f - 2.0f * rng.next();
+      float sn, cs;
+      osincos2pi(rng.next(), &sn, &cs);
+      float rr = std::sqrt(std::fmax(0.0f, 1.0f - z * z));
+      d = v3(rr * cs, rr * sn, z);
+    }
+    float at = box_entry(s, d, rng, o);
+    if (sun) {
+      float f = (s.light * at) * inv;
+      power = v3(f, f, f);
+    } else {
+      power = scale(s.sky, ((4.0f * kPI) * at) * inv);
+    }
+    uint32_t events = 0;
+    while (true) {
+      float t;
+      if (!free_flight(s, o, d, rng, t, c)) break;
+      o = along(o, d, t);
+      per[p].push_back(Photon{F4{o.x, o.y, o.z, 0.f}, F4{power.x, power.y, power.z, 0.f}, F4{d.x, d.y, d.z, 0.f},
+                              p * kPpmMaxEvents + events});
+      ++events;
+      power = scale(power, s.albedo);
+      if ((s.max_events && events >= s.max_events) || events >= kPpmMaxEvents) break;
+      d = hg_sample(s, d, rng, true);
+    }
+  }
+  size_t total = 0;
+  for (auto& v : per) total += v.size();
+  T.ph.clear();
+  T.ph.reserve(std::min<size_t>(total, cap));
+  for (auto& v : per)
+    for (auto& x : v)
+      if (T.ph.size() < cap) T.ph.push_back(x);
+  T.dropped = (uint32_t)(total - T.ph.size());
+}
+
+static void build(const Scene& s, PhotonTree& T) {
+  uint32_t n = (uint32_t)T.ph.size();
+  std::vector<uint32_t> codes(n);
+  V3 e = sub(s.b1, s.b0);
+  for (uint32_t i = 0; i < n; ++i) {
+    F4 p = T.ph[i].pos;
+    float qx = std::fmin(std::fmax(((p.x - s.b0.x) / e.x) * 1024.0f, 0.0f), 1023.0f);
+    float qy = std::fmin(std::fmax(((p.y - s.b0.y) / e.y) * 1024.0f, 0.0f), 1023.0f);
+    float qz = std::fmin(std::fmax(((p.z - s.b0.z) / e.z) * 1024.0f, 0.0f), 1023.0f);
+    codes[i] = (expand10((uint32_t)qx) << 2) | (expand10((uint32_t)qy) << 1) | expand10((uint32_t)qz);
+  }
+  T.order.resize(n);
+  std::iota(T.order.begin(), T.order.end(), 0u);
+  std::stable_sort(T.order.begin(), T.order.end(), [&](uint32_t a, uint32_t b) { return codes[a] < codes[b]; });
+  std::vector<uint32_t> sorted(n);
+  for (uint32_t i = 0; i < n; ++i) sorted[i] = codes[T.order[i]];
+  T.left.assign(n > 1 ? n - 1 : 0, 0);
+  T.right.assign(n > 1 ? n - 1 : 0, 0);
+  T.leaf_lo.assign(n, F4{});
+  T.leaf_hi.assign(n, F4{});
+  T.node_lo.assign(n > 1 ? n - 1 : 0, F4{});
+  T.node_hi.assign(n > 1 ? n - 1 : 0, F4{});
+  if (n > 1) lbvh_build(sorted.data(), (int)n, T.left.data(), T.right.data());
+  for (uint32_t i = 0; i < n; ++i) segment_box(T.ph[T.order[i]].pos, T.ph[T.order[i]].pos, T.leaf_lo[i], T.leaf_hi[i]);
+  if (n > 1) refit(0, T.left.data(), T.right.data(), T.leaf_lo, T.leaf_hi, T.node_lo, T.node_hi);
+}
+
+static void gather(const Scene& s, const PhotonTree& T, const vcr_camera& cam, uint32_t W, uint32_t H,
+                   const vcr_pass_desc* pass, float alpha, double* stats, double* sum, int threads) {
+  uint32_t x0 = pass->crop[0], y0 = pass->crop[1];
+  uint32_t cw = pass->crop[2] ? pass->crop[2] : W, ch = pass->crop[2] ? pass->crop[3] : H;
+  int n = (int)T.ph.size();
+#pragma omp parallel for schedule(dynamic, 1) num_threads(threads > 0 ? threads : 1)
+  for (int64_t row = 0; row < (int64_t)ch; ++row) {
+    for (uint32_t cx = 0; cx < cw; ++cx) {
+      int x = (int)(x0 + cx), y = (int)(y0 + (uint32_t)row);
+      uint32_t pix = (uint32_t)y * W + (uint32_t)x;
+      double* st = stats + 8 * (size_t)pix;
+      Counts c;
+      V3 o, rd;
+      camera_ray(cam, x, y, o, rd);
+      V3 bg = v3(0, 0, 0), phi = bg;
+      uint32_t M = 0;
+      float tmin, tmax;
+      if (!slab(o, rd, s.b0, s.b1, tmin, tmax) || tmax < 0.0f || !(s.ds > 0.0f)) {
+        bg = sky(s, rd);
+      } else {
+        V3 entry = along(o, rd, std::fmax(tmin, 0.0f));
+        Rng rng = rng_pcg(pass->seed ^ kPpmGatherSalt, pix, pass->pass_index);
+        float t;
+        if (!free_flight(s, entry, rd, rng, t, c)) {
+          bg = sky(s, rd);
+        } else if (n > 0) {
+          V3 xm = along(entry, rd, t);
+          float sigma_t = s.k * density(s, xm);
+          float r = (float)st[1];
+          float r2 = r * r;
+          V3 wo = neg(rd);
+          uint32_t stack[64];
+          int sp = 0;
+          uint32_t node = n == 1 ? kLeafBit : 0u;
+          while (true) {
+            if (node & kLeafBit) {
+              uint32_t lf = node & ~kLeafBit;
+              F4 q = T.leaf_lo[lf];
+              V3 dq = sub(v3(q.x, q.y, q.z), xm);
+              if (dot(dq, dq) <= r2) {
+                const Photon& ph = T.ph[T.order[lf]];
+                float f = hg_pdf(s, dot(v3(ph.dir.x, ph.dir.y, ph.dir.z), wo));
+                phi = add(phi, scale(v3(ph.pw.x, ph.pw.y, ph.pw.z), f));
+                ++M;
+              }
+            } else if (box_dist2(xm, T.node_lo[node], T.node_hi[node]) <= r2) {
+              if (sp < 64) stack[sp++] = T.right[node];
+              node = T.left[node];
+              continue;
+            }
+            if (sp == 0) break;
+            node = stack[--sp];
+          }
+          if (sigma_t > 0.0f) phi = v3(phi.x / sigma_t, phi.y / sigma_t, phi.z / sigma_t);
+          else phi = v3(0, 0, 0);
+        }
+      }
+      double N = st[0], R = st[1];
+      double tau[3] = {st[2], st[3], st[4]};
+      if (M > 0) {
+        double am = (double)alpha * (double)M;
+        double ratio = (N + am) / (N + (double)M);
+        st[0] = N + am;
+        st[1] = R * cbrt_ratio(ratio);
+        tau[0] = (tau[0] + (double)phi.x) * ratio;
+        tau[1] = (tau[1] + (double)phi.y) * ratio;
+        tau[2] = (tau[2] + (double)phi.z) * ratio;
+        st[2] = tau[0];
+        st[3] = tau[1];
+        st[4] = tau[2];
+      }
+      st[5] += (double)bg.x;
+      st[6] += (double)bg.y;
+      st[7] += (double)bg.z;
+      double Rn = st[1];
+      double vol = (4.0 / 3.0) * 3.14159265358979323846 * Rn * Rn * Rn;
+      double a = (double)s.albedo / vol;
+      double* o3 = sum + 3 * (size_t)pix;
+      o3[0] = st[5] + a * tau[0];
+      o3[1] = st[6] + a * tau[1];
+      o3[2] = st[7] + a * tau[2];
+    }
+  }
+}
+
+}  // namespace oracle
+
+using namespace oracle;
+
+extern "C" {
+
+// stats: float64 x8 per pixel (N, R, tau rgb, background rgb), initialised
+// by the caller to (0, R0, 0...).  out_n[2] = stored photons, dropped.
+// If `photons_out` is non-null it receives pos/pw/dir (12 floats) + uid per
+// stored photon in (photon, event) order, and `order_out` the leaf order.
+int oracle_ppm_pass(void* h, int level, const vcr_cloud* cl, const vcr_camera* cam, const vcr_params* prm,
+                    uint32_t photons, uint32_t cap, float alpha, uint32_t W, uint32_t H, const vcr_pass_desc* pass,
+                    double* stats, double* sum, uint32_t* out_n, float* photons_out, uint32_t* uid_out,
+                    uint32_t* order_out, uint32_t* left_out, uint32_t* right_out, int threads) {
+  Scene s = make_scene(static_cast<Grid*>(h), *cl, *prm, nullptr, level, nullptr);
+  PhotonTree T;
+  emit(s, photons, cap, pass->seed, pass->pass_index, T, threads);
+  build(s, T);
+  gather(s, T, *cam, W, H, pass, alpha, stats, sum, threads);
+  uint32_t n = (uint32_t)T.ph.size();
+  if (out_n) {
+    out_n[0] = n;
+    out_n[1] = T.dropped;
+  }
+  if (photons_out)
+    for (uint32_t i = 0; i < n; ++i) {
+      const Photon& p = T.ph[i];
+      float* q = photons_out + 12 * (size_t)i;
+      q[0] = p.pos.x; q[1] = p.pos.y; q[2] = p.pos.z; q[3] = p.pos.w;
+      q[4] = p.pw.x; q[5] = p.pw.y; q[6] = p.pw.z; q[7] = p.pw.w;
+      q[8] = p.dir.x; q[9] = p.dir.y; q[10] = p.dir.z; q[11] = p.dir.w;
+    }
+  if (uid_out)
+    for (uint32_t i = 0; i < n; ++i) uid_out[i] = T.ph[i].uid;
+  if (order_out) std::copy(T.order.begin(), T.order.end(), order_out);
+  if (left_out) std::copy(T.left.begin(), T.left.end(), left_out);
+  if (right_out) std::copy(T.right.begin(), T.right.end(), right_out);
+  return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,65 @@
+"""ctypes binding of the oracle's photon-mapping restatement (test
+infrastructure, see oracle.py)."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import oracle as _o
+from .oracle import _abi, _p
+
+_bound = False
+
+
+def _lib():
+    global _bound
+    L = _o.lib()
+    if not _bound:
+        P, u32, f = C.c_void_p, C.c_uint32, C.c_float
+        L.oracle_ppm_pass.restype = C.c_int
+        L.oracle_ppm_pass.argtypes = [P, C.c_int, C.POINTER(_abi.Cloud), C.POINTER(_abi.Camera),
+                                      C.POINTER(_abi.Params), u32, u32, f, u32, u32, C.POINTER(_abi.PassDesc), P, P,
+                                      P, P, P, P, P, P, C.c_int]
+        _bound = True
+    return L
+
+
+def init_stats(width, height, r0):
+    st = np.zeros((height, width, 8), np.float64)
+    st[..., 1] = np.float32(r0)
+    return st
+
+
+def ppm_pass(grid, cloud, cam, params, photons, capacity, alpha, width, height, stats, sum_img=None, seed=0,
+             pass_index=0, crop=(0, 0, 0, 0), level=2, threads=0, want_photons=False):
+    """One oracle photon-mapping pass; updates `stats` in place."""
+    L = _lib()
+    if sum_img is None:
+        sum_img = np.zeros((height, width, 3), np.float64)
+    p = _abi.PassDesc()
+    p.seed, p.pass_index, p.spp = seed, pass_index, 1
+    for i in range(4):
+        p.crop[i] = crop[i]
+    nn = np.zeros(2, np.uint32)
+    out = {}
+    ph = uid = order = left = right = None
+    if want_photons:
+        out = dict(photons=np.zeros((capacity, 12), np.float32), uid=np.zeros(capacity, np.uint32),
+                   order=np.zeros(capacity, np.uint32), left=np.zeros(capacity, np.uint32),
+                   right=np.zeros(capacity, np.uint32))
+        ph, uid, order, left, right = (_p(out[k]) for k in ("photons", "uid", "order", "left", "right"))
+    L.oracle_ppm_pass(grid.h, level, C.byref(cloud), C.byref(cam), C.byref(params), photons, capacity, alpha, width,
+                      height, C.byref(p), _p(stats), _p(sum_img), _p(nn), ph, uid, order, left, right,
+                      threads or os.cpu_count() or 1)
+    n = int(nn[0])
+    info = dict(photons_stored=n, dropped=int(nn[1]))
+    if want_photons:
+        out["photons"] = out["photons"][:n]
+        out["uid"] = out["uid"][:n]
+        out["order"] = out["order"][:n]
+        out["left"] = out["left"][:max(n - 1, 0)]
+        out["right"] = out["right"][:max(n - 1, 0)]
+    out["info"] = info
+    return sum_img, out
