@@ -85,6 +85,7 @@ SceneView scene_view(const vcr_ctx* ctx) {
   s.nee_mode = (int)p.nee_mode;
   s.tracker = (int)p.tracker;
   s.max_events = p.max_events;
+  s.nrc_events = ctx->nrc ? p.nrc_events : 0u;
   return s;
 }
 

@@ -1,0 +1,630 @@
+// Neural radiance cache: a 64 -> 5x64 (ReLU) -> 3 MLP that predicts the
+// radiance leaving a scattering vertex toward the previous vertex, trained
+// online on paths the tracer itself produces and queried where paths
+// terminate into it.  No reference counterpart.
+//
+// Tensor cores: BF16 operands, FP32 accumulation through the warp-level
+// matrix API (16x16x16 tiles).  One CTA holds the BF16 weights in shared
+// memory; each of its 4 warps owns 16 samples of a 64-sample tile, so a
+// layer's activations never leave the warp between layers.  Training fuses
+// encoding, forward, the relative-L2 loss gradient, backward and the
+// weight-gradient accumulation (X_l^T dY_l over the tile, in shared FP32)
+// in one kernel; one atomic add per weight per CTA flushes the gradient;
+// Adam runs on FP32 master weights and refreshes the BF16 copy.
+#include <mma.h>
+
+#include "nrc.cuh"
+#include "track.cuh"
+
+namespace vcr {
+
+using namespace nvcuda;
+using bf16 = __nv_bfloat16;
+
+constexpr int kNrcThreads = 128;
+constexpr int kLd = kNrcWidth;  // leading dimension of activation tiles
+
+struct NrcView {
+  const bf16* wb;
+  f3 b0, inv_ext;
+};
+
+// Encode 16 samples (rows) of a warp into X0 rows [16w, 16w+16): lane 2s+h
+// writes half h of sample s (h = 0: position; h = 1: both SH blocks).
+__device__ __forceinline__ void encode_rows(const NrcRecord* __restrict__ recs, uint32_t first, uint32_t count,
+                                            const NrcView& v, bf16* X0, int warp, int lane) {
+  int s = lane >> 1, h = lane & 1;
+  uint32_t idx = first + (uint32_t)(warp * 16 + s);
+  float enc[kNrcIn];
+  if (idx < count) {
+    NrcRecord r = recs[idx];
+    nrc_encode(r, v.b0, v.inv_ext, enc);
+  } else {
+    for (int i = 0; i < kNrcIn; ++i) enc[i] = 0.0f;
+  }
+  bf16* row = X0 + (warp * 16 + s) * kLd;
+  for (int i = 0; i < 32; ++i) row[h * 32 + i] = __float2bfloat16_rn(enc[h * 32 + i]);
+}
+
+// rows [16w,16w+16) of Y = X_l W_l, fp32 into the warp's staging block
+__device__ __forceinline__ void layer_forward(const bf16* X, const bf16* W, int cols, float* Yw, int warp) {
+  wmma::fragment<wmma::matrix_a, 16, 16, 16, bf16, wmma::row_major> a[4];
+  for (int kt = 0; kt < 4; ++kt) wmma::load_matrix_sync(a[kt], X + warp * 16 * kLd + kt * 16, kLd);
+  for (int nt = 0; nt < cols / 16; ++nt) {
+    wmma::fragment<wmma::accumulator, 16, 16, 16, float> acc;
+    wmma::fill_fragment(acc, 0.0f);
+    for (int kt = 0; kt < 4; ++kt) {
+      wmma::fragment<wmma::matrix_b, 16, 16, 16, bf16, wmma::row_major> b;
+      wmma::load_matrix_sync(b, W + kt * 16 * cols + nt * 16, cols);
+      wmma::mma_sync(acc, a[kt], b, acc);
+    }
+    wmma::store_matrix_sync(Yw + nt * 16, acc, kLd, wmma::mem_row_major);
+  }
+}
+
+// rows of the warp: Xn = bf16(relu(Y))
+__device__ __forceinline__ void relu_store(const float* Yw, bf16* Xn, int warp, int lane) {
+  for (int e = lane; e < 16 * kLd; e += 32) {
+    int r = e / kLd, c = e - r * kLd;
+    Xn[(warp * 16 + r) * kLd + c] = __float2bfloat16_rn(fmaxf(Yw[r * kLd + c], 0.0f));
+  }
+}
+
+// Full forward of the tile's rows owned by this warp; activations h_0..h_5
+// stay in X[0..5] (64x64 bf16 each); output rows left in Yw (fp32, cols 0..15).
+__device__ __forceinline__ void mlp_forward(const bf16* W, bf16* X, float* Yw, int warp, int lane) {
+  for (int l = 0; l < kNrcLayers; ++l) {
+    layer_forward(X + l * kNrcTile * kLd, W + nrc_layer_offset(l), nrc_layer_cols(l), Yw, warp);
+    __syncwarp();
+    if (l < kNrcHidden) relu_store(Yw, X + (l + 1) * kNrcTile * kLd, warp, lane);
+    __syncwarp();
+  }
+}
+
+__device__ __forceinline__ void load_weights(const bf16* __restrict__ g, bf16* s) {
+  const uint4* src = reinterpret_cast<const uint4*>(g);
+  uint4* dst = reinterpret_cast<uint4*>(s);
+  for (int i = threadIdx.x; i < kNrcWeightCount * 2 / 16; i += blockDim.x) dst[i] = src[i];
+}
+
+// ---------------------------------------------------------------------------
+// inference: sum[pix] += throughput * max(cache(x, view, sun), 0)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kNrcThreads) nrc_infer_kernel(NrcView v, const NrcRecord* __restrict__ recs,
+                                                                const uint32_t* __restrict__ count_ptr,
+                                                                uint32_t capacity, double* __restrict__ sum,
+                                                                float* __restrict__ out) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  bf16* W = reinterpret_cast<bf16*>(smem);
+  bf16* X = W + kNrcWeightCount;                                       // 6 activation tiles
+  float* Y = reinterpret_cast<float*>(X + kNrcLayers * kNrcTile * kLd);  // 4 warps x 16 x 64 fp32
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float* Yw = Y + warp * 16 * kLd;
+  load_weights(v.wb, W);
+  __syncthreads();
+  const uint32_t count = min(*count_ptr, capacity);
+  for (uint32_t first = blockIdx.x * kNrcTile; first < count; first += gridDim.x * kNrcTile) {
+    encode_rows(recs, first, count, v, X, warp, lane);
+    __syncwarp();
+    mlp_forward(W, X, Yw, warp, lane);
+    if (lane < 16) {
+      uint32_t idx = first + (uint32_t)(warp * 16 + lane);
+      if (idx < count) {
+        const float* y = Yw + lane * kLd;
+        NrcRecord r = recs[idx];
+        if (out) {
+          out[3 * idx] = y[0];
+          out[3 * idx + 1] = y[1];
+          out[3 * idx + 2] = y[2];
+        }
+        if (sum) {
+          double* o = sum + 3 * (size_t)r.pix;
+          atomicAdd(o + 0, (double)(r.w0 * fmaxf(y[0], 0.0f)));
+          atomicAdd(o + 1, (double)(r.w1 * fmaxf(y[1], 0.0f)));
+          atomicAdd(o + 2, (double)(r.w2 * fmaxf(y[2], 0.0f)));
+        }
+      }
+    }
+    __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// training: relative L2 loss sum_c (y - t)^2 / (sg(y)^2 + 0.01) / (3 B)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kNrcThreads) nrc_train_kernel(NrcView v, const NrcRecord* __restrict__ recs,
+                                                                const uint32_t* __restrict__ count_ptr,
+                                                                uint32_t capacity, float* __restrict__ grad,
+                                                                float* __restrict__ loss) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  bf16* W = reinterpret_cast<bf16*>(smem);
+  bf16* X = W + kNrcWeightCount;                                       // h_0 .. h_5
+  bf16* D = X + kNrcLayers * kNrcTile * kLd;                           // dY ping-pong: 2 x 64x64
+  float* Y = reinterpret_cast<float*>(D + 2 * kNrcTile * kLd);         // 4 x 16 x 64
+  float* G = Y + 4 * 16 * kLd;                                         // dW accumulator [kNrcWeightCount]
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float* Yw = Y + warp * 16 * kLd;
+  load_weights(v.wb, W);
+  for (int i = threadIdx.x; i < kNrcWeightCount; i += blockDim.x) G[i] = 0.0f;
+  __syncthreads();
+  const uint32_t count = min(*count_ptr, capacity);
+  const float inv_n = 1.0f / (3.0f * (float)max(count, 1u));
+  float loss_local = 0.0f;
+  for (uint32_t first = blockIdx.x * kNrcTile; first < count; first += gridDim.x * kNrcTile) {
+    encode_rows(recs, first, count, v, X, warp, lane);
+    __syncwarp();
+    mlp_forward(W, X, Yw, warp, lane);
+    // output gradient (cols 0..2), zero elsewhere and for padding rows
+    bf16* d5 = D;  // dY_5 in buffer 0 (64 x 64, cols 0..15 used)
+    for (int e = lane; e < 16 * kNrcOutPad; e += 32) {
+      int r = e / kNrcOutPad, c = e - r * kNrcOutPad;
+      uint32_t idx = first + (uint32_t)(warp * 16 + r);
+      float gval = 0.0f;
+      if (c < kNrcOut && idx < count) {
+        const NrcRecord& rec = recs[idx];
+        float t = c == 0 ? rec.w0 : (c == 1 ? rec.w1 : rec.w2);
+        float y = Yw[r * kLd + c];
+        float den = y * y + 0.01f;
+        float diff = y - t;
+        loss_local += (diff * diff / den) * inv_n;
+        gval = (2.0f * diff / den) * inv_n;
+      }
+      d5[(warp * 16 + r) * kLd + c] = __float2bfloat16_rn(gval);
+    }
+    __syncthreads();
+    // backward through layers 5..0
+    for (int l = kNrcLayers - 1; l >= 0; --l) {
+      const int cols = nrc_layer_cols(l);
+      const bf16* Xl = X + l * kNrcTile * kLd;
+      bf16* Dl = D + (l & 1 ? 0 : 1) * kNrcTile * kLd;  // l = 5 -> buffer 0
+      if (l == kNrcLayers - 1) Dl = D;
+      // dW_l += X_l^T dY_l : tiles (mt over 64 inputs, nt over cols/16), K = 64 samples
+      const int ntiles = 4 * (cols / 16);
+      for (int tI = warp; tI < ntiles; tI += kNrcThreads / 32) {
+        int mt = tI / (cols / 16), nt = tI - mt * (cols / 16);
+        float* g = G + nrc_layer_offset(l) + mt * 16 * cols + nt * 16;
+        wmma::fragment<wmma::accumulator, 16, 16, 16, float> acc;
+        wmma::load_matrix_sync(acc, g, cols, wmma::mem_row_major);
+        for (int kt = 0; kt < 4; ++kt) {
+          wmma::fragment<wmma::matrix_a, 16, 16, 16, bf16, wmma::col_major> a;  // X_l^T
+          wmma::load_matrix_sync(a, Xl + kt * 16 * kLd + mt * 16, kLd);
+          wmma::fragment<wmma::matrix_b, 16, 16, 16, bf16, wmma::row_major> b;  // dY_l
+          wmma::load_matrix_sync(b, Dl + kt * 16 * kLd + nt * 16, kLd);
+          wmma::mma_sync(acc, a, b, acc);
+        }
+        wmma::store_matrix_sync(g, acc, cols, wmma::mem_row_major);
+      }
+      if (l > 0) {
+        // dY_{l-1} = (dY_l W_l^T) * (h_l > 0), rows of this warp
+        bf16* Dn = (Dl == D) ? D + kNrcTile * kLd : D;
+        const bf16* Wl = W + nrc_layer_offset(l);
+        for (int nt = 0; nt < 4; ++nt) {
+          wmma::fragment<wmma::accumulator, 16, 16, 16, float> acc;
+          wmma::fill_fragment(acc, 0.0f);
+          for (int kt = 0; kt < cols / 16; ++kt) {
+            wmma::fragment<wmma::matrix_a, 16, 16, 16, bf16, wmma::row_major> a;  // dY_l rows
+            wmma::load_matrix_sync(a, Dl + warp * 16 * kLd + kt * 16, kLd);
+            wmma::fragment<wmma::matrix_b, 16, 16, 16, bf16, wmma::col_major> b;  // W_l^T
+            wmma::load_matrix_sync(b, Wl + nt * 16 * cols + kt * 16, cols);
+            wmma::mma_sync(acc, a, b, acc);
+          }
+          wmma::store_matrix_sync(Yw + nt * 16, acc, kLd, wmma::mem_row_major);
+        }
+        __syncwarp();
+        for (int e = lane; e < 16 * kLd; e += 32) {
+          int r = e / kLd, c = e - r * kLd;
+          int row = warp * 16 + r;
+          float mask = __bfloat162float(Xl[row * kLd + c]) > 0.0f ? 1.0f : 0.0f;
+          Dn[row * kLd + c] = __float2bfloat16_rn(Yw[r * kLd + c] * mask);
+        }
+        __syncwarp();
+      }
+      __syncthreads();
+    }
+  }
+  // flush the CTA's gradient and loss
+  for (int i = threadIdx.x; i < kNrcWeightCount; i += blockDim.x) {
+    float gv = G[i];
+    if (gv != 0.0f) atomicAdd(grad + i, gv);
+  }
+  for (int o = 16; o > 0; o >>= 1) loss_local += __shfl_xor_sync(0xffffffffu, loss_local, o);
+  if (lane == 0) atomicAdd(loss, loss_local);
+}
+
+__global__ void nrc_adam_kernel(float* __restrict__ w, bf16* __restrict__ wb, float* __restrict__ m,
+                                float* __restrict__ vv, float* __restrict__ g, float lr, float b1, float b2,
+                                float eps, float c1, float c2) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= kNrcWeightCount) return;
+  float gi = g[i];
+  float mi = b1 * m[i] + (1.0f - b1) * gi;
+  float vi = b2 * vv[i] + (1.0f - b2) * gi * gi;
+  m[i] = mi;
+  vv[i] = vi;
+  float wi = w[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+  w[i] = wi;
+  wb[i] = __float2bfloat16_rn(wi);
+  g[i] = 0.0f;
+}
+
+__global__ void nrc_to_bf16_kernel(const float* __restrict__ w, bf16* __restrict__ wb) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < kNrcWeightCount) wb[i] = __float2bfloat16_rn(w[i]);
+}
+
+// ---------------------------------------------------------------------------
+// training paths: full unbiased paths (DDA free flights, ratio-tracking NEE)
+// recording the radiance leaving each of their first scattering vertices
+// toward the previous vertex: target_i = (L_total - L_before_i) / beta_i.
+// ---------------------------------------------------------------------------
+constexpr int kNrcRecordEvents = 4;
+constexpr uint32_t kNrcTrainSalt = 0x3C6EF372u;
+
+__global__ void __launch_bounds__(128) nrc_train_paths_kernel(GridView g, SceneView s, CamView cam, PassView pv,
+                                                              uint32_t npaths, NrcRecord* __restrict__ out,
+                                                              uint32_t* __restrict__ out_count, uint32_t capacity,
+                                                              Counters cnt) {
+  uint32_t id = blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t lookups = 0, cells = 0, events = 0;
+  if (id < npaths) {
+    Rng rng = rng_pcg(pv.seed ^ kNrcTrainSalt, id, pv.pass);
+    uint32_t pix = (uint32_t)(rng_next(rng) * (float)(pv.cw * pv.ch));
+    pix = min(pix, pv.cw * pv.ch - 1u);
+    int x = (int)(pv.x0 + pix % pv.cw), y = (int)(pv.y0 + pix / pv.cw);
+    f3 pos, dir;
+    camera_ray(cam, x, y, pos, dir);
+    float tmin, tmax;
+    if (slab(pos, dir, s.b0, s.b1, tmin, tmax) && tmax >= 0.0f && s.ds > 0.0f) {
+      pos = along(pos, dir, tmax < tmin ? tmax : tmin);
+      f3 L = mk(0.f, 0.f, 0.f);
+      float beta = 1.0f;
+      NrcRecord rec[kNrcRecordEvents];
+      f3 Lb[kNrcRecordEvents];
+      float bb[kNrcRecordEvents];
+      int nrec = 0;
+      const f3 lsun = -s.sun;
+      while (true) {
+        float t;
+        if (!free_flight(g, s, pos, dir, rng, t, lookups, cells)) {
+          L = L + sky(s, dir) * beta;
+          break;
+        }
+        pos = along(pos, dir, t);
+        if (nrec < kNrcRecordEvents) {
+          NrcRecord& r = rec[nrec];
+          r.px = pos.x; r.py = pos.y; r.pz = pos.z;
+          r.vx = -dir.x; r.vy = -dir.y; r.vz = -dir.z;
+          r.sx = s.sun.x; r.sy = s.sun.y; r.sz = s.sun.z;
+          r.pix = pix;
+          Lb[nrec] = L;
+          bb[nrec] = beta;
+          ++nrec;
+        }
+        ++events;
+        beta = beta * s.albedo;
+        float phase = hg_pdf(s.ph, dot(-dir, s.sun));
+        // ratio-tracking transmittance toward the sun
+        Track tr;
+        track_init(tr, g, s, g.majorants, pos, lsun, cells);
+        float T = 1.0f;
+        while (true) {
+          float tau = -vlog(rng_next(rng));
+          if (track_walk(tr, g, g.majorants, s.k_sigma, tau, cells, 0xFFFFFFFFu) != kCandidate) break;
+          float rho = density_at(g, s, along(pos, lsun, tr.t));
+          ++lookups;
+          T = T * (1.0f - rho / tr.m);
+          if (T < 0.05f) {
+            if (rng_next(rng) >= 0.5f) {
+              T = 0.0f;
+              break;
+            }
+            T = T * 2.0f;
+          }
+        }
+        float c = ((s.light * phase) * T) * beta;
+        L = L + mk(c, c, c);
+        if (s.max_events && events >= s.max_events) break;
+        dir = hg_sample(s.ph, dir, rng, true);
+        if (lookups + cells > kPathWorkCap) break;
+      }
+      if (nrec > 0) {
+        uint32_t base = atomicAdd(out_count, (uint32_t)nrec);
+        for (int i = 0; i < nrec; ++i) {
+          if (base + i >= capacity) break;
+          NrcRecord r = rec[i];
+          float inv = 1.0f / bb[i];
+          r.w0 = (L.x - Lb[i].x) * inv;
+          r.w1 = (L.y - Lb[i].y) * inv;
+          r.w2 = (L.z - Lb[i].z) * inv;
+          out[base + i] = r;
+        }
+      }
+    }
+  }
+  flush_counters(cnt, id < npaths ? 1ull : 0ull, lookups, events, cells);
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+static size_t infer_smem() {
+  return (size_t)kNrcWeightCount * 2 + (size_t)kNrcLayers * kNrcTile * kLd * 2 + 4 * 16 * kLd * 4;
+}
+static size_t train_smem() {
+  return (size_t)kNrcWeightCount * 2 + (size_t)(kNrcLayers + 2) * kNrcTile * kLd * 2 + 4 * 16 * kLd * 4 +
+         (size_t)kNrcWeightCount * 4;
+}
+
+NrcView nrc_view(const vcr_ctx* ctx) {
+  NrcView v;
+  v.wb = reinterpret_cast<const bf16*>(ctx->nrc->wb);
+  const vcr_cloud& c = ctx->cloud;
+  v.b0 = mk(c.bounds_min[0], c.bounds_min[1], c.bounds_min[2]);
+  v.inv_ext = mk(1.0f / (c.bounds_max[0] - c.bounds_min[0]), 1.0f / (c.bounds_max[1] - c.bounds_min[1]),
+                 1.0f / (c.bounds_max[2] - c.bounds_min[2]));
+  return v;
+}
+
+void nrc_free(vcr_ctx* ctx) {
+  NrcState* st = ctx->nrc;
+  if (!st) return;
+  void* ptrs[] = {st->w, st->wb, st->m, st->v, st->grad, st->loss, st->train, st->train_count, st->query,
+                  st->query_count};
+  for (void* p : ptrs) cudaFree(p);
+  delete st;
+  ctx->nrc = nullptr;
+}
+
+// Kaiming-uniform initial weights from a seeded hash (host).
+static void nrc_init_weights(std::vector<float>& w, uint32_t seed) {
+  w.assign(kNrcWeightCount, 0.0f);
+  uint32_t c = 0;
+  for (int l = 0; l < kNrcLayers; ++l) {
+    int cols = nrc_layer_cols(l);
+    float bound = l < kNrcHidden ? sqrtf(6.0f / (float)kNrcWidth) : sqrtf(1.0f / (float)kNrcWidth);
+    for (int i = 0; i < kNrcWidth; ++i)
+      for (int o = 0; o < cols; ++o) {
+        uint32_t hsh = pcg_hash(seed ^ pcg_hash(c++));
+        float u = (float)(hsh >> 8) * 5.96046448e-08f;  // [0,1)
+        w[(size_t)nrc_layer_offset(l) + (size_t)i * cols + o] =
+            (l == kNrcLayers - 1 && o >= kNrcOut) ? 0.0f : (2.0f * u - 1.0f) * bound;
+      }
+  }
+}
+
+vcr_status nrc_setup(vcr_ctx* ctx, const vcr_nrc_params* p) {
+  if (!p || p->train_samples == 0 || p->train_samples > (1u << 22) || !(p->learning_rate > 0.0f) ||
+      p->query_capacity == 0)
+    return fail(ctx, VCR_ERR_INVALID, "nrc params: train_samples 1..2^22, learning_rate > 0, query_capacity > 0");
+  nrc_free(ctx);
+  NrcState* st = new NrcState();
+  ctx->nrc = st;
+  st->prm = *p;
+  st->query_capacity = p->query_capacity;
+#define VCR_ALLOC(ptr, bytes) VCR_CUDA(ctx, cudaMalloc(reinterpret_cast<void**>(&(ptr)), (bytes)))
+  VCR_ALLOC(st->w, kNrcWeightCount * 4);
+  VCR_ALLOC(st->wb, kNrcWeightCount * 2);
+  VCR_ALLOC(st->m, kNrcWeightCount * 4);
+  VCR_ALLOC(st->v, kNrcWeightCount * 4);
+  VCR_ALLOC(st->grad, kNrcWeightCount * 4);
+  VCR_ALLOC(st->loss, 8);
+  VCR_ALLOC(st->train, (size_t)p->train_samples * sizeof(NrcRecord));
+  VCR_ALLOC(st->train_count, 4);
+  VCR_ALLOC(st->query, (size_t)p->query_capacity * sizeof(NrcRecord));
+  VCR_ALLOC(st->query_count, 4);
+#undef VCR_ALLOC
+  std::vector<float> w;
+  nrc_init_weights(w, p->seed);
+  VCR_CUDA(ctx, cudaMemcpy(st->w, w.data(), kNrcWeightCount * 4, cudaMemcpyHostToDevice));
+  VCR_CUDA(ctx, cudaMemset(st->m, 0, kNrcWeightCount * 4));
+  VCR_CUDA(ctx, cudaMemset(st->v, 0, kNrcWeightCount * 4));
+  VCR_CUDA(ctx, cudaMemset(st->grad, 0, kNrcWeightCount * 4));
+  VCR_CUDA(ctx, cudaMemset(st->query_count, 0, 4));
+  nrc_to_bf16_kernel<<<(kNrcWeightCount + 255) / 256, 256>>>(st->w, reinterpret_cast<bf16*>(st->wb));
+  VCR_CUDA(ctx, cudaGetLastError());
+  VCR_CUDA(ctx, cudaFuncSetAttribute(nrc_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)infer_smem()));
+  VCR_CUDA(ctx, cudaFuncSetAttribute(nrc_train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)train_smem()));
+  return VCR_OK;
+}
+
+// Gradient of the loss over `count` records (device), accumulated into grad.
+vcr_status nrc_accumulate_grad(vcr_ctx* ctx, const NrcRecord* recs, const uint32_t* d_count, uint32_t capacity,
+                               cudaStream_t s) {
+  NrcState* st = ctx->nrc;
+  VCR_CUDA(ctx, cudaFuncSetAttribute(nrc_train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)train_smem()));
+  VCR_CUDA(ctx, cudaMemsetAsync(st->loss, 0, 8, s));
+  int blocks = ctx->sm_count;
+  nrc_train_kernel<<<blocks, kNrcThreads, train_smem(), s>>>(nrc_view(ctx), recs, d_count, capacity, st->grad,
+                                                            st->loss);
+  VCR_CUDA(ctx, cudaGetLastError());
+  return VCR_OK;
+}
+
+vcr_status nrc_adam(vcr_ctx* ctx, cudaStream_t s) {
+  NrcState* st = ctx->nrc;
+  st->step += 1;
+  const float b1 = 0.9f, b2 = 0.99f, eps = 1e-8f;
+  float c1 = 1.0f - (float)std::pow(0.9, (double)st->step);
+  float c2 = 1.0f - (float)std::pow(0.99, (double)st->step);
+  nrc_adam_kernel<<<(kNrcWeightCount + 255) / 256, 256, 0, s>>>(st->w, reinterpret_cast<bf16*>(st->wb), st->m, st->v,
+                                                                st->grad, st->prm.learning_rate, b1, b2, eps, c1, c2);
+  VCR_CUDA(ctx, cudaGetLastError());
+  return VCR_OK;
+}
+
+uint32_t nrc_query_capacity(const vcr_ctx* ctx) { return ctx->nrc ? ctx->nrc->query_capacity : 0u; }
+
+vcr_status nrc_reset_queries(vcr_ctx* ctx, cudaStream_t s) {
+  VCR_CUDA(ctx, cudaMemsetAsync(ctx->nrc->query_count, 0, 4, s));
+  return VCR_OK;
+}
+
+vcr_status nrc_infer_queries(vcr_ctx* ctx, cudaStream_t s) {
+  NrcState* st = ctx->nrc;
+  VCR_CUDA(ctx, cudaFuncSetAttribute(nrc_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)infer_smem()));
+  int per_sm = 0;
+  VCR_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, nrc_infer_kernel, kNrcThreads, infer_smem()));
+  int blocks = ctx->sm_count * std::max(per_sm, 1);
+  nrc_infer_kernel<<<blocks, kNrcThreads, infer_smem(), s>>>(nrc_view(ctx), st->query, st->query_count,
+                                                            st->query_capacity, ctx->d_sum, nullptr);
+  VCR_CUDA(ctx, cudaGetLastError());
+  return VCR_OK;
+}
+
+vcr_status nrc_train_step(vcr_ctx* ctx, const vcr_pass_desc* pass, cudaStream_t s) {
+  NrcState* st = ctx->nrc;
+  if (!st) return fail(ctx, VCR_ERR_STATE, "vcr_nrc_train_step needs vcr_nrc_setup");
+  if (!ctx->has_grid || !ctx->has_cloud || !ctx->has_cam || !ctx->has_params || !ctx->d_sum)
+    return fail(ctx, VCR_ERR_STATE, "vcr_nrc_train_step needs a grid, cloud, camera, params and frame");
+  PassView pv;
+  vcr_status vs = make_pass_view(ctx, pass, pv);
+  if (vs) return vs;
+  GridView g = grid_view(ctx);
+  SceneView sc = scene_view(ctx);
+  Counters cnt{ctx->d_counters};
+  const uint32_t cap = st->prm.train_samples;
+  const uint32_t npaths = std::max(1u, cap / 2);  // about two recorded vertices per training path
+  VCR_CUDA(ctx, cudaMemsetAsync(st->train_count, 0, 4, s));
+  VCR_CUDA(ctx, cudaMemsetAsync(ctx->d_counters, 0, 5 * sizeof(unsigned long long), s));
+  nrc_train_paths_kernel<<<(npaths + 127) / 128, 128, 0, s>>>(g, sc, cam_view(ctx->cam), pv, npaths, st->train,
+                                                              st->train_count, cap, cnt);
+  VCR_CUDA(ctx, cudaGetLastError());
+  vs = nrc_accumulate_grad(ctx, st->train, st->train_count, cap, s);
+  if (vs) return vs;
+  vs = nrc_adam(ctx, s);
+  if (vs) return vs;
+  VCR_CUDA(ctx, cudaEventRecord(ctx->work_done, s));
+  return VCR_OK;
+}
+
+}  // namespace vcr
+
+using namespace vcr;
+
+extern "C" VCR_API vcr_status vcr_nrc_setup(vcr_ctx* ctx, const vcr_nrc_params* p) {
+  if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
+  vcr_status st = nrc_setup(ctx, p);
+  if (st) return st;
+  VCR_CUDA(ctx, cudaDeviceSynchronize());
+  return VCR_OK;
+}
+
+extern "C" VCR_API vcr_status vcr_nrc_free(vcr_ctx* ctx) {
+  if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  cudaDeviceSynchronize();
+  nrc_free(ctx);
+  return VCR_OK;
+}
+
+extern "C" VCR_API vcr_status vcr_nrc_train_step(vcr_ctx* ctx, const vcr_pass_desc* pass, void* stream) {
+  if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  if (!pass) return fail(ctx, VCR_ERR_INVALID, "null pass");
+  return nrc_train_step(ctx, pass, (cudaStream_t)stream);
+}
+
+extern "C" VCR_API vcr_status vcr_nrc_info(vcr_ctx* ctx, vcr_nrc_info_t* out) {
+  if (!ctx || !out) return fail(ctx, VCR_ERR_INVALID, "null argument");
+  NrcState* st = ctx->nrc;
+  if (!st) return fail(ctx, VCR_ERR_STATE, "no radiance cache");
+  VCR_CUDA(ctx, cudaEventSynchronize(ctx->work_done));
+  float loss = 0.0f;
+  uint32_t ntrain = 0, nq = 0;
+  VCR_CUDA(ctx, cudaMemcpy(&loss, st->loss, 4, cudaMemcpyDeviceToHost));
+  VCR_CUDA(ctx, cudaMemcpy(&ntrain, st->train_count, 4, cudaMemcpyDeviceToHost));
+  VCR_CUDA(ctx, cudaMemcpy(&nq, st->query_count, 4, cudaMemcpyDeviceToHost));
+  out->steps = st->step;
+  out->last_loss = loss;
+  out->train_records = std::min(ntrain, st->prm.train_samples);
+  out->queries = std::min(nq, st->query_capacity);
+  out->weights = kNrcWeightCount;
+  return VCR_OK;
+}
+
+// Weights: FP32 master copy in the layer layout of vcr_nrc_params.
+extern "C" VCR_API vcr_status vcr_nrc_get_weights(vcr_ctx* ctx, float* host, size_t count) {
+  if (!ctx || !host) return fail(ctx, VCR_ERR_INVALID, "null argument");
+  if (!ctx->nrc) return fail(ctx, VCR_ERR_STATE, "no radiance cache");
+  if (count != (size_t)kNrcWeightCount) return fail(ctx, VCR_ERR_INVALID, "the cache has %d weights", kNrcWeightCount);
+  VCR_CUDA(ctx, cudaEventSynchronize(ctx->work_done));
+  VCR_CUDA(ctx, cudaMemcpy(host, ctx->nrc->w, count * 4, cudaMemcpyDeviceToHost));
+  return VCR_OK;
+}
+
+extern "C" VCR_API vcr_status vcr_nrc_set_weights(vcr_ctx* ctx, const float* host, size_t count) {
+  if (!ctx || !host) return fail(ctx, VCR_ERR_INVALID, "null argument");
+  if (!ctx->nrc) return fail(ctx, VCR_ERR_STATE, "no radiance cache");
+  if (count != (size_t)kNrcWeightCount) return fail(ctx, VCR_ERR_INVALID, "the cache has %d weights", kNrcWeightCount);
+  VCR_CUDA(ctx, cudaMemcpy(ctx->nrc->w, host, count * 4, cudaMemcpyHostToDevice));
+  nrc_to_bf16_kernel<<<(kNrcWeightCount + 255) / 256, 256>>>(ctx->nrc->w, reinterpret_cast<bf16*>(ctx->nrc->wb));
+  VCR_CUDA(ctx, cudaGetLastError());
+  VCR_CUDA(ctx, cudaDeviceSynchronize());
+  return VCR_OK;
+}
+
+// Evaluate the cache on n records (device NrcRecord array, 64 B each);
+// writes 3 floats per record to d_out.  For tests and tools.
+extern "C" VCR_API vcr_status vcr_nrc_forward(vcr_ctx* ctx, const void* d_records, uint32_t n, float* d_out,
+                                              void* stream) {
+  if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  if (!ctx->nrc) return fail(ctx, VCR_ERR_STATE, "no radiance cache");
+  if (n == 0) return VCR_OK;
+  if (!d_records || !d_out) return fail(ctx, VCR_ERR_INVALID, "null buffer");
+  if (!ctx->has_cloud) return fail(ctx, VCR_ERR_STATE, "the encoding needs the cloud box (vcr_set_cloud)");
+  cudaStream_t s = (cudaStream_t)stream;
+  vcr_status vs = ensure_scratch(ctx, 4);
+  if (vs) return vs;
+  uint32_t* d_n = reinterpret_cast<uint32_t*>(ctx->d_scratch);
+  VCR_CUDA(ctx, cudaMemcpyAsync(d_n, &n, 4, cudaMemcpyHostToDevice, s));
+  VCR_CUDA(ctx, cudaFuncSetAttribute(nrc_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)infer_smem()));
+  nrc_infer_kernel<<<ctx->sm_count, kNrcThreads, infer_smem(), s>>>(
+      nrc_view(ctx), reinterpret_cast<const NrcRecord*>(d_records), d_n, n, nullptr, d_out);
+  VCR_CUDA(ctx, cudaGetLastError());
+  VCR_CUDA(ctx, cudaStreamSynchronize(s));
+  return VCR_OK;
+}
+
+// `steps` Adam steps on n caller records (targets in w0..w2).
+extern "C" VCR_API vcr_status vcr_nrc_fit(vcr_ctx* ctx, const void* d_records, uint32_t n, uint32_t steps,
+                                          void* stream) {
+  if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  if (!ctx->nrc) return fail(ctx, VCR_ERR_STATE, "no radiance cache");
+  if (!d_records || n == 0) return fail(ctx, VCR_ERR_INVALID, "bad fit arguments");
+  if (!ctx->has_cloud) return fail(ctx, VCR_ERR_STATE, "the encoding needs the cloud box (vcr_set_cloud)");
+  cudaStream_t s = (cudaStream_t)stream;
+  vcr_status vs = ensure_scratch(ctx, 4);
+  if (vs) return vs;
+  uint32_t* d_n = reinterpret_cast<uint32_t*>(ctx->d_scratch);
+  VCR_CUDA(ctx, cudaMemcpyAsync(d_n, &n, 4, cudaMemcpyHostToDevice, s));
+  for (uint32_t k = 0; k < steps; ++k) {
+    vs = nrc_accumulate_grad(ctx, reinterpret_cast<const NrcRecord*>(d_records), d_n, n, s);
+    if (vs) return vs;
+    vs = nrc_adam(ctx, s);
+    if (vs) return vs;
+  }
+  VCR_CUDA(ctx, cudaEventRecord(ctx->work_done, s));
+  return VCR_OK;
+}
+
+// Loss gradient over n records (targets in w0..w2), without an update:
+// copies the gradient to host (count = weight count) and returns the loss.
+extern "C" VCR_API vcr_status vcr_nrc_gradient(vcr_ctx* ctx, const void* d_records, uint32_t n, float* host_grad,
+                                               size_t count, float* out_loss) {
+  if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  if (!ctx->nrc) return fail(ctx, VCR_ERR_STATE, "no radiance cache");
+  if (!d_records || !host_grad || count != (size_t)kNrcWeightCount || n == 0)
+    return fail(ctx, VCR_ERR_INVALID, "bad gradient arguments");
+  if (!ctx->has_cloud) return fail(ctx, VCR_ERR_STATE, "the encoding needs the cloud box (vcr_set_cloud)");
+  vcr_status vs = ensure_scratch(ctx, 4);
+  if (vs) return vs;
+  uint32_t* d_n = reinterpret_cast<uint32_t*>(ctx->d_scratch);
+  VCR_CUDA(ctx, cudaMemcpy(d_n, &n, 4, cudaMemcpyHostToDevice));
+  VCR_CUDA(ctx, cudaMemset(ctx->nrc->grad, 0, kNrcWeightCount * 4));
+  vs = nrc_accumulate_grad(ctx, reinterpret_cast<const NrcRecord*>(d_records), d_n, n, 0);
+  if (vs) return vs;
+  VCR_CUDA(ctx, cudaDeviceSynchronize());
+  VCR_CUDA(ctx, cudaMemcpy(host_grad, ctx->nrc->grad, count * 4, cudaMemcpyDeviceToHost));
+  if (out_loss) VCR_CUDA(ctx, cudaMemcpy(out_loss, ctx->nrc->loss, 4, cudaMemcpyDeviceToHost));
+  VCR_CUDA(ctx, cudaMemset(ctx->nrc->grad, 0, kNrcWeightCount * 4));
+  return VCR_OK;
+}

@@ -1,0 +1,111 @@
+// Radiance-cache network: encoding, sizes and state (no counterpart in the
+// reference; the target adds it on top of the path tracer).
+#pragma once
+
+#include "vcr_internal.h"
+
+namespace vcr {
+
+constexpr int kNrcIn = 64;       // 32 position + 16 view SH + 16 sun SH
+constexpr int kNrcWidth = 64;
+constexpr int kNrcHidden = 5;    // hidden layers (ReLU)
+constexpr int kNrcLayers = 6;    // weight matrices: 5 x (64x64) + output (64x16, 3 used)
+constexpr int kNrcOut = 3;
+constexpr int kNrcOutPad = 16;
+constexpr int kNrcPosLevels = 16;
+constexpr int kNrcWeightCount = kNrcHidden * kNrcWidth * kNrcWidth + kNrcWidth * kNrcOutPad;  // 21504
+constexpr int kNrcTile = 64;     // samples per CTA tile (4 warps x 16 rows)
+
+// One query / training record: the position of a real collision, the
+// direction radiance leaves toward the previous vertex, the sun direction.
+struct NrcRecord {
+  float px, py, pz;  // world position
+  float vx, vy, vz;  // unit direction toward the viewer (-travel direction)
+  float sx, sy, sz;  // unit direction the sunlight travels
+  float w0, w1, w2;  // query: path throughput (rgb); training: target radiance
+  uint32_t pix;      // query: pixel index; training: unused
+  uint32_t pad[3];
+};
+static_assert(sizeof(NrcRecord) == 64, "record size");
+
+struct NrcState {
+  vcr_nrc_params prm{};
+  float* w = nullptr;        // FP32 master weights [kNrcWeightCount]
+  void* wb = nullptr;        // BF16 copy used by the kernels
+  float* m = nullptr;        // Adam first moment
+  float* v = nullptr;        // Adam second moment
+  float* grad = nullptr;     // gradient accumulator [kNrcWeightCount]
+  float* loss = nullptr;     // [2]: loss sum, sample count of the last step
+  NrcRecord* train = nullptr;  // training records [train_samples]
+  uint32_t* train_count = nullptr;
+  NrcRecord* query = nullptr;  // cache queries of one pass [query_capacity]
+  uint32_t* query_count = nullptr;
+  uint32_t query_capacity = 0;
+  uint32_t step = 0;
+  float last_loss = 0.0f;
+  uint32_t last_train = 0, last_queries = 0;
+};
+
+// Position encoding: level l uses frequency 2^(l/2) cycles per unit box
+// along a fixed unit direction d_l (a spherical Fibonacci set), giving
+// (sin, cos)(2 pi 2^(l/2) d_l . p) with p in [0,1]^3 box coordinates.
+// Directions: real spherical harmonics of degree 3 (16 coefficients, bands
+// 0..3) with the usual normalisation constants.
+__host__ __device__ __forceinline__ void nrc_level_dir(int l, float& dx, float& dy, float& dz) {
+  // spherical Fibonacci point l of 16 (fixed constants, same on host and device)
+  const float z = 1.0f - (2.0f * (float)l + 1.0f) / 16.0f;
+  const float r = sqrtf(fmaxf(0.0f, 1.0f - z * z));
+  float t = 0.61803398875f * (float)l;  // golden-ratio turns
+  t = t - floorf(t);
+  float sn, cs;
+  vsincos2pi(t, &sn, &cs);
+  dx = r * cs;
+  dy = r * sn;
+  dz = z;
+}
+
+__host__ __device__ __forceinline__ void nrc_sh16(float x, float y, float z, float* o) {
+  const float xx = x * x, yy = y * y, zz = z * z;
+  o[0] = 0.28209479177f;
+  o[1] = -0.48860251190f * y;
+  o[2] = 0.48860251190f * z;
+  o[3] = -0.48860251190f * x;
+  o[4] = 1.09254843059f * (x * y);
+  o[5] = -1.09254843059f * (y * z);
+  o[6] = 0.31539156525f * (3.0f * zz - 1.0f);
+  o[7] = -1.09254843059f * (x * z);
+  o[8] = 0.54627421529f * (xx - yy);
+  o[9] = -0.59004358993f * y * (3.0f * xx - yy);
+  o[10] = 2.89061144264f * (x * y) * z;
+  o[11] = -0.45704579946f * y * (5.0f * zz - 1.0f);
+  o[12] = 0.37317633259f * z * (5.0f * zz - 3.0f);
+  o[13] = -0.45704579946f * x * (5.0f * zz - 1.0f);
+  o[14] = 1.44530572132f * z * (xx - yy);
+  o[15] = -0.59004358993f * x * (xx - 3.0f * yy);
+}
+
+// 64 encoded inputs of one record.  `b0`, `inv_ext` map world positions to
+// [0,1]^3 box coordinates.
+__host__ __device__ __forceinline__ void nrc_encode(const NrcRecord& r, f3 b0, f3 inv_ext, float* o) {
+  float ux = (r.px - b0.x) * inv_ext.x, uy = (r.py - b0.y) * inv_ext.y, uz = (r.pz - b0.z) * inv_ext.z;
+  for (int l = 0; l < kNrcPosLevels; ++l) {
+    float dx, dy, dz;
+    nrc_level_dir(l, dx, dy, dz);
+    float f = (float)(1u << (l >> 1)) * ((l & 1) ? 1.41421356f : 1.0f);
+    float ph = f * ((dx * ux + dy * uy) + dz * uz);
+    ph = ph - floorf(ph);
+    float sn, cs;
+    vsincos2pi(ph, &sn, &cs);
+    o[2 * l] = sn;
+    o[2 * l + 1] = cs;
+  }
+  nrc_sh16(r.vx, r.vy, r.vz, o + 32);
+  nrc_sh16(r.sx, r.sy, r.sz, o + 48);
+}
+
+// Layer l weights start at this offset; hidden layers are [in][out] = 64x64
+// row-major, the output layer 64 x 16 (columns 3..15 stay zero).
+__host__ __device__ constexpr int nrc_layer_offset(int l) { return l * kNrcWidth * kNrcWidth; }
+__host__ __device__ constexpr int nrc_layer_cols(int l) { return l < kNrcHidden ? kNrcWidth : kNrcOutPad; }
+
+}  // namespace vcr

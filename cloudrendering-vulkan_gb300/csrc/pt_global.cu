@@ -161,8 +161,19 @@ vcr_status pt_pass_launch(vcr_ctx* ctx, const vcr_pass_desc* pass, cudaStream_t 
   } else {
     if (P.rng_mode != VCR_RNG_PCG || P.nee_mode != VCR_NEE_RATIO)
       return fail(ctx, VCR_ERR_UNSUPPORTED, "the DDA tracker implements PCG streams with ratio-tracking NEE");
+    if (s.nrc_events) {
+      if (total64 > nrc_query_capacity(ctx))
+        return fail(ctx, VCR_ERR_CAPACITY, "the radiance cache holds %u queries, the pass has %llu paths",
+                    nrc_query_capacity(ctx), (unsigned long long)total64);
+      vcr_status qs = nrc_reset_queries(ctx, st);
+      if (qs) return qs;
+    }
     vcr_status ws = wavefront_launch(ctx, g, s, cam, pv, stats, cnt, (uint32_t)total64, st);
     if (ws) return ws;
+    if (s.nrc_events) {  // add throughput x cache prediction where paths ended
+      ws = nrc_infer_queries(ctx, st);
+      if (ws) return ws;
+    }
   }
   VCR_CUDA(ctx, cudaGetLastError());
   VCR_CUDA(ctx, cudaEventRecord(ctx->work_done, st));

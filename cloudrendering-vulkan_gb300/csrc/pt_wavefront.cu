@@ -17,8 +17,16 @@
 // DDA cell visit reads shared memory.  The arithmetic per path is identical
 // to the oracle's sequential loop, so results are bit-exact with it.
 #include "track.cuh"
+#include "nrc.cuh"
 
 namespace vcr {
+
+// Where paths that end in the radiance cache leave their query.
+struct NrcSink {
+  NrcRecord* rec;
+  uint32_t* count;
+  uint32_t capacity;
+};
 
 constexpr uint32_t kMbarSpin = 1u << 24;  // bounded mbarrier wait
 
@@ -94,7 +102,7 @@ template <int kThreads, bool kStage>
 __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
     pt_wavefront_kernel(GridView g, SceneView s, CamView cam, PassView pv, double* __restrict__ sum,
                         uint32_t* __restrict__ stats, Counters cnt, uint32_t total, uint32_t dda_steps,
-                        uint32_t maj_bytes, int* __restrict__ err) {
+                        uint32_t maj_bytes, NrcSink nq, int* __restrict__ err) {
   extern __shared__ __align__(16) float s_maj[];
   __shared__ __align__(8) uint64_t s_bar;
   const float* maj = g.majorants;
@@ -176,12 +184,28 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
             if (xi < rho / tr.m) {  // real collision: start the NEE ray
               pos = p;
               ++events;
-              beta = beta * s.albedo;
-              phase = hg_pdf(s.ph, dot(-dir, s.sun));
-              T = 1.0f;
-              mode = kNee;
-              idir = lsun;
-              need_init = true;
+              if (s.nrc_events && events == s.nrc_events) {
+                // end in the radiance cache: it predicts what leaves this vertex
+                finish = true;
+                uint32_t q = atomicAdd(nq.count, 1u);
+                if (q < nq.capacity) {
+                  NrcRecord r;
+                  r.px = pos.x; r.py = pos.y; r.pz = pos.z;
+                  r.vx = -dir.x; r.vy = -dir.y; r.vz = -dir.z;
+                  r.sx = s.sun.x; r.sy = s.sun.y; r.sz = s.sun.z;
+                  r.w0 = beta; r.w1 = beta; r.w2 = beta;
+                  r.pix = pix;
+                  r.pad[0] = r.pad[1] = r.pad[2] = 0u;
+                  nq.rec[q] = r;
+                }
+              } else {
+                beta = beta * s.albedo;
+                phase = hg_pdf(s.ph, dot(-dir, s.sun));
+                T = 1.0f;
+                mode = kNee;
+                idir = lsun;
+                need_init = true;
+              }
             }
           } else {
             T = T * (1.0f - rho / tr.m);
@@ -252,8 +276,10 @@ static vcr_status launch_t(vcr_ctx* ctx, const GridView& g, const SceneView& s, 
   uint32_t blocks = (uint32_t)(ctx->sm_count * per_sm);
   uint32_t need = (total + kThreads - 1) / kThreads;
   if (blocks > need) blocks = need;
+  NrcSink nq{nullptr, nullptr, 0u};
+  if (s.nrc_events && ctx->nrc) nq = NrcSink{ctx->nrc->query, ctx->nrc->query_count, ctx->nrc->query_capacity};
   kern<<<blocks, kThreads, smem, st>>>(g, s, cam, pv, ctx->d_sum, stats, cnt, total, ctx->tuning.dda_steps,
-                                       maj_bytes, ctx->d_error);
+                                       maj_bytes, nq, ctx->d_error);
   VCR_CUDA(ctx, cudaGetLastError());
   return VCR_OK;
 }

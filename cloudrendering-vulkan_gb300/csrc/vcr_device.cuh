@@ -42,6 +42,7 @@ struct SceneView {
   f3 sky;
   int sky_mode, rng_mode, nee_mode, tracker;
   uint32_t max_events;
+  uint32_t nrc_events;  // > 0: paths end in the radiance cache at this event
 };
 
 #if defined(__CUDACC__)

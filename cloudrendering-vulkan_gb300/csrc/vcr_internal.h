@@ -109,6 +109,11 @@ void ppb_free(vcr_ctx* ctx);
 void ppm_free(vcr_ctx* ctx);
 void nrc_free(vcr_ctx* ctx);
 
+// nrc.cu: queries of paths that end in the radiance cache
+uint32_t nrc_query_capacity(const vcr_ctx* ctx);
+vcr_status nrc_reset_queries(vcr_ctx* ctx, cudaStream_t s);
+vcr_status nrc_infer_queries(vcr_ctx* ctx, cudaStream_t s);
+
 // sv.cu
 vcr_status sv_build_launch(vcr_ctx* ctx, const vcr_shadow_volume* sv, cudaStream_t s);
 

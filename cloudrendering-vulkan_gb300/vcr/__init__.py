@@ -189,6 +189,47 @@ class Context:
     def synchronize(self):
         self._ck(lib().vcr_synchronize(self.h))
 
+    # radiance cache ---------------------------------------------------------
+    NRC_WEIGHTS = 21504
+
+    def nrc_setup(self, train_samples=65536, learning_rate=1e-3, query_capacity=1 << 21, seed=1):
+        p = _abi.NrcParams(train_samples, learning_rate, query_capacity, seed)
+        self._ck(lib().vcr_nrc_setup(self.h, C.byref(p)))
+
+    def nrc_free(self):
+        self._ck(lib().vcr_nrc_free(self.h))
+
+    def nrc_train_step(self, seed=0, pass_index=0, stream=0):
+        p = _abi.PassDesc()
+        p.seed, p.pass_index, p.spp = seed, pass_index, 1
+        self._ck(lib().vcr_nrc_train_step(self.h, C.byref(p), C.c_void_p(stream)))
+
+    def nrc_info(self) -> dict:
+        i = _abi.NrcInfo()
+        self._ck(lib().vcr_nrc_info(self.h, C.byref(i)))
+        return {f: getattr(i, f) for f, _ in _abi.NrcInfo._fields_}
+
+    def nrc_get_weights(self) -> np.ndarray:
+        w = np.empty(self.NRC_WEIGHTS, np.float32)
+        self._ck(lib().vcr_nrc_get_weights(self.h, _ptr(w), w.size))
+        return w
+
+    def nrc_set_weights(self, w) -> None:
+        w = np.ascontiguousarray(w, np.float32)
+        self._ck(lib().vcr_nrc_set_weights(self.h, _ptr(w), w.size))
+
+    def nrc_forward(self, d_records, n, d_out, stream=0):
+        self._ck(lib().vcr_nrc_forward(self.h, C.c_void_p(d_records), n, C.c_void_p(d_out), C.c_void_p(stream)))
+
+    def nrc_fit(self, d_records, n, steps, stream=0):
+        self._ck(lib().vcr_nrc_fit(self.h, C.c_void_p(d_records), n, steps, C.c_void_p(stream)))
+
+    def nrc_gradient(self, d_records, n):
+        g = np.empty(self.NRC_WEIGHTS, np.float32)
+        loss = C.c_float()
+        self._ck(lib().vcr_nrc_gradient(self.h, C.c_void_p(d_records), n, _ptr(g), g.size, C.byref(loss)))
+        return g, loss.value
+
     # photon mapping ---------------------------------------------------------
     def ppm_setup(self, photons, capacity, radius, alpha=0.7):
         p = _abi.PpmParams(photons, capacity, radius, alpha)

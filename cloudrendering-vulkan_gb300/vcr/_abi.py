@@ -63,6 +63,16 @@ class Tuning(C.Structure):
                 ("block_threads", C.c_uint32)]
 
 
+class NrcParams(C.Structure):
+    _fields_ = [("train_samples", C.c_uint32), ("learning_rate", C.c_float), ("query_capacity", C.c_uint32),
+                ("seed", C.c_uint32)]
+
+
+class NrcInfo(C.Structure):
+    _fields_ = [("steps", C.c_uint32), ("last_loss", C.c_float), ("train_records", C.c_uint32),
+                ("queries", C.c_uint32), ("weights", C.c_uint32)]
+
+
 class PpmParams(C.Structure):
     _fields_ = [("photons", C.c_uint32), ("capacity", C.c_uint32), ("radius", C.c_float), ("alpha", C.c_float)]
 
@@ -132,6 +142,15 @@ SIGNATURES = {
     "vcr_pt_pass": (_S, [_P, C.POINTER(PassDesc), _P]),
     "vcr_pt_counters": (_S, [_P, C.POINTER(_u64)]),
     "vcr_dda_trace": (_S, [_P, _P, _P, _u32, _u32, _P, _P, _P, _P]),
+    "vcr_nrc_setup": (_S, [_P, C.POINTER(NrcParams)]),
+    "vcr_nrc_free": (_S, [_P]),
+    "vcr_nrc_train_step": (_S, [_P, C.POINTER(PassDesc), _P]),
+    "vcr_nrc_info": (_S, [_P, C.POINTER(NrcInfo)]),
+    "vcr_nrc_get_weights": (_S, [_P, _P, _sz]),
+    "vcr_nrc_set_weights": (_S, [_P, _P, _sz]),
+    "vcr_nrc_forward": (_S, [_P, _P, _u32, _P, _P]),
+    "vcr_nrc_gradient": (_S, [_P, _P, _u32, _P, _sz, C.POINTER(_f)]),
+    "vcr_nrc_fit": (_S, [_P, _P, _u32, _u32, _P]),
     "vcr_ppm_setup": (_S, [_P, C.POINTER(PpmParams)]),
     "vcr_ppm_free": (_S, [_P]),
     "vcr_ppm_pass": (_S, [_P, C.POINTER(PassDesc), _P]),

@@ -322,6 +322,57 @@ VCR_API vcr_status vcr_dda_trace(vcr_ctx* ctx, const float* d_origin, const floa
                                  float* d_out_t, uint32_t* d_out_count, void* stream);
 
 /* ------------------------------------------------------------------------ */
+/* Neural radiance cache (no reference counterpart)                         */
+/* ------------------------------------------------------------------------ */
+/* A 64 -> 5 x 64 (ReLU) -> 3 MLP, BF16 weights and activations with FP32
+ * accumulation on tensor cores, no biases.  Inputs: a 16-level frequency
+ * encoding of the box position (per level sin and cos of 2 pi f_l d_l . p,
+ * f_l = 2^(l/2), d_l a fixed spherical Fibonacci direction) and real
+ * spherical harmonics of 4 bands (l = 0..3, 16 coefficients: "degree 4"
+ * counted in bands) of the view and sun directions.  Output: radiance
+ * leaving a scattering vertex toward the
+ * viewer.  Weight layout: 5 hidden matrices [in][out] 64x64 row-major, then
+ * the output matrix [64][16] (columns 3..15 zero), 21504 floats. */
+typedef struct vcr_nrc_params {
+  uint32_t train_samples;  /* training records per step (65,536 in the NRC configuration) */
+  float learning_rate;     /* Adam step size (1e-3) */
+  uint32_t query_capacity; /* cache queries per pass (>= paths of a pass) */
+  uint32_t seed;           /* weight initialisation */
+} vcr_nrc_params;
+
+typedef struct vcr_nrc_info_t {
+  uint32_t steps;         /* Adam steps taken */
+  float last_loss;        /* relative L2 loss of the last step */
+  uint32_t train_records; /* training records of the last step */
+  uint32_t queries;       /* cache queries of the last pass */
+  uint32_t weights;       /* parameter count */
+} vcr_nrc_info_t;
+
+VCR_API vcr_status vcr_nrc_setup(vcr_ctx* ctx, const vcr_nrc_params* p);
+VCR_API vcr_status vcr_nrc_free(vcr_ctx* ctx);
+/* One online training step: training paths from the current camera
+ * (unbiased, full length) record the radiance leaving their first
+ * scattering vertices; the fused kernel computes the relative L2 loss
+ * gradient; Adam updates the weights.  With vcr_params.nrc_events = k > 0,
+ * vcr_pt_pass (DDA tracker) ends paths at their k-th scattering event and
+ * adds throughput x cache prediction there. */
+VCR_API vcr_status vcr_nrc_train_step(vcr_ctx* ctx, const vcr_pass_desc* pass, void* stream);
+VCR_API vcr_status vcr_nrc_info(vcr_ctx* ctx, vcr_nrc_info_t* out);
+VCR_API vcr_status vcr_nrc_get_weights(vcr_ctx* ctx, float* host_out, size_t count);
+VCR_API vcr_status vcr_nrc_set_weights(vcr_ctx* ctx, const float* host, size_t count);
+/* Cache predictions for n device records (64-byte records: position,
+ * direction toward the viewer, sun direction as float3 each, then 3 floats
+ * and 4 words unused here); 3 floats per record. */
+VCR_API vcr_status vcr_nrc_forward(vcr_ctx* ctx, const void* d_records, uint32_t n, float* d_out, void* stream);
+/* `steps` Adam steps on n caller-provided device records (the 3 floats
+ * after the directions are the targets): offline fitting and warm starts. */
+VCR_API vcr_status vcr_nrc_fit(vcr_ctx* ctx, const void* d_records, uint32_t n, uint32_t steps, void* stream);
+/* Loss gradient over n device records (the 3 floats after the directions
+ * are the targets) without a weight update; synchronous. */
+VCR_API vcr_status vcr_nrc_gradient(vcr_ctx* ctx, const void* d_records, uint32_t n, float* host_grad,
+                                    size_t count, float* out_loss);
+
+/* ------------------------------------------------------------------------ */
 /* Volumetric progressive photon mapping (RenderTechniquePPM)               */
 /* ------------------------------------------------------------------------ */
 typedef struct vcr_ppm_params {

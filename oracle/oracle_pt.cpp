@@ -407,6 +407,7 @@ V3 trace_path(const Scene& s, const vcr_camera& cam, int x, int y, Rng& rng, Cou
     if (c.lookups + c.cells > kPathWorkCap) break;
     pos = p;
     ++c.events;
+    if (s.nrc_events && c.events == s.nrc_events) break;  // ends in the radiance cache (added separately)
     beta = beta * s.albedo;
     float phase = hg_pdf(s, dot(neg(dir), s.sun));
     float T = 1.0f;
@@ -460,6 +461,7 @@ Scene make_scene(const Grid* g, const vcr_cloud& cl, const vcr_params& p, const 
   s.nee_mode = p.nee_mode;
   s.tracker = p.tracker;
   s.max_events = p.max_events;
+  s.nrc_events = p.nrc_events;
   if (sv && sv_tex) {
     s.sv_tex = sv_tex;
     s.sv_n = (int)sv->voxel_axis_count;

@@ -38,6 +38,7 @@ struct Scene {
   float albedo, light;
   V3 sun, sky;
   uint32_t sky_mode, rng_mode, nee_mode, tracker, max_events;
+  uint32_t nrc_events = 0;  // > 0: paths end at this event (radiance cache)
   const float* sv_tex = nullptr;  // shadow volume (reference-parity NEE)
   int sv_n = 0;
   V3 sv_b0, sv_ext;

@@ -1,0 +1,169 @@
+"""GPU tests of the radiance cache through the C-ABI: forward pass and
+loss gradient against the oracle's FP64 restatement (with the GPU's BF16
+roundings), online training lowers the loss, and paths that end in the
+cache render exactly the oracle's truncated paths plus the cache term."""
+import numpy as np
+import pytest
+
+import vcr
+from oracle import oracle as orc
+from oracle import oracle_nrc as onrc
+from vcr import configs
+
+pytestmark = pytest.mark.gpu
+
+
+def _cloud():
+    desc = vcr.grid_desc((64, 32, 64), (1 / 64,) * 3)
+    return desc, vcr.cloud_from_grid(desc, 1.0, 16.0)
+
+
+def _ctx_with_cloud(ctx, desc, cloud, dense=None):
+    if dense is None:
+        dense = orc.fbm_fill((64, 32, 64), seed=3, octaves=4)
+    ctx.grid_upload(desc, dense)
+    ctx.set_cloud(cloud)
+    return dense
+
+
+def _dev_records(recs, cuda):
+    import torch
+    return torch.from_numpy(recs.view(np.uint8).copy()).to(cuda)
+
+
+def test_forward_matches_oracle(cuda):
+    import torch
+    desc, cloud = _cloud()
+    rng = np.random.default_rng(1)
+    recs = onrc.random_records(1000, cloud, rng)
+    with vcr.Context() as ctx:
+        _ctx_with_cloud(ctx, desc, cloud)
+        ctx.nrc_setup(train_samples=4096, seed=7)
+        w = ctx.nrc_get_weights()
+        dr = _dev_records(recs, cuda)
+        out = torch.zeros(3 * len(recs), dtype=torch.float32, device=cuda)
+        ctx.nrc_forward(dr.data_ptr(), len(recs), out.data_ptr())
+        got = out.cpu().numpy().reshape(-1, 3)
+    ref = onrc.forward(w, recs, cloud)
+    scale = np.abs(ref).mean() + 1e-3
+    assert np.abs(got - ref).max() <= 3e-2 * scale, (np.abs(got - ref).max(), scale)
+    assert np.abs(got - ref).mean() <= 3e-3 * scale
+
+
+def test_gradient_matches_oracle(cuda):
+    desc, cloud = _cloud()
+    rng = np.random.default_rng(2)
+    recs = onrc.random_records(4096, cloud, rng)
+    with vcr.Context() as ctx:
+        _ctx_with_cloud(ctx, desc, cloud)
+        ctx.nrc_setup(train_samples=4096, seed=11)
+        w = ctx.nrc_get_weights()
+        dr = _dev_records(recs, cuda)
+        g, loss = ctx.nrc_gradient(dr.data_ptr(), len(recs))
+    gref, lref = onrc.gradient(w, recs, cloud)
+    assert abs(loss - lref) <= 1e-2 * abs(lref)
+    cos = float(g @ gref / (np.linalg.norm(g) * np.linalg.norm(gref)))
+    rel = float(np.linalg.norm(g - gref) / np.linalg.norm(gref))
+    assert cos > 0.999 and rel < 3e-2, (cos, rel)
+    # padded output columns never receive gradient
+    out = g[5 * 64 * 64:].reshape(64, 16)
+    assert np.all(out[:, 3:] == 0)
+
+
+def _smooth_targets(recs, cloud):
+    b0, b1 = np.array(cloud.bounds_min), np.array(cloud.bounds_max)
+    x = (recs["p"] - b0) / (b1 - b0)
+    base = 0.3 + 0.12 * np.sin(2 * np.pi * x[:, 0]) * np.cos(2 * np.pi * x[:, 2]) + 0.08 * recs["v"][:, 1]
+    recs["w"] = base[:, None] * np.array([1.0, 0.8, 0.6])
+
+
+def test_fit_converges_on_a_deterministic_target(cuda):
+    desc, cloud = _cloud()
+    rng = np.random.default_rng(4)
+    recs = onrc.random_records(8192, cloud, rng)
+    _smooth_targets(recs, cloud)
+    with vcr.Context() as ctx:
+        _ctx_with_cloud(ctx, desc, cloud)
+        ctx.nrc_setup(train_samples=8192, learning_rate=3e-3, seed=5)
+        dr = _dev_records(recs, cuda)
+        _, l0 = ctx.nrc_gradient(dr.data_ptr(), len(recs))
+        ctx.nrc_fit(dr.data_ptr(), len(recs), 400)
+        ctx.synchronize()
+        _, l1 = ctx.nrc_gradient(dr.data_ptr(), len(recs))
+        assert ctx.nrc_info()["steps"] == 400
+    assert np.isfinite(l1) and l1 < 0.05 * l0, (l0, l1)
+
+
+def _image_mean(ctx, passes, seed):
+    ctx.reset()
+    for k in range(passes):
+        ctx.pt_pass(seed=seed, pass_index=k)
+    ctx.synchronize()
+    return float(ctx.image_mean().mean())
+
+
+def test_online_training_makes_the_cached_render_consistent(cuda):
+    """Paths cut at the second event lose the energy of the rest of the
+    path; after online training the cache must give most of it back, so the
+    cached render approaches the unbiased render's mean."""
+    sc = configs.C1_PT
+    W = H = 64
+    with vcr.Context() as ctx:
+        configs.setup_context(ctx, sc, width=W, height=H)
+        prm = sc.params(vcr.TRACKER_DDA)
+        full = _image_mean(ctx, 64, seed=21)
+        prm.nrc_events = 2
+        ctx.set_params(prm)
+        ctx.nrc_setup(train_samples=16384, learning_rate=2e-3, query_capacity=W * H, seed=3)
+        ctx.nrc_set_weights(np.zeros(ctx.NRC_WEIGHTS, np.float32))
+        cut = _image_mean(ctx, 64, seed=22)
+        ctx.nrc_setup(train_samples=16384, learning_rate=2e-3, query_capacity=W * H, seed=3)
+        for k in range(300):
+            ctx.nrc_train_step(seed=5, pass_index=k)
+        info = ctx.nrc_info()
+        cached = _image_mean(ctx, 64, seed=23)
+    assert info["steps"] == 300 and info["train_records"] > 4000 and np.isfinite(info["last_loss"])
+    assert full - cut > 0.05 * full, (full, cut)
+    assert abs(cached - full) < 0.35 * (full - cut), (full, cut, cached)
+
+
+def test_paths_ending_in_the_cache_match_the_oracle(cuda):
+    """nrc_events = 2 with an all-zero network: the image is exactly the
+    oracle's truncated paths; with trained weights the cache adds a
+    non-negative term only where paths reached the second event."""
+    sc = configs.C1_PT
+    dense = orc.fbm_fill(sc.size, seed=sc.seed, octaves=sc.octaves)
+    og = orc.Grid(dense, 0)
+    W = H = 96
+    crop = (0, 0, W, H)
+    prm = sc.params(vcr.TRACKER_DDA)
+    prm.nrc_events = 2
+    cloud = sc.cloud()
+    cloud.max_extinction = max(og.max_density(), 0.01)
+    with vcr.Context() as ctx:
+        ctx.grid_upload(sc.grid_desc(), dense)
+        ctx.set_cloud(cloud)
+        ctx.set_camera(sc.camera(W, H))
+        ctx.set_params(prm)
+        ctx.set_frame(W, H)
+        ctx.nrc_setup(train_samples=8192, query_capacity=W * H, seed=1)
+        ctx.nrc_set_weights(np.zeros(ctx.NRC_WEIGHTS, np.float32))
+        ctx.pt_pass(seed=4, pass_index=0, flags=vcr.PASS_RECORD_STATS)
+        ctx.synchronize()
+        g0, st = ctx.image_sum(), ctx.path_stats()
+        o0, ost = og.pt_pass(cloud, sc.camera(W, H), prm, W, H, seed=4, pass_index=0, flags=vcr.PASS_RECORD_STATS)
+        np.testing.assert_array_equal(st[..., :2], ost[..., :2])
+        np.testing.assert_array_equal(g0, o0)
+        assert ctx.nrc_info()["queries"] == int((st[..., 0] >= 2).sum())
+        # an all-zero ReLU network has zero gradient: start training from a fresh init
+        ctx.nrc_setup(train_samples=8192, query_capacity=W * H, seed=1)
+        for k in range(20):
+            ctx.nrc_train_step(seed=9, pass_index=k)
+        ctx.reset()
+        ctx.pt_pass(seed=4, pass_index=0)
+        ctx.synchronize()
+        g1 = ctx.image_sum()
+    ended = st[..., 0] >= 2
+    assert np.all(g1 >= g0 - 1e-7)
+    np.testing.assert_array_equal(g1[~ended], g0[~ended])
+    assert (g1[ended] > g0[ended]).mean() > 0.5
