@@ -94,6 +94,30 @@ __global__ void mean_kernel(const double* __restrict__ sum, float* __restrict__ 
   if (i < n) out[i] = (float)(sum[i] * inv);
 }
 
+// sum over pixels of sum_c (sum*inv - ref)^2 / (ref^2 + 1e-2); block partials
+// into acc (zeroed by the caller), finished by rel_rmse_finish.
+__global__ void rel_rmse_kernel(const double* __restrict__ sum, const double* __restrict__ ref, size_t n, double inv,
+                                double* __restrict__ acc) {
+  double s = 0.0;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    double r = ref[i], d = sum[i] * inv - r;
+    s += d * d / (r * r + 1e-2);
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  __shared__ double part[32];
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    s = threadIdx.x < (blockDim.x >> 5) ? part[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (threadIdx.x == 0) atomicAdd(acc, s);
+  }
+}
+
+__global__ void rel_rmse_finish(const double* __restrict__ acc, double px, double* __restrict__ out) {
+  *out = sqrt(*acc / px);
+}
+
 }  // namespace vcr
 
 using namespace vcr;
@@ -554,29 +578,46 @@ extern "C" VCR_API vcr_status vcr_readback(vcr_ctx* ctx, vcr_buffer_id id, void*
       size_t n = px * 3;
       mean_kernel<<<(unsigned)((n + 255) / 256), 256>>>(ctx->d_sum, (float*)ctx->d_scratch, n, inv);
       VCR_CUDA(ctx, cudaGetLastError());
-      VCR_CUDA(ctx, cudaMemcpy(host, ctx->d_scratch, bytes, cudaMemcpyDeviceToHost));
+      VCR_CUDA(ctx, cudaMemcpy(host, ctx->d_scratch, bytes, cudaMemcpyDefault));
       return VCR_OK;
     }
     case VCR_BUF_IMAGE_SUM:
       if (!ctx->d_sum) return fail(ctx, VCR_ERR_STATE, "no frame");
       if (bytes != px * 3 * sizeof(double)) return fail(ctx, VCR_ERR_INVALID, "sum image is %zu bytes", px * 24);
-      VCR_CUDA(ctx, cudaMemcpy(host, ctx->d_sum, bytes, cudaMemcpyDeviceToHost));
+      VCR_CUDA(ctx, cudaMemcpy(host, ctx->d_sum, bytes, cudaMemcpyDefault));
       return VCR_OK;
     case VCR_BUF_PATH_STATS:
       if (!ctx->d_stats) return fail(ctx, VCR_ERR_STATE, "no frame");
       if (bytes != px * 4 * sizeof(uint32_t)) return fail(ctx, VCR_ERR_INVALID, "stats are %zu bytes", px * 16);
-      VCR_CUDA(ctx, cudaMemcpy(host, ctx->d_stats, bytes, cudaMemcpyDeviceToHost));
+      VCR_CUDA(ctx, cudaMemcpy(host, ctx->d_stats, bytes, cudaMemcpyDefault));
       return VCR_OK;
     case VCR_BUF_SHADOW_VOLUME: {
       if (!ctx->has_sv) return fail(ctx, VCR_ERR_STATE, "no shadow volume");
       size_t n = (size_t)ctx->sv.voxel_axis_count;
       if (bytes != n * n * n * sizeof(float)) return fail(ctx, VCR_ERR_INVALID, "shadow volume is %zu bytes", n * n * n * 4);
-      VCR_CUDA(ctx, cudaMemcpy(host, ctx->d_sv, bytes, cudaMemcpyDeviceToHost));
+      VCR_CUDA(ctx, cudaMemcpy(host, ctx->d_sv, bytes, cudaMemcpyDefault));
       return VCR_OK;
     }
     default:
       return fail(ctx, VCR_ERR_UNSUPPORTED, "buffer id %d not readable here", (int)id);
   }
+}
+
+extern "C" VCR_API vcr_status vcr_image_rel_rmse(vcr_ctx* ctx, const double* d_ref, double* d_out, void* stream) {
+  if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  if (!d_ref || !d_out) return fail(ctx, VCR_ERR_INVALID, "null reference or output");
+  if (!ctx->d_sum) return fail(ctx, VCR_ERR_STATE, "no frame");
+  cudaStream_t s = (cudaStream_t)stream;
+  size_t px = (size_t)ctx->width * ctx->height;
+  double inv = ctx->samples ? 1.0 / (double)ctx->samples : 0.0;
+  double* acc = reinterpret_cast<double*>(ctx->d_counters + 7);
+  VCR_CUDA(ctx, cudaMemsetAsync(acc, 0, sizeof(double), s));
+  unsigned blocks = (unsigned)std::min<size_t>((px * 3 + 255) / 256, (size_t)ctx->sm_count * 8);
+  rel_rmse_kernel<<<blocks, 256, 0, s>>>(ctx->d_sum, d_ref, px * 3, inv, acc);
+  VCR_CUDA(ctx, cudaGetLastError());
+  rel_rmse_finish<<<1, 1, 0, s>>>(acc, (double)px, d_out);
+  VCR_CUDA(ctx, cudaGetLastError());
+  return VCR_OK;
 }
 
 extern "C" VCR_API vcr_status vcr_pass_count(vcr_ctx* ctx, uint32_t* out) {

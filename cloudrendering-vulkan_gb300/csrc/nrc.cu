@@ -13,6 +13,8 @@
 // Adam runs on FP32 master weights and refreshes the BF16 copy.
 #include <mma.h>
 
+#include <cstring>
+
 #include "nrc.cuh"
 #include "track.cuh"
 
@@ -25,7 +27,8 @@ constexpr int kNrcThreads = 128;
 constexpr int kLd = kNrcWidth;  // leading dimension of activation tiles
 
 struct NrcView {
-  const bf16* wb;
+  const bf16* wb;   // training weights
+  const bf16* wbi;  // inference weights (the moving average, or wb)
   f3 b0, inv_ext;
 };
 
@@ -100,7 +103,7 @@ __global__ void __launch_bounds__(kNrcThreads) nrc_infer_kernel(NrcView v, const
   float* Y = reinterpret_cast<float*>(X + kNrcLayers * kNrcTile * kLd);  // 4 warps x 16 x 64 fp32
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   float* Yw = Y + warp * 16 * kLd;
-  load_weights(v.wb, W);
+  load_weights(v.wbi, W);
   __syncthreads();
   const uint32_t count = min(*count_ptr, capacity);
   for (uint32_t first = blockIdx.x * kNrcTile; first < count; first += gridDim.x * kNrcTile) {
@@ -233,7 +236,8 @@ __global__ void __launch_bounds__(kNrcThreads) nrc_train_kernel(NrcView v, const
 
 __global__ void nrc_adam_kernel(float* __restrict__ w, bf16* __restrict__ wb, float* __restrict__ m,
                                 float* __restrict__ vv, float* __restrict__ g, float lr, float b1, float b2,
-                                float eps, float c1, float c2) {
+                                float eps, float c1, float c2, float* __restrict__ ema, bf16* __restrict__ wbi,
+                                float decay) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= kNrcWeightCount) return;
   float gi = g[i];
@@ -245,103 +249,24 @@ __global__ void nrc_adam_kernel(float* __restrict__ w, bf16* __restrict__ wb, fl
   w[i] = wi;
   wb[i] = __float2bfloat16_rn(wi);
   g[i] = 0.0f;
+  if (ema) {
+    float e = decay * ema[i] + (1.0f - decay) * wi;
+    ema[i] = e;
+    wbi[i] = __float2bfloat16_rn(e);
+  }
+}
+
+__global__ void nrc_copy_weights_kernel(const float* __restrict__ w, float* __restrict__ ema, bf16* __restrict__ wbi) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < kNrcWeightCount) {
+    ema[i] = w[i];
+    wbi[i] = __float2bfloat16_rn(w[i]);
+  }
 }
 
 __global__ void nrc_to_bf16_kernel(const float* __restrict__ w, bf16* __restrict__ wb) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < kNrcWeightCount) wb[i] = __float2bfloat16_rn(w[i]);
-}
-
-// ---------------------------------------------------------------------------
-// training paths: full unbiased paths (DDA free flights, ratio-tracking NEE)
-// recording the radiance leaving each of their first scattering vertices
-// toward the previous vertex: target_i = (L_total - L_before_i) / beta_i.
-// ---------------------------------------------------------------------------
-constexpr int kNrcRecordEvents = 4;
-constexpr uint32_t kNrcTrainSalt = 0x3C6EF372u;
-
-__global__ void __launch_bounds__(128) nrc_train_paths_kernel(GridView g, SceneView s, CamView cam, PassView pv,
-                                                              uint32_t npaths, NrcRecord* __restrict__ out,
-                                                              uint32_t* __restrict__ out_count, uint32_t capacity,
-                                                              Counters cnt) {
-  uint32_t id = blockIdx.x * blockDim.x + threadIdx.x;
-  uint32_t lookups = 0, cells = 0, events = 0;
-  if (id < npaths) {
-    Rng rng = rng_pcg(pv.seed ^ kNrcTrainSalt, id, pv.pass);
-    uint32_t pix = (uint32_t)(rng_next(rng) * (float)(pv.cw * pv.ch));
-    pix = min(pix, pv.cw * pv.ch - 1u);
-    int x = (int)(pv.x0 + pix % pv.cw), y = (int)(pv.y0 + pix / pv.cw);
-    f3 pos, dir;
-    camera_ray(cam, x, y, pos, dir);
-    float tmin, tmax;
-    if (slab(pos, dir, s.b0, s.b1, tmin, tmax) && tmax >= 0.0f && s.ds > 0.0f) {
-      pos = along(pos, dir, tmax < tmin ? tmax : tmin);
-      f3 L = mk(0.f, 0.f, 0.f);
-      float beta = 1.0f;
-      NrcRecord rec[kNrcRecordEvents];
-      f3 Lb[kNrcRecordEvents];
-      float bb[kNrcRecordEvents];
-      int nrec = 0;
-      const f3 lsun = -s.sun;
-      while (true) {
-        float t;
-        if (!free_flight(g, s, pos, dir, rng, t, lookups, cells)) {
-          L = L + sky(s, dir) * beta;
-          break;
-        }
-        pos = along(pos, dir, t);
-        if (nrec < kNrcRecordEvents) {
-          NrcRecord& r = rec[nrec];
-          r.px = pos.x; r.py = pos.y; r.pz = pos.z;
-          r.vx = -dir.x; r.vy = -dir.y; r.vz = -dir.z;
-          r.sx = s.sun.x; r.sy = s.sun.y; r.sz = s.sun.z;
-          r.pix = pix;
-          Lb[nrec] = L;
-          bb[nrec] = beta;
-          ++nrec;
-        }
-        ++events;
-        beta = beta * s.albedo;
-        float phase = hg_pdf(s.ph, dot(-dir, s.sun));
-        // ratio-tracking transmittance toward the sun
-        Track tr;
-        track_init(tr, g, s, g.majorants, pos, lsun, cells);
-        float T = 1.0f;
-        while (true) {
-          float tau = -vlog(rng_next(rng));
-          if (track_walk(tr, g, g.majorants, s.k_sigma, tau, cells, 0xFFFFFFFFu) != kCandidate) break;
-          float rho = density_at(g, s, along(pos, lsun, tr.t));
-          ++lookups;
-          T = T * (1.0f - rho / tr.m);
-          if (T < 0.05f) {
-            if (rng_next(rng) >= 0.5f) {
-              T = 0.0f;
-              break;
-            }
-            T = T * 2.0f;
-          }
-        }
-        float c = ((s.light * phase) * T) * beta;
-        L = L + mk(c, c, c);
-        if (s.max_events && events >= s.max_events) break;
-        dir = hg_sample(s.ph, dir, rng, true);
-        if (lookups + cells > kPathWorkCap) break;
-      }
-      if (nrec > 0) {
-        uint32_t base = atomicAdd(out_count, (uint32_t)nrec);
-        for (int i = 0; i < nrec; ++i) {
-          if (base + i >= capacity) break;
-          NrcRecord r = rec[i];
-          float inv = 1.0f / bb[i];
-          r.w0 = (L.x - Lb[i].x) * inv;
-          r.w1 = (L.y - Lb[i].y) * inv;
-          r.w2 = (L.z - Lb[i].z) * inv;
-          out[base + i] = r;
-        }
-      }
-    }
-  }
-  flush_counters(cnt, id < npaths ? 1ull : 0ull, lookups, events, cells);
 }
 
 // ---------------------------------------------------------------------------
@@ -358,6 +283,7 @@ static size_t train_smem() {
 NrcView nrc_view(const vcr_ctx* ctx) {
   NrcView v;
   v.wb = reinterpret_cast<const bf16*>(ctx->nrc->wb);
+  v.wbi = reinterpret_cast<const bf16*>(ctx->nrc->wbi ? ctx->nrc->wbi : ctx->nrc->wb);
   const vcr_cloud& c = ctx->cloud;
   v.b0 = mk(c.bounds_min[0], c.bounds_min[1], c.bounds_min[2]);
   v.inv_ext = mk(1.0f / (c.bounds_max[0] - c.bounds_min[0]), 1.0f / (c.bounds_max[1] - c.bounds_min[1]),
@@ -368,8 +294,8 @@ NrcView nrc_view(const vcr_ctx* ctx) {
 void nrc_free(vcr_ctx* ctx) {
   NrcState* st = ctx->nrc;
   if (!st) return;
-  void* ptrs[] = {st->w, st->wb, st->m, st->v, st->grad, st->loss, st->train, st->train_count, st->query,
-                  st->query_count};
+  void* ptrs[] = {st->w, st->wb, st->m, st->v, st->grad, st->ema, st->wbi, st->loss, st->train, st->train_count,
+                  st->query, st->query_count};
   for (void* p : ptrs) cudaFree(p);
   delete st;
   ctx->nrc = nullptr;
@@ -394,13 +320,15 @@ static void nrc_init_weights(std::vector<float>& w, uint32_t seed) {
 
 vcr_status nrc_setup(vcr_ctx* ctx, const vcr_nrc_params* p) {
   if (!p || p->train_samples == 0 || p->train_samples > (1u << 22) || !(p->learning_rate > 0.0f) ||
-      p->query_capacity == 0)
-    return fail(ctx, VCR_ERR_INVALID, "nrc params: train_samples 1..2^22, learning_rate > 0, query_capacity > 0");
+      p->query_capacity == 0 || !(p->ema_decay >= 0.0f && p->ema_decay < 1.0f))
+    return fail(ctx, VCR_ERR_INVALID,
+                "nrc params: train_samples 1..2^22, learning_rate > 0, query_capacity > 0, ema_decay in [0,1)");
   nrc_free(ctx);
   NrcState* st = new NrcState();
   ctx->nrc = st;
   st->prm = *p;
   st->query_capacity = p->query_capacity;
+  st->train_cap = 2 * p->train_samples;
 #define VCR_ALLOC(ptr, bytes) VCR_CUDA(ctx, cudaMalloc(reinterpret_cast<void**>(&(ptr)), (bytes)))
   VCR_ALLOC(st->w, kNrcWeightCount * 4);
   VCR_ALLOC(st->wb, kNrcWeightCount * 2);
@@ -408,11 +336,16 @@ vcr_status nrc_setup(vcr_ctx* ctx, const vcr_nrc_params* p) {
   VCR_ALLOC(st->v, kNrcWeightCount * 4);
   VCR_ALLOC(st->grad, kNrcWeightCount * 4);
   VCR_ALLOC(st->loss, 8);
-  VCR_ALLOC(st->train, (size_t)p->train_samples * sizeof(NrcRecord));
+  VCR_ALLOC(st->train, (size_t)st->train_cap * sizeof(NrcRecord));
+  if (p->ema_decay > 0.0f) {
+    VCR_ALLOC(st->ema, kNrcWeightCount * 4);
+    VCR_ALLOC(st->wbi, kNrcWeightCount * 2);
+  }
   VCR_ALLOC(st->train_count, 4);
   VCR_ALLOC(st->query, (size_t)p->query_capacity * sizeof(NrcRecord));
   VCR_ALLOC(st->query_count, 4);
 #undef VCR_ALLOC
+  VCR_CUDA(ctx, cudaMemset(st->train_count, 0, 4));
   std::vector<float> w;
   nrc_init_weights(w, p->seed);
   VCR_CUDA(ctx, cudaMemcpy(st->w, w.data(), kNrcWeightCount * 4, cudaMemcpyHostToDevice));
@@ -422,6 +355,10 @@ vcr_status nrc_setup(vcr_ctx* ctx, const vcr_nrc_params* p) {
   VCR_CUDA(ctx, cudaMemset(st->query_count, 0, 4));
   nrc_to_bf16_kernel<<<(kNrcWeightCount + 255) / 256, 256>>>(st->w, reinterpret_cast<bf16*>(st->wb));
   VCR_CUDA(ctx, cudaGetLastError());
+  if (st->ema) {
+    nrc_copy_weights_kernel<<<(kNrcWeightCount + 255) / 256, 256>>>(st->w, st->ema, reinterpret_cast<bf16*>(st->wbi));
+    VCR_CUDA(ctx, cudaGetLastError());
+  }
   VCR_CUDA(ctx, cudaFuncSetAttribute(nrc_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)infer_smem()));
   VCR_CUDA(ctx, cudaFuncSetAttribute(nrc_train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)train_smem()));
   return VCR_OK;
@@ -446,8 +383,11 @@ vcr_status nrc_adam(vcr_ctx* ctx, cudaStream_t s) {
   const float b1 = 0.9f, b2 = 0.99f, eps = 1e-8f;
   float c1 = 1.0f - (float)std::pow(0.9, (double)st->step);
   float c2 = 1.0f - (float)std::pow(0.99, (double)st->step);
-  nrc_adam_kernel<<<(kNrcWeightCount + 255) / 256, 256, 0, s>>>(st->w, reinterpret_cast<bf16*>(st->wb), st->m, st->v,
-                                                                st->grad, st->prm.learning_rate, b1, b2, eps, c1, c2);
+  // moving-average decay ramps up over the first steps: min(d, (1+k)/(10+k))
+  float decay = std::min(st->prm.ema_decay, (1.0f + (float)st->step) / (10.0f + (float)st->step));
+  nrc_adam_kernel<<<(kNrcWeightCount + 255) / 256, 256, 0, s>>>(
+      st->w, reinterpret_cast<bf16*>(st->wb), st->m, st->v, st->grad, st->prm.learning_rate, b1, b2, eps, c1, c2,
+      st->ema, reinterpret_cast<bf16*>(st->wbi), decay);
   VCR_CUDA(ctx, cudaGetLastError());
   return VCR_OK;
 }
@@ -471,27 +411,107 @@ vcr_status nrc_infer_queries(vcr_ctx* ctx, cudaStream_t s) {
   return VCR_OK;
 }
 
-vcr_status nrc_train_step(vcr_ctx* ctx, const vcr_pass_desc* pass, cudaStream_t s) {
-  NrcState* st = ctx->nrc;
-  if (!st) return fail(ctx, VCR_ERR_STATE, "vcr_nrc_train_step needs vcr_nrc_setup");
+static vcr_status nrc_check_scene(vcr_ctx* ctx, const char* who) {
+  if (!ctx->nrc) return fail(ctx, VCR_ERR_STATE, "%s needs vcr_nrc_setup", who);
   if (!ctx->has_grid || !ctx->has_cloud || !ctx->has_cam || !ctx->has_params || !ctx->d_sum)
-    return fail(ctx, VCR_ERR_STATE, "vcr_nrc_train_step needs a grid, cloud, camera, params and frame");
-  PassView pv;
-  vcr_status vs = make_pass_view(ctx, pass, pv);
-  if (vs) return vs;
-  GridView g = grid_view(ctx);
-  SceneView sc = scene_view(ctx);
-  Counters cnt{ctx->d_counters};
-  const uint32_t cap = st->prm.train_samples;
-  const uint32_t npaths = std::max(1u, cap / 2);  // about two recorded vertices per training path
-  VCR_CUDA(ctx, cudaMemsetAsync(st->train_count, 0, 4, s));
+    return fail(ctx, VCR_ERR_STATE, "%s needs a grid, cloud, camera, params and frame", who);
+  return VCR_OK;
+}
+
+static bool nrc_calibrated(const vcr_ctx* ctx) {
+  const NrcState* st = ctx->nrc;
+  return st->npaths && !memcmp(&st->calib_cam, &ctx->cam, sizeof(vcr_camera)) &&
+         !memcmp(&st->calib_cloud, &ctx->cloud, sizeof(vcr_cloud)) && st->calib_w == ctx->width &&
+         st->calib_h == ctx->height;
+}
+
+// Training paths: extended paths from uniformly drawn pixels that record
+// the radiance leaving each of their first kNrcRecordEvents scattering
+// vertices toward the previous vertex, target_i = (L_total - L_before_i) /
+// beta_i.  They run in the persistent wavefront kernel, alone
+// (vcr_nrc_train_step) or as the first work items of a pass (vcr_nrc_frame),
+// where their long paths overlap the pass's short ones.  The first step for
+// a camera/cloud/frame calibrates the path count so that a step yields
+// about train_samples records (synchronises once; deterministic, as the
+// yield of a seeded launch is).
+static NrcTrainSink nrc_sink(vcr_ctx* ctx) {
+  NrcState* st = ctx->nrc;
+  return NrcTrainSink{st->train, st->train_count, st->train_cap, st->npaths};
+}
+
+static vcr_status nrc_launch_training(vcr_ctx* ctx, const PassView& pv, uint32_t paths, cudaStream_t s) {
+  NrcTrainSink ts = nrc_sink(ctx);
+  ts.paths = paths;
+  VCR_CUDA(ctx, cudaMemsetAsync(ts.count, 0, 4, s));
   VCR_CUDA(ctx, cudaMemsetAsync(ctx->d_counters, 0, 5 * sizeof(unsigned long long), s));
-  nrc_train_paths_kernel<<<(npaths + 127) / 128, 128, 0, s>>>(g, sc, cam_view(ctx->cam), pv, npaths, st->train,
-                                                              st->train_count, cap, cnt);
-  VCR_CUDA(ctx, cudaGetLastError());
-  vs = nrc_accumulate_grad(ctx, st->train, st->train_count, cap, s);
+  return wavefront_launch(ctx, grid_view(ctx), scene_view(ctx), cam_view(ctx->cam), pv, nullptr,
+                          Counters{ctx->d_counters}, 0u, s, &ts);
+}
+
+static vcr_status nrc_calibrate(vcr_ctx* ctx, const PassView& pv, cudaStream_t s) {
+  NrcState* st = ctx->nrc;
+  const uint32_t want = st->prm.train_samples, paths = std::max(1u, want / 2);
+  vcr_status vs = nrc_launch_training(ctx, pv, paths, s);
   if (vs) return vs;
-  vs = nrc_adam(ctx, s);
+  uint32_t got = 0;
+  VCR_CUDA(ctx, cudaMemcpyAsync(&got, st->train_count, 4, cudaMemcpyDeviceToHost, s));
+  VCR_CUDA(ctx, cudaStreamSynchronize(s));
+  double n = std::ceil((double)paths * (double)want / (double)std::max(got, 1u));
+  st->npaths = (uint32_t)std::min(std::max(n, (double)std::max(1u, want / 4)), 16.0 * (double)want);
+  st->calib_cam = ctx->cam;
+  st->calib_cloud = ctx->cloud;
+  st->calib_w = ctx->width;
+  st->calib_h = ctx->height;
+  return VCR_OK;
+}
+
+// Loss gradient over the step's records, then Adam.
+static vcr_status nrc_update(vcr_ctx* ctx, cudaStream_t s) {
+  NrcState* st = ctx->nrc;
+  vcr_status vs = nrc_accumulate_grad(ctx, st->train, st->train_count, st->train_cap, s);
+  if (vs) return vs;
+  return nrc_adam(ctx, s);
+}
+
+vcr_status nrc_train_step(vcr_ctx* ctx, const vcr_pass_desc* pass, cudaStream_t s) {
+  vcr_status vs = nrc_check_scene(ctx, "vcr_nrc_train_step");
+  if (vs) return vs;
+  PassView pv;
+  vs = make_pass_view(ctx, pass, pv);
+  if (vs) return vs;
+  if (!nrc_calibrated(ctx)) vs = nrc_calibrate(ctx, pv, s);  // its records serve this step
+  else vs = nrc_launch_training(ctx, pv, ctx->nrc->npaths, s);
+  if (vs) return vs;
+  vs = nrc_update(ctx, s);
+  if (vs) return vs;
+  VCR_CUDA(ctx, cudaEventRecord(ctx->work_done, s));
+  return VCR_OK;
+}
+
+// One frame of the cached tracker: one wavefront launch runs this frame's
+// training paths first and the pass's camera paths after them (the latter
+// end in the cache at nrc_events, queried with the weights before this
+// frame's update), then the loss gradient and Adam.  Same result as
+// vcr_pt_pass followed by vcr_nrc_train_step with the same pass.
+vcr_status nrc_frame(vcr_ctx* ctx, const vcr_pass_desc* pass, cudaStream_t s) {
+  vcr_status vs = nrc_check_scene(ctx, "vcr_nrc_frame");
+  if (vs) return vs;
+  if (ctx->params.nrc_events == 0 || ctx->params.tracker != VCR_TRACKER_DDA)
+    return fail(ctx, VCR_ERR_STATE, "vcr_nrc_frame needs the DDA tracker and params.nrc_events > 0");
+  PassView pv;
+  vs = make_pass_view(ctx, pass, pv);
+  if (vs) return vs;
+  if (!nrc_calibrated(ctx)) {  // the calibration synchronises: training launch first, then the pass
+    vs = nrc_calibrate(ctx, pv, s);
+    if (vs) return vs;
+    vs = pt_pass_launch(ctx, pass, s);
+  } else {
+    NrcTrainSink ts = nrc_sink(ctx);
+    VCR_CUDA(ctx, cudaMemsetAsync(ts.count, 0, 4, s));
+    vs = pt_pass_launch(ctx, pass, s, &ts);
+  }
+  if (vs) return vs;
+  vs = nrc_update(ctx, s);
   if (vs) return vs;
   VCR_CUDA(ctx, cudaEventRecord(ctx->work_done, s));
   return VCR_OK;
@@ -523,6 +543,12 @@ extern "C" VCR_API vcr_status vcr_nrc_train_step(vcr_ctx* ctx, const vcr_pass_de
   return nrc_train_step(ctx, pass, (cudaStream_t)stream);
 }
 
+extern "C" VCR_API vcr_status vcr_nrc_frame(vcr_ctx* ctx, const vcr_pass_desc* pass, void* stream) {
+  if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  if (!pass) return fail(ctx, VCR_ERR_INVALID, "null pass");
+  return nrc_frame(ctx, pass, (cudaStream_t)stream);
+}
+
 extern "C" VCR_API vcr_status vcr_nrc_info(vcr_ctx* ctx, vcr_nrc_info_t* out) {
   if (!ctx || !out) return fail(ctx, VCR_ERR_INVALID, "null argument");
   NrcState* st = ctx->nrc;
@@ -535,7 +561,7 @@ extern "C" VCR_API vcr_status vcr_nrc_info(vcr_ctx* ctx, vcr_nrc_info_t* out) {
   VCR_CUDA(ctx, cudaMemcpy(&nq, st->query_count, 4, cudaMemcpyDeviceToHost));
   out->steps = st->step;
   out->last_loss = loss;
-  out->train_records = std::min(ntrain, st->prm.train_samples);
+  out->train_records = std::min(ntrain, st->train_cap);
   out->queries = std::min(nq, st->query_capacity);
   out->weights = kNrcWeightCount;
   return VCR_OK;
@@ -558,6 +584,11 @@ extern "C" VCR_API vcr_status vcr_nrc_set_weights(vcr_ctx* ctx, const float* hos
   VCR_CUDA(ctx, cudaMemcpy(ctx->nrc->w, host, count * 4, cudaMemcpyHostToDevice));
   nrc_to_bf16_kernel<<<(kNrcWeightCount + 255) / 256, 256>>>(ctx->nrc->w, reinterpret_cast<bf16*>(ctx->nrc->wb));
   VCR_CUDA(ctx, cudaGetLastError());
+  if (ctx->nrc->ema) {
+    nrc_copy_weights_kernel<<<(kNrcWeightCount + 255) / 256, 256>>>(ctx->nrc->w, ctx->nrc->ema,
+                                                                     reinterpret_cast<bf16*>(ctx->nrc->wbi));
+    VCR_CUDA(ctx, cudaGetLastError());
+  }
   VCR_CUDA(ctx, cudaDeviceSynchronize());
   return VCR_OK;
 }

@@ -24,9 +24,25 @@ struct NrcRecord {
   float sx, sy, sz;  // unit direction the sunlight travels
   float w0, w1, w2;  // query: path throughput (rgb); training: target radiance
   uint32_t pix;      // query: pixel index; training: unused
-  uint32_t pad[3];
+  uint32_t pad[3];   // training, while its path runs: beta before the vertex
+                     // (float bits), slot of the path's previous record
 };
 static_assert(sizeof(NrcRecord) == 64, "record size");
+
+// Training paths: extended (unbiased, full length) paths from uniformly
+// drawn pixels of the crop that record their first kNrcRecordEvents
+// scattering vertices.  They run as the first work items of a wavefront
+// launch, ahead of the pass's camera paths.
+constexpr int kNrcRecordEvents = 4;
+constexpr uint32_t kNrcTrainSalt = 0x3C6EF372u;  // RNG stream salt of training paths
+constexpr uint32_t kNrcNoSlot = 0xFFFFFFFFu;
+
+struct NrcTrainSink {
+  NrcRecord* rec;
+  uint32_t* count;
+  uint32_t capacity;
+  uint32_t paths;  // training paths of the launch (0: none)
+};
 
 struct NrcState {
   vcr_nrc_params prm{};
@@ -35,15 +51,24 @@ struct NrcState {
   float* m = nullptr;        // Adam first moment
   float* v = nullptr;        // Adam second moment
   float* grad = nullptr;     // gradient accumulator [kNrcWeightCount]
+  float* ema = nullptr;      // exponential moving average of w (ema_decay > 0)
+  void* wbi = nullptr;       // BF16 copy of ema used for inference (ema_decay > 0)
   float* loss = nullptr;     // [2]: loss sum, sample count of the last step
-  NrcRecord* train = nullptr;  // training records [train_samples]
+  NrcRecord* train = nullptr;  // training records [train_cap]
   uint32_t* train_count = nullptr;
+  uint32_t train_cap = 0;      // 2 x train_samples: room for the yield's spread
   NrcRecord* query = nullptr;  // cache queries of one pass [query_capacity]
   uint32_t* query_count = nullptr;
   uint32_t query_capacity = 0;
   uint32_t step = 0;
   float last_loss = 0.0f;
   uint32_t last_train = 0, last_queries = 0;
+  // training paths per step, calibrated so that a step yields about
+  // train_samples records for the bound camera and cloud (0 = recalibrate)
+  uint32_t npaths = 0;
+  vcr_camera calib_cam{};
+  vcr_cloud calib_cloud{};
+  uint32_t calib_w = 0, calib_h = 0;
 };
 
 // Position encoding: level l uses frequency 2^(l/2) cycles per unit box

@@ -163,7 +163,11 @@ inline vcr_status make_pass_view(vcr_ctx* ctx, const vcr_pass_desc* pass, PassVi
 }
 
 // DDA wavefront tracker launch (pt_wavefront.cu).
+// `total` camera paths of the pass, preceded by train->paths training paths
+// of the radiance cache when `train` is given.
+struct NrcTrainSink;
 vcr_status wavefront_launch(vcr_ctx* ctx, const GridView& g, const SceneView& s, const CamView& cam,
-                            const PassView& pv, uint32_t* stats, Counters cnt, uint32_t total, cudaStream_t st);
+                            const PassView& pv, uint32_t* stats, Counters cnt, uint32_t total, cudaStream_t st,
+                            const NrcTrainSink* train = nullptr);
 
 }  // namespace vcr

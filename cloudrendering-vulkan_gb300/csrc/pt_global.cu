@@ -122,7 +122,7 @@ __global__ void __launch_bounds__(256) pt_global_kernel(GridView g, SceneView s,
 // host launch
 // ---------------------------------------------------------------------------
 
-vcr_status pt_pass_launch(vcr_ctx* ctx, const vcr_pass_desc* pass, cudaStream_t st) {
+vcr_status pt_pass_launch(vcr_ctx* ctx, const vcr_pass_desc* pass, cudaStream_t st, const NrcTrainSink* train) {
   if (!ctx->has_grid || !ctx->has_cloud || !ctx->has_cam || !ctx->has_params || !ctx->d_sum)
     return fail(ctx, VCR_ERR_STATE, "vcr_pt_pass needs a grid, cloud, camera, params and frame");
   PassView pv;
@@ -135,8 +135,8 @@ vcr_status pt_pass_launch(vcr_ctx* ctx, const vcr_pass_desc* pass, cudaStream_t 
     return fail(ctx, VCR_ERR_STATE, "shadow-volume NEE needs vcr_shadow_volume_build first");
   uint64_t total64 = (uint64_t)pv.cw * pv.ch * pv.spp;
   uint64_t pixels = (uint64_t)ctx->width * ctx->height * pv.spp;
-  if (total64 > 0xFFFFFFFFull || pixels > 0xFFFFFFFFull)
-    return fail(ctx, VCR_ERR_UNSUPPORTED, "more than 2^32 paths in one pass");
+  if (total64 > 0x7FFFFFFFull || pixels > 0xFFFFFFFFull)
+    return fail(ctx, VCR_ERR_UNSUPPORTED, "more than 2^31 paths in one pass");
   GridView g = grid_view(ctx);
   SceneView s = scene_view(ctx);
   CamView cam = cam_view(ctx->cam);
@@ -168,7 +168,7 @@ vcr_status pt_pass_launch(vcr_ctx* ctx, const vcr_pass_desc* pass, cudaStream_t 
       vcr_status qs = nrc_reset_queries(ctx, st);
       if (qs) return qs;
     }
-    vcr_status ws = wavefront_launch(ctx, g, s, cam, pv, stats, cnt, (uint32_t)total64, st);
+    vcr_status ws = wavefront_launch(ctx, g, s, cam, pv, stats, cnt, (uint32_t)total64, st, train);
     if (ws) return ws;
     if (s.nrc_events) {  // add throughput x cache prediction where paths ended
       ws = nrc_infer_queries(ctx, st);

@@ -96,13 +96,50 @@ __device__ __noinline__ bool start_path(const CamView& cam, const SceneView& s, 
   return true;
 }
 
+// A training path's radiance is final: turn the recorded radiance-before
+// and throughput-before of each of its vertices into the target
+// (L - L_before) / beta_before, walking the chain of its record slots.
+__device__ __noinline__ void finish_training(const NrcTrainSink& ts, uint32_t slot, f3 L) {
+  for (int i = 0; i < kNrcRecordEvents && slot != kNrcNoSlot; ++i) {
+    NrcRecord* r = ts.rec + slot;
+    float inv = 1.0f / __uint_as_float(r->pad[0]);
+    r->w0 = (L.x - r->w0) * inv;
+    r->w1 = (L.y - r->w1) * inv;
+    r->w2 = (L.z - r->w2) * inv;
+    slot = r->pad[1];
+  }
+}
+
+// Append a training vertex; returns the slot (or the previous one if full).
+__device__ __noinline__ uint32_t record_training(const NrcTrainSink& ts, const SceneView& s, f3 pos, f3 dir, f3 L,
+                                                 float beta, uint32_t prev) {
+  uint32_t q = atomicAdd(ts.count, 1u);
+  if (q >= ts.capacity) return prev;
+  NrcRecord r;
+  r.px = pos.x; r.py = pos.y; r.pz = pos.z;
+  r.vx = -dir.x; r.vy = -dir.y; r.vz = -dir.z;
+  r.sx = s.sun.x; r.sy = s.sun.y; r.sz = s.sun.z;
+  r.w0 = L.x; r.w1 = L.y; r.w2 = L.z;
+  r.pix = kNrcNoSlot;
+  r.pad[0] = __float_as_uint(beta);
+  r.pad[1] = prev;
+  r.pad[2] = 0u;
+  ts.rec[q] = r;
+  return q;
+}
+
+constexpr uint32_t kTrainPath = 0x80000000u;  // pid flag of a training path
+
 // 4 x 256 threads per SM: 64 registers a thread (a few spill to L1), which
 // measured ~7% faster than 3 CTAs at 77 registers on the 1024x512x1024 scene.
+// Work items [0, ts.paths) are training paths (their pid carries kTrainPath
+// and their pix the slot of their last record); the pass's camera paths
+// follow.
 template <int kThreads, bool kStage>
 __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
     pt_wavefront_kernel(GridView g, SceneView s, CamView cam, PassView pv, double* __restrict__ sum,
                         uint32_t* __restrict__ stats, Counters cnt, uint32_t total, uint32_t dda_steps,
-                        uint32_t maj_bytes, NrcSink nq, int* __restrict__ err) {
+                        uint32_t maj_bytes, NrcSink nq, NrcTrainSink ts, int* __restrict__ err) {
   extern __shared__ __align__(16) float s_maj[];
   __shared__ __align__(8) uint64_t s_bar;
   const float* maj = g.majorants;
@@ -134,9 +171,25 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
       base = __shfl_sync(0xffffffffu, base, leader);
       if (need) {
         uint32_t id = base + __popc(mask & ((1u << lane) - 1u));
-        if (id >= total) {
+        if (id >= total + ts.paths) {
           exhausted = true;
+        } else if (id < ts.paths) {  // training path from a uniformly drawn pixel of the crop
+          rng = rng_pcg(pv.seed ^ kNrcTrainSalt, id, pv.pass);
+          uint32_t pp = (uint32_t)(rng_next(rng) * (float)(pv.cw * pv.ch));
+          pp = min(pp, pv.cw * pv.ch - 1u);
+          pid = kTrainPath;
+          pix = kNrcNoSlot;
+          L = mk(0.f, 0.f, 0.f);
+          beta = 1.0f;
+          events = lookups = cells = 0;
+          ++n_paths;
+          if (start_path(cam, s, (int)(pv.x0 + pp % pv.cw), (int)(pv.y0 + pp / pv.cw), pos, dir, L)) {
+            mode = kScatter;
+            idir = dir;
+            need_init = true;
+          }
         } else {
+          id -= ts.paths;
           pid = id;
           uint32_t per_row = pv.cw * pv.spp;
           uint32_t cy = id / per_row, rem = id - cy * per_row;
@@ -184,7 +237,10 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
             if (xi < rho / tr.m) {  // real collision: start the NEE ray
               pos = p;
               ++events;
-              if (s.nrc_events && events == s.nrc_events) {
+              const bool training = (pid & kTrainPath) != 0u;
+              if (training && events <= (uint32_t)kNrcRecordEvents)
+                pix = record_training(ts, s, pos, dir, L, beta, pix);
+              if (s.nrc_events && events == s.nrc_events && !training) {
                 // end in the radiance cache: it predicts what leaves this vertex
                 finish = true;
                 uint32_t q = atomicAdd(nq.count, 1u);
@@ -237,7 +293,14 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
           }
         }
         if (lookups + cells > kPathWorkCap) finish = true;  // runaway guard (non-finite input)
-        if (finish) {
+        if (finish && (pid & kTrainPath)) {
+          finish_training(ts, pix, L);
+          n_look += lookups;
+          n_ev += events;
+          n_cells += cells;
+          mode = kIdle;
+          need_init = false;
+        } else if (finish) {
           write_result(pv, sum, pix, L, atomic);
           if (stats && (pid % pv.spp) == 0) {
             uint32_t* st = stats + 4 * (size_t)pix;
@@ -265,7 +328,7 @@ constexpr uint32_t kMaxStagedBytes = 96u * 1024u;
 template <int kThreads, bool kStage>
 static vcr_status launch_t(vcr_ctx* ctx, const GridView& g, const SceneView& s, const CamView& cam,
                            const PassView& pv, uint32_t* stats, Counters cnt, uint32_t total, uint32_t maj_bytes,
-                           cudaStream_t st) {
+                           const NrcTrainSink& ts, cudaStream_t st) {
   auto kern = pt_wavefront_kernel<kThreads, kStage>;
   size_t smem = kStage ? maj_bytes : 0;
   if (kStage)  // the attribute is per device, so it is set on every launch (a host-side call)
@@ -274,27 +337,33 @@ static vcr_status launch_t(vcr_ctx* ctx, const GridView& g, const SceneView& s, 
   VCR_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem));
   if (per_sm < 1) per_sm = 1;
   uint32_t blocks = (uint32_t)(ctx->sm_count * per_sm);
-  uint32_t need = (total + kThreads - 1) / kThreads;
+  uint32_t need = (total + ts.paths + kThreads - 1) / kThreads;
   if (blocks > need) blocks = need;
+  if (blocks == 0) return VCR_OK;
   NrcSink nq{nullptr, nullptr, 0u};
   if (s.nrc_events && ctx->nrc) nq = NrcSink{ctx->nrc->query, ctx->nrc->query_count, ctx->nrc->query_capacity};
   kern<<<blocks, kThreads, smem, st>>>(g, s, cam, pv, ctx->d_sum, stats, cnt, total, ctx->tuning.dda_steps,
-                                       maj_bytes, nq, ctx->d_error);
+                                       maj_bytes, nq, ts, ctx->d_error);
   VCR_CUDA(ctx, cudaGetLastError());
   return VCR_OK;
 }
 
 vcr_status wavefront_launch(vcr_ctx* ctx, const GridView& g, const SceneView& s, const CamView& cam,
-                            const PassView& pv, uint32_t* stats, Counters cnt, uint32_t total, cudaStream_t st) {
+                            const PassView& pv, uint32_t* stats, Counters cnt, uint32_t total, cudaStream_t st,
+                            const NrcTrainSink* train) {
   const vcr_tuning& t = ctx->tuning;
+  NrcTrainSink ts{nullptr, nullptr, 0u, 0u};
+  if (train) ts = *train;
+  if ((uint64_t)total + ts.paths >= (uint64_t)kTrainPath)
+    return fail(ctx, VCR_ERR_UNSUPPORTED, "more than 2^31 paths in one launch");
   size_t cells = (size_t)g.mnb[0] * g.mnb[1] * g.mnb[2];
   uint32_t bytes = (uint32_t)(((cells + 3) & ~(size_t)3) * sizeof(float));  // padded level: 16-byte multiple
   bool stage = t.stage_majorants && bytes <= kMaxStagedBytes;
   if (t.block_threads == 128)
-    return stage ? launch_t<128, true>(ctx, g, s, cam, pv, stats, cnt, total, bytes, st)
-                 : launch_t<128, false>(ctx, g, s, cam, pv, stats, cnt, total, bytes, st);
-  return stage ? launch_t<256, true>(ctx, g, s, cam, pv, stats, cnt, total, bytes, st)
-               : launch_t<256, false>(ctx, g, s, cam, pv, stats, cnt, total, bytes, st);
+    return stage ? launch_t<128, true>(ctx, g, s, cam, pv, stats, cnt, total, bytes, ts, st)
+                 : launch_t<128, false>(ctx, g, s, cam, pv, stats, cnt, total, bytes, ts, st);
+  return stage ? launch_t<256, true>(ctx, g, s, cam, pv, stats, cnt, total, bytes, ts, st)
+               : launch_t<256, false>(ctx, g, s, cam, pv, stats, cnt, total, bytes, ts, st);
 }
 
 }  // namespace vcr

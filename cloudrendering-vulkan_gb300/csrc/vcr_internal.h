@@ -53,6 +53,7 @@ struct vcr_ctx {
   cudaEvent_t work_done = nullptr;
 
   // device counters: [0] paths [1] lookups [2] events [3] dda cells [4] work cursor
+  // [5] grid max (u32 bits) [7] relRMSE accumulator (double bits)
   unsigned long long* d_counters = nullptr;
   int* d_error = nullptr;  // device error word (bounded waits, index checks)
 
@@ -101,8 +102,11 @@ vcr_status dda_trace_launch(vcr_ctx* ctx, const float* d_o, const float* d_d, ui
                             uint32_t max_cells, uint32_t* d_cells, float* d_t, uint32_t* d_count,
                             cudaStream_t s);
 
-// pt_global.cu
-vcr_status pt_pass_launch(vcr_ctx* ctx, const vcr_pass_desc* pass, cudaStream_t s);
+// pt_global.cu: one pass; with `train`, the radiance cache's training
+// paths run in the same wavefront launch ahead of the camera paths
+struct NrcTrainSink;
+vcr_status pt_pass_launch(vcr_ctx* ctx, const vcr_pass_desc* pass, cudaStream_t s,
+                          const NrcTrainSink* train = nullptr);
 
 // ppb.cu / ppm.cu / nrc.cu: release technique state (vcr_destroy)
 void ppb_free(vcr_ctx* ctx);

@@ -192,8 +192,8 @@ class Context:
     # radiance cache ---------------------------------------------------------
     NRC_WEIGHTS = 21504
 
-    def nrc_setup(self, train_samples=65536, learning_rate=1e-3, query_capacity=1 << 21, seed=1):
-        p = _abi.NrcParams(train_samples, learning_rate, query_capacity, seed)
+    def nrc_setup(self, train_samples=65536, learning_rate=1e-3, query_capacity=1 << 21, seed=1, ema_decay=0.0):
+        p = _abi.NrcParams(train_samples, learning_rate, query_capacity, seed, ema_decay)
         self._ck(lib().vcr_nrc_setup(self.h, C.byref(p)))
 
     def nrc_free(self):
@@ -203,6 +203,11 @@ class Context:
         p = _abi.PassDesc()
         p.seed, p.pass_index, p.spp = seed, pass_index, 1
         self._ck(lib().vcr_nrc_train_step(self.h, C.byref(p), C.c_void_p(stream)))
+
+    def nrc_frame(self, seed=0, pass_index=0, stream=0):
+        p = _abi.PassDesc()
+        p.seed, p.pass_index, p.spp = seed, pass_index, 1
+        self._ck(lib().vcr_nrc_frame(self.h, C.byref(p), C.c_void_p(stream)))
 
     def nrc_info(self) -> dict:
         i = _abi.NrcInfo()
@@ -330,6 +335,13 @@ class Context:
         out = np.empty((n, n, n), np.float32)
         self._ck(lib().vcr_readback(self.h, _abi.BUF_SHADOW_VOLUME, _ptr(out), out.nbytes))
         return out
+
+    def readback_to(self, buf_id, d_ptr, nbytes):
+        """Copy a context buffer into caller memory (host or device)."""
+        self._ck(lib().vcr_readback(self.h, buf_id, C.c_void_p(d_ptr), nbytes))
+
+    def image_rel_rmse(self, d_ref, d_out, stream=0):
+        self._ck(lib().vcr_image_rel_rmse(self.h, C.c_void_p(d_ref), C.c_void_p(d_out), C.c_void_p(stream)))
 
     def pass_count(self) -> int:
         v = C.c_uint32()

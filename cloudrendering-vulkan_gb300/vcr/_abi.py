@@ -65,7 +65,7 @@ class Tuning(C.Structure):
 
 class NrcParams(C.Structure):
     _fields_ = [("train_samples", C.c_uint32), ("learning_rate", C.c_float), ("query_capacity", C.c_uint32),
-                ("seed", C.c_uint32)]
+                ("seed", C.c_uint32), ("ema_decay", C.c_float)]
 
 
 class NrcInfo(C.Structure):
@@ -145,6 +145,7 @@ SIGNATURES = {
     "vcr_nrc_setup": (_S, [_P, C.POINTER(NrcParams)]),
     "vcr_nrc_free": (_S, [_P]),
     "vcr_nrc_train_step": (_S, [_P, C.POINTER(PassDesc), _P]),
+    "vcr_nrc_frame": (_S, [_P, C.POINTER(PassDesc), _P]),
     "vcr_nrc_info": (_S, [_P, C.POINTER(NrcInfo)]),
     "vcr_nrc_get_weights": (_S, [_P, _P, _sz]),
     "vcr_nrc_set_weights": (_S, [_P, _P, _sz]),
@@ -167,6 +168,7 @@ SIGNATURES = {
     "vcr_morton_codes": (_S, [_P, _P, _u32, F3, F3, _u32, _P, _P]),
     "vcr_readback": (_S, [_P, C.c_int, _P, _sz]),
     "vcr_pass_count": (_S, [_P, C.POINTER(_u32)]),
+    "vcr_image_rel_rmse": (_S, [_P, _P, _P, _P]),
 }
 
 _lib = None

@@ -338,6 +338,9 @@ typedef struct vcr_nrc_params {
   float learning_rate;     /* Adam step size (1e-3) */
   uint32_t query_capacity; /* cache queries per pass (>= paths of a pass) */
   uint32_t seed;           /* weight initialisation */
+  float ema_decay;         /* 0: queries use the training weights; in (0,1):
+                              they use a moving average of them with this
+                              decay (ramped in as min(d, (1+k)/(10+k))) */
 } vcr_nrc_params;
 
 typedef struct vcr_nrc_info_t {
@@ -357,6 +360,14 @@ VCR_API vcr_status vcr_nrc_free(vcr_ctx* ctx);
  * vcr_pt_pass (DDA tracker) ends paths at their k-th scattering event and
  * adds throughput x cache prediction there. */
 VCR_API vcr_status vcr_nrc_train_step(vcr_ctx* ctx, const vcr_pass_desc* pass, void* stream);
+/* One frame of the cached tracker, the same as vcr_pt_pass followed by
+ * vcr_nrc_train_step with the same pass: one wavefront launch runs the
+ * frame's training paths (which never read the weights) first and the
+ * pass's camera paths after them, so the long training paths overlap the
+ * short camera paths; the camera paths end in the cache, answered with the
+ * weights before this frame's update; then the gradient and Adam step.
+ * Needs the DDA tracker and params.nrc_events > 0. */
+VCR_API vcr_status vcr_nrc_frame(vcr_ctx* ctx, const vcr_pass_desc* pass, void* stream);
 VCR_API vcr_status vcr_nrc_info(vcr_ctx* ctx, vcr_nrc_info_t* out);
 VCR_API vcr_status vcr_nrc_get_weights(vcr_ctx* ctx, float* host_out, size_t count);
 VCR_API vcr_status vcr_nrc_set_weights(vcr_ctx* ctx, const float* host, size_t count);
@@ -512,10 +523,18 @@ VCR_API vcr_status vcr_morton_codes(vcr_ctx* ctx, const float* d_points, uint32_
 /* ------------------------------------------------------------------------ */
 /* Read back                                                                */
 /* ------------------------------------------------------------------------ */
-/* Synchronous copy of a context buffer to host memory (bytes must match). */
+/* Synchronous copy of a context buffer (bytes must match). host_out may be
+ * host, pinned or device memory of the context's device. */
 VCR_API vcr_status vcr_readback(vcr_ctx* ctx, vcr_buffer_id id, void* host_out, size_t bytes);
 /* Number of passes accumulated into the sums so far. */
 VCR_API vcr_status vcr_pass_count(vcr_ctx* ctx, uint32_t* out);
+/* Relative RMSE of the running mean image I against a reference mean image
+ * R (device, FP64 RGB, W*H*3):
+ *     sqrt( mean_p sum_c (I - R)^2 / (R^2 + 1e-2) ),
+ * written as one double to d_out (device). Stream-ordered and asynchronous,
+ * so an error curve can be recorded after every pass without a host sync.
+ * No reference counterpart (the reference only displays the image). */
+VCR_API vcr_status vcr_image_rel_rmse(vcr_ctx* ctx, const double* d_ref, double* d_out, void* stream);
 
 #ifdef __cplusplus
 }

@@ -94,6 +94,85 @@ def test_fit_converges_on_a_deterministic_target(cuda):
     assert np.isfinite(l1) and l1 < 0.05 * l0, (l0, l1)
 
 
+def test_moving_average_weights_serve_queries(cuda):
+    """With ema_decay > 0 queries use the averaged weights: right after
+    set_weights they equal the training weights (oracle forward of w); after
+    training they lag behind the training weights."""
+    import torch
+    desc, cloud = _cloud()
+    rng = np.random.default_rng(6)
+    recs = onrc.random_records(2048, cloud, rng)
+    _smooth_targets(recs, cloud)
+    with vcr.Context() as ctx:
+        _ctx_with_cloud(ctx, desc, cloud)
+        ctx.nrc_setup(train_samples=4096, learning_rate=3e-3, seed=8, ema_decay=0.99)
+        w = ctx.nrc_get_weights()
+        ctx.nrc_set_weights(w)
+        dr = _dev_records(recs, cuda)
+        out = torch.zeros(3 * len(recs), dtype=torch.float32, device=cuda)
+        ctx.nrc_forward(dr.data_ptr(), len(recs), out.data_ptr())
+        y0 = out.cpu().numpy().reshape(-1, 3)
+        ctx.nrc_fit(dr.data_ptr(), len(recs), 100)
+        ctx.synchronize()
+        ctx.nrc_forward(dr.data_ptr(), len(recs), out.data_ptr())
+        y1 = out.cpu().numpy().reshape(-1, 3)
+        w1 = ctx.nrc_get_weights()
+    ref0 = onrc.forward(w, recs, cloud)
+    scale = np.abs(ref0).mean() + 1e-3
+    assert np.abs(y0 - ref0).mean() <= 3e-3 * scale
+    ref1 = onrc.forward(w1, recs, cloud)
+    t = recs["w"]
+    err_avg, err_train = np.abs(y1 - t).mean(), np.abs(ref1 - t).mean()
+    assert np.abs(y1 - ref1).mean() > 1e-3 * scale  # not the training weights
+    assert err_avg < np.abs(ref0 - t).mean()  # but it has moved toward the targets
+    assert err_train < np.abs(ref0 - t).mean()
+
+
+def test_training_paths_are_calibrated_to_the_record_budget(cuda):
+    sc = configs.C1_PT
+    with vcr.Context() as ctx:
+        configs.setup_context(ctx, sc, width=128, height=128)
+        ctx.nrc_setup(train_samples=16384, seed=3)
+        counts = []
+        for k in range(4):
+            ctx.nrc_train_step(seed=5, pass_index=k)
+            counts.append(ctx.nrc_info()["train_records"])
+        ctx.set_camera(vcr.camera_look((0.2, 0.1, -0.4), (0.0, 0.0, 1.0), 70.0, 0.1, 128, 128))  # recalibrates
+        ctx.nrc_train_step(seed=5, pass_index=9)
+        ctx.nrc_train_step(seed=5, pass_index=10)
+        counts.append(ctx.nrc_info()["train_records"])
+    for c in counts[1:]:
+        assert 0.7 * 16384 <= c <= 1.4 * 16384, counts
+
+
+def test_frame_equals_pass_then_train_step(cuda):
+    """vcr_nrc_frame overlaps the training paths with the pass; its result
+    is the sequential pass + train step (up to the order of the gradient's
+    float atomics)."""
+    sc = configs.C1_PT
+    W = H = 96
+    prm = sc.params(vcr.TRACKER_DDA)
+    prm.nrc_events = 2
+    res = []
+    for mode in ("sequential", "frame"):
+        with vcr.Context() as ctx:
+            configs.setup_context(ctx, sc, width=W, height=H)
+            ctx.set_params(prm)
+            ctx.nrc_setup(train_samples=8192, learning_rate=3e-3, query_capacity=W * H, seed=2)
+            for k in range(4):
+                if mode == "frame":
+                    ctx.nrc_frame(seed=4, pass_index=k)
+                else:
+                    ctx.pt_pass(seed=4, pass_index=k)
+                    ctx.nrc_train_step(seed=4, pass_index=k)
+            ctx.synchronize()
+            res.append((ctx.image_sum(), ctx.nrc_get_weights(), ctx.nrc_info()))
+    (ia, wa, na), (ib, wb, nb) = res
+    assert na["steps"] == nb["steps"] == 4 and na["train_records"] == nb["train_records"]
+    np.testing.assert_allclose(wb, wa, rtol=0, atol=1e-5)
+    np.testing.assert_allclose(ib, ia, rtol=1e-4, atol=1e-7)
+
+
 def _image_mean(ctx, passes, seed):
     ctx.reset()
     for k in range(passes):
