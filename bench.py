@@ -16,6 +16,18 @@ e2e    : the same metric through the C-ABI with host buffers: the grid is
 roofline: the wavefront kernel's algorithmic bytes (8 texels x 2 B per
          density lookup) per launch / its launch time, against the measured
          HBM copy bandwidth.
+time_to_1pct: the headline comparison on the same scene.  R is an FP64
+         high-spp image of the plain tracker (two independent halves; their
+         difference measures R's own noise, which is subtracted from every
+         error below).  relRMSE = sqrt(mean_p sum_c (I - R)^2 / (R^2 + 1e-2)).
+         Plain tracker: unbiased, so its error is sqrt(V / passes) with V
+         the per-sample relative variance measured from R's halves (the
+         measured curve is reported beside it); time = passes to 1 % x
+         measured pass time.  Cached tracker (paths end in the radiance
+         cache after 2 events, 65,536 training records a frame, Adam lr
+         1e-3, moving-average weights for queries): warm-up steps, then
+         frames until its corrected error reaches 1 %; time = warm-up +
+         frames, device-timed.
 --impl reference: the CPU restatement of the reference's tracker (the
          oracle) on all host cores, on a bounded sample of the same passes.
 """
@@ -162,6 +174,7 @@ def run_vcr(args):
             c = ctx.counters()
             paths.append(c[0]); looks.append(c[1]); events.append(c[2])
         img = ctx.image_mean()
+        conv = convergence(ctx, sc, stream, args) if rank == 0 and not args.no_convergence else None
     if ws > 1:
         import torch.distributed as dist
         t = torch.tensor([ms_total], device="cuda")
@@ -201,12 +214,155 @@ def run_vcr(args):
                      "lookups_per_launch": int(lookups), "launch_ms": round(dur_ms, 4),
                      "lookups_per_s": round(lookups / (dur_ms / 1e3), 1)},
         "clocks": clocks,
+        "time_to_1pct": conv,
         "e2e": e2e,
         "cpu_baseline": cpu,
         "stats": {"events_per_path": round(float(np.sum(events)) / max(1, float(np.sum(paths))), 3),
                   "lookups_per_path": round(lookups / samples_per_step, 2), "image_mean": float(img.mean())},
     }
     print(json.dumps(line), flush=True)
+
+
+CONV = {"ref_passes": 4000, "plain_passes": 1000, "warm_steps": 1000, "max_frames": 8000, "chunk": 500,
+        "train_samples": 65536, "learning_rate": 1e-3, "ema_decay": 0.99, "nrc_events": 2}
+
+
+def convergence(ctx, sc, stream, args):
+    """Time to 1 % relRMSE against an FP64 high-spp image: plain tracker
+    and radiance-cached tracker on the bound scene (see the module text)."""
+    import torch
+    import vcr
+
+    sh = stream.cuda_stream
+    W, H = sc.width, sc.height
+    px = W * H
+    nr = CONV["ref_passes"]
+
+    def render(seed, n):
+        ctx.reset()
+        for k in range(n):
+            ctx.pt_pass(seed=seed, pass_index=k, stream=sh)
+        ctx.synchronize()
+        buf = torch.empty(px * 3, dtype=torch.float64, device="cuda")
+        ctx.readback_to(vcr.BUF_IMAGE_SUM, buf.data_ptr(), px * 24)
+        return buf / n
+
+    t0 = time.perf_counter()
+    ra = render(100, nr)
+    rb = render(200, nr)
+    ref_s = time.perf_counter() - t0
+    R = (ra + rb) / 2
+    e_ab = torch.sqrt(torch.sum((ra - rb) ** 2 / (R ** 2 + 1e-2)) / px).item()
+    noise2 = e_ab ** 2 / 4  # R's own relative MSE
+    V = e_ab ** 2 * nr / 2  # per-sample relative variance of the plain tracker
+    del ra, rb
+
+    def corrected(e):
+        return float(np.sqrt(max(e * e - noise2, 0.0)))
+
+    def run(n, frame, errs, ms, first):
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n)]
+        for k in range(n):
+            evs[k][0].record(stream)
+            frame(first + k)
+            evs[k][1].record(stream)
+            ctx.image_rel_rmse(R.data_ptr(), errs[first + k:].data_ptr(), stream=sh)
+        torch.cuda.synchronize()
+        ms.extend(a.elapsed_time(b) for a, b in evs)
+
+    # plain tracker
+    np_ = CONV["plain_passes"]
+    errs = torch.zeros(np_, dtype=torch.float64, device="cuda")
+    ms = []
+    ctx.reset()
+    run(np_, lambda k: ctx.pt_pass(seed=300, pass_index=k, stream=sh), errs, ms, 0)
+    e_plain = errs.cpu().numpy()
+    pass_ms = float(np.mean(ms))
+    plain_passes = V / 1e-4
+    plain = {"time_s": round(plain_passes * pass_ms / 1e3, 3), "passes": int(np.ceil(plain_passes)),
+             "pass_ms": round(pass_ms, 4),
+             "basis": "unbiased: relRMSE = sqrt(V/passes), V from the reference halves",
+             "check": {"passes": np_, "measured": round(corrected(e_plain[-1]), 5),
+                       "predicted": round(float(np.sqrt(V / np_)), 5)}}
+
+    # radiance-cached tracker
+    prm = sc.params(vcr.TRACKER_DDA)
+    prm.nrc_events = CONV["nrc_events"]
+    ctx.set_params(prm)
+    ctx.nrc_setup(train_samples=CONV["train_samples"], learning_rate=CONV["learning_rate"], query_capacity=px,
+                  seed=1, ema_decay=CONV["ema_decay"])
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for k in range(CONV["warm_steps"]):
+        ctx.nrc_train_step(seed=400, pass_index=k, stream=sh)
+    b.record(stream)
+    b.synchronize()
+    warm_ms = a.elapsed_time(b)
+    ctx.reset()
+    nmax, chunk = CONV["max_frames"], CONV["chunk"]
+    errs = torch.zeros(nmax, dtype=torch.float64, device="cuda")
+    ms = []
+    hit = None
+    done = 0
+    while done < nmax and hit is None:
+        run(chunk, lambda k: ctx.nrc_frame(seed=500, pass_index=CONV["warm_steps"] + k, stream=sh), errs, ms, done)
+        done += chunk
+        e = errs[:done].cpu().numpy()
+        for i in range(done - chunk, done):
+            if corrected(e[i]) <= 0.01:
+                hit = i
+                break
+    info = ctx.nrc_info()
+    ctx.set_params(sc.params(vcr.TRACKER_DDA))
+    e = errs[:done].cpu().numpy()
+    frames_ms = np.cumsum(ms)
+    nrc = {"frames": (hit + 1) if hit is not None else None, "frame_ms": round(float(np.mean(ms)), 4),
+           "warm_steps": CONV["warm_steps"], "warm_s": round(warm_ms / 1e3, 3),
+           "time_s": round((warm_ms + frames_ms[hit]) / 1e3, 3) if hit is not None else None,
+           "relrmse_last": round(corrected(e[-1]), 5), "frames_run": done,
+           "curve": {str(i + 1): round(corrected(e[i]), 5) for i in (0, 9, 99, 499, 999, 1999, 3999, done - 1)
+                     if i < done},
+           "train_records": info["train_records"], "loss": round(info["last_loss"], 4)}
+    out = {"plain": plain, "nrc": nrc,
+           "speedup": round(plain["time_s"] / nrc["time_s"], 2) if nrc["time_s"] else None,
+           "reference": {"passes": 2 * nr, "own_relrmse": round(float(np.sqrt(noise2)), 5), "render_s": round(ref_s, 2),
+                         "per_sample_rel_variance": round(V, 4)},
+           "settings": dict(CONV)}
+    return out
+
+
+def run_nrc_frames(args):
+    """Radiance-cached frames alone: warm-up steps, then args.nrc_frames
+    frames, each timed on the device; one JSON line with the means."""
+    import torch
+    import vcr
+    from vcr import configs
+
+    sc = configs.C5_NRC
+    stream = torch.cuda.Stream()
+    sh = stream.cuda_stream
+    with vcr.Context() as ctx:
+        configs.setup_context(ctx, sc)
+        ctx.set_tuning(majorant_level=1, dda_steps=8, stage_majorants=1, block_threads=256)
+        prm = sc.params(vcr.TRACKER_DDA)
+        prm.nrc_events = CONV["nrc_events"]
+        ctx.set_params(prm)
+        ctx.nrc_setup(train_samples=CONV["train_samples"], learning_rate=CONV["learning_rate"],
+                      query_capacity=sc.width * sc.height, seed=1, ema_decay=CONV["ema_decay"])
+        for k in range(args.warmup):
+            ctx.nrc_train_step(seed=400, pass_index=k, stream=sh)
+        ms = []
+        for k in range(args.nrc_frames):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            ctx.nrc_frame(seed=500, pass_index=args.warmup + k, stream=sh)
+            b.record(stream)
+            b.synchronize()
+            ms.append(a.elapsed_time(b))
+        info = ctx.nrc_info()
+    print(json.dumps({"workload": sc.name + " radiance-cached frames", "frames": args.nrc_frames,
+                      "frame_ms": round(float(np.mean(ms)), 4), "queries": info["queries"],
+                      "train_records": info["train_records"]}), flush=True)
 
 
 def run_e2e(args, sc, device, sh):
@@ -274,17 +430,21 @@ class OracleScene:
         return int(max(1, min(self.sc.height, seconds / max(per_row, 1e-6))))
 
 
-def cpu_baseline(sc, args, budget_s=15.0):
+def cpu_baseline(sc, args, budget_s=12.0):
+    """Passes over a band of rows through the image centre until about
+    budget_s seconds of work are done (at most 64 passes)."""
     os_ = OracleScene(sc)
     rows = os_.rows_for(budget_s / 4)
     done = t = 0.0
-    for k in range(4):
+    k = 0
+    while (t < budget_s and k < 64) or k < 2:
         p, dt = os_.pass_rows(rows, k + 1)
         done += p
         t += dt
+        k += 1
     return {"value": round(done / t / 1e6, 4), "unit": UNIT, "cores": os_.threads, "kind": "port",
-            "sample": f"4 passes x {rows} full-width rows through the image centre = {int(done)} camera paths, "
-                      f"{t:.1f} s of CPU time (grid setup {os_.setup_s:.1f} s not counted)"}
+            "sample": f"{k} passes x {rows} full-width rows through the image centre = {int(done)} camera paths, "
+                      f"{t:.1f} s on {os_.threads} threads (grid setup {os_.setup_s:.1f} s not counted)"}
 
 
 def run_reference(args):
@@ -323,10 +483,17 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="vcr", choices=["vcr", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    ap.add_argument("--no-convergence", action="store_true", help="skip the time-to-1 %% comparison")
+    ap.add_argument("--nrc-frames", type=int, default=0,
+                    help="only time this many radiance-cached frames on the scene (a profiling workload)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.impl == "reference":
+    if args.nrc_frames:
+        import __graft_entry__ as ge
+        ge.build()
+        run_nrc_frames(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         import __graft_entry__ as ge
