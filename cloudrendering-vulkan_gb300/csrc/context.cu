@@ -172,6 +172,7 @@ extern "C" VCR_API vcr_status vcr_destroy(vcr_ctx* ctx) {
   ppb_free(ctx);
   ppm_free(ctx);
   nrc_free(ctx);
+  batch_free(ctx);
   if (ctx->work_done) cudaEventDestroy(ctx->work_done);
   delete ctx;
   return VCR_OK;

@@ -162,12 +162,36 @@ inline vcr_status make_pass_view(vcr_ctx* ctx, const vcr_pass_desc* pass, PassVi
   return VCR_OK;
 }
 
+// One view of a batched launch (vcr_batch_*): camera, frame and sun, and
+// where the view's work items and pixels start in the batch's ranges.
+struct BatchView {
+  CamView cam;
+  f3 sun;              // direction the sunlight travels
+  uint32_t width, height;
+  uint32_t path0;      // first work item of the view
+  uint32_t pix0;       // first pixel of the view in the batch's sums
+};
+// View v of a batch draws its paths' streams with seed + v * kViewSeedStep,
+// keyed like a single-view pass by its own pixel index and the pass.
+constexpr uint32_t kViewSeedStep = 0x9E3779B9u;
+static_assert(sizeof(BatchView) % 8 == 0, "BatchView is copied in 8-byte words");
+constexpr uint32_t kMaxBatchViews = 256;
+
+struct BatchSink {
+  const BatchView* views;    // device table, ascending path0
+  uint32_t count;
+  const uint32_t* pass_ctr;  // device pass counter added to the pass index
+};
+
 // DDA wavefront tracker launch (pt_wavefront.cu).
 // `total` camera paths of the pass, preceded by train->paths training paths
-// of the radiance cache when `train` is given.
+// of the radiance cache when `train` is given.  With `batch`, the camera
+// paths are those of the batch's views (cam is unused) and sum is the
+// batch's sums.
 struct NrcTrainSink;
 vcr_status wavefront_launch(vcr_ctx* ctx, const GridView& g, const SceneView& s, const CamView& cam,
                             const PassView& pv, uint32_t* stats, Counters cnt, uint32_t total, cudaStream_t st,
-                            const NrcTrainSink* train = nullptr);
+                            const NrcTrainSink* train = nullptr, const BatchSink* batch = nullptr,
+                            double* sum = nullptr);
 
 }  // namespace vcr

@@ -134,21 +134,36 @@ constexpr uint32_t kTrainPath = 0x80000000u;  // pid flag of a training path
 // measured ~7% faster than 3 CTAs at 77 registers on the 1024x512x1024 scene.
 // Work items [0, ts.paths) are training paths (their pid carries kTrainPath
 // and their pix the slot of their last record); the pass's camera paths
-// follow.
-template <int kThreads, bool kStage>
+// follow.  kBatch: the camera paths are those of bt's views (pid holds the
+// view, whose sun the path uses), the view table sits in shared memory
+// after the staged majorants, and the pass index adds *bt.pass_ctr (so a
+// replayed graph renders consecutive passes).
+__host__ __device__ constexpr uint32_t align16(uint32_t b) { return (b + 15u) & ~15u; }
+
+template <int kThreads, bool kStage, bool kBatch>
 __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
     pt_wavefront_kernel(GridView g, SceneView s, CamView cam, PassView pv, double* __restrict__ sum,
                         uint32_t* __restrict__ stats, Counters cnt, uint32_t total, uint32_t dda_steps,
-                        uint32_t maj_bytes, NrcSink nq, NrcTrainSink ts, int* __restrict__ err) {
+                        uint32_t maj_bytes, NrcSink nq, NrcTrainSink ts, BatchSink bt, int* __restrict__ err) {
   extern __shared__ __align__(16) float s_maj[];
   __shared__ __align__(8) uint64_t s_bar;
   const float* maj = g.majorants;
   if (kStage) {
     if (stage_to_smem(s_maj, g.majorants, maj_bytes, &s_bar, err)) maj = s_maj;
   }
+  BatchView* s_views = reinterpret_cast<BatchView*>(reinterpret_cast<char*>(s_maj) + (kStage ? align16(maj_bytes) : 0u));
+  uint32_t pass = pv.pass;
+  if (kBatch) {
+    const uint2* src = reinterpret_cast<const uint2*>(bt.views);
+    uint2* dst = reinterpret_cast<uint2*>(s_views);
+    const uint32_t words = bt.count * (uint32_t)(sizeof(BatchView) / 8);
+    for (uint32_t i = threadIdx.x; i < words; i += blockDim.x) dst[i] = src[i];
+    pass += *bt.pass_ctr;
+    __syncthreads();
+  }
   const uint32_t lane = threadIdx.x & 31u;
   const float k = s.k_sigma;
-  const f3 lsun = -s.sun;
+  const f3 lsun0 = -s.sun;
   uint32_t mode = kIdle;
   bool exhausted = false, flying = false, need_init = false;
   float tau = 0.0f;
@@ -173,8 +188,35 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
         uint32_t id = base + __popc(mask & ((1u << lane) - 1u));
         if (id >= total + ts.paths) {
           exhausted = true;
+        } else if (kBatch) {  // camera path of a view: the last view with path0 <= id
+          uint32_t lo = 0, hi = bt.count - 1u;
+          while (lo < hi) {
+            uint32_t mid = (lo + hi + 1u) >> 1;
+            if (s_views[mid].path0 <= id) lo = mid;
+            else hi = mid - 1u;
+          }
+          const BatchView& bv = s_views[lo];
+          uint32_t local = id - bv.path0;
+          uint32_t per_row = bv.width * pv.spp;
+          uint32_t cy = local / per_row, rem = local - cy * per_row;
+          uint32_t cx = rem / pv.spp, sp = rem - cx * pv.spp;
+          uint32_t lp = cy * bv.width + cx;
+          pid = lo;
+          pix = bv.pix0 + lp;
+          rng = rng_pcg(pv.seed + kViewSeedStep * lo, lp * pv.spp + sp, pass);
+          L = mk(0.f, 0.f, 0.f);
+          beta = 1.0f;
+          events = lookups = cells = 0;
+          ++n_paths;
+          if (start_path(bv.cam, s, (int)cx, (int)cy, pos, dir, L)) {
+            mode = kScatter;
+            idir = dir;
+            need_init = true;
+          } else {
+            write_result(pv, sum, pix, L, atomic);
+          }
         } else if (id < ts.paths) {  // training path from a uniformly drawn pixel of the crop
-          rng = rng_pcg(pv.seed ^ kNrcTrainSalt, id, pv.pass);
+          rng = rng_pcg(pv.seed ^ kNrcTrainSalt, id, pass);
           uint32_t pp = (uint32_t)(rng_next(rng) * (float)(pv.cw * pv.ch));
           pp = min(pp, pv.cw * pv.ch - 1u);
           pid = kTrainPath;
@@ -196,7 +238,7 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
           uint32_t cx = rem / pv.spp, sp = rem - cx * pv.spp;
           int x = (int)(pv.x0 + cx), y = (int)(pv.y0 + cy);
           pix = (uint32_t)y * pv.width + (uint32_t)x;
-          rng = rng_pcg(pv.seed, pix * pv.spp + sp, pv.pass);
+          rng = rng_pcg(pv.seed, pix * pv.spp + sp, pass);
           L = mk(0.f, 0.f, 0.f);
           beta = 1.0f;
           events = lookups = cells = 0;
@@ -227,6 +269,7 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
       if (r != kPending) {
         flying = false;
         bool nee_done = false, finish = false;
+        const f3 lsun = kBatch ? -s_views[pid].sun : lsun0;
         if (r == kCandidate) {
           f3 rd = mode == kScatter ? dir : lsun;
           f3 p = along(pos, rd, tr.t);
@@ -256,7 +299,7 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
                 }
               } else {
                 beta = beta * s.albedo;
-                phase = hg_pdf(s.ph, dot(-dir, s.sun));
+                phase = hg_pdf(s.ph, dot(-dir, -lsun));
                 T = 1.0f;
                 mode = kNee;
                 idir = lsun;
@@ -325,14 +368,15 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
 
 constexpr uint32_t kMaxStagedBytes = 96u * 1024u;
 
-template <int kThreads, bool kStage>
+template <int kThreads, bool kStage, bool kBatch>
 static vcr_status launch_t(vcr_ctx* ctx, const GridView& g, const SceneView& s, const CamView& cam,
                            const PassView& pv, uint32_t* stats, Counters cnt, uint32_t total, uint32_t maj_bytes,
-                           const NrcTrainSink& ts, cudaStream_t st) {
-  auto kern = pt_wavefront_kernel<kThreads, kStage>;
-  size_t smem = kStage ? maj_bytes : 0;
-  if (kStage)  // the attribute is per device, so it is set on every launch (a host-side call)
-    VCR_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxStagedBytes));
+                           const NrcTrainSink& ts, const BatchSink& bt, double* sum, cudaStream_t st) {
+  auto kern = pt_wavefront_kernel<kThreads, kStage, kBatch>;
+  size_t smem = (kStage ? align16(maj_bytes) : 0u) + (kBatch ? bt.count * sizeof(BatchView) : 0u);
+  if (kStage || kBatch)  // the attribute is per device, so it is set on every launch (a host-side call)
+    VCR_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)(kMaxStagedBytes + kMaxBatchViews * sizeof(BatchView))));
   int per_sm = 0;
   VCR_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem));
   if (per_sm < 1) per_sm = 1;
@@ -342,28 +386,41 @@ static vcr_status launch_t(vcr_ctx* ctx, const GridView& g, const SceneView& s, 
   if (blocks == 0) return VCR_OK;
   NrcSink nq{nullptr, nullptr, 0u};
   if (s.nrc_events && ctx->nrc) nq = NrcSink{ctx->nrc->query, ctx->nrc->query_count, ctx->nrc->query_capacity};
-  kern<<<blocks, kThreads, smem, st>>>(g, s, cam, pv, ctx->d_sum, stats, cnt, total, ctx->tuning.dda_steps,
-                                       maj_bytes, nq, ts, ctx->d_error);
+  kern<<<blocks, kThreads, smem, st>>>(g, s, cam, pv, sum, stats, cnt, total, ctx->tuning.dda_steps, maj_bytes, nq,
+                                       ts, bt, ctx->d_error);
   VCR_CUDA(ctx, cudaGetLastError());
   return VCR_OK;
 }
 
+template <bool kBatch>
+static vcr_status launch_b(vcr_ctx* ctx, const GridView& g, const SceneView& s, const CamView& cam,
+                           const PassView& pv, uint32_t* stats, Counters cnt, uint32_t total, uint32_t bytes,
+                           bool stage, const NrcTrainSink& ts, const BatchSink& bt, double* sum, cudaStream_t st) {
+  if (ctx->tuning.block_threads == 128)
+    return stage ? launch_t<128, true, kBatch>(ctx, g, s, cam, pv, stats, cnt, total, bytes, ts, bt, sum, st)
+                 : launch_t<128, false, kBatch>(ctx, g, s, cam, pv, stats, cnt, total, bytes, ts, bt, sum, st);
+  return stage ? launch_t<256, true, kBatch>(ctx, g, s, cam, pv, stats, cnt, total, bytes, ts, bt, sum, st)
+               : launch_t<256, false, kBatch>(ctx, g, s, cam, pv, stats, cnt, total, bytes, ts, bt, sum, st);
+}
+
 vcr_status wavefront_launch(vcr_ctx* ctx, const GridView& g, const SceneView& s, const CamView& cam,
                             const PassView& pv, uint32_t* stats, Counters cnt, uint32_t total, cudaStream_t st,
-                            const NrcTrainSink* train) {
+                            const NrcTrainSink* train, const BatchSink* batch, double* sum) {
   const vcr_tuning& t = ctx->tuning;
   NrcTrainSink ts{nullptr, nullptr, 0u, 0u};
   if (train) ts = *train;
+  BatchSink bt{nullptr, 0u, nullptr};
+  if (batch) bt = *batch;
   if ((uint64_t)total + ts.paths >= (uint64_t)kTrainPath)
     return fail(ctx, VCR_ERR_UNSUPPORTED, "more than 2^31 paths in one launch");
+  if (batch && (train || bt.count == 0 || bt.count > kMaxBatchViews || !bt.views || !bt.pass_ctr))
+    return fail(ctx, VCR_ERR_INVALID, "a batch launch needs 1..%u views and no training paths", kMaxBatchViews);
   size_t cells = (size_t)g.mnb[0] * g.mnb[1] * g.mnb[2];
   uint32_t bytes = (uint32_t)(((cells + 3) & ~(size_t)3) * sizeof(float));  // padded level: 16-byte multiple
   bool stage = t.stage_majorants && bytes <= kMaxStagedBytes;
-  if (t.block_threads == 128)
-    return stage ? launch_t<128, true>(ctx, g, s, cam, pv, stats, cnt, total, bytes, ts, st)
-                 : launch_t<128, false>(ctx, g, s, cam, pv, stats, cnt, total, bytes, ts, st);
-  return stage ? launch_t<256, true>(ctx, g, s, cam, pv, stats, cnt, total, bytes, ts, st)
-               : launch_t<256, false>(ctx, g, s, cam, pv, stats, cnt, total, bytes, ts, st);
+  if (!sum) sum = ctx->d_sum;
+  return batch ? launch_b<true>(ctx, g, s, cam, pv, stats, cnt, total, bytes, stage, ts, bt, sum, st)
+               : launch_b<false>(ctx, g, s, cam, pv, stats, cnt, total, bytes, stage, ts, bt, sum, st);
 }
 
 }  // namespace vcr

@@ -15,6 +15,7 @@ namespace vcr {
 struct PpbState;
 struct PpmState;
 struct NrcState;
+struct BatchState;
 }  // namespace vcr
 
 struct vcr_ctx {
@@ -70,6 +71,7 @@ struct vcr_ctx {
   vcr::PpbState* ppb = nullptr;
   vcr::PpmState* ppm = nullptr;
   vcr::NrcState* nrc = nullptr;
+  vcr::BatchState* batch = nullptr;
 };
 
 namespace vcr {
@@ -112,6 +114,7 @@ vcr_status pt_pass_launch(vcr_ctx* ctx, const vcr_pass_desc* pass, cudaStream_t 
 void ppb_free(vcr_ctx* ctx);
 void ppm_free(vcr_ctx* ctx);
 void nrc_free(vcr_ctx* ctx);
+void batch_free(vcr_ctx* ctx);
 
 // nrc.cu: queries of paths that end in the radiance cache
 uint32_t nrc_query_capacity(const vcr_ctx* ctx);

@@ -235,6 +235,55 @@ class Context:
         self._ck(lib().vcr_nrc_gradient(self.h, C.c_void_p(d_records), n, _ptr(g), g.size, C.byref(loss)))
         return g, loss.value
 
+    # batched views ----------------------------------------------------------
+    def batch_setup(self, views):
+        """views: list of (camera, width, height, sun_dir)."""
+        arr = (_abi.ViewDesc * len(views))()
+        for i, (cam, w, h, sun) in enumerate(views):
+            arr[i].camera = cam
+            arr[i].width, arr[i].height = w, h
+            for a in range(3):
+                arr[i].sun_dir[a] = sun[a]
+        self._batch_sizes = [(w, h) for _, w, h, _ in views]
+        self._ck(lib().vcr_batch_setup(self.h, arr, len(views)))
+
+    def batch_free(self):
+        self._ck(lib().vcr_batch_free(self.h))
+
+    def batch_pass(self, seed=0, pass_index=0, spp=1, stream=0):
+        p = _abi.PassDesc()
+        p.seed, p.pass_index, p.spp = seed, pass_index, spp
+        self._ck(lib().vcr_batch_pass(self.h, C.byref(p), C.c_void_p(stream)))
+
+    def batch_graph_record(self, seed=0, pass_index=0, spp=1):
+        p = _abi.PassDesc()
+        p.seed, p.pass_index, p.spp = seed, pass_index, spp
+        self._ck(lib().vcr_batch_graph_record(self.h, C.byref(p)))
+
+    def batch_graph_replay(self, count, stream=0):
+        self._ck(lib().vcr_batch_graph_replay(self.h, count, C.c_void_p(stream)))
+
+    def batch_autotune(self, seed=0, pass_index=0, spp=1, stream=0) -> dict:
+        p = _abi.PassDesc()
+        p.seed, p.pass_index, p.spp = seed, pass_index, spp
+        t = _abi.Tuning()
+        self._ck(lib().vcr_batch_autotune(self.h, C.byref(p), C.byref(t), C.c_void_p(stream)))
+        return {f: getattr(t, f) for f, _ in _abi.Tuning._fields_}
+
+    def batch_read(self, view) -> np.ndarray:
+        w, h = self._batch_sizes[view]
+        out = np.empty((h, w, 3), np.float64)
+        self._ck(lib().vcr_batch_read(self.h, view, _ptr(out), out.nbytes))
+        return out
+
+    def batch_info(self) -> dict:
+        i = _abi.BatchInfo()
+        self._ck(lib().vcr_batch_info(self.h, C.byref(i)))
+        return {f: getattr(i, f) for f, _ in _abi.BatchInfo._fields_}
+
+    def batch_reset(self):
+        self._ck(lib().vcr_batch_reset(self.h))
+
     # photon mapping ---------------------------------------------------------
     def ppm_setup(self, photons, capacity, radius, alpha=0.7):
         p = _abi.PpmParams(photons, capacity, radius, alpha)

@@ -63,6 +63,15 @@ class Tuning(C.Structure):
                 ("block_threads", C.c_uint32)]
 
 
+class ViewDesc(C.Structure):
+    _fields_ = [("camera", Camera), ("width", C.c_uint32), ("height", C.c_uint32), ("sun_dir", F3),
+                ("reserved", C.c_uint32)]
+
+
+class BatchInfo(C.Structure):
+    _fields_ = [("views", C.c_uint32), ("passes", C.c_uint32), ("pixels", C.c_uint64), ("samples", C.c_uint64)]
+
+
 class NrcParams(C.Structure):
     _fields_ = [("train_samples", C.c_uint32), ("learning_rate", C.c_float), ("query_capacity", C.c_uint32),
                 ("seed", C.c_uint32), ("ema_decay", C.c_float)]
@@ -152,6 +161,15 @@ SIGNATURES = {
     "vcr_nrc_forward": (_S, [_P, _P, _u32, _P, _P]),
     "vcr_nrc_gradient": (_S, [_P, _P, _u32, _P, _sz, C.POINTER(_f)]),
     "vcr_nrc_fit": (_S, [_P, _P, _u32, _u32, _P]),
+    "vcr_batch_setup": (_S, [_P, C.POINTER(ViewDesc), _u32]),
+    "vcr_batch_free": (_S, [_P]),
+    "vcr_batch_pass": (_S, [_P, C.POINTER(PassDesc), _P]),
+    "vcr_batch_graph_record": (_S, [_P, C.POINTER(PassDesc)]),
+    "vcr_batch_graph_replay": (_S, [_P, _u32, _P]),
+    "vcr_batch_autotune": (_S, [_P, C.POINTER(PassDesc), C.POINTER(Tuning), _P]),
+    "vcr_batch_read": (_S, [_P, _u32, _P, _sz]),
+    "vcr_batch_info": (_S, [_P, C.POINTER(BatchInfo)]),
+    "vcr_batch_reset": (_S, [_P]),
     "vcr_ppm_setup": (_S, [_P, C.POINTER(PpmParams)]),
     "vcr_ppm_free": (_S, [_P]),
     "vcr_ppm_pass": (_S, [_P, C.POINTER(PassDesc), _P]),

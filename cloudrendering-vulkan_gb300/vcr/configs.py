@@ -89,6 +89,31 @@ C5_NRC = Scene("C5-nrc-1024x512x1024-fp16-1920x1080", (1024, 512, 1024), 8, 32.0
 
 ALL = [C1_PT, C2_PPM, C3_PPB, C4_BATCH, C5_NRC]
 
+C4_ELEVATIONS = tuple(5.0 + 75.0 * i / 7.0 for i in range(8))  # 5 .. 80 deg
+
+
+def c4_views(count=64, seed=1, fov_y_deg=60.0):
+    """The batched configuration's views: square frames with sides drawn
+    uniformly from [256, 1024] (numpy generator seeded `seed`); cameras on a
+    ring around the cloud centre (0, 0, 0.5) at radius 1.4, 0.25 above its
+    plane, looking at the centre; view v uses sun elevation index v mod 8
+    (C4_ELEVATIONS) at the default azimuth.  Returns (camera, w, h, sun)."""
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    sides = rng.integers(256, 1025, size=count)
+    centre = np.array([0.0, 0.0, 0.5])
+    out = []
+    for v in range(count):
+        a = 2.0 * math.pi * v / count
+        pos = centre + np.array([1.4 * math.sin(a), 0.25, -1.4 * math.cos(a)])
+        fwd = centre - pos
+        fwd = fwd / np.linalg.norm(fwd)
+        s = int(sides[v])
+        cam = camera_look(tuple(pos), tuple(fwd), fov_y_deg, 0.1, s, s)
+        out.append((cam, s, s, sun_travel_dir(C4_ELEVATIONS[v % 8])))
+    return out
+
 
 def setup_context(ctx, scene: Scene, tracker=_abi.TRACKER_DDA, precision=None, width=None, height=None):
     """Generate the scene's grid on the device and bind cloud, camera, params, frame."""

@@ -521,6 +521,52 @@ VCR_API vcr_status vcr_morton_codes(vcr_ctx* ctx, const float* d_points, uint32_
                                     const float bounds_max[3], uint32_t bits, uint32_t* d_codes, void* stream);
 
 /* ------------------------------------------------------------------------ */
+/* Batched multi-view tracking                                              */
+/* ------------------------------------------------------------------------ */
+/* Many views, each a camera with its own frame size and sun direction, in
+ * one persistent DDA-wavefront launch over one work range.  The reference
+ * dispatches one camera per RecordDrawCommands (RenderTechniquePT.cpp:
+ * 129-168); a batch pass is that dispatch for every view at once.  View v
+ * draws its streams with seed + v * 0x9E3779B9, keyed by its own pixel
+ * index and the pass like vcr_pt_pass, so each view equals a single-view
+ * pass with that seed.  The scene (grid, cloud, params except the sun) is
+ * the context's; params must select the DDA tracker, PCG streams, ratio
+ * NEE and no cache. */
+typedef struct vcr_view_desc {
+  vcr_camera camera;
+  uint32_t width, height;
+  float sun_dir[3];   /* direction the sunlight travels (unit) */
+  uint32_t reserved;
+} vcr_view_desc;
+
+typedef struct vcr_batch_info_t {
+  uint32_t views;
+  uint32_t passes;
+  uint64_t pixels;   /* all views */
+  uint64_t samples;  /* camera samples per pixel summed over passes */
+} vcr_batch_info_t;
+
+/* 1..256 views, < 2^31 pixels in all; allocates the FP64 sums. */
+VCR_API vcr_status vcr_batch_setup(vcr_ctx* ctx, const vcr_view_desc* views, uint32_t count);
+VCR_API vcr_status vcr_batch_free(vcr_ctx* ctx);
+/* One pass over every view (pass->spp samples per pixel; crop and flags
+ * must be zero). */
+VCR_API vcr_status vcr_batch_pass(vcr_ctx* ctx, const vcr_pass_desc* pass, void* stream);
+/* Record one batch pass as a CUDA graph (synchronous).  Each replay renders
+ * the next pass index, starting at pass->pass_index; a later pass with a
+ * different spp drops the graph. */
+VCR_API vcr_status vcr_batch_graph_record(vcr_ctx* ctx, const vcr_pass_desc* pass);
+VCR_API vcr_status vcr_batch_graph_replay(vcr_ctx* ctx, uint32_t count, void* stream);
+/* Times a batch pass per candidate tuning (majorant level x DDA cells per
+ * wavefront step x CTA size), keeps the fastest, clears the sums. */
+VCR_API vcr_status vcr_batch_autotune(vcr_ctx* ctx, const vcr_pass_desc* pass, vcr_tuning* out, void* stream);
+/* FP64 RGB sums of one view (width * height * 3 doubles; host or device
+ * memory). */
+VCR_API vcr_status vcr_batch_read(vcr_ctx* ctx, uint32_t view, double* out, size_t bytes);
+VCR_API vcr_status vcr_batch_info(vcr_ctx* ctx, vcr_batch_info_t* out);
+VCR_API vcr_status vcr_batch_reset(vcr_ctx* ctx);
+
+/* ------------------------------------------------------------------------ */
 /* Read back                                                                */
 /* ------------------------------------------------------------------------ */
 /* Synchronous copy of a context buffer (bytes must match). host_out may be

@@ -617,14 +617,16 @@ int oracle_pt_pass(void* h, int level, const vcr_cloud* cl, const vcr_camera* ca
     for (uint32_t cx = 0; cx < cw; ++cx) {
       int x = (int)(x0 + cx), y = (int)(y0 + (uint32_t)row);
       uint32_t pix = (uint32_t)y * width + (uint32_t)x;
-      V3 Ls = v3(0, 0, 0);
+      double Ls[3] = {0.0, 0.0, 0.0};  // every sample is added in FP64, as the GPU does
       Counts c;
       for (uint32_t sp = 0; sp < spp; ++sp) {
         Rng rng = ref ? rng_xorshift(pass->seed * ((uint32_t)x + (uint32_t)y * padded_w))
                       : rng_pcg(pass->seed, pix * spp + sp, pass->pass_index);
         Counts cs;
         V3 L = trace_path(s, *cam, x, y, rng, cs);
-        Ls = add(Ls, L);
+        Ls[0] += (double)L.x;
+        Ls[1] += (double)L.y;
+        Ls[2] += (double)L.z;
         if (sp == 0 || s.tracker == 0) {
           c.events += cs.events;
           c.lookups += cs.lookups;
@@ -633,9 +635,9 @@ int oracle_pt_pass(void* h, int level, const vcr_cloud* cl, const vcr_camera* ca
       }
       double* o = sum + 3 * (size_t)pix;
       if (pass->flags & VCR_PASS_NO_ACCUMULATE) {
-        o[0] = Ls.x; o[1] = Ls.y; o[2] = Ls.z;
+        o[0] = Ls[0]; o[1] = Ls[1]; o[2] = Ls[2];
       } else {
-        o[0] += Ls.x; o[1] += Ls.y; o[2] += Ls.z;
+        o[0] += Ls[0]; o[1] += Ls[1]; o[2] += Ls[2];
       }
       if (stats) {
         uint32_t* st = stats + 4 * (size_t)pix;
