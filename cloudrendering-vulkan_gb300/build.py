@@ -45,6 +45,7 @@ def _compile(src: str, extra: list[str]) -> str:
     deps = [src] + [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".cuh", ".h"))]
     deps += [os.path.join(HOST, h) for h in os.listdir(HOST) if h.endswith(".h")]
     deps.append(os.path.join(HERE, "..", "include", "vcr", "abi.h"))
+    deps.append(os.path.join(HERE, "..", "include", "vcr", "render_technique.hpp"))
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(d) for d in deps if os.path.exists(d)):
         return obj
     lang = ["-x", "cu"] if src.endswith(".cu") else ["-x", "c++"]

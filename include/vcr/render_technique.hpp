@@ -1,0 +1,194 @@
+/* C++ host layer over the vcr C-ABI: the reference's RenderTechnique
+ * lifecycle (RenderTechnique.h:15-67) for a headless GB300 device.
+ *
+ *   reference (Vulkan)                           here
+ *   RenderTechnique(VulkanDevice*, PushConstants*)  RenderTechnique(Device&, PushConstants*)
+ *   QueueUpdateCloudData / ...Sampler             BindCloud(grid, cloud, precision)
+ *   QueueUpdateCameraProperties                   BindCamera
+ *   QueueUpdateParameters                         BindParameters
+ *   QueueUpdateShadowVolume / ...Sampler          BindShadowVolume
+ *   UpdateDescriptorSets (RenderTechnique.cpp:14-18)  Commit: applies the queued bindings
+ *   SetFrameReferences / ClearFrameReferences     SetFrameTarget / ClearFrameTarget (device sums)
+ *   RecordDrawCommands(VkCommandBuffer, image)    RecordPass(stream, passIndex)
+ *   RenderTechniquePPM/PPB::AllocateResources /   AllocateResources / FreeResources
+ *   FreeResources
+ *   RenderTechniquePPB::UpdatePhotonMapProperties UpdatePhotonMapProperties
+ *
+ * Errors: the reference aborts (Validation.cpp:4-10) or throws
+ * std::runtime_error; every failing vcr call here throws vcr::Error with the
+ * status and the context's message.  Ownership: as in the reference, a
+ * technique holds non-owning pointers to the device and the push
+ * constants, and updates pushConstants->pmRadius (RenderTechniquePPM.cpp:
+ * 306-310) and frameCount.  Streams are cudaStream_t passed as void*.
+ * One host thread drives a device (the reference's single recording
+ * thread, main.cpp:603-712). */
+#pragma once
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "abi.h"
+
+namespace vcr {
+
+class VCR_API Error : public std::runtime_error {
+ public:
+  Error(vcr_status status, const std::string& msg) : std::runtime_error(msg), status_(status) {}
+  vcr_status status() const { return status_; }
+
+ private:
+  vcr_status status_;
+};
+
+/* Throws vcr::Error for a status other than VCR_OK. */
+VCR_API void Check(vcr_status status, const vcr_ctx* ctx = nullptr);
+
+/* PushConstants (UniformBuffers.h:6-13). */
+struct PushConstants {
+  double time = 0;
+  int seed = 100;
+  uint32_t frameCount = 1;
+  float pmRadius = 0;
+  uint32_t currentBuffer = 0;
+};
+
+/* A GPU context (stands for VulkanDevice). */
+class VCR_API Device {
+ public:
+  explicit Device(int device = 0);
+  ~Device();
+  Device(const Device&) = delete;
+  Device& operator=(const Device&) = delete;
+  vcr_ctx* Handle() const { return ctx_; }
+  void Synchronize();
+
+ private:
+  vcr_ctx* ctx_ = nullptr;
+};
+
+/* Grid3D<float> (Grid3D.h:5-192): a dense x-fastest grid with its voxel
+ * size; Load / Save use the .xyz format (Grid3D.h:44-90, 166-178). */
+struct VCR_API Grid {
+  vcr_grid_desc desc{};
+  std::vector<float> data;
+
+  static Grid Load(const std::string& path);
+  void Save(const std::string& path) const;
+  /* Seeded Perlin fBm of the given size (the synthetic cloud). */
+  static Grid Generate(uint32_t x, uint32_t y, uint32_t z, const vcr_fbm_desc& fbm);
+  float GetMajorant() const; /* max density (Grid3D.h:180-192) */
+};
+
+class VCR_API RenderTechnique {
+ public:
+  RenderTechnique(Device& device, PushConstants* pushConstants);
+  virtual ~RenderTechnique() = default;
+  RenderTechnique(const RenderTechnique&) = delete;
+  RenderTechnique& operator=(const RenderTechnique&) = delete;
+
+  /* Queue updates; nothing reaches the device before Commit. */
+  void BindCloud(const Grid& grid, const vcr_cloud& cloud, int precision = VCR_PREC_FP32);
+  void BindCamera(const vcr_camera& camera);
+  void BindParameters(const vcr_params& params);
+  void BindShadowVolume(const vcr_shadow_volume& shadowVolume);
+  /* Apply the queued updates (UpdateDescriptorSets).  A changed cloud,
+   * camera, parameters or frame restarts the progressive accumulation. */
+  void Commit();
+
+  void SetFrameTarget(uint32_t width, uint32_t height);
+  void ClearFrameTarget();
+
+  /* One progressive pass on `stream` (RecordDrawCommands).  Increments
+   * pushConstants->frameCount. */
+  virtual void RecordPass(void* stream, uint32_t passIndex) = 0;
+  virtual void AllocateResources() {}
+  virtual void FreeResources() {}
+
+  /* The accumulated mean image, float RGB, width * height * 3. */
+  std::vector<float> ReadMean() const;
+  uint32_t PassCount() const;
+  uint32_t Width() const { return width_; }
+  uint32_t Height() const { return height_; }
+  vcr_ctx* Context() const { return device_->Handle(); }
+
+ protected:
+  void Require(bool condition, const char* what) const;
+  vcr_pass_desc PassDesc(uint32_t passIndex, uint32_t spp = 1) const;
+  void Advance();  // after a recorded pass: frameCount += 1
+
+  Device* device_ = nullptr;
+  PushConstants* pushConstants_ = nullptr;
+  bool frameSet_ = false;
+  uint32_t width_ = 0, height_ = 0;
+
+ private:
+  const Grid* pendingGrid_ = nullptr;
+  vcr_cloud pendingCloud_{};
+  int pendingPrecision_ = VCR_PREC_FP32;
+  bool hasPendingCloud_ = false;
+  vcr_camera pendingCamera_{};
+  bool hasPendingCamera_ = false;
+  vcr_params pendingParams_{};
+  bool hasPendingParams_ = false;
+  vcr_shadow_volume pendingShadowVolume_{};
+  bool hasPendingShadowVolume_ = false;
+};
+
+/* RenderTechniquePT (RenderTechniquePT.h:11): delta/ratio tracking. */
+class VCR_API TechniquePT : public RenderTechnique {
+ public:
+  using RenderTechnique::RenderTechnique;
+  void RecordPass(void* stream, uint32_t passIndex) override;
+  uint32_t samplesPerPass = 1;
+};
+
+/* RenderTechniquePPM (RenderTechniquePPM.h:19): progressive photon mapping
+ * with per-pixel FP64 statistics. */
+class VCR_API TechniquePPM : public RenderTechnique {
+ public:
+  TechniquePPM(Device& device, PushConstants* pushConstants, const vcr_ppm_params& photonMap);
+  ~TechniquePPM() override;
+  void AllocateResources() override;
+  void FreeResources() override;
+  void RecordPass(void* stream, uint32_t passIndex) override;
+
+ private:
+  vcr_ppm_params photonMap_;
+  bool allocated_ = false;
+};
+
+/* RenderTechniquePPB (RenderTechniquePPB.h:10): progressive photon beams. */
+class VCR_API TechniquePPB : public RenderTechnique {
+ public:
+  TechniquePPB(Device& device, PushConstants* pushConstants, const vcr_ppb_params& beams);
+  ~TechniquePPB() override;
+  void AllocateResources() override;
+  void FreeResources() override;
+  /* UpdatePhotonMapProperties (RenderTechniquePPB.cpp:357-363): new beam
+   * parameters; reallocates if resources are live. */
+  void UpdatePhotonMapProperties(const vcr_ppb_params& beams);
+  void RecordPass(void* stream, uint32_t passIndex) override;
+
+ private:
+  vcr_ppb_params beams_;
+  bool allocated_ = false;
+};
+
+/* The DDA tracker with the learned radiance cache: paths end in the cache
+ * after params.nrc_events events; every pass also trains it. */
+class VCR_API TechniqueNRC : public RenderTechnique {
+ public:
+  TechniqueNRC(Device& device, PushConstants* pushConstants, const vcr_nrc_params& cache);
+  ~TechniqueNRC() override;
+  void AllocateResources() override;
+  void FreeResources() override;
+  void RecordPass(void* stream, uint32_t passIndex) override;
+
+ private:
+  vcr_nrc_params cache_;
+  bool allocated_ = false;
+};
+
+}  // namespace vcr
