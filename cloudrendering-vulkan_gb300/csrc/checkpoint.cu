@@ -1,0 +1,244 @@
+// Checkpoint / resume of the progressive state: a long render (thousands
+// of passes, hours of a PPM estimate, an online-trained cache) survives a
+// restart.  The reference keeps this state only in GPU memory for the life
+// of the process (frameCount and the accumulated image, main.cpp:262,
+// PathTracer.comp:420-424; pmRadius, RenderTechniquePPM.cpp:302-312).
+//
+// File: "VCRCKPT\0", u32 version (1), u32 section count, then sections of
+// { char tag[4]; u32 zero; u64 bytes; payload }:
+//   FRAM  u32 width, height, passes, 0; u64 samples; f64 sums [w*h*3]
+//   PPMS  u64 pixels; f64 statistics [pixels*8] (N, R, tau rgb, bg rgb)
+//   NRCW  u32 step, has_average, training paths per step, weight count;
+//         f32 weights, Adam m, Adam v [, moving average]
+//   BTCH  u64 pixels; u32 passes, 0; u64 samples; f64 sums [pixels*3]
+// Loading checks every section against the context's current setup (same
+// frame size, the technique set up with the same sizes) and leaves the
+// rest of the context as it is; unknown tags are skipped.
+#include <cstring>
+#include <fstream>
+
+#include "batch.cuh"
+#include "nrc.cuh"
+#include "ppm.cuh"
+
+namespace vcr {
+
+static const char kMagic[8] = {'V', 'C', 'R', 'C', 'K', 'P', 'T', '\0'};
+constexpr uint32_t kCkptVersion = 1;
+
+struct Section {
+  char tag[4];
+  std::vector<uint8_t> data;
+};
+
+template <typename T>
+static void put(std::vector<uint8_t>& v, const T& x) {
+  const uint8_t* p = reinterpret_cast<const uint8_t*>(&x);
+  v.insert(v.end(), p, p + sizeof(T));
+}
+
+static vcr_status put_device(vcr_ctx* ctx, std::vector<uint8_t>& v, const void* d, size_t bytes) {
+  size_t at = v.size();
+  v.resize(at + bytes);
+  VCR_CUDA(ctx, cudaMemcpy(v.data() + at, d, bytes, cudaMemcpyDeviceToHost));
+  return VCR_OK;
+}
+
+static vcr_status save_sections(vcr_ctx* ctx, std::vector<Section>& out) {
+  if (ctx->d_sum) {
+    Section s{{'F', 'R', 'A', 'M'}, {}};
+    put(s.data, ctx->width);
+    put(s.data, ctx->height);
+    put(s.data, ctx->passes);
+    put(s.data, 0u);
+    put(s.data, (uint64_t)ctx->samples);
+    vcr_status vs = put_device(ctx, s.data, ctx->d_sum, (size_t)ctx->width * ctx->height * 3 * sizeof(double));
+    if (vs) return vs;
+    out.push_back(std::move(s));
+  }
+  if (ctx->ppm) {
+    Section s{{'P', 'P', 'M', 'S'}, {}};
+    put(s.data, (uint64_t)ctx->ppm->pixels);
+    vcr_status vs = put_device(ctx, s.data, ctx->ppm->stats, ctx->ppm->pixels * 8 * sizeof(double));
+    if (vs) return vs;
+    out.push_back(std::move(s));
+  }
+  if (ctx->nrc) {
+    NrcState* st = ctx->nrc;
+    Section s{{'N', 'R', 'C', 'W'}, {}};
+    put(s.data, st->step);
+    put(s.data, st->ema ? 1u : 0u);
+    put(s.data, st->npaths);
+    put(s.data, (uint32_t)kNrcWeightCount);
+    const size_t nb = (size_t)kNrcWeightCount * sizeof(float);
+    const float* parts[] = {st->w, st->m, st->v, st->ema};
+    for (const float* d : parts)
+      if (d) {
+        vcr_status vs = put_device(ctx, s.data, d, nb);
+        if (vs) return vs;
+      }
+    out.push_back(std::move(s));
+  }
+  if (ctx->batch) {
+    BatchState* b = ctx->batch;
+    Section s{{'B', 'T', 'C', 'H'}, {}};
+    put(s.data, (uint64_t)b->pixels);
+    put(s.data, b->passes);
+    put(s.data, 0u);
+    put(s.data, (uint64_t)b->samples);
+    vcr_status vs = put_device(ctx, s.data, b->d_sum, b->pixels * 3 * sizeof(double));
+    if (vs) return vs;
+    out.push_back(std::move(s));
+  }
+  return VCR_OK;
+}
+
+}  // namespace vcr
+
+using namespace vcr;
+
+extern "C" VCR_API vcr_status vcr_checkpoint_save(vcr_ctx* ctx, const char* path) {
+  if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  if (!path) return fail(ctx, VCR_ERR_INVALID, "null path");
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
+  VCR_CUDA(ctx, cudaDeviceSynchronize());
+  std::vector<Section> secs;
+  vcr_status vs = save_sections(ctx, secs);
+  if (vs) return vs;
+  std::string tmp = std::string(path) + ".partial";
+  {
+    std::ofstream f(tmp, std::ios::binary | std::ios::trunc);
+    if (!f) return fail(ctx, VCR_ERR_IO, "cannot write %s", tmp.c_str());
+    f.write(kMagic, 8);
+    uint32_t hdr[2] = {kCkptVersion, (uint32_t)secs.size()};
+    f.write(reinterpret_cast<const char*>(hdr), sizeof hdr);
+    for (const Section& s : secs) {
+      uint32_t zero = 0;
+      uint64_t n = s.data.size();
+      f.write(s.tag, 4);
+      f.write(reinterpret_cast<const char*>(&zero), 4);
+      f.write(reinterpret_cast<const char*>(&n), 8);
+      f.write(reinterpret_cast<const char*>(s.data.data()), (std::streamsize)n);
+    }
+    if (!f) return fail(ctx, VCR_ERR_IO, "write to %s failed", tmp.c_str());
+  }
+  // the checkpoint replaces the old one only once it is complete
+  if (std::rename(tmp.c_str(), path) != 0) return fail(ctx, VCR_ERR_IO, "cannot rename %s to %s", tmp.c_str(), path);
+  return VCR_OK;
+}
+
+namespace {
+
+// Reads fixed-size fields from a section payload, failing on a short one.
+struct Reader {
+  const uint8_t* p;
+  size_t left;
+  template <typename T>
+  bool get(T& x) {
+    if (left < sizeof(T)) return false;
+    std::memcpy(&x, p, sizeof(T));
+    p += sizeof(T);
+    left -= sizeof(T);
+    return true;
+  }
+};
+
+}  // namespace
+
+extern "C" VCR_API vcr_status vcr_checkpoint_load(vcr_ctx* ctx, const char* path) {
+  if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  if (!path) return fail(ctx, VCR_ERR_INVALID, "null path");
+  std::ifstream f(path, std::ios::binary);
+  if (!f) return fail(ctx, VCR_ERR_IO, "cannot open %s", path);
+  char magic[8];
+  uint32_t hdr[2];
+  if (!f.read(magic, 8) || std::memcmp(magic, kMagic, 8) != 0 || !f.read(reinterpret_cast<char*>(hdr), 8))
+    return fail(ctx, VCR_ERR_IO, "%s is not a vcr checkpoint", path);
+  if (hdr[0] != kCkptVersion) return fail(ctx, VCR_ERR_UNSUPPORTED, "checkpoint version %u", hdr[0]);
+  std::vector<Section> secs;
+  for (uint32_t i = 0; i < hdr[1]; ++i) {
+    Section s;
+    uint32_t zero;
+    uint64_t n;
+    if (!f.read(s.tag, 4) || !f.read(reinterpret_cast<char*>(&zero), 4) || !f.read(reinterpret_cast<char*>(&n), 8) ||
+        n > (1ull << 40))
+      return fail(ctx, VCR_ERR_IO, "truncated checkpoint %s", path);
+    s.data.resize(n);
+    if (!f.read(reinterpret_cast<char*>(s.data.data()), (std::streamsize)n))
+      return fail(ctx, VCR_ERR_IO, "truncated checkpoint %s", path);
+    secs.push_back(std::move(s));
+  }
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
+  VCR_CUDA(ctx, cudaDeviceSynchronize());
+  // validate every section before changing anything
+  for (const Section& s : secs) {
+    Reader r{s.data.data(), s.data.size()};
+    if (!std::memcmp(s.tag, "FRAM", 4)) {
+      uint32_t w, h, passes, z;
+      uint64_t samples;
+      if (!r.get(w) || !r.get(h) || !r.get(passes) || !r.get(z) || !r.get(samples)) return fail(ctx, VCR_ERR_IO, "bad FRAM");
+      if (!ctx->d_sum || w != ctx->width || h != ctx->height)
+        return fail(ctx, VCR_ERR_STATE, "checkpoint frame %ux%u, context frame %ux%u", w, h, ctx->width, ctx->height);
+      if (r.left != (size_t)w * h * 3 * sizeof(double)) return fail(ctx, VCR_ERR_IO, "bad FRAM size");
+    } else if (!std::memcmp(s.tag, "PPMS", 4)) {
+      uint64_t px;
+      if (!r.get(px)) return fail(ctx, VCR_ERR_IO, "bad PPMS");
+      if (!ctx->ppm || ctx->ppm->pixels != px) return fail(ctx, VCR_ERR_STATE, "checkpoint holds PPM statistics: vcr_ppm_setup first");
+      if (r.left != px * 8 * sizeof(double)) return fail(ctx, VCR_ERR_IO, "bad PPMS size");
+    } else if (!std::memcmp(s.tag, "NRCW", 4)) {
+      uint32_t step, has_avg, npaths, count;
+      if (!r.get(step) || !r.get(has_avg) || !r.get(npaths) || !r.get(count)) return fail(ctx, VCR_ERR_IO, "bad NRCW");
+      if (!ctx->nrc || count != (uint32_t)kNrcWeightCount || (has_avg != 0) != (ctx->nrc->ema != nullptr))
+        return fail(ctx, VCR_ERR_STATE, "checkpoint holds a radiance cache: vcr_nrc_setup with the same ema_decay first");
+      if (r.left != (size_t)count * sizeof(float) * (3u + has_avg)) return fail(ctx, VCR_ERR_IO, "bad NRCW size");
+    } else if (!std::memcmp(s.tag, "BTCH", 4)) {
+      uint64_t px, samples;
+      uint32_t passes, z;
+      if (!r.get(px) || !r.get(passes) || !r.get(z) || !r.get(samples)) return fail(ctx, VCR_ERR_IO, "bad BTCH");
+      if (!ctx->batch || ctx->batch->pixels != px) return fail(ctx, VCR_ERR_STATE, "checkpoint holds a batch: vcr_batch_setup with the same views first");
+      if (r.left != px * 3 * sizeof(double)) return fail(ctx, VCR_ERR_IO, "bad BTCH size");
+    }
+  }
+  // apply
+  for (const Section& s : secs) {
+    Reader r{s.data.data(), s.data.size()};
+    if (!std::memcmp(s.tag, "FRAM", 4)) {
+      uint32_t w, h, passes, z;
+      uint64_t samples;
+      r.get(w); r.get(h); r.get(passes); r.get(z); r.get(samples);
+      VCR_CUDA(ctx, cudaMemcpy(ctx->d_sum, r.p, r.left, cudaMemcpyHostToDevice));
+      ctx->passes = passes;
+      ctx->samples = samples;
+    } else if (!std::memcmp(s.tag, "PPMS", 4)) {
+      uint64_t px;
+      r.get(px);
+      VCR_CUDA(ctx, cudaMemcpy(ctx->ppm->stats, r.p, r.left, cudaMemcpyHostToDevice));
+    } else if (!std::memcmp(s.tag, "NRCW", 4)) {
+      NrcState* st = ctx->nrc;
+      uint32_t step, has_avg, npaths, count;
+      r.get(step); r.get(has_avg); r.get(npaths); r.get(count);
+      const size_t nb = (size_t)count * sizeof(float);
+      float* parts[] = {st->w, st->m, st->v, st->ema};
+      for (int i = 0; i < 3 + (int)has_avg; ++i) VCR_CUDA(ctx, cudaMemcpy(parts[i], r.p + i * nb, nb, cudaMemcpyHostToDevice));
+      st->step = step;
+      // the calibrated training-path count applies to the scene bound now
+      st->npaths = npaths;
+      st->calib_cam = ctx->cam;
+      st->calib_cloud = ctx->cloud;
+      st->calib_w = ctx->width;
+      st->calib_h = ctx->height;
+      vcr_status vs = nrc_refresh_copies(ctx);
+      if (vs) return vs;
+    } else if (!std::memcmp(s.tag, "BTCH", 4)) {
+      BatchState* b = ctx->batch;
+      uint64_t px, samples;
+      uint32_t passes, z;
+      r.get(px); r.get(passes); r.get(z); r.get(samples);
+      VCR_CUDA(ctx, cudaMemcpy(b->d_sum, r.p, r.left, cudaMemcpyHostToDevice));
+      b->passes = passes;
+      b->samples = samples;
+    }
+  }
+  VCR_CUDA(ctx, cudaDeviceSynchronize());
+  return VCR_OK;
+}

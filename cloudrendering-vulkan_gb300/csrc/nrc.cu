@@ -392,6 +392,19 @@ vcr_status nrc_adam(vcr_ctx* ctx, cudaStream_t s) {
   return VCR_OK;
 }
 
+// BF16 copies from the FP32 master weights and their moving average (after
+// the FP32 state was written from outside, e.g. a checkpoint).
+vcr_status nrc_refresh_copies(vcr_ctx* ctx) {
+  NrcState* st = ctx->nrc;
+  nrc_to_bf16_kernel<<<(kNrcWeightCount + 255) / 256, 256>>>(st->w, reinterpret_cast<bf16*>(st->wb));
+  VCR_CUDA(ctx, cudaGetLastError());
+  if (st->ema) {
+    nrc_to_bf16_kernel<<<(kNrcWeightCount + 255) / 256, 256>>>(st->ema, reinterpret_cast<bf16*>(st->wbi));
+    VCR_CUDA(ctx, cudaGetLastError());
+  }
+  return VCR_OK;
+}
+
 uint32_t nrc_query_capacity(const vcr_ctx* ctx) { return ctx->nrc ? ctx->nrc->query_capacity : 0u; }
 
 vcr_status nrc_reset_queries(vcr_ctx* ctx, cudaStream_t s) {

@@ -120,6 +120,7 @@ void batch_free(vcr_ctx* ctx);
 uint32_t nrc_query_capacity(const vcr_ctx* ctx);
 vcr_status nrc_reset_queries(vcr_ctx* ctx, cudaStream_t s);
 vcr_status nrc_infer_queries(vcr_ctx* ctx, cudaStream_t s);
+vcr_status nrc_refresh_copies(vcr_ctx* ctx);
 
 // sv.cu
 vcr_status sv_build_launch(vcr_ctx* ctx, const vcr_shadow_volume* sv, cudaStream_t s);

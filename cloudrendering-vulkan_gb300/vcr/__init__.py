@@ -6,6 +6,7 @@ module only wraps the C entry points with numpy buffers for convenience.
 from __future__ import annotations
 
 import ctypes as C
+import os
 
 import numpy as np
 
@@ -234,6 +235,13 @@ class Context:
         loss = C.c_float()
         self._ck(lib().vcr_nrc_gradient(self.h, C.c_void_p(d_records), n, _ptr(g), g.size, C.byref(loss)))
         return g, loss.value
+
+    # checkpoints ------------------------------------------------------------
+    def checkpoint_save(self, path):
+        self._ck(lib().vcr_checkpoint_save(self.h, os.fsencode(path)))
+
+    def checkpoint_load(self, path):
+        self._ck(lib().vcr_checkpoint_load(self.h, os.fsencode(path)))
 
     # batched views ----------------------------------------------------------
     def batch_setup(self, views):

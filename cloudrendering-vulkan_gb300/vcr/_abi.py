@@ -161,6 +161,8 @@ SIGNATURES = {
     "vcr_nrc_forward": (_S, [_P, _P, _u32, _P, _P]),
     "vcr_nrc_gradient": (_S, [_P, _P, _u32, _P, _sz, C.POINTER(_f)]),
     "vcr_nrc_fit": (_S, [_P, _P, _u32, _u32, _P]),
+    "vcr_checkpoint_save": (_S, [_P, C.c_char_p]),
+    "vcr_checkpoint_load": (_S, [_P, C.c_char_p]),
     "vcr_batch_setup": (_S, [_P, C.POINTER(ViewDesc), _u32]),
     "vcr_batch_free": (_S, [_P]),
     "vcr_batch_pass": (_S, [_P, C.POINTER(PassDesc), _P]),

@@ -567,6 +567,21 @@ VCR_API vcr_status vcr_batch_info(vcr_ctx* ctx, vcr_batch_info_t* out);
 VCR_API vcr_status vcr_batch_reset(vcr_ctx* ctx);
 
 /* ------------------------------------------------------------------------ */
+/* Checkpoint / resume of the progressive state                             */
+/* ------------------------------------------------------------------------ */
+/* Saves the frame's FP64 sums and pass/sample counts, the PPM per-pixel
+ * statistics, the radiance cache's weights and Adam state, and a batch's
+ * sums, whichever exist (the reference keeps frameCount, the accumulated
+ * image and pmRadius only in memory: main.cpp:262, PathTracer.comp:420-424,
+ * RenderTechniquePPM.cpp:302-312).  Written to path + ".partial" and renamed
+ * when complete.  Synchronous. */
+VCR_API vcr_status vcr_checkpoint_save(vcr_ctx* ctx, const char* path);
+/* Restores a checkpoint into a context set up the same way (frame size,
+ * techniques and their sizes); the grid, cloud, camera and params are the
+ * caller's to bind.  Every section is checked before anything changes. */
+VCR_API vcr_status vcr_checkpoint_load(vcr_ctx* ctx, const char* path);
+
+/* ------------------------------------------------------------------------ */
 /* Read back                                                                */
 /* ------------------------------------------------------------------------ */
 /* Synchronous copy of a context buffer (bytes must match). host_out may be

@@ -1,0 +1,129 @@
+"""Checkpoint / resume through the C-ABI: an interrupted render resumed
+from its checkpoint in a fresh context continues exactly as the
+uninterrupted one (PT sums, PPM statistics, the radiance cache's training,
+a batch), and a checkpoint is refused by a context set up differently."""
+import numpy as np
+import pytest
+
+import vcr
+from vcr import configs
+
+pytestmark = pytest.mark.gpu
+
+W, H = 80, 64
+
+
+def _scene(ctx, nrc=False):
+    sc = configs.C1_PT
+    configs.setup_context(ctx, sc, width=W, height=H)
+    if nrc:
+        prm = sc.params(vcr.TRACKER_DDA)
+        prm.nrc_events = 2
+        ctx.set_params(prm)
+    return sc
+
+
+def test_pt_resume_equals_uninterrupted(cuda, tmp_path):
+    path = str(tmp_path / "pt.ckpt")
+    with vcr.Context() as ctx:
+        _scene(ctx)
+        for k in range(5):
+            ctx.pt_pass(seed=2, pass_index=k)
+            if k == 2:
+                ctx.checkpoint_save(path)
+        ctx.synchronize()
+        full = ctx.image_sum()
+    with vcr.Context() as ctx:
+        _scene(ctx)
+        ctx.checkpoint_load(path)
+        assert ctx.pass_count() == 3
+        for k in range(3, 5):
+            ctx.pt_pass(seed=2, pass_index=k)
+        ctx.synchronize()
+        resumed = ctx.image_sum()
+        assert ctx.pass_count() == 5
+    np.testing.assert_array_equal(resumed, full)
+
+
+def test_ppm_statistics_resume(cuda, tmp_path):
+    path = str(tmp_path / "ppm.ckpt")
+    with vcr.Context() as ctx:
+        _scene(ctx)
+        ctx.ppm_setup(photons=1 << 14, capacity=1 << 16, radius=0.02, alpha=0.7)
+        for k in range(4):
+            ctx.ppm_pass(seed=3, pass_index=k)
+            if k == 1:
+                ctx.checkpoint_save(path)
+        ctx.synchronize()
+        full = ctx.ppm_read("stats")
+    with vcr.Context() as ctx:
+        _scene(ctx)
+        ctx.ppm_setup(photons=1 << 14, capacity=1 << 16, radius=0.02, alpha=0.7)
+        ctx.checkpoint_load(path)
+        for k in range(2, 4):
+            ctx.ppm_pass(seed=3, pass_index=k)
+        ctx.synchronize()
+        resumed = ctx.ppm_read("stats")
+    # photon gathers add in an order set by atomics: equal to rounding
+    np.testing.assert_allclose(resumed, full, rtol=1e-9, atol=1e-12)
+
+
+def test_radiance_cache_training_resumes(cuda, tmp_path):
+    path = str(tmp_path / "nrc.ckpt")
+    with vcr.Context() as ctx:
+        _scene(ctx, nrc=True)
+        ctx.nrc_setup(train_samples=8192, learning_rate=3e-3, query_capacity=W * H, seed=4, ema_decay=0.9)
+        for k in range(6):
+            ctx.nrc_frame(seed=5, pass_index=k)
+            if k == 3:
+                ctx.checkpoint_save(path)
+        ctx.synchronize()
+        w_full, info_full = ctx.nrc_get_weights(), ctx.nrc_info()
+    with vcr.Context() as ctx:
+        _scene(ctx, nrc=True)
+        ctx.nrc_setup(train_samples=8192, learning_rate=3e-3, query_capacity=W * H, seed=99, ema_decay=0.9)
+        ctx.checkpoint_load(path)
+        for k in range(4, 6):
+            ctx.nrc_frame(seed=5, pass_index=k)
+        ctx.synchronize()
+        w_res, info_res = ctx.nrc_get_weights(), ctx.nrc_info()
+    assert info_res["steps"] == info_full["steps"] == 6
+    assert info_res["train_records"] == info_full["train_records"]
+    # gradients are flushed with float atomics: the same up to their order
+    np.testing.assert_allclose(w_res, w_full, rtol=0, atol=2e-5)
+
+
+def test_batch_resume_and_refusals(cuda, tmp_path):
+    path = str(tmp_path / "batch.ckpt")
+    sc = configs.C1_PT
+    views = [(sc.camera(48, 40), 48, 40, configs.sun_travel_dir(20.0)),
+             (sc.camera(32, 32), 32, 32, configs.sun_travel_dir(60.0))]
+    with vcr.Context() as ctx:
+        _scene(ctx)
+        ctx.batch_setup(views)
+        for k in range(4):
+            ctx.batch_pass(seed=6, pass_index=k)
+            if k == 1:
+                ctx.checkpoint_save(path)
+        ctx.synchronize()
+        full = [ctx.batch_read(v) for v in range(2)]
+    with vcr.Context() as ctx:
+        _scene(ctx)
+        with pytest.raises(vcr.VcrError):  # no batch set up: refused, nothing changed
+            ctx.checkpoint_load(path)
+        ctx.batch_setup(views)
+        ctx.checkpoint_load(path)
+        assert ctx.batch_info()["passes"] == 2
+        for k in range(2, 4):
+            ctx.batch_pass(seed=6, pass_index=k)
+        ctx.synchronize()
+        resumed = [ctx.batch_read(v) for v in range(2)]
+    for a, b in zip(full, resumed):
+        np.testing.assert_array_equal(a, b)
+    with vcr.Context() as ctx:
+        configs.setup_context(ctx, sc, width=W + 8, height=H)
+        ctx.batch_setup(views)
+        with pytest.raises(vcr.VcrError):  # frame size differs
+            ctx.checkpoint_load(path)
+        with pytest.raises(vcr.VcrError):
+            ctx.checkpoint_load(str(tmp_path / "missing.ckpt"))
