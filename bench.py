@@ -60,6 +60,30 @@ def dist_env():
     return ws, rank, local
 
 
+def replica_seed(rank: int) -> int:
+    """Ranks render independent replicas of the pass: disjoint stream seeds."""
+    return 1000 + rank
+
+
+def max_over_ranks(x: float, device=None) -> float:
+    """Max of a per-rank time over the default process group (x alone when
+    there is none)."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(world: int, samples_per_step: int, steps: int, ms_max: float) -> float:
+    """Msamples/s of all replicas: every rank renders samples_per_step per
+    step; the job takes the slowest rank's time."""
+    return world * samples_per_step * steps / (ms_max / 1e3) / 1e6
+
+
 def measured_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -148,7 +172,7 @@ def run_vcr(args):
         configs.setup_context(ctx, sc, tracker=vcr.TRACKER_DDA)
         ctx.synchronize()
         tuning = ctx.autotune(seed=999, stream=sh)  # picks majorant level / DDA steps / CTA size
-        seed = 1000 + rank
+        seed = replica_seed(rank)
         for k in range(args.warmup):
             ctx.pt_pass(seed=seed, pass_index=k, stream=sh)
         barrier()
@@ -161,7 +185,7 @@ def run_vcr(args):
         ev1.record(stream)
         barrier()
         clocks = clk.stop()
-        ms_total = ev0.elapsed_time(ev1)
+        ms_total = max_over_ranks(ev0.elapsed_time(ev1), device="cuda")
         # per-launch kernel durations and lookups (for the roofline)
         durs, looks, events, paths = [], [], [], []
         for k in range(min(args.steps, 3)):
@@ -175,14 +199,8 @@ def run_vcr(args):
             paths.append(c[0]); looks.append(c[1]); events.append(c[2])
         img = ctx.image_mean()
         conv = convergence(ctx, sc, stream, args) if rank == 0 and not args.no_convergence else None
-    if ws > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms_total], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_total = float(t.item())
-
     samples_per_step = W * H
-    value = ws * samples_per_step * args.steps / (ms_total / 1e3) / 1e6
+    value = whole_job_rate(ws, samples_per_step, args.steps, ms_total)
     peak, peak_kind = measured_peaks()
     bpl = BYTES_PER_LOOKUP[prec]
     lookups = float(np.mean(looks))
