@@ -418,6 +418,80 @@ def run_batch(args):
         "precision_relrmse_vs_fp32": err, "precision_passes": 4, "clocks": clocks}), flush=True)
 
 
+def _timed_passes(stream, fn, steps):
+    import torch
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for k in range(steps):
+        fn(k)
+    b.record(stream)
+    b.synchronize()
+    return a.elapsed_time(b) / steps
+
+
+def run_ppm(args):
+    """C2: 256^3 FP32 cloud (sigma_t = 16 rho), 1,048,576 photons a pass, r0
+    0.01, alpha 0.7, 960x540; one JSON line of pass time and rates."""
+    import torch
+    import vcr
+    from vcr import configs
+
+    sc = configs.C2_PPM
+    stream = torch.cuda.Stream()
+    sh = stream.cuda_stream
+    ex = sc.extra
+    with vcr.Context() as ctx:
+        configs.setup_context(ctx, sc)
+        ctx.synchronize()
+        ctx.ppm_setup(ex["photons"], 8 * ex["photons"], ex["r0"], ex["alpha"])
+        for k in range(args.warmup):
+            ctx.ppm_pass(seed=1, pass_index=k, stream=sh)
+        ms = _timed_passes(stream, lambda k: ctx.ppm_pass(seed=1, pass_index=args.warmup + k, stream=sh), args.steps)
+        info = ctx.ppm_info()
+        stats = ctx.ppm_read("stats")
+    print(json.dumps({
+        "metric": "PPM pass", "workload": sc.name, "ms_per_pass": round(ms, 4), "steps": args.steps,
+        "photons_emitted_per_s": round(ex["photons"] / (ms / 1e3), 1),
+        "photons_stored": info["photons_stored"], "dropped": info["dropped"],
+        "pixel_gathers_per_s": round(sc.width * sc.height / (ms / 1e3), 1),
+        "mean_radius": float(stats[..., 1].mean()), "mean_photon_count": float(stats[..., 0].mean())}), flush=True)
+
+
+def run_ppb(args):
+    """C3: 256^3 FP32 cloud, photons scaled so that a pass deposits about
+    262,144 beams, r0 0.02, alpha 0.8, 1280x720; segments are 30-bit
+    Morton-keyed, radix-sorted and put in an LBVH every pass."""
+    import torch
+    import vcr
+    from vcr import configs
+
+    sc = configs.C3_PPB
+    stream = torch.cuda.Stream()
+    sh = stream.cuda_stream
+    want = sc.extra["beams"]
+    with vcr.Context() as ctx:
+        configs.setup_context(ctx, sc)
+        ctx.synchronize()
+        probe = 16384
+        ctx.ppb_setup(probe, 1 << 24, 0.02, 0.8)
+        ctx.ppb_pass(seed=1, pass_index=0, stream=sh)
+        ctx.synchronize()
+        per_photon = max(float(ctx.ppb_read("nbeams", probe).sum()) / probe, 1e-3)
+        photons = int(want / per_photon)
+        ctx.ppb_setup(photons, 1 << 24, 0.02, 0.8)
+        ctx.reset()
+        for k in range(args.warmup):
+            ctx.ppb_pass(seed=1, pass_index=k, stream=sh)
+        ms = _timed_passes(stream, lambda k: ctx.ppb_pass(seed=1, pass_index=args.warmup + k, stream=sh), args.steps)
+        info = ctx.ppb_info()
+        beams = int(ctx.ppb_read("nbeams", photons).sum())
+    print(json.dumps({
+        "metric": "PPB pass", "workload": sc.name, "ms_per_pass": round(ms, 4), "steps": args.steps,
+        "photons": photons, "beams": beams, "segments": info["segments"], "dropped": info["dropped"],
+        "segments_per_s": round(info["segments"] / (ms / 1e3), 1),
+        "pixel_gathers_per_s": round(sc.width * sc.height / (ms / 1e3), 1), "radius": info["radius"]}), flush=True)
+
+
 def run_nrc_frames(args):
     """Radiance-cached frames alone: warm-up steps, then args.nrc_frames
     frames, each timed on the device; one JSON line with the means."""
@@ -575,10 +649,16 @@ def main():
                     help="only time this many radiance-cached frames on the scene (a profiling workload)")
     ap.add_argument("--batch", action="store_true",
                     help="only measure the batched 64-view configuration (CUDA graph, autotuned)")
+    ap.add_argument("--ppm", action="store_true", help="only measure the photon-mapping configuration")
+    ap.add_argument("--ppb", action="store_true", help="only measure the photon-beam configuration")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.batch:
+    if args.ppm or args.ppb:
+        import __graft_entry__ as ge
+        ge.build()
+        run_ppm(args) if args.ppm else run_ppb(args)
+    elif args.batch:
         import __graft_entry__ as ge
         ge.build()
         run_batch(args)
