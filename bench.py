@@ -25,9 +25,10 @@ time_to_1pct: the headline comparison on the same scene.  R is an FP64
          measured curve is reported beside it); time = passes to 1 % x
          measured pass time.  Cached tracker (paths end in the radiance
          cache after 2 events, 65,536 training records a frame, Adam lr
-         1e-3, moving-average weights for queries): warm-up steps, then
-         frames until its corrected error reaches 1 %; time = warm-up +
-         frames, device-timed.
+         1e-3, moving-average weights for queries): a warm-up of 3,000 Adam
+         steps (300 training launches, each followed by 9 more steps on
+         the same records), then frames (training every frame) until its
+         corrected error reaches 1 %; time = warm-up + frames, device-timed.
 --impl reference: the CPU restatement of the reference's tracker (the
          oracle) on all host cores, on a bounded sample of the same passes.
 """
@@ -241,112 +242,152 @@ def run_vcr(args):
     print(json.dumps(line), flush=True)
 
 
-CONV = {"ref_passes": 4000, "plain_passes": 1000, "warm_steps": 1000, "max_frames": 8000, "chunk": 500,
-        "train_samples": 65536, "learning_rate": 1e-3, "ema_decay": 0.99, "nrc_events": 2}
+CONV = {"ref_passes": 4000, "plain_passes": 1000, "warm_steps": 3000, "warm_more": 9, "max_frames": 8000,
+        "chunk": 500, "spp": 1, "train_samples": 65536, "learning_rate": 1e-3, "ema_decay": 0.99, "nrc_events": 2}
 
 
-def convergence(ctx, sc, stream, args):
-    """Time to 1 % relRMSE against an FP64 high-spp image: plain tracker
-    and radiance-cached tracker on the bound scene (see the module text)."""
+class Reference:
+    """FP64 high-spp image R of the plain tracker from two independent
+    halves; their difference gives R's own relative MSE (noise2) and the
+    per-sample relative variance V of the plain tracker."""
+
+    def __init__(self, ctx, sc, stream, passes):
+        import torch
+        import vcr
+
+        sh = stream.cuda_stream
+        px = sc.width * sc.height
+
+        def render(seed):
+            ctx.reset()
+            for k in range(passes):
+                ctx.pt_pass(seed=seed, pass_index=k, stream=sh)
+            ctx.synchronize()
+            buf = torch.empty(px * 3, dtype=torch.float64, device="cuda")
+            ctx.readback_to(vcr.BUF_IMAGE_SUM, buf.data_ptr(), px * 24)
+            return buf / passes
+
+        t0 = time.perf_counter()
+        ra, rb = render(100), render(200)
+        self.render_s = time.perf_counter() - t0
+        self.R = (ra + rb) / 2
+        e_ab = torch.sqrt(torch.sum((ra - rb) ** 2 / (self.R ** 2 + 1e-2)) / px).item()
+        self.noise2 = e_ab ** 2 / 4
+        self.V = e_ab ** 2 * passes / 2
+        self.passes = passes
+
+    def corrected(self, e):
+        return float(np.sqrt(max(e * e - self.noise2, 0.0)))
+
+
+def _error_curve(ctx, stream, ref, n, frame, errs, ms, first):
+    """Runs n frames, each timed with CUDA events, and records the relRMSE
+    against R after each (outside the timed events)."""
+    import torch
+
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n)]
+    for k in range(n):
+        evs[k][0].record(stream)
+        frame(first + k)
+        evs[k][1].record(stream)
+        ctx.image_rel_rmse(ref.R.data_ptr(), errs[first + k:].data_ptr(), stream=stream.cuda_stream)
+    torch.cuda.synchronize()
+    ms.extend(a.elapsed_time(b) for a, b in evs)
+
+
+def plain_time_to_1pct(ctx, sc, stream, ref, passes):
+    import torch
+
+    errs = torch.zeros(passes, dtype=torch.float64, device="cuda")
+    ms = []
+    ctx.reset()
+    _error_curve(ctx, stream, ref, passes, lambda k: ctx.pt_pass(seed=300, pass_index=k, stream=stream.cuda_stream),
+                 errs, ms, 0)
+    e = errs.cpu().numpy()
+    pass_ms = float(np.mean(ms))
+    need = ref.V / 1e-4
+    return {"time_s": round(need * pass_ms / 1e3, 3), "passes": int(np.ceil(need)), "pass_ms": round(pass_ms, 4),
+            "basis": "unbiased: relRMSE = sqrt(V/passes), V from the reference halves",
+            "check": {"passes": passes, "measured": round(ref.corrected(e[-1]), 5),
+                      "predicted": round(float(np.sqrt(ref.V / passes)), 5)}}
+
+
+def cached_time_to_1pct(ctx, sc, stream, ref, cfg):
+    """Warm-up (training steps, each optionally followed by cfg["warm_more"]
+    extra Adam steps on the same records), then frames of cfg["spp"]
+    samples per pixel until the corrected relRMSE reaches 1 %."""
     import torch
     import vcr
 
     sh = stream.cuda_stream
-    W, H = sc.width, sc.height
-    px = W * H
-    nr = CONV["ref_passes"]
-
-    def render(seed, n):
-        ctx.reset()
-        for k in range(n):
-            ctx.pt_pass(seed=seed, pass_index=k, stream=sh)
-        ctx.synchronize()
-        buf = torch.empty(px * 3, dtype=torch.float64, device="cuda")
-        ctx.readback_to(vcr.BUF_IMAGE_SUM, buf.data_ptr(), px * 24)
-        return buf / n
-
-    t0 = time.perf_counter()
-    ra = render(100, nr)
-    rb = render(200, nr)
-    ref_s = time.perf_counter() - t0
-    R = (ra + rb) / 2
-    e_ab = torch.sqrt(torch.sum((ra - rb) ** 2 / (R ** 2 + 1e-2)) / px).item()
-    noise2 = e_ab ** 2 / 4  # R's own relative MSE
-    V = e_ab ** 2 * nr / 2  # per-sample relative variance of the plain tracker
-    del ra, rb
-
-    def corrected(e):
-        return float(np.sqrt(max(e * e - noise2, 0.0)))
-
-    def run(n, frame, errs, ms, first):
-        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n)]
-        for k in range(n):
-            evs[k][0].record(stream)
-            frame(first + k)
-            evs[k][1].record(stream)
-            ctx.image_rel_rmse(R.data_ptr(), errs[first + k:].data_ptr(), stream=sh)
-        torch.cuda.synchronize()
-        ms.extend(a.elapsed_time(b) for a, b in evs)
-
-    # plain tracker
-    np_ = CONV["plain_passes"]
-    errs = torch.zeros(np_, dtype=torch.float64, device="cuda")
-    ms = []
-    ctx.reset()
-    run(np_, lambda k: ctx.pt_pass(seed=300, pass_index=k, stream=sh), errs, ms, 0)
-    e_plain = errs.cpu().numpy()
-    pass_ms = float(np.mean(ms))
-    plain_passes = V / 1e-4
-    plain = {"time_s": round(plain_passes * pass_ms / 1e3, 3), "passes": int(np.ceil(plain_passes)),
-             "pass_ms": round(pass_ms, 4),
-             "basis": "unbiased: relRMSE = sqrt(V/passes), V from the reference halves",
-             "check": {"passes": np_, "measured": round(corrected(e_plain[-1]), 5),
-                       "predicted": round(float(np.sqrt(V / np_)), 5)}}
-
-    # radiance-cached tracker
+    px = sc.width * sc.height
+    spp = cfg["spp"]
     prm = sc.params(vcr.TRACKER_DDA)
-    prm.nrc_events = CONV["nrc_events"]
+    prm.nrc_events = cfg["nrc_events"]
     ctx.set_params(prm)
-    ctx.nrc_setup(train_samples=CONV["train_samples"], learning_rate=CONV["learning_rate"], query_capacity=px,
-                  seed=1, ema_decay=CONV["ema_decay"])
+    ctx.nrc_setup(train_samples=cfg["train_samples"], learning_rate=cfg["learning_rate"], query_capacity=px * spp,
+                  seed=1, ema_decay=cfg["ema_decay"])
+    batches = max(1, cfg["warm_steps"] // (1 + cfg["warm_more"]))
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     a.record(stream)
-    for k in range(CONV["warm_steps"]):
+    for k in range(batches):
         ctx.nrc_train_step(seed=400, pass_index=k, stream=sh)
+        if cfg["warm_more"]:
+            ctx.nrc_train_more(cfg["warm_more"], stream=sh)
     b.record(stream)
     b.synchronize()
     warm_ms = a.elapsed_time(b)
     ctx.reset()
-    nmax, chunk = CONV["max_frames"], CONV["chunk"]
+    nmax, chunk = cfg["max_frames"], cfg["chunk"]
     errs = torch.zeros(nmax, dtype=torch.float64, device="cuda")
     ms = []
     hit = None
     done = 0
+    more = cfg.get("frame_more", 0)
+    every = cfg.get("train_every", 1)  # frames between training frames (0: none after the warm-up)
+
+    def frame(k):
+        if every and k % every == 0:
+            ctx.nrc_frame(seed=500, pass_index=batches + k, spp=spp, stream=sh)
+            if more:
+                ctx.nrc_train_more(more, stream=sh)
+        else:  # render only: paths still end in the (current) cache
+            ctx.pt_pass(seed=500 ^ 0x5bd1e995, pass_index=batches + k, spp=spp, stream=sh)
+
     while done < nmax and hit is None:
-        run(chunk, lambda k: ctx.nrc_frame(seed=500, pass_index=CONV["warm_steps"] + k, stream=sh), errs, ms, done)
+        _error_curve(ctx, stream, ref, chunk, frame, errs, ms, done)
         done += chunk
         e = errs[:done].cpu().numpy()
         for i in range(done - chunk, done):
-            if corrected(e[i]) <= 0.01:
+            if ref.corrected(e[i]) <= 0.01:
                 hit = i
                 break
     info = ctx.nrc_info()
     ctx.set_params(sc.params(vcr.TRACKER_DDA))
     e = errs[:done].cpu().numpy()
     frames_ms = np.cumsum(ms)
-    nrc = {"frames": (hit + 1) if hit is not None else None, "frame_ms": round(float(np.mean(ms)), 4),
-           "warm_steps": CONV["warm_steps"], "warm_s": round(warm_ms / 1e3, 3),
-           "time_s": round((warm_ms + frames_ms[hit]) / 1e3, 3) if hit is not None else None,
-           "relrmse_last": round(corrected(e[-1]), 5), "frames_run": done,
-           "curve": {str(i + 1): round(corrected(e[i]), 5) for i in (0, 9, 99, 499, 999, 1999, 3999, done - 1)
-                     if i < done},
-           "train_records": info["train_records"], "loss": round(info["last_loss"], 4)}
-    out = {"plain": plain, "nrc": nrc,
-           "speedup": round(plain["time_s"] / nrc["time_s"], 2) if nrc["time_s"] else None,
-           "reference": {"passes": 2 * nr, "own_relrmse": round(float(np.sqrt(noise2)), 5), "render_s": round(ref_s, 2),
-                         "per_sample_rel_variance": round(V, 4)},
-           "settings": dict(CONV)}
-    return out
+    return {"frames": (hit + 1) if hit is not None else None, "spp_per_frame": spp,
+            "frame_ms": round(float(np.mean(ms)), 4), "warm_steps": cfg["warm_steps"],
+            "warm_training_launches": batches, "warm_s": round(warm_ms / 1e3, 3),
+            "time_s": round((warm_ms + frames_ms[hit]) / 1e3, 3) if hit is not None else None,
+            "relrmse_last": round(ref.corrected(e[-1]), 5), "frames_run": done,
+            "curve": {str(i + 1): round(ref.corrected(e[i]), 5) for i in (0, 9, 99, 499, 999, 1999, 3999, done - 1)
+                      if i < done},
+            "train_records": info["train_records"], "loss": round(info["last_loss"], 4)}
+
+
+def convergence(ctx, sc, stream, args, overrides=None):
+    """Time to 1 % relRMSE against an FP64 high-spp image: plain tracker
+    and radiance-cached tracker on the bound scene (see the module text)."""
+    cfg = dict(CONV, **(overrides or {}))
+    ref = Reference(ctx, sc, stream, cfg["ref_passes"])
+    plain = plain_time_to_1pct(ctx, sc, stream, ref, cfg["plain_passes"])
+    nrc = cached_time_to_1pct(ctx, sc, stream, ref, cfg)
+    return {"plain": plain, "nrc": nrc,
+            "speedup": round(plain["time_s"] / nrc["time_s"], 2) if nrc["time_s"] else None,
+            "reference": {"passes": 2 * ref.passes, "own_relrmse": round(float(np.sqrt(ref.noise2)), 5),
+                          "render_s": round(ref.render_s, 2), "per_sample_rel_variance": round(ref.V, 4)},
+            "settings": cfg}
 
 
 def run_batch(args):

@@ -556,6 +556,19 @@ extern "C" VCR_API vcr_status vcr_nrc_train_step(vcr_ctx* ctx, const vcr_pass_de
   return nrc_train_step(ctx, pass, (cudaStream_t)stream);
 }
 
+extern "C" VCR_API vcr_status vcr_nrc_train_more(vcr_ctx* ctx, uint32_t steps, void* stream) {
+  if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  if (!ctx->nrc) return fail(ctx, VCR_ERR_STATE, "no radiance cache");
+  if (ctx->nrc->step == 0) return fail(ctx, VCR_ERR_STATE, "no training records yet (vcr_nrc_train_step)");
+  cudaStream_t s = (cudaStream_t)stream;
+  for (uint32_t k = 0; k < steps; ++k) {
+    vcr_status vs = nrc_update(ctx, s);
+    if (vs) return vs;
+  }
+  VCR_CUDA(ctx, cudaEventRecord(ctx->work_done, s));
+  return VCR_OK;
+}
+
 extern "C" VCR_API vcr_status vcr_nrc_frame(vcr_ctx* ctx, const vcr_pass_desc* pass, void* stream) {
   if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
   if (!pass) return fail(ctx, VCR_ERR_INVALID, "null pass");

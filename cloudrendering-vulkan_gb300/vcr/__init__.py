@@ -205,10 +205,13 @@ class Context:
         p.seed, p.pass_index, p.spp = seed, pass_index, 1
         self._ck(lib().vcr_nrc_train_step(self.h, C.byref(p), C.c_void_p(stream)))
 
-    def nrc_frame(self, seed=0, pass_index=0, stream=0):
+    def nrc_frame(self, seed=0, pass_index=0, spp=1, stream=0):
         p = _abi.PassDesc()
-        p.seed, p.pass_index, p.spp = seed, pass_index, 1
+        p.seed, p.pass_index, p.spp = seed, pass_index, spp
         self._ck(lib().vcr_nrc_frame(self.h, C.byref(p), C.c_void_p(stream)))
+
+    def nrc_train_more(self, steps, stream=0):
+        self._ck(lib().vcr_nrc_train_more(self.h, steps, C.c_void_p(stream)))
 
     def nrc_info(self) -> dict:
         i = _abi.NrcInfo()
