@@ -326,7 +326,7 @@ def cached_time_to_1pct(ctx, sc, stream, ref, cfg):
     prm.nrc_events = cfg["nrc_events"]
     ctx.set_params(prm)
     ctx.nrc_setup(train_samples=cfg["train_samples"], learning_rate=cfg["learning_rate"], query_capacity=px * spp,
-                  seed=1, ema_decay=cfg["ema_decay"])
+                  seed=1, ema_decay=cfg["ema_decay"], tail_survival=cfg.get("tail_survival", 0.0))
     batches = max(1, cfg["warm_steps"] // (1 + cfg["warm_more"]))
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     a.record(stream)

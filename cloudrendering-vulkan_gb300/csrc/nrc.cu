@@ -24,7 +24,18 @@ using namespace nvcuda;
 using bf16 = __nv_bfloat16;
 
 constexpr int kNrcThreads = 128;
-constexpr int kLd = kNrcWidth;  // leading dimension of activation tiles
+
+// Shared-memory row strides are padded off powers of two, so the 16 rows of
+// a matrix fragment load or store fall on different banks.
+constexpr int kLdX = kNrcWidth + 8;  // BF16 activation / gradient tiles: 144-byte rows
+constexpr int kLdY = kNrcWidth + 4;  // FP32 staging: 272-byte rows
+__host__ __device__ constexpr int ldw(int l) { return nrc_layer_cols(l) + 8; }  // BF16 weights of layer l
+__host__ __device__ constexpr int ldg(int l) { return nrc_layer_cols(l) + 4; }  // FP32 gradient of layer l
+__host__ __device__ constexpr int woff(int l) { return l * kNrcWidth * (kNrcWidth + 8); }
+__host__ __device__ constexpr int goff(int l) { return l * kNrcWidth * (kNrcWidth + 4); }
+constexpr int kWs = woff(kNrcLayers - 1) + kNrcWidth * (kNrcOutPad + 8);  // BF16 weights in shared memory
+constexpr int kGs = goff(kNrcLayers - 1) + kNrcWidth * (kNrcOutPad + 4);  // FP32 gradient in shared memory
+constexpr int kTileX = kNrcTile * kLdX;                                    // one activation tile
 
 struct NrcView {
   const bf16* wb;   // training weights
@@ -38,56 +49,76 @@ __device__ __forceinline__ void encode_rows(const NrcRecord* __restrict__ recs, 
                                             const NrcView& v, bf16* X0, int warp, int lane) {
   int s = lane >> 1, h = lane & 1;
   uint32_t idx = first + (uint32_t)(warp * 16 + s);
-  float enc[kNrcIn];
+  float e[32];
   if (idx < count) {
     NrcRecord r = recs[idx];
-    nrc_encode(r, v.b0, v.inv_ext, enc);
+    if (h == 0) nrc_encode_position(r, v.b0, v.inv_ext, e);
+    else nrc_encode_directions(r, e);
   } else {
-    for (int i = 0; i < kNrcIn; ++i) enc[i] = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 32; ++i) e[i] = 0.0f;
   }
-  bf16* row = X0 + (warp * 16 + s) * kLd;
-  for (int i = 0; i < 32; ++i) row[h * 32 + i] = __float2bfloat16_rn(enc[h * 32 + i]);
+  bf16* row = X0 + (warp * 16 + s) * kLdX + h * 32;
+#pragma unroll
+  for (int i = 0; i < 32; i += 2)
+    *reinterpret_cast<__nv_bfloat162*>(row + i) = __floats2bfloat162_rn(e[i], e[i + 1]);
 }
 
 // rows [16w,16w+16) of Y = X_l W_l, fp32 into the warp's staging block
-__device__ __forceinline__ void layer_forward(const bf16* X, const bf16* W, int cols, float* Yw, int warp) {
+__device__ __forceinline__ void layer_forward(const bf16* X, const bf16* W, int l, float* Yw, int warp) {
+  const int cols = nrc_layer_cols(l), ld = ldw(l);
   wmma::fragment<wmma::matrix_a, 16, 16, 16, bf16, wmma::row_major> a[4];
-  for (int kt = 0; kt < 4; ++kt) wmma::load_matrix_sync(a[kt], X + warp * 16 * kLd + kt * 16, kLd);
+#pragma unroll
+  for (int kt = 0; kt < 4; ++kt) wmma::load_matrix_sync(a[kt], X + warp * 16 * kLdX + kt * 16, kLdX);
   for (int nt = 0; nt < cols / 16; ++nt) {
     wmma::fragment<wmma::accumulator, 16, 16, 16, float> acc;
     wmma::fill_fragment(acc, 0.0f);
+#pragma unroll
     for (int kt = 0; kt < 4; ++kt) {
       wmma::fragment<wmma::matrix_b, 16, 16, 16, bf16, wmma::row_major> b;
-      wmma::load_matrix_sync(b, W + kt * 16 * cols + nt * 16, cols);
+      wmma::load_matrix_sync(b, W + kt * 16 * ld + nt * 16, ld);
       wmma::mma_sync(acc, a[kt], b, acc);
     }
-    wmma::store_matrix_sync(Yw + nt * 16, acc, kLd, wmma::mem_row_major);
+    wmma::store_matrix_sync(Yw + nt * 16, acc, kLdY, wmma::mem_row_major);
   }
 }
 
-// rows of the warp: Xn = bf16(relu(Y))
+// rows of the warp: Xn = bf16(relu(Y)), two columns per step
 __device__ __forceinline__ void relu_store(const float* Yw, bf16* Xn, int warp, int lane) {
-  for (int e = lane; e < 16 * kLd; e += 32) {
-    int r = e / kLd, c = e - r * kLd;
-    Xn[(warp * 16 + r) * kLd + c] = __float2bfloat16_rn(fmaxf(Yw[r * kLd + c], 0.0f));
+#pragma unroll 4
+  for (int e = lane * 2; e < 16 * kNrcWidth; e += 64) {
+    int r = e / kNrcWidth, c = e - r * kNrcWidth;
+    float2 y = *reinterpret_cast<const float2*>(Yw + r * kLdY + c);
+    *reinterpret_cast<__nv_bfloat162*>(Xn + (warp * 16 + r) * kLdX + c) =
+        __floats2bfloat162_rn(fmaxf(y.x, 0.0f), fmaxf(y.y, 0.0f));
   }
 }
 
-// Full forward of the tile's rows owned by this warp; activations h_0..h_5
-// stay in X[0..5] (64x64 bf16 each); output rows left in Yw (fp32, cols 0..15).
-__device__ __forceinline__ void mlp_forward(const bf16* W, bf16* X, float* Yw, int warp, int lane) {
+// Full forward of the tile's rows owned by this warp; the output rows are
+// left in Yw (fp32, cols 0..15).  keep: activations h_0..h_5 stay in
+// X[0..5] (training needs them); otherwise two tiles alternate.
+__device__ __forceinline__ void mlp_forward(const bf16* W, bf16* X, float* Yw, int warp, int lane, bool keep) {
   for (int l = 0; l < kNrcLayers; ++l) {
-    layer_forward(X + l * kNrcTile * kLd, W + nrc_layer_offset(l), nrc_layer_cols(l), Yw, warp);
+    const bf16* Xl = X + (keep ? l : (l & 1)) * kTileX;
+    layer_forward(Xl, W + woff(l), l, Yw, warp);
     __syncwarp();
-    if (l < kNrcHidden) relu_store(Yw, X + (l + 1) * kNrcTile * kLd, warp, lane);
+    if (l < kNrcHidden) relu_store(Yw, X + (keep ? l + 1 : ((l + 1) & 1)) * kTileX, warp, lane);
     __syncwarp();
   }
 }
 
+// Global [in][out] BF16 weights (ld = cols) into the padded shared layout,
+// 16 bytes at a time.
 __device__ __forceinline__ void load_weights(const bf16* __restrict__ g, bf16* s) {
   const uint4* src = reinterpret_cast<const uint4*>(g);
-  uint4* dst = reinterpret_cast<uint4*>(s);
-  for (int i = threadIdx.x; i < kNrcWeightCount * 2 / 16; i += blockDim.x) dst[i] = src[i];
+  for (int c = threadIdx.x; c < kNrcWeightCount / 8; c += blockDim.x) {
+    const int e = c * 8;
+    const int l = e < kNrcHidden * kNrcWidth * kNrcWidth ? e / (kNrcWidth * kNrcWidth) : kNrcHidden;
+    const int cols = nrc_layer_cols(l);
+    const int rel = e - nrc_layer_offset(l);
+    const int row = rel / cols, col = rel - row * cols;
+    *reinterpret_cast<uint4*>(s + woff(l) + row * ldw(l) + col) = src[c];
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -99,21 +130,21 @@ __global__ void __launch_bounds__(kNrcThreads) nrc_infer_kernel(NrcView v, const
                                                                 float* __restrict__ out) {
   extern __shared__ __align__(128) unsigned char smem[];
   bf16* W = reinterpret_cast<bf16*>(smem);
-  bf16* X = W + kNrcWeightCount;                                       // 6 activation tiles
-  float* Y = reinterpret_cast<float*>(X + kNrcLayers * kNrcTile * kLd);  // 4 warps x 16 x 64 fp32
+  bf16* X = W + kWs;                                       // 2 activation tiles, alternating
+  float* Y = reinterpret_cast<float*>(X + 2 * kTileX);      // 4 warps x 16 x kLdY fp32
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  float* Yw = Y + warp * 16 * kLd;
+  float* Yw = Y + warp * 16 * kLdY;
   load_weights(v.wbi, W);
   __syncthreads();
   const uint32_t count = min(*count_ptr, capacity);
   for (uint32_t first = blockIdx.x * kNrcTile; first < count; first += gridDim.x * kNrcTile) {
     encode_rows(recs, first, count, v, X, warp, lane);
     __syncwarp();
-    mlp_forward(W, X, Yw, warp, lane);
+    mlp_forward(W, X, Yw, warp, lane, false);
     if (lane < 16) {
       uint32_t idx = first + (uint32_t)(warp * 16 + lane);
       if (idx < count) {
-        const float* y = Yw + lane * kLd;
+        const float* y = Yw + lane * kLdY;
         NrcRecord r = recs[idx];
         if (out) {
           out[3 * idx] = y[0];
@@ -141,14 +172,14 @@ __global__ void __launch_bounds__(kNrcThreads) nrc_train_kernel(NrcView v, const
                                                                 float* __restrict__ loss) {
   extern __shared__ __align__(128) unsigned char smem[];
   bf16* W = reinterpret_cast<bf16*>(smem);
-  bf16* X = W + kNrcWeightCount;                                       // h_0 .. h_5
-  bf16* D = X + kNrcLayers * kNrcTile * kLd;                           // dY ping-pong: 2 x 64x64
-  float* Y = reinterpret_cast<float*>(D + 2 * kNrcTile * kLd);         // 4 x 16 x 64
-  float* G = Y + 4 * 16 * kLd;                                         // dW accumulator [kNrcWeightCount]
+  bf16* X = W + kWs;                                        // h_0 .. h_5
+  bf16* D = X + kNrcLayers * kTileX;                         // dY ping-pong: 2 tiles
+  float* Y = reinterpret_cast<float*>(D + 2 * kTileX);       // 4 x 16 x kLdY
+  float* G = Y + 4 * 16 * kLdY;                              // dW accumulator [kGs]
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  float* Yw = Y + warp * 16 * kLd;
+  float* Yw = Y + warp * 16 * kLdY;
   load_weights(v.wb, W);
-  for (int i = threadIdx.x; i < kNrcWeightCount; i += blockDim.x) G[i] = 0.0f;
+  for (int i = threadIdx.x; i < kGs; i += blockDim.x) G[i] = 0.0f;
   __syncthreads();
   const uint32_t count = min(*count_ptr, capacity);
   const float inv_n = 1.0f / (3.0f * (float)max(count, 1u));
@@ -156,9 +187,9 @@ __global__ void __launch_bounds__(kNrcThreads) nrc_train_kernel(NrcView v, const
   for (uint32_t first = blockIdx.x * kNrcTile; first < count; first += gridDim.x * kNrcTile) {
     encode_rows(recs, first, count, v, X, warp, lane);
     __syncwarp();
-    mlp_forward(W, X, Yw, warp, lane);
+    mlp_forward(W, X, Yw, warp, lane, true);
     // output gradient (cols 0..2), zero elsewhere and for padding rows
-    bf16* d5 = D;  // dY_5 in buffer 0 (64 x 64, cols 0..15 used)
+    bf16* d5 = D;  // dY_5 in buffer 0 (cols 0..15 used)
     for (int e = lane; e < 16 * kNrcOutPad; e += 32) {
       int r = e / kNrcOutPad, c = e - r * kNrcOutPad;
       uint32_t idx = first + (uint32_t)(warp * 16 + r);
@@ -166,68 +197,76 @@ __global__ void __launch_bounds__(kNrcThreads) nrc_train_kernel(NrcView v, const
       if (c < kNrcOut && idx < count) {
         const NrcRecord& rec = recs[idx];
         float t = c == 0 ? rec.w0 : (c == 1 ? rec.w1 : rec.w2);
-        float y = Yw[r * kLd + c];
+        float y = Yw[r * kLdY + c];
         float den = y * y + 0.01f;
         float diff = y - t;
         loss_local += (diff * diff / den) * inv_n;
         gval = (2.0f * diff / den) * inv_n;
       }
-      d5[(warp * 16 + r) * kLd + c] = __float2bfloat16_rn(gval);
+      d5[(warp * 16 + r) * kLdX + c] = __float2bfloat16_rn(gval);
     }
     __syncthreads();
     // backward through layers 5..0
     for (int l = kNrcLayers - 1; l >= 0; --l) {
       const int cols = nrc_layer_cols(l);
-      const bf16* Xl = X + l * kNrcTile * kLd;
-      bf16* Dl = D + (l & 1 ? 0 : 1) * kNrcTile * kLd;  // l = 5 -> buffer 0
+      const bf16* Xl = X + l * kTileX;
+      bf16* Dl = D + (l & 1 ? 0 : 1) * kTileX;  // l = 5 -> buffer 0
       if (l == kNrcLayers - 1) Dl = D;
       // dW_l += X_l^T dY_l : tiles (mt over 64 inputs, nt over cols/16), K = 64 samples
       const int ntiles = 4 * (cols / 16);
       for (int tI = warp; tI < ntiles; tI += kNrcThreads / 32) {
         int mt = tI / (cols / 16), nt = tI - mt * (cols / 16);
-        float* g = G + nrc_layer_offset(l) + mt * 16 * cols + nt * 16;
+        float* g = G + goff(l) + mt * 16 * ldg(l) + nt * 16;
         wmma::fragment<wmma::accumulator, 16, 16, 16, float> acc;
-        wmma::load_matrix_sync(acc, g, cols, wmma::mem_row_major);
+        wmma::load_matrix_sync(acc, g, ldg(l), wmma::mem_row_major);
+#pragma unroll
         for (int kt = 0; kt < 4; ++kt) {
           wmma::fragment<wmma::matrix_a, 16, 16, 16, bf16, wmma::col_major> a;  // X_l^T
-          wmma::load_matrix_sync(a, Xl + kt * 16 * kLd + mt * 16, kLd);
+          wmma::load_matrix_sync(a, Xl + kt * 16 * kLdX + mt * 16, kLdX);
           wmma::fragment<wmma::matrix_b, 16, 16, 16, bf16, wmma::row_major> b;  // dY_l
-          wmma::load_matrix_sync(b, Dl + kt * 16 * kLd + nt * 16, kLd);
+          wmma::load_matrix_sync(b, Dl + kt * 16 * kLdX + nt * 16, kLdX);
           wmma::mma_sync(acc, a, b, acc);
         }
-        wmma::store_matrix_sync(g, acc, cols, wmma::mem_row_major);
+        wmma::store_matrix_sync(g, acc, ldg(l), wmma::mem_row_major);
       }
       if (l > 0) {
         // dY_{l-1} = (dY_l W_l^T) * (h_l > 0), rows of this warp
-        bf16* Dn = (Dl == D) ? D + kNrcTile * kLd : D;
-        const bf16* Wl = W + nrc_layer_offset(l);
+        bf16* Dn = (Dl == D) ? D + kTileX : D;
+        const bf16* Wl = W + woff(l);
         for (int nt = 0; nt < 4; ++nt) {
           wmma::fragment<wmma::accumulator, 16, 16, 16, float> acc;
           wmma::fill_fragment(acc, 0.0f);
           for (int kt = 0; kt < cols / 16; ++kt) {
             wmma::fragment<wmma::matrix_a, 16, 16, 16, bf16, wmma::row_major> a;  // dY_l rows
-            wmma::load_matrix_sync(a, Dl + warp * 16 * kLd + kt * 16, kLd);
+            wmma::load_matrix_sync(a, Dl + warp * 16 * kLdX + kt * 16, kLdX);
             wmma::fragment<wmma::matrix_b, 16, 16, 16, bf16, wmma::col_major> b;  // W_l^T
-            wmma::load_matrix_sync(b, Wl + nt * 16 * cols + kt * 16, cols);
+            wmma::load_matrix_sync(b, Wl + nt * 16 * ldw(l) + kt * 16, ldw(l));
             wmma::mma_sync(acc, a, b, acc);
           }
-          wmma::store_matrix_sync(Yw + nt * 16, acc, kLd, wmma::mem_row_major);
+          wmma::store_matrix_sync(Yw + nt * 16, acc, kLdY, wmma::mem_row_major);
         }
         __syncwarp();
-        for (int e = lane; e < 16 * kLd; e += 32) {
-          int r = e / kLd, c = e - r * kLd;
+#pragma unroll 4
+        for (int e = lane * 2; e < 16 * kNrcWidth; e += 64) {
+          int r = e / kNrcWidth, c = e - r * kNrcWidth;
           int row = warp * 16 + r;
-          float mask = __bfloat162float(Xl[row * kLd + c]) > 0.0f ? 1.0f : 0.0f;
-          Dn[row * kLd + c] = __float2bfloat16_rn(Yw[r * kLd + c] * mask);
+          float2 y = *reinterpret_cast<const float2*>(Yw + r * kLdY + c);
+          __nv_bfloat162 h = *reinterpret_cast<const __nv_bfloat162*>(Xl + row * kLdX + c);
+          float m0 = __low2float(h) > 0.0f ? 1.0f : 0.0f, m1 = __high2float(h) > 0.0f ? 1.0f : 0.0f;
+          *reinterpret_cast<__nv_bfloat162*>(Dn + row * kLdX + c) = __floats2bfloat162_rn(y.x * m0, y.y * m1);
         }
         __syncwarp();
       }
       __syncthreads();
     }
   }
-  // flush the CTA's gradient and loss
+  // flush the CTA's gradient (padded layout -> [in][out]) and loss
   for (int i = threadIdx.x; i < kNrcWeightCount; i += blockDim.x) {
-    float gv = G[i];
+    const int l = i < kNrcHidden * kNrcWidth * kNrcWidth ? i / (kNrcWidth * kNrcWidth) : kNrcHidden;
+    const int cols = nrc_layer_cols(l);
+    const int rel = i - nrc_layer_offset(l);
+    const int row = rel / cols, col = rel - row * cols;
+    float gv = G[goff(l) + row * ldg(l) + col];
     if (gv != 0.0f) atomicAdd(grad + i, gv);
   }
   for (int o = 16; o > 0; o >>= 1) loss_local += __shfl_xor_sync(0xffffffffu, loss_local, o);
@@ -273,11 +312,10 @@ __global__ void nrc_to_bf16_kernel(const float* __restrict__ w, bf16* __restrict
 // host side
 // ---------------------------------------------------------------------------
 static size_t infer_smem() {
-  return (size_t)kNrcWeightCount * 2 + (size_t)kNrcLayers * kNrcTile * kLd * 2 + 4 * 16 * kLd * 4;
+  return (size_t)kWs * 2 + (size_t)2 * kTileX * 2 + (size_t)4 * 16 * kLdY * 4;
 }
 static size_t train_smem() {
-  return (size_t)kNrcWeightCount * 2 + (size_t)(kNrcLayers + 2) * kNrcTile * kLd * 2 + 4 * 16 * kLd * 4 +
-         (size_t)kNrcWeightCount * 4;
+  return (size_t)kWs * 2 + (size_t)(kNrcLayers + 2) * kTileX * 2 + (size_t)4 * 16 * kLdY * 4 + (size_t)kGs * 4;
 }
 
 NrcView nrc_view(const vcr_ctx* ctx) {
@@ -320,9 +358,11 @@ static void nrc_init_weights(std::vector<float>& w, uint32_t seed) {
 
 vcr_status nrc_setup(vcr_ctx* ctx, const vcr_nrc_params* p) {
   if (!p || p->train_samples == 0 || p->train_samples > (1u << 22) || !(p->learning_rate > 0.0f) ||
-      p->query_capacity == 0 || !(p->ema_decay >= 0.0f && p->ema_decay < 1.0f))
+      p->query_capacity == 0 || !(p->ema_decay >= 0.0f && p->ema_decay < 1.0f) ||
+      !(p->tail_survival >= 0.0f && p->tail_survival < 1.0f))
     return fail(ctx, VCR_ERR_INVALID,
-                "nrc params: train_samples 1..2^22, learning_rate > 0, query_capacity > 0, ema_decay in [0,1)");
+                "nrc params: train_samples 1..2^22, learning_rate > 0, query_capacity > 0, ema_decay and "
+                "tail_survival in [0,1)");
   nrc_free(ctx);
   NrcState* st = new NrcState();
   ctx->nrc = st;
@@ -449,7 +489,7 @@ static bool nrc_calibrated(const vcr_ctx* ctx) {
 // yield of a seeded launch is).
 static NrcTrainSink nrc_sink(vcr_ctx* ctx) {
   NrcState* st = ctx->nrc;
-  return NrcTrainSink{st->train, st->train_count, st->train_cap, st->npaths};
+  return NrcTrainSink{st->train, st->train_count, st->train_cap, st->npaths, st->prm.tail_survival};
 }
 
 static vcr_status nrc_launch_training(vcr_ctx* ctx, const PassView& pv, uint32_t paths, cudaStream_t s) {

@@ -41,7 +41,8 @@ struct NrcTrainSink {
   NrcRecord* rec;
   uint32_t* count;
   uint32_t capacity;
-  uint32_t paths;  // training paths of the launch (0: none)
+  uint32_t paths;   // training paths of the launch (0: none)
+  float survival;   // Russian-roulette survival past the last recorded vertex (0: off)
 };
 
 struct NrcState {
@@ -111,8 +112,9 @@ __host__ __device__ __forceinline__ void nrc_sh16(float x, float y, float z, flo
 
 // 64 encoded inputs of one record.  `b0`, `inv_ext` map world positions to
 // [0,1]^3 box coordinates.
-__host__ __device__ __forceinline__ void nrc_encode(const NrcRecord& r, f3 b0, f3 inv_ext, float* o) {
+__host__ __device__ __forceinline__ void nrc_encode_position(const NrcRecord& r, f3 b0, f3 inv_ext, float* o) {
   float ux = (r.px - b0.x) * inv_ext.x, uy = (r.py - b0.y) * inv_ext.y, uz = (r.pz - b0.z) * inv_ext.z;
+#pragma unroll
   for (int l = 0; l < kNrcPosLevels; ++l) {
     float dx, dy, dz;
     nrc_level_dir(l, dx, dy, dz);
@@ -124,8 +126,17 @@ __host__ __device__ __forceinline__ void nrc_encode(const NrcRecord& r, f3 b0, f
     o[2 * l] = sn;
     o[2 * l + 1] = cs;
   }
-  nrc_sh16(r.vx, r.vy, r.vz, o + 32);
-  nrc_sh16(r.sx, r.sy, r.sz, o + 48);
+}
+
+// The 32 direction inputs: SH of the view direction, then of the sun.
+__host__ __device__ __forceinline__ void nrc_encode_directions(const NrcRecord& r, float* o) {
+  nrc_sh16(r.vx, r.vy, r.vz, o);
+  nrc_sh16(r.sx, r.sy, r.sz, o + 16);
+}
+
+__host__ __device__ __forceinline__ void nrc_encode(const NrcRecord& r, f3 b0, f3 inv_ext, float* o) {
+  nrc_encode_position(r, b0, inv_ext, o);
+  nrc_encode_directions(r, o + 32);
 }
 
 // Layer l weights start at this offset; hidden layers are [in][out] = 64x64

@@ -130,6 +130,14 @@ __device__ __noinline__ uint32_t record_training(const NrcTrainSink& ts, const S
 
 constexpr uint32_t kTrainPath = 0x80000000u;  // pid flag of a training path
 
+// Russian roulette of a training path's continuation: survive with
+// probability p and carry weight 1/p.
+__device__ __noinline__ bool roulette_survives(Rng& rng, float p, float& beta) {
+  if (rng_next(rng) >= p) return false;
+  beta = beta / p;
+  return true;
+}
+
 // 4 x 256 threads per SM: 64 registers a thread (a few spill to L1), which
 // measured ~7% faster than 3 CTAs at 77 registers on the 1024x512x1024 scene.
 // Work items [0, ts.paths) are training paths (their pid carries kTrainPath
@@ -328,6 +336,9 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
           L = L + mk(c, c, c);
           if (s.max_events && events >= s.max_events) {
             finish = true;
+          } else if ((pid & kTrainPath) && ts.survival > 0.0f && events >= (uint32_t)kNrcRecordEvents &&
+                     !roulette_survives(rng, ts.survival, beta)) {
+            finish = true;  // past the recorded vertices: Russian roulette
           } else {
             dir = sample_direction(s.ph, dir, rng);
             mode = kScatter;
@@ -407,7 +418,7 @@ vcr_status wavefront_launch(vcr_ctx* ctx, const GridView& g, const SceneView& s,
                             const PassView& pv, uint32_t* stats, Counters cnt, uint32_t total, cudaStream_t st,
                             const NrcTrainSink* train, const BatchSink* batch, double* sum) {
   const vcr_tuning& t = ctx->tuning;
-  NrcTrainSink ts{nullptr, nullptr, 0u, 0u};
+  NrcTrainSink ts{nullptr, nullptr, 0u, 0u, 0.0f};
   if (train) ts = *train;
   BatchSink bt{nullptr, 0u, nullptr};
   if (batch) bt = *batch;

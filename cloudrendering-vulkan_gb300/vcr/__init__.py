@@ -193,8 +193,9 @@ class Context:
     # radiance cache ---------------------------------------------------------
     NRC_WEIGHTS = 21504
 
-    def nrc_setup(self, train_samples=65536, learning_rate=1e-3, query_capacity=1 << 21, seed=1, ema_decay=0.0):
-        p = _abi.NrcParams(train_samples, learning_rate, query_capacity, seed, ema_decay)
+    def nrc_setup(self, train_samples=65536, learning_rate=1e-3, query_capacity=1 << 21, seed=1, ema_decay=0.0,
+                  tail_survival=0.0):
+        p = _abi.NrcParams(train_samples, learning_rate, query_capacity, seed, ema_decay, tail_survival)
         self._ck(lib().vcr_nrc_setup(self.h, C.byref(p)))
 
     def nrc_free(self):

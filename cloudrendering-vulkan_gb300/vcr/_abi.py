@@ -74,7 +74,7 @@ class BatchInfo(C.Structure):
 
 class NrcParams(C.Structure):
     _fields_ = [("train_samples", C.c_uint32), ("learning_rate", C.c_float), ("query_capacity", C.c_uint32),
-                ("seed", C.c_uint32), ("ema_decay", C.c_float)]
+                ("seed", C.c_uint32), ("ema_decay", C.c_float), ("tail_survival", C.c_float)]
 
 
 class NrcInfo(C.Structure):

@@ -341,6 +341,11 @@ typedef struct vcr_nrc_params {
   float ema_decay;         /* 0: queries use the training weights; in (0,1):
                               they use a moving average of them with this
                               decay (ramped in as min(d, (1+k)/(10+k))) */
+  float tail_survival;     /* 0: training paths run to escape / max_events;
+                              in (0,1): after their last recorded vertex they
+                              continue each event with this probability and
+                              weight 1/p (Russian roulette: unbiased targets,
+                              a shorter latency tail) */
 } vcr_nrc_params;
 
 typedef struct vcr_nrc_info_t {
