@@ -25,10 +25,12 @@ time_to_1pct: the headline comparison on the same scene.  R is an FP64
          measured curve is reported beside it); time = passes to 1 % x
          measured pass time.  Cached tracker (paths end in the radiance
          cache after 2 events, 65,536 training records a frame, Adam lr
-         1e-3, moving-average weights for queries): a warm-up of 3,000 Adam
-         steps (300 training launches, each followed by 9 more steps on
-         the same records), then frames (training every frame) until its
-         corrected error reaches 1 %; time = warm-up + frames, device-timed.
+         1e-3, moving-average weights for queries): a warm-up of 6,000 Adam
+         steps (300 training launches, each followed by 19 more steps on
+         16,384-record batches of the same records), then frames until its
+         corrected error reaches 1 %: every 3rd frame traces new training
+         paths in its launch and steps on them, the others render and step
+         once more on those records; time = warm-up + frames, device-timed.
 --impl reference: the CPU restatement of the reference's tracker (the
          oracle) on all host cores, on a bounded sample of the same passes.
 """
@@ -242,8 +244,9 @@ def run_vcr(args):
     print(json.dumps(line), flush=True)
 
 
-CONV = {"ref_passes": 4000, "plain_passes": 1000, "warm_steps": 3000, "warm_more": 9, "max_frames": 8000,
-        "chunk": 500, "spp": 1, "train_samples": 65536, "learning_rate": 1e-3, "ema_decay": 0.99, "nrc_events": 2}
+CONV = {"ref_passes": 4000, "plain_passes": 1000, "warm_steps": 6000, "warm_more": 19, "warm_batch": 16384,
+        "train_every": 3, "reuse_steps": 1, "max_frames": 8000, "chunk": 500, "spp": 1, "train_samples": 65536,
+        "learning_rate": 1e-3, "ema_decay": 0.99, "nrc_events": 2}
 
 
 class Reference:
@@ -333,7 +336,7 @@ def cached_time_to_1pct(ctx, sc, stream, ref, cfg):
     for k in range(batches):
         ctx.nrc_train_step(seed=400, pass_index=k, stream=sh)
         if cfg["warm_more"]:
-            ctx.nrc_train_more(cfg["warm_more"], stream=sh)
+            ctx.nrc_train_more(cfg["warm_more"], max_records=cfg.get("warm_batch", 0), stream=sh)
     b.record(stream)
     b.synchronize()
     warm_ms = a.elapsed_time(b)
@@ -353,6 +356,8 @@ def cached_time_to_1pct(ctx, sc, stream, ref, cfg):
                 ctx.nrc_train_more(more, stream=sh)
         else:  # render only: paths still end in the (current) cache
             ctx.pt_pass(seed=500 ^ 0x5bd1e995, pass_index=batches + k, spp=spp, stream=sh)
+            if cfg.get("reuse_steps", 0):  # and train on the last frame's records again
+                ctx.nrc_train_more(cfg["reuse_steps"], stream=sh)
 
     while done < nmax and hit is None:
         _error_curve(ctx, stream, ref, chunk, frame, errs, ms, done)

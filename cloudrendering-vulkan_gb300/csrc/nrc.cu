@@ -16,6 +16,7 @@
 #include <cstring>
 
 #include "nrc.cuh"
+#include "nrc_mma.cuh"
 #include "track.cuh"
 
 namespace vcr {
@@ -122,30 +123,42 @@ __device__ __forceinline__ void load_weights(const bf16* __restrict__ g, bf16* s
 }
 
 // ---------------------------------------------------------------------------
-// inference: sum[pix] += throughput * max(cache(x, view, sun), 0)
+// inference: sum[pix] += throughput * max(cache(x, view, sun), 0); out (if
+// given) receives the 3 outputs.  Register-resident forward (nrc_mma.cuh):
+// every warp runs whole 16-sample tiles, the CTA shares only the weights.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kNrcThreads) nrc_infer_kernel(NrcView v, const NrcRecord* __restrict__ recs,
-                                                                const uint32_t* __restrict__ count_ptr,
-                                                                uint32_t capacity, double* __restrict__ sum,
-                                                                float* __restrict__ out) {
+constexpr int kInferThreads = 256;
+
+__global__ void __launch_bounds__(kInferThreads, 3) nrc_infer_kernel(NrcView v, const NrcRecord* __restrict__ recs,
+                                                                     const uint32_t* __restrict__ count_ptr,
+                                                                     uint32_t capacity, double* __restrict__ sum,
+                                                                     float* __restrict__ out) {
   extern __shared__ __align__(128) unsigned char smem[];
-  bf16* W = reinterpret_cast<bf16*>(smem);
-  bf16* X = W + kWs;                                       // 2 activation tiles, alternating
-  float* Y = reinterpret_cast<float*>(X + 2 * kTileX);      // 4 warps x 16 x kLdY fp32
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  float* Yw = Y + warp * 16 * kLdY;
-  load_weights(v.wbi, W);
+  bf16* Wt = reinterpret_cast<bf16*>(smem);
+  float* dirs = reinterpret_cast<float*>(Wt + kWtElems);  // 16 level directions
+  load_weights_transposed(v.wbi, Wt);
+  load_level_dirs(dirs);
   __syncthreads();
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
   const uint32_t count = min(*count_ptr, capacity);
-  for (uint32_t first = blockIdx.x * kNrcTile; first < count; first += gridDim.x * kNrcTile) {
-    encode_rows(recs, first, count, v, X, warp, lane);
-    __syncwarp();
-    mlp_forward(W, X, Yw, warp, lane, false);
-    if (lane < 16) {
-      uint32_t idx = first + (uint32_t)(warp * 16 + lane);
-      if (idx < count) {
-        const float* y = Yw + lane * kLdY;
-        NrcRecord r = recs[idx];
+  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t tile = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); tile * 16u < count; tile += warps) {
+    const uint32_t i0 = tile * 16u + (uint32_t)g, i1 = i0 + 8u;
+    NrcRecord r0{}, r1{};
+    if (i0 < count) r0 = recs[i0];
+    if (i1 < count) r1 = recs[i1];
+    uint32_t a[4][4];
+    encode_a(r0, i0 < count, v.b0, v.inv_ext, dirs, t, 0, a);
+    encode_a(r1, i1 < count, v.b0, v.inv_ext, dirs, t, 1, a);
+    float yg[3], yh[3];
+    mlp_forward_mma(Wt, a, g, t, yg, yh);
+    if (t == 0) {
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const uint32_t idx = h ? i1 : i0;
+        if (idx >= count) continue;
+        const NrcRecord& r = h ? r1 : r0;
+        const float* y = h ? yh : yg;
         if (out) {
           out[3 * idx] = y[0];
           out[3 * idx + 1] = y[1];
@@ -159,7 +172,6 @@ __global__ void __launch_bounds__(kNrcThreads) nrc_infer_kernel(NrcView v, const
         }
       }
     }
-    __syncwarp();
   }
 }
 
@@ -168,8 +180,8 @@ __global__ void __launch_bounds__(kNrcThreads) nrc_infer_kernel(NrcView v, const
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kNrcThreads) nrc_train_kernel(NrcView v, const NrcRecord* __restrict__ recs,
                                                                 const uint32_t* __restrict__ count_ptr,
-                                                                uint32_t capacity, float* __restrict__ grad,
-                                                                float* __restrict__ loss) {
+                                                                uint32_t capacity, uint32_t first_rec,
+                                                                float* __restrict__ grad, float* __restrict__ loss) {
   extern __shared__ __align__(128) unsigned char smem[];
   bf16* W = reinterpret_cast<bf16*>(smem);
   bf16* X = W + kWs;                                        // h_0 .. h_5
@@ -181,7 +193,10 @@ __global__ void __launch_bounds__(kNrcThreads) nrc_train_kernel(NrcView v, const
   load_weights(v.wb, W);
   for (int i = threadIdx.x; i < kGs; i += blockDim.x) G[i] = 0.0f;
   __syncthreads();
-  const uint32_t count = min(*count_ptr, capacity);
+  // records [first_rec, first_rec + capacity) of the *count_ptr written
+  const uint32_t total = *count_ptr;
+  const uint32_t count = total > first_rec ? min(total - first_rec, capacity) : 0u;
+  recs += first_rec;
   const float inv_n = 1.0f / (3.0f * (float)max(count, 1u));
   float loss_local = 0.0f;
   for (uint32_t first = blockIdx.x * kNrcTile; first < count; first += gridDim.x * kNrcTile) {
@@ -311,9 +326,7 @@ __global__ void nrc_to_bf16_kernel(const float* __restrict__ w, bf16* __restrict
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
-static size_t infer_smem() {
-  return (size_t)kWs * 2 + (size_t)2 * kTileX * 2 + (size_t)4 * 16 * kLdY * 4;
-}
+static size_t infer_smem() { return (size_t)kWtElems * 2 + kNrcPosLevels * 3 * sizeof(float); }
 static size_t train_smem() {
   return (size_t)kWs * 2 + (size_t)(kNrcLayers + 2) * kTileX * 2 + (size_t)4 * 16 * kLdY * 4 + (size_t)kGs * 4;
 }
@@ -404,15 +417,16 @@ vcr_status nrc_setup(vcr_ctx* ctx, const vcr_nrc_params* p) {
   return VCR_OK;
 }
 
-// Gradient of the loss over `count` records (device), accumulated into grad.
+// Gradient of the loss over records [first, first + capacity) of the
+// *d_count written (device), accumulated into grad.
 vcr_status nrc_accumulate_grad(vcr_ctx* ctx, const NrcRecord* recs, const uint32_t* d_count, uint32_t capacity,
-                               cudaStream_t s) {
+                               cudaStream_t s, uint32_t first = 0) {
   NrcState* st = ctx->nrc;
   VCR_CUDA(ctx, cudaFuncSetAttribute(nrc_train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)train_smem()));
   VCR_CUDA(ctx, cudaMemsetAsync(st->loss, 0, 8, s));
   int blocks = ctx->sm_count;
-  nrc_train_kernel<<<blocks, kNrcThreads, train_smem(), s>>>(nrc_view(ctx), recs, d_count, capacity, st->grad,
-                                                            st->loss);
+  nrc_train_kernel<<<blocks, kNrcThreads, train_smem(), s>>>(nrc_view(ctx), recs, d_count, capacity, first,
+                                                            st->grad, st->loss);
   VCR_CUDA(ctx, cudaGetLastError());
   return VCR_OK;
 }
@@ -456,10 +470,10 @@ vcr_status nrc_infer_queries(vcr_ctx* ctx, cudaStream_t s) {
   NrcState* st = ctx->nrc;
   VCR_CUDA(ctx, cudaFuncSetAttribute(nrc_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)infer_smem()));
   int per_sm = 0;
-  VCR_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, nrc_infer_kernel, kNrcThreads, infer_smem()));
+  VCR_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, nrc_infer_kernel, kInferThreads, infer_smem()));
   int blocks = ctx->sm_count * std::max(per_sm, 1);
-  nrc_infer_kernel<<<blocks, kNrcThreads, infer_smem(), s>>>(nrc_view(ctx), st->query, st->query_count,
-                                                            st->query_capacity, ctx->d_sum, nullptr);
+  nrc_infer_kernel<<<blocks, kInferThreads, infer_smem(), s>>>(nrc_view(ctx), st->query, st->query_count,
+                                                               st->query_capacity, ctx->d_sum, nullptr);
   VCR_CUDA(ctx, cudaGetLastError());
   return VCR_OK;
 }
@@ -519,9 +533,9 @@ static vcr_status nrc_calibrate(vcr_ctx* ctx, const PassView& pv, cudaStream_t s
 }
 
 // Loss gradient over the step's records, then Adam.
-static vcr_status nrc_update(vcr_ctx* ctx, cudaStream_t s) {
+static vcr_status nrc_update(vcr_ctx* ctx, cudaStream_t s, uint32_t first = 0, uint32_t limit = 0) {
   NrcState* st = ctx->nrc;
-  vcr_status vs = nrc_accumulate_grad(ctx, st->train, st->train_count, st->train_cap, s);
+  vcr_status vs = nrc_accumulate_grad(ctx, st->train, st->train_count, limit ? limit : st->train_cap, s, first);
   if (vs) return vs;
   return nrc_adam(ctx, s);
 }
@@ -596,13 +610,18 @@ extern "C" VCR_API vcr_status vcr_nrc_train_step(vcr_ctx* ctx, const vcr_pass_de
   return nrc_train_step(ctx, pass, (cudaStream_t)stream);
 }
 
-extern "C" VCR_API vcr_status vcr_nrc_train_more(vcr_ctx* ctx, uint32_t steps, void* stream) {
+extern "C" VCR_API vcr_status vcr_nrc_train_more(vcr_ctx* ctx, uint32_t steps, uint32_t max_records,
+                                                 void* stream) {
   if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
   if (!ctx->nrc) return fail(ctx, VCR_ERR_STATE, "no radiance cache");
   if (ctx->nrc->step == 0) return fail(ctx, VCR_ERR_STATE, "no training records yet (vcr_nrc_train_step)");
   cudaStream_t s = (cudaStream_t)stream;
+  const uint32_t want = ctx->nrc->prm.train_samples;
+  const uint32_t batch = (max_records && max_records < want) ? max_records : 0u;
+  const uint32_t subsets = batch ? want / batch : 1u;
   for (uint32_t k = 0; k < steps; ++k) {
-    vcr_status vs = nrc_update(ctx, s);
+    // consecutive steps walk through the records batch by batch
+    vcr_status vs = batch ? nrc_update(ctx, s, (k % subsets) * batch, batch) : nrc_update(ctx, s);
     if (vs) return vs;
   }
   VCR_CUDA(ctx, cudaEventRecord(ctx->work_done, s));
@@ -674,7 +693,7 @@ extern "C" VCR_API vcr_status vcr_nrc_forward(vcr_ctx* ctx, const void* d_record
   uint32_t* d_n = reinterpret_cast<uint32_t*>(ctx->d_scratch);
   VCR_CUDA(ctx, cudaMemcpyAsync(d_n, &n, 4, cudaMemcpyHostToDevice, s));
   VCR_CUDA(ctx, cudaFuncSetAttribute(nrc_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)infer_smem()));
-  nrc_infer_kernel<<<ctx->sm_count, kNrcThreads, infer_smem(), s>>>(
+  nrc_infer_kernel<<<ctx->sm_count * 3, kInferThreads, infer_smem(), s>>>(
       nrc_view(ctx), reinterpret_cast<const NrcRecord*>(d_records), d_n, n, nullptr, d_out);
   VCR_CUDA(ctx, cudaGetLastError());
   VCR_CUDA(ctx, cudaStreamSynchronize(s));

@@ -112,20 +112,36 @@ __host__ __device__ __forceinline__ void nrc_sh16(float x, float y, float z, flo
 
 // 64 encoded inputs of one record.  `b0`, `inv_ext` map world positions to
 // [0,1]^3 box coordinates.
+// (sin, cos) of position level l along its direction (dx, dy, dz) for box
+// coordinates (ux, uy, uz).
+__host__ __device__ __forceinline__ void nrc_encode_level_dir(int l, float dx, float dy, float dz, float ux, float uy,
+                                                              float uz, float* sn, float* cs) {
+  float f = (float)(1u << (l >> 1)) * ((l & 1) ? 1.41421356f : 1.0f);
+  float ph = f * ((dx * ux + dy * uy) + dz * uz);
+  ph = ph - floorf(ph);
+  vsincos2pi(ph, sn, cs);
+}
+
+// (sin, cos) of position level l for box coordinates (ux, uy, uz).
+__host__ __device__ __forceinline__ void nrc_encode_level(int l, float ux, float uy, float uz, float* sn, float* cs) {
+  float dx, dy, dz;
+  nrc_level_dir(l, dx, dy, dz);
+  nrc_encode_level_dir(l, dx, dy, dz, ux, uy, uz, sn, cs);
+}
+
+
+__host__ __device__ __forceinline__ void nrc_box_coords(const NrcRecord& r, f3 b0, f3 inv_ext, float& ux, float& uy,
+                                                        float& uz) {
+  ux = (r.px - b0.x) * inv_ext.x;
+  uy = (r.py - b0.y) * inv_ext.y;
+  uz = (r.pz - b0.z) * inv_ext.z;
+}
+
 __host__ __device__ __forceinline__ void nrc_encode_position(const NrcRecord& r, f3 b0, f3 inv_ext, float* o) {
-  float ux = (r.px - b0.x) * inv_ext.x, uy = (r.py - b0.y) * inv_ext.y, uz = (r.pz - b0.z) * inv_ext.z;
+  float ux, uy, uz;
+  nrc_box_coords(r, b0, inv_ext, ux, uy, uz);
 #pragma unroll
-  for (int l = 0; l < kNrcPosLevels; ++l) {
-    float dx, dy, dz;
-    nrc_level_dir(l, dx, dy, dz);
-    float f = (float)(1u << (l >> 1)) * ((l & 1) ? 1.41421356f : 1.0f);
-    float ph = f * ((dx * ux + dy * uy) + dz * uz);
-    ph = ph - floorf(ph);
-    float sn, cs;
-    vsincos2pi(ph, &sn, &cs);
-    o[2 * l] = sn;
-    o[2 * l + 1] = cs;
-  }
+  for (int l = 0; l < kNrcPosLevels; ++l) nrc_encode_level(l, ux, uy, uz, &o[2 * l], &o[2 * l + 1]);
 }
 
 // The 32 direction inputs: SH of the view direction, then of the sun.

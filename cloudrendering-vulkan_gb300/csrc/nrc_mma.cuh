@@ -1,0 +1,146 @@
+// Register-resident forward pass of the radiance-cache MLP on the tensor
+// cores: mma.sync m16n8k16 with BF16 operands and FP32 accumulation.  A warp
+// owns 16 samples; their activations never leave registers, because the
+// accumulator fragment of one layer (rows g and g+8, columns 2t and 2t+1 of
+// each 8-column tile, g = lane/4, t = lane%4) is, after ReLU and BF16
+// packing, exactly the A fragment of the next layer (rows g and g+8,
+// columns 2t, 2t+1 and 2t+8, 2t+9 of each 16-column tile).  Only the
+// weights live in shared memory, transposed to [out][in] with 144-byte rows
+// so that the B-fragment loads (column g, rows 2t..2t+1) of a warp touch 32
+// distinct banks.
+#pragma once
+
+#include "nrc.cuh"
+
+namespace vcr {
+
+constexpr int kLdT = kNrcWidth + 8;                                      // [out][in] rows: 72 BF16
+constexpr int kWtElems = kNrcHidden * kNrcWidth * kLdT + kNrcOutPad * kLdT;  // 24,192 BF16
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+  __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<uint32_t*>(&v);
+}
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// Global [in][out] BF16 weights (row length = the layer's columns) into
+// shared [out][in] rows of kLdT.
+__device__ __forceinline__ void load_weights_transposed(const __nv_bfloat16* __restrict__ g, __nv_bfloat16* s) {
+  for (int e = threadIdx.x; e < kNrcWeightCount; e += blockDim.x) {
+    const int l = e < kNrcHidden * kNrcWidth * kNrcWidth ? e / (kNrcWidth * kNrcWidth) : kNrcHidden;
+    const int cols = nrc_layer_cols(l);
+    const int rel = e - nrc_layer_offset(l);
+    const int i = rel / cols, o = rel - i * cols;
+    s[l * kNrcWidth * kLdT + o * kLdT + i] = g[e];
+  }
+}
+
+// acc[nt] = X W_l for the NT 8-column output tiles; X is the A fragments
+// a[kt] of the 4 16-column input tiles, Wt the layer's [out][in] rows.
+template <int NT>
+__device__ __forceinline__ void mma_layer(const __nv_bfloat16* Wt, const uint32_t (&a)[4][4], float (&acc)[NT][4],
+                                          int g, int t) {
+#pragma unroll
+  for (int nt = 0; nt < NT; ++nt) {
+    acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
+    const __nv_bfloat16* row = Wt + (nt * 8 + g) * kLdT + 2 * t;
+#pragma unroll
+    for (int kt = 0; kt < 4; ++kt) {
+      const uint32_t b0 = *reinterpret_cast<const uint32_t*>(row + kt * 16);
+      const uint32_t b1 = *reinterpret_cast<const uint32_t*>(row + kt * 16 + 8);
+      mma_bf16(acc[nt], a[kt], b0, b1);
+    }
+  }
+}
+
+// The 16 position-level directions into shared memory (x, y, z each): the
+// same function as the per-sample encoder, so the values are identical.
+__device__ __forceinline__ void load_level_dirs(float* dirs) {
+  if (threadIdx.x < kNrcPosLevels)
+    nrc_level_dir((int)threadIdx.x, dirs[3 * threadIdx.x], dirs[3 * threadIdx.x + 1], dirs[3 * threadIdx.x + 2]);
+}
+
+// ReLU, BF16, and the accumulator layout of 8 tiles turned into the A
+// fragments of 4 input tiles.
+__device__ __forceinline__ void relu_to_a(const float (&acc)[8][4], uint32_t (&a)[4][4]) {
+#pragma unroll
+  for (int kt = 0; kt < 4; ++kt) {
+    a[kt][0] = pack_bf16(fmaxf(acc[2 * kt][0], 0.0f), fmaxf(acc[2 * kt][1], 0.0f));
+    a[kt][1] = pack_bf16(fmaxf(acc[2 * kt][2], 0.0f), fmaxf(acc[2 * kt][3], 0.0f));
+    a[kt][2] = pack_bf16(fmaxf(acc[2 * kt + 1][0], 0.0f), fmaxf(acc[2 * kt + 1][1], 0.0f));
+    a[kt][3] = pack_bf16(fmaxf(acc[2 * kt + 1][2], 0.0f), fmaxf(acc[2 * kt + 1][3], 0.0f));
+  }
+}
+
+// Coefficients 2t, 2t+1, 8+2t, 9+2t of a 16-vector (constant indices only).
+__device__ __forceinline__ void pick4(const float (&v)[16], int t, float& x0, float& x1, float& x2, float& x3) {
+  x0 = t == 0 ? v[0] : t == 1 ? v[2] : t == 2 ? v[4] : v[6];
+  x1 = t == 0 ? v[1] : t == 1 ? v[3] : t == 2 ? v[5] : v[7];
+  x2 = t == 0 ? v[8] : t == 1 ? v[10] : t == 2 ? v[12] : v[14];
+  x3 = t == 0 ? v[9] : t == 1 ? v[11] : t == 2 ? v[13] : v[15];
+}
+
+// The A fragments of the 64 encoded inputs of one sample row (h = 0: the
+// row g half of each register pair, h = 1: row g + 8).  Column 2l / 2l+1
+// are sin / cos of position level l (k-tiles 0, 1), columns 32.. the view
+// SH, 48.. the sun SH (k-tiles 2, 3), as nrc_encode lays them out.
+// `dirs` holds the 16 level directions (nrc_level_dir) as x, y, z triples.
+__device__ __forceinline__ void encode_a(const NrcRecord& r, bool valid, f3 b0, f3 inv_ext, const float* dirs, int t,
+                                         int h, uint32_t (&a)[4][4]) {
+  float s[4] = {0.f, 0.f, 0.f, 0.f}, c[4] = {0.f, 0.f, 0.f, 0.f};
+  float v0 = 0.f, v1 = 0.f, v2 = 0.f, v3 = 0.f, w0 = 0.f, w1 = 0.f, w2 = 0.f, w3 = 0.f;
+  if (valid) {
+    float ux, uy, uz;
+    nrc_box_coords(r, b0, inv_ext, ux, uy, uz);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int l = 4 * j + t;
+      nrc_encode_level_dir(l, dirs[3 * l], dirs[3 * l + 1], dirs[3 * l + 2], ux, uy, uz, &s[j], &c[j]);
+    }
+    float sh[16];
+    nrc_sh16(r.vx, r.vy, r.vz, sh);
+    pick4(sh, t, v0, v1, v2, v3);
+    nrc_sh16(r.sx, r.sy, r.sz, sh);
+    pick4(sh, t, w0, w1, w2, w3);
+  }
+  a[0][h] = pack_bf16(s[0], c[0]);      // cols 2t, 2t+1: level t
+  a[0][h + 2] = pack_bf16(s[1], c[1]);  // cols 8+2t: level 4+t
+  a[1][h] = pack_bf16(s[2], c[2]);      // level 8+t
+  a[1][h + 2] = pack_bf16(s[3], c[3]);  // level 12+t
+  a[2][h] = pack_bf16(v0, v1);
+  a[2][h + 2] = pack_bf16(v2, v3);
+  a[3][h] = pack_bf16(w0, w1);
+  a[3][h + 2] = pack_bf16(w2, w3);
+}
+
+// Forward of rows g and g+8 of one 16-sample tile: outputs y (cols 0..2)
+// land in lanes with t == 0 (row g in yg, row g + 8 in yh).
+__device__ __forceinline__ void mlp_forward_mma(const __nv_bfloat16* Wt, uint32_t (&a)[4][4], int g, int t,
+                                                float (&yg)[3], float (&yh)[3]) {
+#pragma unroll 1
+  for (int l = 0; l < kNrcHidden; ++l) {
+    float acc[8][4];
+    mma_layer<8>(Wt + l * kNrcWidth * kLdT, a, acc, g, t);
+    relu_to_a(acc, a);
+  }
+  float out[2][4];
+  mma_layer<2>(Wt + kNrcHidden * kNrcWidth * kLdT, a, out, g, t);
+  // tile 0 holds cols 2t, 2t+1: lane t = 0 has cols 0, 1 and lane t = 1 col 2
+  const float c2g = __shfl_down_sync(0xffffffffu, out[0][0], 1);
+  const float c2h = __shfl_down_sync(0xffffffffu, out[0][2], 1);
+  yg[0] = out[0][0];
+  yg[1] = out[0][1];
+  yg[2] = c2g;
+  yh[0] = out[0][2];
+  yh[1] = out[0][3];
+  yh[2] = c2h;
+}
+
+}  // namespace vcr

@@ -211,8 +211,8 @@ class Context:
         p.seed, p.pass_index, p.spp = seed, pass_index, spp
         self._ck(lib().vcr_nrc_frame(self.h, C.byref(p), C.c_void_p(stream)))
 
-    def nrc_train_more(self, steps, stream=0):
-        self._ck(lib().vcr_nrc_train_more(self.h, steps, C.c_void_p(stream)))
+    def nrc_train_more(self, steps, max_records=0, stream=0):
+        self._ck(lib().vcr_nrc_train_more(self.h, steps, max_records, C.c_void_p(stream)))
 
     def nrc_info(self) -> dict:
         i = _abi.NrcInfo()

@@ -374,8 +374,10 @@ VCR_API vcr_status vcr_nrc_train_step(vcr_ctx* ctx, const vcr_pass_desc* pass, v
  * Needs the DDA tracker and params.nrc_events > 0. */
 VCR_API vcr_status vcr_nrc_frame(vcr_ctx* ctx, const vcr_pass_desc* pass, void* stream);
 /* `steps` further gradient + Adam steps on the records of the last training
- * step or frame (a cheap warm-up: the records are reused, not re-traced). */
-VCR_API vcr_status vcr_nrc_train_more(vcr_ctx* ctx, uint32_t steps, void* stream);
+ * step or frame (a cheap warm-up: the records are reused, not re-traced).
+ * max_records > 0 makes each step use a batch of that many records, the
+ * steps walking through the records batch by batch; 0 uses them all. */
+VCR_API vcr_status vcr_nrc_train_more(vcr_ctx* ctx, uint32_t steps, uint32_t max_records, void* stream);
 VCR_API vcr_status vcr_nrc_info(vcr_ctx* ctx, vcr_nrc_info_t* out);
 VCR_API vcr_status vcr_nrc_get_weights(vcr_ctx* ctx, float* host_out, size_t count);
 VCR_API vcr_status vcr_nrc_set_weights(vcr_ctx* ctx, const float* host, size_t count);
