@@ -700,23 +700,21 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.ppm or args.ppb:
-        import __graft_entry__ as ge
+    if args.impl == "reference" and not (args.ppm or args.ppb or args.batch or args.nrc_frames):
+        run_reference(args)
+        return
+    import contextlib
+
+    import __graft_entry__ as ge
+    with contextlib.redirect_stdout(sys.stderr):  # stdout carries only the JSON line
         ge.build()
+    if args.ppm or args.ppb:
         run_ppm(args) if args.ppm else run_ppb(args)
     elif args.batch:
-        import __graft_entry__ as ge
-        ge.build()
         run_batch(args)
     elif args.nrc_frames:
-        import __graft_entry__ as ge
-        ge.build()
         run_nrc_frames(args)
-    elif args.impl == "reference":
-        run_reference(args)
     else:
-        import __graft_entry__ as ge
-        ge.build()
         run_vcr(args)
 
 

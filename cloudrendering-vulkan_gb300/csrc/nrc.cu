@@ -3,14 +3,17 @@
 // online on paths the tracer itself produces and queried where paths
 // terminate into it.  No reference counterpart.
 //
-// Tensor cores: BF16 operands, FP32 accumulation through the warp-level
-// matrix API (16x16x16 tiles).  One CTA holds the BF16 weights in shared
-// memory; each of its 4 warps owns 16 samples of a 64-sample tile, so a
-// layer's activations never leave the warp between layers.  Training fuses
-// encoding, forward, the relative-L2 loss gradient, backward and the
-// weight-gradient accumulation (X_l^T dY_l over the tile, in shared FP32)
-// in one kernel; one atomic add per weight per CTA flushes the gradient;
-// Adam runs on FP32 master weights and refreshes the BF16 copy.
+// Tensor cores, BF16 operands, FP32 accumulation.  Queries: a
+// register-resident forward (mma.sync m16n8k16, nrc_mma.cuh) — each warp
+// runs 16-sample tiles whose activations stay in the MMA fragments, the CTA
+// shares only the transposed BF16 weights.  Training: one CTA per SM holds
+// the BF16 weights, the six activation tiles of a 64-sample tile, the
+// gradient ping-pong and an FP32 weight-gradient accumulator in padded
+// shared memory (227 KB); the warp-level matrix API (16x16x16) runs the
+// forward, the relative-L2 loss gradient, the backward and X_l^T dY_l over
+// the tile; one atomic add per weight per CTA flushes the gradient.  Adam
+// runs on FP32 master weights and refreshes the BF16 copies (training
+// weights, and the moving average the queries use).
 #include <mma.h>
 
 #include <cstring>
