@@ -475,6 +475,17 @@ def _timed_passes(stream, fn, steps):
     return a.elapsed_time(b) / steps
 
 
+def _divided(sc, div):
+    """The scene with its image sides divided by div (a small case of the
+    same workload, for profiler captures)."""
+    import dataclasses
+
+    if div <= 1:
+        return sc
+    return dataclasses.replace(sc, name=f"{sc.name}/{div}", width=max(1, sc.width // div),
+                               height=max(1, sc.height // div))
+
+
 def run_ppm(args):
     """C2: 256^3 FP32 cloud (sigma_t = 16 rho), 1,048,576 photons a pass, r0
     0.01, alpha 0.7, 960x540; one JSON line of pass time and rates."""
@@ -482,7 +493,7 @@ def run_ppm(args):
     import vcr
     from vcr import configs
 
-    sc = configs.C2_PPM
+    sc = _divided(configs.C2_PPM, args.image_div)
     stream = torch.cuda.Stream()
     sh = stream.cuda_stream
     ex = sc.extra
@@ -511,7 +522,7 @@ def run_ppb(args):
     import vcr
     from vcr import configs
 
-    sc = configs.C3_PPB
+    sc = _divided(configs.C3_PPB, args.image_div)
     stream = torch.cuda.Stream()
     sh = stream.cuda_stream
     want = sc.extra["beams"]
@@ -697,6 +708,8 @@ def main():
                     help="only measure the batched 64-view configuration (CUDA graph, autotuned)")
     ap.add_argument("--ppm", action="store_true", help="only measure the photon-mapping configuration")
     ap.add_argument("--ppb", action="store_true", help="only measure the photon-beam configuration")
+    ap.add_argument("--image-div", type=int, default=1,
+                    help="divide the --ppm / --ppb image sides (a small case for profiler captures)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -338,25 +338,41 @@ __device__ __forceinline__ f3 beam_contribution(const GridView& g, const SceneVi
   return mk(sl[7] * w, sl[8] * w, sl[9] * w);
 }
 
-__global__ void __launch_bounds__(128) ppb_gather_kernel(GridView g, SceneView s, CamView cam, PassView pv,
-                                                         PpbGatherView v, double* __restrict__ sum, Counters cnt) {
-  uint32_t id = blockIdx.x * blockDim.x + threadIdx.x;
+// Per-pixel gather with a warp-coherent traversal: a warp takes an 8x4
+// pixel tile and walks the tree once for all its rays.  Each stack entry
+// carries the mask of lanes whose rays hit the parent, and a lane tests and
+// evaluates exactly the nodes and leaves its own single-ray depth-first walk
+// would, in the same order (so its sum is the same); node data are loaded
+// once for the warp (one broadcast transaction instead of one per lane).
+constexpr int kGatherThreads = 128;
+
+__global__ void __launch_bounds__(kGatherThreads) ppb_gather_kernel(GridView g, SceneView s, CamView cam, PassView pv,
+                                                                    PpbGatherView v, double* __restrict__ sum,
+                                                                    Counters cnt) {
+  __shared__ uint2 s_stack[kGatherThreads / 32][kGatherStack];
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t tiles_x = (pv.cw + 7u) / 8u;
+  const uint32_t cx = (wid % tiles_x) * 8u + (lane & 7u), cy = (wid / tiles_x) * 4u + (lane >> 3);
+  const bool valid = cx < pv.cw && cy < pv.ch;
   uint32_t lookups = 0, cells = 0;
-  if (id < pv.cw * pv.ch) {
-    uint32_t cy = id / pv.cw, cx = id - cy * pv.cw;
+  uint32_t pix = 0;
+  f3 o = mk(0.f, 0.f, 0.f), rd = mk(0.f, 0.f, 1.f), L = mk(0.f, 0.f, 0.f);
+  float t_in = 0.0f, t_out = 0.0f;
+  float cam_d[kBeamDists];
+  bool trav = false;
+  if (valid) {
     int x = (int)(pv.x0 + cx), y = (int)(pv.y0 + cy);
-    uint32_t pix = (uint32_t)y * pv.width + (uint32_t)x;
-    f3 o, rd;
+    pix = (uint32_t)y * pv.width + (uint32_t)x;
     camera_ray(cam, x, y, o, rd);
-    f3 L = mk(0.f, 0.f, 0.f);
     float tmin, tmax;
     if (!slab(o, rd, s.b0, s.b1, tmin, tmax) || tmax < 0.0f || !(s.ds > 0.0f)) {
       L = sky(s, rd);
     } else {
-      float t_in = fmaxf(tmin, 0.0f), t_out = tmax;
+      t_in = fmaxf(tmin, 0.0f);
+      t_out = tmax;
       f3 entry = along(o, rd, t_in);
       Rng rng = rng_pcg(v.seed ^ kGatherSalt, pix, v.pass);
-      float cam_d[kBeamDists];
       for (int i = 0; i < kBeamDists; ++i) {
         float t;
         free_flight(g, s, entry, rd, rng, t, lookups, cells);
@@ -365,29 +381,47 @@ __global__ void __launch_bounds__(128) ppb_gather_kernel(GridView g, SceneView s
       uint32_t cexit = 0;
       for (int i = 0; i < kBeamDists; ++i) cexit += cam_d[i] >= (t_out - t_in) ? 1u : 0u;
       L = sky(s, rd) * ((float)cexit * (1.0f / kBeamDists));
-      if (v.n > 0) {
-        f3 inv = mk(1.0f / rd.x, 1.0f / rd.y, 1.0f / rd.z);
-        uint32_t stack[kGatherStack];
-        int sp = 0;
-        uint32_t node = v.n == 1 ? (0u | kLeafBit) : 0u;
-        while (true) {
-          if (node & kLeafBit) {
-            uint32_t lf = node & ~kLeafBit;
-            if (ray_box(o, inv, t_in, t_out, v.leaf_lo[lf], v.leaf_hi[lf]))
-              L = L + beam_contribution(g, s, v, v.order[lf], o, rd, t_in, t_out, cam_d, lookups);
-          } else if (ray_box(o, inv, t_in, t_out, v.node_lo[node], v.node_hi[node])) {
-            if (sp < kGatherStack) stack[sp++] = v.right[node];  // depth bounded by 64 (30-bit keys + index bits)
-            node = v.left[node];
-            continue;
+      trav = v.n > 0;
+    }
+  }
+  uint32_t active = __ballot_sync(0xffffffffu, trav);
+  if (active) {
+    uint2* stk = s_stack[threadIdx.x >> 5];
+    const f3 inv = mk(1.0f / rd.x, 1.0f / rd.y, 1.0f / rd.z);
+    int sp = 0;  // warp-uniform, as are node and active
+    uint32_t node = v.n == 1 ? (0u | kLeafBit) : 0u;
+    while (true) {
+      const bool mine = (active >> lane) & 1u;
+      if (node & kLeafBit) {
+        const uint32_t lf = node & ~kLeafBit;
+        const float4 lo = v.leaf_lo[lf], hi = v.leaf_hi[lf];
+        if (mine && ray_box(o, inv, t_in, t_out, lo, hi))
+          L = L + beam_contribution(g, s, v, v.order[lf], o, rd, t_in, t_out, cam_d, lookups);
+      } else {
+        const float4 lo = v.node_lo[node], hi = v.node_hi[node];
+        const uint32_t hit = __ballot_sync(0xffffffffu, mine && ray_box(o, inv, t_in, t_out, lo, hi));
+        if (hit) {
+          const uint32_t l = v.left[node], r = v.right[node];
+          if (sp < kGatherStack) {  // depth bounded by 64 (30-bit keys + index bits)
+            if (lane == 0) stk[sp] = make_uint2(r, hit);
+            ++sp;
           }
-          if (sp == 0) break;
-          node = stack[--sp];
+          node = l;
+          active = hit;
+          continue;
         }
       }
+      if (sp == 0) break;
+      --sp;
+      __syncwarp();
+      const uint2 e = stk[sp];
+      __syncwarp();
+      node = e.x;
+      active = e.y;
     }
-    write_result(pv, sum, pix, L, false);
   }
-  flush_counters(cnt, id < pv.cw * pv.ch ? 1ull : 0ull, lookups, 0, cells);
+  if (valid) write_result(pv, sum, pix, L, false);
+  flush_counters(cnt, valid ? 1ull : 0ull, lookups, 0, cells);
 }
 
 // ---------------------------------------------------------------------------
@@ -513,8 +547,11 @@ vcr_status ppb_pass_launch(vcr_ctx* ctx, const vcr_pass_desc* pass, cudaStream_t
   if (vs) return vs;
   PpbGatherView gv{st->seg_a, st->seg_b, st->seg_beam, st->slots, st->idx_sorted, st->left, st->right,
                    st->leaf_lo, st->leaf_hi, st->node_lo, st->node_hi, (int)n, pass->seed, pass->pass_index};
-  uint32_t pixels = pv.cw * pv.ch;
-  ppb_gather_kernel<<<(pixels + 127) / 128, 128, 0, st_>>>(g, s, cam_view(ctx->cam), pv, gv, ctx->d_sum, cnt);
+  // one warp per 8x4 pixel tile
+  uint32_t tiles = ((pv.cw + 7u) / 8u) * ((pv.ch + 3u) / 4u);
+  uint32_t warps_per_block = kGatherThreads / 32;
+  ppb_gather_kernel<<<(tiles + warps_per_block - 1) / warps_per_block, kGatherThreads, 0, st_>>>(
+      g, s, cam_view(ctx->cam), pv, gv, ctx->d_sum, cnt);
   VCR_CUDA(ctx, cudaGetLastError());
   VCR_CUDA(ctx, cudaEventRecord(ctx->work_done, st_));
   if (!(pv.flags & VCR_PASS_NO_ACCUMULATE)) {
