@@ -108,8 +108,7 @@ __global__ void __launch_bounds__(128) ppb_emit_kernel(GridView g, SceneView s, 
       sl[7] = power.x; sl[8] = power.y; sl[9] = power.z;
       for (int i = 0; i < kBeamDists; ++i) {
         float t;
-        free_flight(g, s, o, d, rng, t, lookups, cells);
-        sl[10 + i] = t;
+        sl[10 + i] = free_flight(g, s, o, d, rng, t, lookups, cells) ? t : kEscaped;
       }
       uint32_t ns = segments_of(tmax, v.radius);
       v.slot_segs[(size_t)p * v.K + beams] = ns;
@@ -375,8 +374,7 @@ __global__ void __launch_bounds__(kGatherThreads) ppb_gather_kernel(GridView g, 
       Rng rng = rng_pcg(v.seed ^ kGatherSalt, pix, v.pass);
       for (int i = 0; i < kBeamDists; ++i) {
         float t;
-        free_flight(g, s, entry, rd, rng, t, lookups, cells);
-        cam_d[i] = t;
+        cam_d[i] = free_flight(g, s, entry, rd, rng, t, lookups, cells) ? t : kEscaped;
       }
       uint32_t cexit = 0;
       for (int i = 0; i < kBeamDists; ++i) cexit += cam_d[i] >= (t_out - t_in) ? 1u : 0u;

@@ -7,6 +7,9 @@
 namespace vcr {
 
 constexpr int kBeamDists = 16;             // BEAM_TRANSMITTANCE_SAMPLES (PPB_PT.comp, PPB_PE.comp:31)
+// A transmittance distance whose free flight left the box: beyond every point
+// of the beam or camera ray, whatever the rounding of the box exit.
+constexpr float kEscaped = 3.0e38f;
 constexpr int kSlotFloats = 28;            // start 3, dir 3, length, power 3, 16 distances, 2 pad
 constexpr uint32_t kMaxBeamsPerPhoton = 65;  // 64 scatter events + the entering beam
 constexpr uint32_t kMaxSegPerBeam = 4096;

@@ -25,6 +25,9 @@
 namespace oracle {
 
 const int kBeamDists = 16;
+// A transmittance distance whose free flight left the box: beyond every
+// point of the beam or camera ray, whatever the rounding of the box exit.
+const float kEscaped = 3.0e38f;
 const int kSlotFloats = 28;
 const uint32_t kMaxBeamsPerPhoton = 65;
 const uint32_t kMaxSegPerBeam = 4096;
@@ -233,8 +236,7 @@ static void run_ppb(const Scene& s, uint32_t P, uint32_t cap, float radius, uint
       sl[7] = power.x; sl[8] = power.y; sl[9] = power.z;
       for (int i = 0; i < kBeamDists; ++i) {
         float t;
-        free_flight(s, o, d, rng, t, c);
-        sl[10 + i] = t;
+        sl[10 + i] = free_flight(s, o, d, rng, t, c) ? t : kEscaped;
       }
       uint32_t ns = segments_of(tmax, radius);
       B.slot_segs[(size_t)p * K + beams] = ns;
@@ -332,8 +334,7 @@ static void gather(const Scene& s, const Beams& B, const vcr_camera& cam, uint32
         float cam_d[kBeamDists];
         for (int i = 0; i < kBeamDists; ++i) {
           float t;
-          free_flight(s, entry, rd, rng, t, c);
-          cam_d[i] = t;
+          cam_d[i] = free_flight(s, entry, rd, rng, t, c) ? t : kEscaped;
         }
         uint32_t cexit = 0;
         for (int i = 0; i < kBeamDists; ++i) cexit += cam_d[i] >= (t_out - t_in) ? 1u : 0u;

@@ -90,3 +90,23 @@ def test_oracle_beam_pass_is_deterministic_and_conserves_segments():
     used = np.unique(b1["seg_beam"])
     np.testing.assert_allclose(tot[used], lens[used], rtol=1e-4)
     assert n == len(b1["codes"]) and np.all(np.diff(b1["codes"][b1["order"]].astype(np.int64)) >= 0)
+
+
+def test_empty_cloud_gathers_the_whole_sky():
+    """Every free flight in an all-zero cloud escapes the box, so the camera
+    transmittance estimate is 1 at every pixel, grazing rays included: an
+    escaped flight counts as farther than the ray's box exit, however the
+    exit distances computed from the camera and from the entry point round."""
+    size = (16, 16, 16)
+    og = orc.Grid(np.zeros(size, np.float32), 0)
+    desc = vcr.grid_desc(size, (1.0 / 16,) * 3)
+    cloud = vcr.cloud_from_grid(desc, 1.0, 16.0)
+    cloud.max_extinction = 0.01
+    sc = configs.C1_PT
+    W, H = 20, 12
+    s, b = orc.ppb_pass(og, cloud, sc.camera(W, H), sc.params(vcr.TRACKER_DDA), 512, 4096, 0.05, 0.8, W, H,
+                        seed=2, pass_index=0)
+    np.testing.assert_array_equal(s, np.float64(np.float32(0.1)))
+    # escaped transmittance samples sit beyond every beam point
+    used = b["slots"][np.unique(b["seg_beam"])]
+    assert len(used) and (used[:, 10:26] > 1e38).all()
