@@ -208,7 +208,7 @@ extern "C" VCR_API vcr_status vcr_batch_autotune(vcr_ctx* ctx, const vcr_pass_de
   VCR_CUDA(ctx, cudaEventCreate(&e1));
   vcr_tuning saved = ctx->tuning, best = saved;
   float best_ms = 1e30f;
-  const uint32_t levels[] = {0, 1, 2, 3}, steps[] = {2, 8}, threads[] = {128, 256};
+  const uint32_t levels[] = {0, 1, 2, 3}, steps[] = {2, 8, 16}, threads[] = {128, 256};
   for (uint32_t lv : levels)
     for (uint32_t sp : steps)
       for (uint32_t th : threads) {

@@ -11,7 +11,13 @@
 // lanes never idle while paths remain.  A wavefront step is one bounded DDA
 // walk (at most `dda_steps` majorant cells, resumable: the optical depth
 // left over is kept) followed by at most one density lookup, so a lane
-// crossing many empty cells cannot hold its warp for a whole flight.  When
+// crossing many empty cells cannot hold its warp for a whole flight.  The
+// step runs as warp-converged phases with __syncwarp() between them: DDA
+// set-up of new rays, then every live lane's walk (a ray set up this step
+// walks this step), then the density lookups of all candidate lanes at
+// once, then the collision / escape bookkeeping.  Without the explicit
+// reconvergence, lanes leaving the walk loop after different cell counts
+// reached the lookup in separate groups (1.4x slower on the C5 pass).  When
 // the selected majorant level fits, one thread stages it into shared memory
 // with a TMA bulk copy (cp.async.bulk + mbarrier) at CTA start and every
 // DDA cell visit reads shared memory.  The arithmetic per path is identical
@@ -78,22 +84,48 @@ enum : uint32_t { kIdle = 0, kScatter = 1, kNee = 2 };
 
 // Rarely-taken bodies live out of line: the persistent loop then stays small
 // enough for the instruction cache (a fully inlined loop stalled on
-// instruction fetch more than on memory).
-__device__ __noinline__ f3 sample_direction(const Phase& ph, f3 dir, Rng& rng) { return hg_sample(ph, dir, rng, true); }
+// instruction fetch more than on memory).  They take and return values, not
+// references, so the path state they touch stays in registers instead of
+// being stored to the stack around each call; the kernel's struct
+// parameters are __grid_constant__ so that passing them by const reference
+// does not copy them to local memory.
+struct DirRng {
+  f3 d;
+  Rng r;
+};
+__device__ __noinline__ DirRng sample_direction(const Phase& ph, f3 dir, Rng rng) {
+  DirRng o;
+  o.d = hg_sample(ph, dir, rng, true);
+  o.r = rng;
+  return o;
+}
 
 __device__ __noinline__ f3 escape_radiance(const SceneView& s, f3 dir) { return sky(s, dir); }
 
 // Camera ray of a path; returns false (L = sky) if it misses the cloud.
-__device__ __noinline__ bool start_path(const CamView& cam, const SceneView& s, int x, int y, f3& pos, f3& dir,
-                                        f3& L) {
-  camera_ray(cam, x, y, pos, dir);
+struct PathStart {
+  f3 pos, dir, L;
+  bool hit;
+};
+__device__ __noinline__ PathStart start_path(const CamView& cam, const SceneView& s, int x, int y) {
+  PathStart o;
+  camera_ray(cam, x, y, o.pos, o.dir);
+  o.L = mk(0.f, 0.f, 0.f);
   float tmin, tmax;
-  if (!slab(pos, dir, s.b0, s.b1, tmin, tmax) || tmax < 0.0f || !(s.ds > 0.0f)) {
-    L = sky(s, dir);
-    return false;
+  if (!slab(o.pos, o.dir, s.b0, s.b1, tmin, tmax) || tmax < 0.0f || !(s.ds > 0.0f)) {
+    o.L = sky(s, o.dir);
+    o.hit = false;
+    return o;
   }
-  pos = along(pos, dir, tmax < tmin ? tmax : tmin);
-  return true;
+  o.pos = along(o.pos, o.dir, tmax < tmin ? tmax : tmin);
+  o.hit = true;
+  return o;
+}
+__device__ __forceinline__ bool begin(const PathStart& o, f3& pos, f3& dir, f3& L) {
+  pos = o.pos;
+  dir = o.dir;
+  L = o.L;
+  return o.hit;
 }
 
 // A training path's radiance is final: turn the recorded radiance-before
@@ -132,14 +164,28 @@ constexpr uint32_t kTrainPath = 0x80000000u;  // pid flag of a training path
 
 // Russian roulette of a training path's continuation: survive with
 // probability p and carry weight 1/p.
-__device__ __noinline__ bool roulette_survives(Rng& rng, float p, float& beta) {
-  if (rng_next(rng) >= p) return false;
-  beta = beta / p;
-  return true;
+struct Roulette {
+  Rng r;
+  float beta;
+  bool alive;
+};
+__device__ __noinline__ Roulette roulette(Rng rng, float p, float beta) {
+  Roulette o;
+  o.alive = rng_next(rng) < p;
+  o.r = rng;
+  o.beta = o.alive ? beta / p : beta;
+  return o;
+}
+__device__ __forceinline__ bool roulette_survives(Rng& rng, float p, float& beta) {
+  Roulette o = roulette(rng, p, beta);
+  rng = o.r;
+  beta = o.beta;
+  return o.alive;
 }
 
-// 4 x 256 threads per SM: 64 registers a thread (a few spill to L1), which
-// measured ~7% faster than 3 CTAs at 77 registers on the 1024x512x1024 scene.
+// 1024 threads per SM: 64 registers a thread (a few spill to L1).  On the
+// 1024x512x1024 scene this measured 6% faster than 768 threads at 80
+// registers (no spills) and 18% faster than 1280 threads at 48 registers.
 // Work items [0, ts.paths) are training paths (their pid carries kTrainPath
 // and their pix the slot of their last record); the pass's camera paths
 // follow.  kBatch: the camera paths are those of bt's views (pid holds the
@@ -150,9 +196,12 @@ __host__ __device__ constexpr uint32_t align16(uint32_t b) { return (b + 15u) & 
 
 template <int kThreads, bool kStage, bool kBatch>
 __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
-    pt_wavefront_kernel(GridView g, SceneView s, CamView cam, PassView pv, double* __restrict__ sum,
-                        uint32_t* __restrict__ stats, Counters cnt, uint32_t total, uint32_t dda_steps,
-                        uint32_t maj_bytes, NrcSink nq, NrcTrainSink ts, BatchSink bt, int* __restrict__ err) {
+    pt_wavefront_kernel(const __grid_constant__ GridView g, const __grid_constant__ SceneView s,
+                        const __grid_constant__ CamView cam, const __grid_constant__ PassView pv,
+                        double* __restrict__ sum, uint32_t* __restrict__ stats, Counters cnt, uint32_t total,
+                        uint32_t dda_steps, uint32_t maj_bytes, const __grid_constant__ NrcSink nq,
+                        const __grid_constant__ NrcTrainSink ts, const __grid_constant__ BatchSink bt,
+                        int* __restrict__ err) {
   extern __shared__ __align__(16) float s_maj[];
   __shared__ __align__(8) uint64_t s_bar;
   const float* maj = g.majorants;
@@ -216,7 +265,7 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
           beta = 1.0f;
           events = lookups = cells = 0;
           ++n_paths;
-          if (start_path(bv.cam, s, (int)cx, (int)cy, pos, dir, L)) {
+          if (begin(start_path(bv.cam, s, (int)cx, (int)cy), pos, dir, L)) {
             mode = kScatter;
             idir = dir;
             need_init = true;
@@ -233,7 +282,7 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
           beta = 1.0f;
           events = lookups = cells = 0;
           ++n_paths;
-          if (start_path(cam, s, (int)(pv.x0 + pp % pv.cw), (int)(pv.y0 + pp / pv.cw), pos, dir, L)) {
+          if (begin(start_path(cam, s, (int)(pv.x0 + pp % pv.cw), (int)(pv.y0 + pp / pv.cw)), pos, dir, L)) {
             mode = kScatter;
             idir = dir;
             need_init = true;
@@ -251,7 +300,7 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
           beta = 1.0f;
           events = lookups = cells = 0;
           ++n_paths;
-          if (start_path(cam, s, x, y, pos, dir, L)) {
+          if (begin(start_path(cam, s, x, y), pos, dir, L)) {
             mode = kScatter;
             idir = dir;
             need_init = true;
@@ -267,21 +316,39 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
     }
     if (__all_sync(0xffffffffu, exhausted && mode == kIdle)) break;
 
-    // ---- one bounded walk + at most one lookup ----------------------------
-    if (mode != kIdle && !need_init) {
+    // ---- the one DDA set-up site (camera ray, NEE ray, scattered ray) ------
+    if (need_init) {
+      track_init(tr, g, s, maj, pos, idir, cells);
+      need_init = false;
+    }
+    __syncwarp();
+    // ---- one bounded walk ---------------------------------------------------
+    const bool act = mode != kIdle;
+    int r = kPending;
+    if (act) {
       if (!flying) {
         tau = -vlog(rng_next(rng));
         flying = true;
       }
-      int r = track_walk(tr, g, maj, k, tau, cells, dda_steps);
+      r = track_walk(tr, g, maj, k, tau, cells, dda_steps);
+    }
+    __syncwarp();
+    // ---- at most one density lookup (the candidate lanes together) ---------
+    const f3 lsun = kBatch ? -s_views[pid].sun : lsun0;
+    f3 p = pos;
+    float rho = 0.0f;
+    if (r == kCandidate) {
+      f3 rd = mode == kScatter ? dir : lsun;
+      p = along(pos, rd, tr.t);
+      rho = density_at(g, s, p);
+    }
+    __syncwarp();
+    // ---- collision, escape and path bookkeeping -----------------------------
+    if (act) {
       if (r != kPending) {
         flying = false;
         bool nee_done = false, finish = false;
-        const f3 lsun = kBatch ? -s_views[pid].sun : lsun0;
         if (r == kCandidate) {
-          f3 rd = mode == kScatter ? dir : lsun;
-          f3 p = along(pos, rd, tr.t);
-          float rho = density_at(g, s, p);
           ++lookups;
           if (mode == kScatter) {
             float xi = rng_next(rng);
@@ -340,7 +407,9 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
                      !roulette_survives(rng, ts.survival, beta)) {
             finish = true;  // past the recorded vertices: Russian roulette
           } else {
-            dir = sample_direction(s.ph, dir, rng);
+            DirRng nd = sample_direction(s.ph, dir, rng);
+            dir = nd.d;
+            rng = nd.r;
             mode = kScatter;
             idir = dir;
             need_init = true;
@@ -368,11 +437,7 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
         }
       }
     }
-    // ---- the one DDA set-up site (camera ray, NEE ray, scattered ray) ------
-    if (need_init) {
-      track_init(tr, g, s, maj, pos, idir, cells);
-      need_init = false;
-    }
+    __syncwarp();
   }
   flush_counters(cnt, n_paths, n_look, n_ev, n_cells);
 }
@@ -452,7 +517,7 @@ extern "C" VCR_API vcr_status vcr_autotune_pt(vcr_ctx* ctx, const vcr_pass_desc*
   vcr_tuning saved = ctx->tuning, best = saved;
   float best_ms = 1e30f;
   const uint32_t levels[] = {0, 1, 2, 3};
-  const uint32_t steps[] = {2, 8};
+  const uint32_t steps[] = {2, 8, 16};
   const uint32_t threads[] = {128, 256};
   vcr_status status = VCR_OK;
   for (uint32_t lv : levels)

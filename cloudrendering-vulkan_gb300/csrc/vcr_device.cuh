@@ -78,10 +78,46 @@ __device__ __forceinline__ float trilinear(const GridView& g, f3 nrm) {
   x0 = min(max(x0, 0), g.n[0] - 1);
   y0 = min(max(y0, 0), g.n[1] - 1);
   z0 = min(max(z0, 0), g.n[2] - 1);
-  float v000 = texel(g, x0, y0, z0), v100 = texel(g, x1, y0, z0);
-  float v010 = texel(g, x0, y1, z0), v110 = texel(g, x1, y1, z0);
-  float v001 = texel(g, x0, y0, z1), v101 = texel(g, x1, y0, z1);
-  float v011 = texel(g, x0, y1, z1), v111 = texel(g, x1, y1, z1);
+  // One brick address for (x0, y0, z0); each +1 neighbour is a step of the
+  // element offset (and of the brick index, for the scale) that is 0 where
+  // the coordinate is clamped at the grid's edge, 1 / 8 / 64 inside a brick,
+  // and the brick stride minus 7 / 56 / 448 where it crosses into the next
+  // brick.  The texels read are exactly those of texel(g, x, y, z).
+  const uint32_t nb0 = (uint32_t)g.nb[0], nb01 = nb0 * (uint32_t)g.nb[1];
+  const uint32_t b = (uint32_t)(x0 >> kBrickLog2) + nb0 * (uint32_t)(y0 >> kBrickLog2) + nb01 * (uint32_t)(z0 >> kBrickLog2);
+  const uint32_t o = (b << 9) + (uint32_t)(x0 & 7) + ((uint32_t)(y0 & 7) << 3) + ((uint32_t)(z0 & 7) << 6);
+  const bool cx = (x0 & 7) == 7, cy = (y0 & 7) == 7, cz = (z0 & 7) == 7;
+  const uint32_t bx = (x1 != x0 && cx) ? 1u : 0u, by = (y1 != y0 && cy) ? nb0 : 0u, bz = (z1 != z0 && cz) ? nb01 : 0u;
+  const uint32_t ox = x1 == x0 ? 0u : (cx ? 505u : 1u);
+  const uint32_t oy = y1 == y0 ? 0u : (cy ? (nb0 << 9) - 56u : 8u);
+  const uint32_t oz = z1 == z0 ? 0u : (cz ? (nb01 << 9) - 448u : 64u);
+  float v000, v100, v010, v110, v001, v101, v011, v111;
+  if (g.precision == 0) {
+    const float* t = reinterpret_cast<const float*>(g.bricks);
+    v000 = __ldg(t + o); v100 = __ldg(t + o + ox);
+    v010 = __ldg(t + o + oy); v110 = __ldg(t + o + ox + oy);
+    v001 = __ldg(t + o + oz); v101 = __ldg(t + o + ox + oz);
+    v011 = __ldg(t + o + oy + oz); v111 = __ldg(t + o + ox + oy + oz);
+  } else {
+    const float* sc = g.scales + b;
+    const float s000 = __ldg(sc), s100 = __ldg(sc + bx), s010 = __ldg(sc + by), s110 = __ldg(sc + bx + by);
+    const float s001 = __ldg(sc + bz), s101 = __ldg(sc + bx + bz), s011 = __ldg(sc + by + bz);
+    const float s111 = __ldg(sc + bx + by + bz);
+    if (g.precision == 1) {
+      const __half* t = reinterpret_cast<const __half*>(g.bricks);
+      v000 = __half2float(__ldg(t + o)) * s000; v100 = __half2float(__ldg(t + o + ox)) * s100;
+      v010 = __half2float(__ldg(t + o + oy)) * s010; v110 = __half2float(__ldg(t + o + ox + oy)) * s110;
+      v001 = __half2float(__ldg(t + o + oz)) * s001; v101 = __half2float(__ldg(t + o + ox + oz)) * s101;
+      v011 = __half2float(__ldg(t + o + oy + oz)) * s011; v111 = __half2float(__ldg(t + o + ox + oy + oz)) * s111;
+    } else {
+      const __nv_bfloat16* t = reinterpret_cast<const __nv_bfloat16*>(g.bricks);
+      v000 = __bfloat162float(__ldg(t + o)) * s000; v100 = __bfloat162float(__ldg(t + o + ox)) * s100;
+      v010 = __bfloat162float(__ldg(t + o + oy)) * s010; v110 = __bfloat162float(__ldg(t + o + ox + oy)) * s110;
+      v001 = __bfloat162float(__ldg(t + o + oz)) * s001; v101 = __bfloat162float(__ldg(t + o + ox + oz)) * s101;
+      v011 = __bfloat162float(__ldg(t + o + oy + oz)) * s011;
+      v111 = __bfloat162float(__ldg(t + o + ox + oy + oz)) * s111;
+    }
+  }
   float c00 = fmaf(tx, v100 - v000, v000);
   float c10 = fmaf(tx, v110 - v010, v010);
   float c01 = fmaf(tx, v101 - v001, v001);
