@@ -128,7 +128,7 @@ __global__ void dda_trace_kernel(SceneView s, int nc0, int nc1, int nc2, const f
       slab(org, dir, s.b0, s.b1, tmin, tmax);
     }
     Dda dd;
-    dda_init(dd, org, dir, s.b0, s.cell, nc);
+    dda_init(dd, org, dir, recip(dir), s.b0, s.cell, s.icell, nc);
     float t = 0.0f;
     while (k < max_cells) {
       float e = dda_cell_exit(dd);

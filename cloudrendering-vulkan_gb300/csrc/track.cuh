@@ -14,10 +14,11 @@ struct Track {
 __device__ __forceinline__ void track_init(Track& tr, const GridView& g, const SceneView& s, const float* maj, f3 o,
                                            f3 d, uint32_t& cells) {
   float tmin, tmax;
-  if (!slab(o, d, s.b0, s.b1, tmin, tmax) || !finite_pos(tmax)) tmax = 0.0f;
+  const f3 inv = recip(d);
+  if (!slab_inv(o, inv, s.b0, s.b1, tmin, tmax) || !finite_pos(tmax)) tmax = 0.0f;
   tr.t = 0.0f;
   tr.t_end = tmax;
-  dda_init(tr.dda, o, d, s.b0, s.cell, g.mnb);
+  dda_init(tr.dda, o, d, inv, s.b0, s.cell, s.icell, g.mnb);
   tr.m = maj[dda_linear(tr.dda, g.mnb)];
   ++cells;
 }

@@ -35,6 +35,7 @@ struct SceneView {
   float ds, bs;     // CloudProperties.densityScaling, baseScaling
   float k_sigma;    // ds / bs: sigma_t = k_sigma * density
   f3 cell;          // world size of one majorant cell (8 voxels per axis)
+  f3 icell;         // 1 / cell per axis
   Phase ph;
   float albedo;
   float light;      // sun irradiance
@@ -145,16 +146,20 @@ struct Dda {
   float tdel[3];
 };
 
-VCR_HD void dda_axis_init(float o, float d, float b0, float cs, int c, int& step, float& tmax,
+// The set-up multiplies by the reciprocal direction `inv` = 1/d (computed
+// once per ray and shared with the slab test) and by the reciprocal cell
+// size `ics`, so a ray's DDA costs three divisions in all; the sign test is
+// on d itself because 1/(+-0) is +-inf.
+VCR_HD void dda_axis_init(float o, float d, float inv, float b0, float cs, int c, int& step, float& tmax,
                           float& tdel) {
   if (d > 0.0f) {
     step = 1;
-    tmax = ((b0 + (float)(c + 1) * cs) - o) / d;
-    tdel = cs / d;
+    tmax = ((b0 + (float)(c + 1) * cs) - o) * inv;
+    tdel = cs * inv;
   } else if (d < 0.0f) {
     step = -1;
-    tmax = ((b0 + (float)c * cs) - o) / d;
-    tdel = -cs / d;
+    tmax = ((b0 + (float)c * cs) - o) * inv;
+    tdel = -(cs * inv);
   } else {
     step = 0;
     tmax = INFINITY;
@@ -162,18 +167,18 @@ VCR_HD void dda_axis_init(float o, float d, float b0, float cs, int c, int& step
   }
 }
 
-VCR_HD int cell_of(float o, float b0, float cs, int nc) {
-  int c = (int)floorf((o - b0) / cs);
+VCR_HD int cell_of(float o, float b0, float ics, int nc) {
+  int c = (int)floorf((o - b0) * ics);
   return c < 0 ? 0 : (c > nc - 1 ? nc - 1 : c);
 }
 
-VCR_HD void dda_init(Dda& d, f3 o, f3 dir, f3 b0, f3 cs, const int nc[3]) {
-  d.c[0] = cell_of(o.x, b0.x, cs.x, nc[0]);
-  d.c[1] = cell_of(o.y, b0.y, cs.y, nc[1]);
-  d.c[2] = cell_of(o.z, b0.z, cs.z, nc[2]);
-  dda_axis_init(o.x, dir.x, b0.x, cs.x, d.c[0], d.step[0], d.tmax[0], d.tdel[0]);
-  dda_axis_init(o.y, dir.y, b0.y, cs.y, d.c[1], d.step[1], d.tmax[1], d.tdel[1]);
-  dda_axis_init(o.z, dir.z, b0.z, cs.z, d.c[2], d.step[2], d.tmax[2], d.tdel[2]);
+VCR_HD void dda_init(Dda& d, f3 o, f3 dir, f3 inv, f3 b0, f3 cs, f3 ics, const int nc[3]) {
+  d.c[0] = cell_of(o.x, b0.x, ics.x, nc[0]);
+  d.c[1] = cell_of(o.y, b0.y, ics.y, nc[1]);
+  d.c[2] = cell_of(o.z, b0.z, ics.z, nc[2]);
+  dda_axis_init(o.x, dir.x, inv.x, b0.x, cs.x, d.c[0], d.step[0], d.tmax[0], d.tdel[0]);
+  dda_axis_init(o.y, dir.y, inv.y, b0.y, cs.y, d.c[1], d.step[1], d.tmax[1], d.tdel[1]);
+  dda_axis_init(o.z, dir.z, inv.z, b0.z, cs.z, d.c[2], d.step[2], d.tmax[2], d.tdel[2]);
 }
 
 VCR_HD float dda_cell_exit(const Dda& d) { return fminf(fminf(d.tmax[0], d.tmax[1]), d.tmax[2]); }

@@ -266,8 +266,10 @@ VCR_HD f3 hg_sample(const Phase& ph, f3 in, Rng& rng, bool renorm) {
 // Geometry
 // ---------------------------------------------------------------------------
 // Slab test (intersectCloud, PathTracer.comp:154-184), same comparisons.
-VCR_HD bool slab(f3 pos, f3 dir, f3 b0, f3 b1, float& tmin, float& tmax) {
-  f3 inv = f3{1.0f / dir.x, 1.0f / dir.y, 1.0f / dir.z};
+VCR_HD f3 recip(f3 d) { return f3{1.0f / d.x, 1.0f / d.y, 1.0f / d.z}; }
+
+// Slab test with the ray's reciprocal direction already computed.
+VCR_HD bool slab_inv(f3 pos, f3 inv, f3 b0, f3 b1, float& tmin, float& tmax) {
   bool sx = inv.x < 0.0f, sy = inv.y < 0.0f, sz = inv.z < 0.0f;
   tmin = ((sx ? b1.x : b0.x) - pos.x) * inv.x;
   tmax = ((sx ? b0.x : b1.x) - pos.x) * inv.x;
@@ -282,6 +284,10 @@ VCR_HD bool slab(f3 pos, f3 dir, f3 b0, f3 b1, float& tmin, float& tmax) {
   if (tzmin > tmin) tmin = tzmin;
   if (tzmax < tmax) tmax = tzmax;
   return true;
+}
+
+VCR_HD bool slab(f3 pos, f3 dir, f3 b0, f3 b1, float& tmin, float& tmax) {
+  return slab_inv(pos, recip(dir), b0, b1, tmin, tmax);
 }
 
 VCR_HD bool in_box(f3 p, f3 b0, f3 b1) {

@@ -275,15 +275,17 @@ float ratio_global(const Scene& s, float sigma_bar, V3 pos, V3 ldir, Rng& rng, C
 // DDA over 8^3-voxel majorant cells (Amanatides & Woo); ties x < y < z
 // ---------------------------------------------------------------------------
 
-static void dda_axis(float o, float d, float b0, float cs, int c, int& step, float& tmax, float& tdel) {
+// Set-up by multiplication with the reciprocal direction inv = 1/d and the
+// reciprocal cell size ics; the sign test is on d (1/(+-0) is +-inf).
+static void dda_axis(float o, float d, float inv, float b0, float cs, int c, int& step, float& tmax, float& tdel) {
   if (d > 0.0f) {
     step = 1;
-    tmax = ((b0 + (float)(c + 1) * cs) - o) / d;
-    tdel = cs / d;
+    tmax = ((b0 + (float)(c + 1) * cs) - o) * inv;
+    tdel = cs * inv;
   } else if (d < 0.0f) {
     step = -1;
-    tmax = ((b0 + (float)c * cs) - o) / d;
-    tdel = -cs / d;
+    tmax = ((b0 + (float)c * cs) - o) * inv;
+    tdel = -(cs * inv);
   } else {
     step = 0;
     tmax = INFINITY;
@@ -291,18 +293,19 @@ static void dda_axis(float o, float d, float b0, float cs, int c, int& step, flo
   }
 }
 
-static int cell_of(float o, float b0, float cs, int nc) {
-  int c = (int)std::floor((o - b0) / cs);
+static int cell_of(float o, float b0, float ics, int nc) {
+  int c = (int)std::floor((o - b0) * ics);
   return c < 0 ? 0 : (c > nc - 1 ? nc - 1 : c);
 }
 
-void dda_init(Dda& d, V3 o, V3 dir, V3 b0, V3 cs, const int nc[3]) {
-  d.c[0] = cell_of(o.x, b0.x, cs.x, nc[0]);
-  d.c[1] = cell_of(o.y, b0.y, cs.y, nc[1]);
-  d.c[2] = cell_of(o.z, b0.z, cs.z, nc[2]);
-  dda_axis(o.x, dir.x, b0.x, cs.x, d.c[0], d.step[0], d.tmax[0], d.tdel[0]);
-  dda_axis(o.y, dir.y, b0.y, cs.y, d.c[1], d.step[1], d.tmax[1], d.tdel[1]);
-  dda_axis(o.z, dir.z, b0.z, cs.z, d.c[2], d.step[2], d.tmax[2], d.tdel[2]);
+void dda_init(Dda& d, V3 o, V3 dir, V3 b0, V3 cs, V3 ics, const int nc[3]) {
+  V3 inv = v3(1.0f / dir.x, 1.0f / dir.y, 1.0f / dir.z);
+  d.c[0] = cell_of(o.x, b0.x, ics.x, nc[0]);
+  d.c[1] = cell_of(o.y, b0.y, ics.y, nc[1]);
+  d.c[2] = cell_of(o.z, b0.z, ics.z, nc[2]);
+  dda_axis(o.x, dir.x, inv.x, b0.x, cs.x, d.c[0], d.step[0], d.tmax[0], d.tdel[0]);
+  dda_axis(o.y, dir.y, inv.y, b0.y, cs.y, d.c[1], d.step[1], d.tmax[1], d.tdel[1]);
+  dda_axis(o.z, dir.z, inv.z, b0.z, cs.z, d.c[2], d.step[2], d.tmax[2], d.tdel[2]);
 }
 
 float dda_exit(const Dda& d) { return std::fmin(std::fmin(d.tmax[0], d.tmax[1]), d.tmax[2]); }
@@ -324,7 +327,7 @@ void track_init(const Scene& s, Track& tr, V3 o, V3 d, Counts& c) {
   if (!slab(o, d, s.b0, s.b1, tmin, tmax) || !finite_pos(tmax)) tmax = 0.0f;
   tr.t = 0.0f;
   tr.t_end = tmax;
-  dda_init(tr.dda, o, d, s.b0, s.cell, s.mnb);
+  dda_init(tr.dda, o, d, s.b0, s.cell, s.icell, s.mnb);
   tr.m = s.maj[dda_linear(tr.dda, s.mnb)];
   ++c.cells;
 }
@@ -445,6 +448,7 @@ Scene make_scene(const Grid* g, const vcr_cloud& cl, const vcr_params& p, const 
   V3 ext = sub(s.b1, s.b0);
   const float cv = (float)(8 << level);  // voxels per majorant cell
   s.cell = v3((ext.x / (float)g->n[0]) * cv, (ext.y / (float)g->n[1]) * cv, (ext.z / (float)g->n[2]) * cv);
+  s.icell = v3(1.0f / s.cell.x, 1.0f / s.cell.y, 1.0f / s.cell.z);
   s.maj = g->lv[level].data();
   for (int a = 0; a < 3; ++a) s.mnb[a] = g->lnb[level][a];
   s.g_ = p.phase_g;
@@ -582,7 +586,7 @@ void oracle_dda_trace(void* h, const vcr_cloud* cl, int level, const float* o, c
         slab(org, dir, s.b0, s.b1, tmin, tmax);
       }
       Dda dd;
-      dda_init(dd, org, dir, s.b0, s.cell, nc);
+      dda_init(dd, org, dir, s.b0, s.cell, s.icell, nc);
       float t = 0.0f;
       while (k < max_cells) {
         float e = dda_exit(dd);

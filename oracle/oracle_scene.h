@@ -33,6 +33,7 @@ struct Scene {
   V3 b0, b1;
   float max_ext, ds, bs, k;
   V3 cell;
+  V3 icell;  // 1 / cell
   float g_, opg2, omg2, o2g;  // Parameters (UniformBuffers.h:80-112)
   bool iso;
   float albedo, light;
