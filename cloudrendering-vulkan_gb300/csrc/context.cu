@@ -71,6 +71,7 @@ SceneView scene_view(const vcr_ctx* ctx) {
   s.cell.y = (ext.y / (float)ctx->gdesc.size[1]) * cv;
   s.cell.z = (ext.z / (float)ctx->gdesc.size[2]) * cv;
   s.icell = mk(1.0f / s.cell.x, 1.0f / s.cell.y, 1.0f / s.cell.z);
+  s.iext = mk(1.0f / ext.x, 1.0f / ext.y, 1.0f / ext.z);
   const vcr_params& p = ctx->params;
   s.ph.g = p.phase_g;
   s.ph.opg2 = p.phase_one_plus_g2;

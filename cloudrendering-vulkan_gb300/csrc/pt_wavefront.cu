@@ -352,7 +352,7 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
           ++lookups;
           if (mode == kScatter) {
             float xi = rng_next(rng);
-            if (xi < rho / tr.m) {  // real collision: start the NEE ray
+            if (xi * tr.m < rho) {  // real collision (xi < rho / m): start the NEE ray
               pos = p;
               ++events;
               const bool training = (pid & kTrainPath) != 0u;

@@ -65,7 +65,7 @@ __device__ __forceinline__ bool free_flight(const GridView& g, const SceneView& 
     }
     float rho = density_at(g, s, along(o, d, tr.t));
     ++lookups;
-    if (rng_next(rng) < rho / tr.m) {
+    if (rng_next(rng) * tr.m < rho) {  // xi < rho / m without the division
       t = tr.t;
       return true;
     }

@@ -36,6 +36,7 @@ struct SceneView {
   float k_sigma;    // ds / bs: sigma_t = k_sigma * density
   f3 cell;          // world size of one majorant cell (8 voxels per axis)
   f3 icell;         // 1 / cell per axis
+  f3 iext;          // 1 / (b1 - b0) per axis
   Phase ph;
   float albedo;
   float light;      // sun irradiance
@@ -128,9 +129,12 @@ __device__ __forceinline__ float trilinear(const GridView& g, f3 nrm) {
   return fmaf(tz, c1 - c0, c0);
 }
 
+// Normalised coordinates (p - b0) / (b1 - b0) as in sampleCloud
+// (PathTracer.comp:117), by multiplication with the box's reciprocal extent
+// (a GLSL division may be evaluated that way, within 2.5 ulp).
 __device__ __forceinline__ float density_at(const GridView& g, const SceneView& s, f3 p) {
-  f3 ext = s.b1 - s.b0;
-  return trilinear(g, div(p - s.b0, ext));
+  const f3 q = p - s.b0;
+  return trilinear(g, mk(q.x * s.iext.x, q.y * s.iext.y, q.z * s.iext.z));
 }
 
 #endif  // __CUDACC__

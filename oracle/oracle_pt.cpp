@@ -109,7 +109,11 @@ float trilinear(const float* tex, const int n[3], V3 nrm) {
 }
 
 // sampleCloud (PathTracer.comp:115-119)
-float density(const Scene& s, V3 p) { return trilinear(s.g->tex.data(), s.g->n, vdiv(sub(p, s.b0), sub(s.b1, s.b0))); }
+// normalised coordinates (p - b0) / (b1 - b0), by the reciprocal extent
+float density(const Scene& s, V3 p) {
+  V3 q = sub(p, s.b0);
+  return trilinear(s.g->tex.data(), s.g->n, v3(q.x * s.iext.x, q.y * s.iext.y, q.z * s.iext.z));
+}
 
 // slab test, intersectCloud (PathTracer.comp:154-184)
 bool slab(V3 pos, V3 dir, V3 b0, V3 b1, float& tmin, float& tmax) {
@@ -397,7 +401,7 @@ V3 trace_path(const Scene& s, const vcr_camera& cam, int x, int y, Rng& rng, Cou
       float rho = density(s, p);
       ++c.lookups;
       float xi = rng.next();
-      if (xi < rho / tr.m) {
+      if (xi * tr.m < rho) {
         hit = true;
         break;
       }
@@ -449,6 +453,7 @@ Scene make_scene(const Grid* g, const vcr_cloud& cl, const vcr_params& p, const 
   const float cv = (float)(8 << level);  // voxels per majorant cell
   s.cell = v3((ext.x / (float)g->n[0]) * cv, (ext.y / (float)g->n[1]) * cv, (ext.z / (float)g->n[2]) * cv);
   s.icell = v3(1.0f / s.cell.x, 1.0f / s.cell.y, 1.0f / s.cell.z);
+  s.iext = v3(1.0f / ext.x, 1.0f / ext.y, 1.0f / ext.z);
   s.maj = g->lv[level].data();
   for (int a = 0; a < 3; ++a) s.mnb[a] = g->lnb[level][a];
   s.g_ = p.phase_g;

@@ -34,6 +34,7 @@ struct Scene {
   float max_ext, ds, bs, k;
   V3 cell;
   V3 icell;  // 1 / cell
+  V3 iext;   // 1 / (b1 - b0)
   float g_, opg2, omg2, o2g;  // Parameters (UniformBuffers.h:80-112)
   bool iso;
   float albedo, light;
@@ -91,7 +92,7 @@ inline bool free_flight(const Scene& s, V3 o, V3 d, Rng& rng, float& t, Counts& 
     }
     float rho = density(s, along(o, d, tr.t));
     ++c.lookups;
-    if (rng.next() < rho / tr.m) {
+    if (rng.next() * tr.m < rho) {
       t = tr.t;
       return true;
     }
