@@ -418,7 +418,7 @@ __global__ void __launch_bounds__(kGatherThreads) ppb_gather_kernel(GridView g, 
       active = e.y;
     }
   }
-  if (valid) write_result(pv, sum, pix, L, false);
+  if (valid) write_result(pv, sum, pix, L);
   flush_counters(cnt, valid ? 1ull : 0ull, lookups, 0, cells);
 }
 

@@ -96,22 +96,20 @@ __device__ __forceinline__ void flush_counters(Counters c, unsigned long long pa
   }
 }
 
-__device__ __forceinline__ void write_result(const PassView& pv, double* __restrict__ sum, uint32_t pix, f3 L,
-                                             bool atomic) {
+// Adds a sample to the pixel's FP64 sums.  The adds are reductions whose
+// result is not read back, so the lane does not wait for the old value; with
+// one sample of a pixel per pass they give the same sums as a load-add-store.
+__device__ __forceinline__ void write_result(const PassView& pv, double* __restrict__ sum, uint32_t pix, f3 L) {
   double* o = sum + 3 * (size_t)pix;
   if (pv.flags & VCR_PASS_NO_ACCUMULATE) {
     // only valid with spp == 1 (checked on the host)
     o[0] = L.x;
     o[1] = L.y;
     o[2] = L.z;
-  } else if (atomic) {
+  } else {
     atomicAdd(o + 0, (double)L.x);
     atomicAdd(o + 1, (double)L.y);
     atomicAdd(o + 2, (double)L.z);
-  } else {
-    o[0] += (double)L.x;
-    o[1] += (double)L.y;
-    o[2] += (double)L.z;
   }
 }
 

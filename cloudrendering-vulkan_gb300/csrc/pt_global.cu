@@ -103,7 +103,7 @@ __global__ void __launch_bounds__(256) pt_global_kernel(GridView g, SceneView s,
       ev_total += events;
       look_total += lookups;
     }
-    write_result(pv, sum, pix, Lsum, false);
+    write_result(pv, sum, pix, Lsum);
     if (stats) {
       uint32_t* st = stats + 4 * (size_t)pix;
       st[0] = ev_total;

@@ -82,6 +82,17 @@ __device__ bool stage_to_smem(void* dst, const void* src, uint32_t bytes, uint64
 
 enum : uint32_t { kIdle = 0, kScatter = 1, kNee = 2 };
 
+// Adds one path's count to a lane's 32-bit total; a total that could pass
+// 2^31 goes to the 64-bit launch counter first (a path adds < 2^27, the
+// work cap, so this is rare and never wraps).
+__device__ __forceinline__ void tally(unsigned long long* dst, uint32_t& acc, uint32_t add) {
+  if (acc + add >= 0x80000000u) {
+    atomicAdd(dst, (unsigned long long)acc);
+    acc = 0;
+  }
+  acc += add;
+}
+
 // Rarely-taken bodies live out of line: the persistent loop then stays small
 // enough for the instruction cache (a fully inlined loop stalled on
 // instruction fetch more than on memory).  They take and return values, not
@@ -225,12 +236,11 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
   bool exhausted = false, flying = false, need_init = false;
   float tau = 0.0f;
   uint32_t pid = 0, pix = 0, events = 0, lookups = 0, cells = 0;
-  unsigned long long n_paths = 0, n_look = 0, n_ev = 0, n_cells = 0;
+  uint32_t n_paths = 0, n_look = 0, n_ev = 0, n_cells = 0;  // this lane's totals (see tally)
   Rng rng{0u, 0u};
-  f3 pos = mk(0.f, 0.f, 0.f), dir = pos, L = pos, idir = pos;
-  float beta = 1.0f, T = 1.0f, phase = 0.0f;
+  f3 pos = mk(0.f, 0.f, 0.f), dir = pos, L = pos;
+  float beta = 1.0f, T = 1.0f;
   Track tr;
-  const bool atomic = pv.spp > 1;
 
   while (true) {
     // ---- warp-aggregated refill of idle lanes ---------------------------
@@ -267,10 +277,9 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
           ++n_paths;
           if (begin(start_path(bv.cam, s, (int)cx, (int)cy), pos, dir, L)) {
             mode = kScatter;
-            idir = dir;
             need_init = true;
           } else {
-            write_result(pv, sum, pix, L, atomic);
+            write_result(pv, sum, pix, L);
           }
         } else if (id < ts.paths) {  // training path from a uniformly drawn pixel of the crop
           rng = rng_pcg(pv.seed ^ kNrcTrainSalt, id, pass);
@@ -284,7 +293,6 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
           ++n_paths;
           if (begin(start_path(cam, s, (int)(pv.x0 + pp % pv.cw), (int)(pv.y0 + pp / pv.cw)), pos, dir, L)) {
             mode = kScatter;
-            idir = dir;
             need_init = true;
           }
         } else {
@@ -302,10 +310,9 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
           ++n_paths;
           if (begin(start_path(cam, s, x, y), pos, dir, L)) {
             mode = kScatter;
-            idir = dir;
             need_init = true;
           } else {
-            write_result(pv, sum, pix, L, atomic);
+            write_result(pv, sum, pix, L);
             if (stats && sp == 0) {
               uint32_t* st = stats + 4 * (size_t)pix;
               st[0] = 0; st[1] = 0; st[2] = pv.pass; st[3] = 0;
@@ -317,8 +324,9 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
     if (__all_sync(0xffffffffu, exhausted && mode == kIdle)) break;
 
     // ---- the one DDA set-up site (camera ray, NEE ray, scattered ray) ------
-    if (need_init) {
-      track_init(tr, g, s, maj, pos, idir, cells);
+    const f3 lsun = kBatch ? -s_views[pid].sun : lsun0;
+    if (need_init) {  // a NEE ray runs towards the sun, a scattering ray along dir
+      track_init(tr, g, s, maj, pos, mode == kNee ? lsun : dir, cells);
       need_init = false;
     }
     __syncwarp();
@@ -334,7 +342,6 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
     }
     __syncwarp();
     // ---- at most one density lookup (the candidate lanes together) ---------
-    const f3 lsun = kBatch ? -s_views[pid].sun : lsun0;
     f3 p = pos;
     float rho = 0.0f;
     if (r == kCandidate) {
@@ -344,10 +351,13 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
     }
     __syncwarp();
     // ---- collision, escape and path bookkeeping -----------------------------
+    // Decisions first; the two costly continuations (a new scattering
+    // direction, a finished path) then run as converged groups below.
+    bool want_dir = false, finish = false, escaped = false;
     if (act) {
       if (r != kPending) {
         flying = false;
-        bool nee_done = false, finish = false;
+        bool nee_done = false;
         if (r == kCandidate) {
           ++lookups;
           if (mode == kScatter) {
@@ -374,10 +384,8 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
                 }
               } else {
                 beta = beta * s.albedo;
-                phase = hg_pdf(s.ph, dot(-dir, -lsun));
                 T = 1.0f;
                 mode = kNee;
-                idir = lsun;
                 need_init = true;
               }
             }
@@ -393,12 +401,13 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
             }
           }
         } else if (mode == kScatter) {
-          L = L + escape_radiance(s, dir) * beta;
+          escaped = true;
           finish = true;
         } else {
           nee_done = true;
         }
         if (nee_done) {
+          const float phase = hg_pdf(s.ph, dot(-dir, -lsun));
           float c = ((s.light * phase) * T) * beta;
           L = L + mk(c, c, c);
           if (s.max_events && events >= s.max_events) {
@@ -407,39 +416,44 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
                      !roulette_survives(rng, ts.survival, beta)) {
             finish = true;  // past the recorded vertices: Russian roulette
           } else {
-            DirRng nd = sample_direction(s.ph, dir, rng);
-            dir = nd.d;
-            rng = nd.r;
-            mode = kScatter;
-            idir = dir;
-            need_init = true;
+            want_dir = true;
           }
         }
-        if (lookups + cells > kPathWorkCap) finish = true;  // runaway guard (non-finite input)
-        if (finish && (pid & kTrainPath)) {
-          finish_training(ts, pix, L);
-          n_look += lookups;
-          n_ev += events;
-          n_cells += cells;
-          mode = kIdle;
-          need_init = false;
-        } else if (finish) {
-          write_result(pv, sum, pix, L, atomic);
-          if (stats && (pid % pv.spp) == 0) {
-            uint32_t* st = stats + 4 * (size_t)pix;
-            st[0] = events; st[1] = lookups; st[2] = pv.pass; st[3] = cells;
-          }
-          n_look += lookups;
-          n_ev += events;
-          n_cells += cells;
-          mode = kIdle;
-          need_init = false;
+        if (lookups + cells > kPathWorkCap) {  // runaway guard (non-finite input)
+          finish = true;
+          want_dir = false;
         }
       }
     }
     __syncwarp();
+    if (want_dir) {
+      DirRng nd = sample_direction(s.ph, dir, rng);
+      dir = nd.d;
+      rng = nd.r;
+      mode = kScatter;
+      need_init = true;
+    }
+    __syncwarp();
+    if (finish) {
+      if (escaped) L = L + escape_radiance(s, dir) * beta;
+      if (pid & kTrainPath) {
+        finish_training(ts, pix, L);
+      } else {
+        write_result(pv, sum, pix, L);
+        if (stats && (pid % pv.spp) == 0) {
+          uint32_t* st = stats + 4 * (size_t)pix;
+          st[0] = events; st[1] = lookups; st[2] = pv.pass; st[3] = cells;
+        }
+      }
+      tally(cnt.c + 1, n_look, lookups);
+      tally(cnt.c + 2, n_ev, events);
+      tally(cnt.c + 3, n_cells, cells);
+      mode = kIdle;
+      need_init = false;
+    }
+    __syncwarp();
   }
-  flush_counters(cnt, n_paths, n_look, n_ev, n_cells);
+  flush_counters(cnt, n_paths, n_look, n_ev, n_cells);  // widened to 64 bits
 }
 
 constexpr uint32_t kMaxStagedBytes = 96u * 1024u;

@@ -144,28 +144,23 @@ __device__ __forceinline__ float density_at(const GridView& g, const SceneView& 
 // Ties between axes advance x before y before z.
 // ---------------------------------------------------------------------------
 struct Dda {
-  int c[3];      // current cell
-  int step[3];
+  int c[3];       // current cell
   float tmax[3];  // ray t of the next boundary per axis
-  float tdel[3];
+  float tdel[3];  // t per cell along the axis, signed like the step (+inf: the axis never advances)
 };
 
 // The set-up multiplies by the reciprocal direction `inv` = 1/d (computed
 // once per ray and shared with the slab test) and by the reciprocal cell
 // size `ics`, so a ray's DDA costs three divisions in all; the sign test is
 // on d itself because 1/(+-0) is +-inf.
-VCR_HD void dda_axis_init(float o, float d, float inv, float b0, float cs, int c, int& step, float& tmax,
-                          float& tdel) {
+VCR_HD void dda_axis_init(float o, float d, float inv, float b0, float cs, int c, float& tmax, float& tdel) {
   if (d > 0.0f) {
-    step = 1;
     tmax = ((b0 + (float)(c + 1) * cs) - o) * inv;
     tdel = cs * inv;
   } else if (d < 0.0f) {
-    step = -1;
     tmax = ((b0 + (float)c * cs) - o) * inv;
-    tdel = -(cs * inv);
+    tdel = cs * inv;  // negative: the axis steps down
   } else {
-    step = 0;
     tmax = INFINITY;
     tdel = INFINITY;
   }
@@ -180,28 +175,29 @@ VCR_HD void dda_init(Dda& d, f3 o, f3 dir, f3 inv, f3 b0, f3 cs, f3 ics, const i
   d.c[0] = cell_of(o.x, b0.x, ics.x, nc[0]);
   d.c[1] = cell_of(o.y, b0.y, ics.y, nc[1]);
   d.c[2] = cell_of(o.z, b0.z, ics.z, nc[2]);
-  dda_axis_init(o.x, dir.x, inv.x, b0.x, cs.x, d.c[0], d.step[0], d.tmax[0], d.tdel[0]);
-  dda_axis_init(o.y, dir.y, inv.y, b0.y, cs.y, d.c[1], d.step[1], d.tmax[1], d.tdel[1]);
-  dda_axis_init(o.z, dir.z, inv.z, b0.z, cs.z, d.c[2], d.step[2], d.tmax[2], d.tdel[2]);
+  dda_axis_init(o.x, dir.x, inv.x, b0.x, cs.x, d.c[0], d.tmax[0], d.tdel[0]);
+  dda_axis_init(o.y, dir.y, inv.y, b0.y, cs.y, d.c[1], d.tmax[1], d.tdel[1]);
+  dda_axis_init(o.z, dir.z, inv.z, b0.z, cs.z, d.c[2], d.tmax[2], d.tdel[2]);
 }
 
 VCR_HD float dda_cell_exit(const Dda& d) { return fminf(fminf(d.tmax[0], d.tmax[1]), d.tmax[2]); }
 
-// Advance to the next cell; false when it leaves the grid.
+// Advance to the next cell; false when it leaves the grid.  The step is the
+// sign of tdel and tmax grows by |tdel| (the cell's t extent).
 // (Each axis is spelled out so the state stays in registers.)
 VCR_HD bool dda_advance(Dda& d, const int nc[3]) {
   if (d.tmax[0] <= d.tmax[1] && d.tmax[0] <= d.tmax[2]) {
-    d.c[0] += d.step[0];
-    d.tmax[0] = d.tmax[0] + d.tdel[0];
+    d.c[0] += d.tdel[0] < 0.0f ? -1 : 1;
+    d.tmax[0] = d.tmax[0] + fabsf(d.tdel[0]);
     return d.c[0] >= 0 && d.c[0] < nc[0];
   }
   if (d.tmax[1] <= d.tmax[2]) {
-    d.c[1] += d.step[1];
-    d.tmax[1] = d.tmax[1] + d.tdel[1];
+    d.c[1] += d.tdel[1] < 0.0f ? -1 : 1;
+    d.tmax[1] = d.tmax[1] + fabsf(d.tdel[1]);
     return d.c[1] >= 0 && d.c[1] < nc[1];
   }
-  d.c[2] += d.step[2];
-  d.tmax[2] = d.tmax[2] + d.tdel[2];
+  d.c[2] += d.tdel[2] < 0.0f ? -1 : 1;
+  d.tmax[2] = d.tmax[2] + fabsf(d.tdel[2]);
   return d.c[2] >= 0 && d.c[2] < nc[2];
 }
 

@@ -113,7 +113,7 @@ def test_batch_autotune_picks_a_candidate_and_clears(cuda):
         _setup(ctx, sc)
         ctx.batch_setup(_views())
         t = ctx.batch_autotune(seed=1, spp=2)
-        assert t["majorant_level"] in (0, 1, 2, 3) and t["dda_steps"] in (2, 8) and t["block_threads"] in (128, 256)
+        assert t["majorant_level"] in (0, 1, 2, 3) and t["dda_steps"] in (2, 8, 16) and t["block_threads"] in (128, 256)
         assert ctx.get_tuning() == t
         info = ctx.batch_info()
         assert info["passes"] == 0 and info["samples"] == 0
