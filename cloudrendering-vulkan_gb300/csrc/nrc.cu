@@ -6,12 +6,14 @@
 // Tensor cores, BF16 operands, FP32 accumulation.  Queries: a
 // register-resident forward (mma.sync m16n8k16, nrc_mma.cuh) — each warp
 // runs 16-sample tiles whose activations stay in the MMA fragments, the CTA
-// shares only the transposed BF16 weights.  Training: one CTA per SM holds
-// the BF16 weights, the six activation tiles of a 64-sample tile, the
-// gradient ping-pong and an FP32 weight-gradient accumulator in padded
-// shared memory (227 KB); the warp-level matrix API (16x16x16) runs the
-// forward, the relative-L2 loss gradient, the backward and X_l^T dY_l over
-// the tile; one atomic add per weight per CTA flushes the gradient.  Adam
+// shares only the transposed BF16 weights.  Training: one 8-warp CTA per
+// SM holds the BF16 weights and, for a 128-sample tile, the six activation
+// tiles and the gradient ping-pong in padded shared memory (202 KB); the
+// warp-level matrix API (16x16x16) runs the forward, the relative-L2 loss
+// gradient, the backward and X_l^T dY_l over the tile.  The weight gradient
+// stays in the warps' accumulator fragments (each warp owns two 16x16 tiles
+// of every layer) across all the CTA's tiles; one atomic add per weight per
+// CTA flushes it at the end.  Adam
 // runs on FP32 master weights and refreshes the BF16 copies (training
 // weights, and the moving average the queries use).
 #include <mma.h>
@@ -27,19 +29,19 @@ namespace vcr {
 using namespace nvcuda;
 using bf16 = __nv_bfloat16;
 
-constexpr int kNrcThreads = 128;
+// Training CTA: 8 warps, 16 records each, one 128-record tile at a time.
+constexpr int kTrainWarps = 8;
+constexpr int kTrainThreads = kTrainWarps * 32;
+constexpr int kTrainTile = kTrainWarps * 16;
 
 // Shared-memory row strides are padded off powers of two, so the 16 rows of
 // a matrix fragment load or store fall on different banks.
 constexpr int kLdX = kNrcWidth + 8;  // BF16 activation / gradient tiles: 144-byte rows
-constexpr int kLdY = kNrcWidth + 4;  // FP32 staging: 272-byte rows
+constexpr int kLdS = 16 + 4;         // FP32 staging of one 16x16 accumulator: 80-byte rows
 __host__ __device__ constexpr int ldw(int l) { return nrc_layer_cols(l) + 8; }  // BF16 weights of layer l
-__host__ __device__ constexpr int ldg(int l) { return nrc_layer_cols(l) + 4; }  // FP32 gradient of layer l
 __host__ __device__ constexpr int woff(int l) { return l * kNrcWidth * (kNrcWidth + 8); }
-__host__ __device__ constexpr int goff(int l) { return l * kNrcWidth * (kNrcWidth + 4); }
 constexpr int kWs = woff(kNrcLayers - 1) + kNrcWidth * (kNrcOutPad + 8);  // BF16 weights in shared memory
-constexpr int kGs = goff(kNrcLayers - 1) + kNrcWidth * (kNrcOutPad + 4);  // FP32 gradient in shared memory
-constexpr int kTileX = kNrcTile * kLdX;                                    // one activation tile
+constexpr int kTileX = kTrainTile * kLdX;                                  // one activation tile
 
 struct NrcView {
   const bf16* wb;   // training weights
@@ -68,46 +70,37 @@ __device__ __forceinline__ void encode_rows(const NrcRecord* __restrict__ recs, 
     *reinterpret_cast<__nv_bfloat162*>(row + i) = __floats2bfloat162_rn(e[i], e[i + 1]);
 }
 
-// rows [16w,16w+16) of Y = X_l W_l, fp32 into the warp's staging block
-__device__ __forceinline__ void layer_forward(const bf16* X, const bf16* W, int l, float* Yw, int warp) {
+// Layer l for the warp's rows [16w, 16w + 16): Y = X_l W_l, 16 columns at a
+// time through the warp's 16x16 FP32 staging block S.  Hidden layers store
+// bf16(relu(Y)) into Xn; the output layer (16 columns) is left in S.
+__device__ __forceinline__ void forward_layer(const bf16* Xl, const bf16* Wl, int l, bf16* Xn, float* S, int warp,
+                                              int lane) {
   const int cols = nrc_layer_cols(l), ld = ldw(l);
   wmma::fragment<wmma::matrix_a, 16, 16, 16, bf16, wmma::row_major> a[4];
 #pragma unroll
-  for (int kt = 0; kt < 4; ++kt) wmma::load_matrix_sync(a[kt], X + warp * 16 * kLdX + kt * 16, kLdX);
+  for (int kt = 0; kt < 4; ++kt) wmma::load_matrix_sync(a[kt], Xl + warp * 16 * kLdX + kt * 16, kLdX);
   for (int nt = 0; nt < cols / 16; ++nt) {
     wmma::fragment<wmma::accumulator, 16, 16, 16, float> acc;
     wmma::fill_fragment(acc, 0.0f);
 #pragma unroll
     for (int kt = 0; kt < 4; ++kt) {
       wmma::fragment<wmma::matrix_b, 16, 16, 16, bf16, wmma::row_major> b;
-      wmma::load_matrix_sync(b, W + kt * 16 * ld + nt * 16, ld);
+      wmma::load_matrix_sync(b, Wl + kt * 16 * ld + nt * 16, ld);
       wmma::mma_sync(acc, a[kt], b, acc);
     }
-    wmma::store_matrix_sync(Yw + nt * 16, acc, kLdY, wmma::mem_row_major);
-  }
-}
-
-// rows of the warp: Xn = bf16(relu(Y)), two columns per step
-__device__ __forceinline__ void relu_store(const float* Yw, bf16* Xn, int warp, int lane) {
-#pragma unroll 4
-  for (int e = lane * 2; e < 16 * kNrcWidth; e += 64) {
-    int r = e / kNrcWidth, c = e - r * kNrcWidth;
-    float2 y = *reinterpret_cast<const float2*>(Yw + r * kLdY + c);
-    *reinterpret_cast<__nv_bfloat162*>(Xn + (warp * 16 + r) * kLdX + c) =
-        __floats2bfloat162_rn(fmaxf(y.x, 0.0f), fmaxf(y.y, 0.0f));
-  }
-}
-
-// Full forward of the tile's rows owned by this warp; the output rows are
-// left in Yw (fp32, cols 0..15).  keep: activations h_0..h_5 stay in
-// X[0..5] (training needs them); otherwise two tiles alternate.
-__device__ __forceinline__ void mlp_forward(const bf16* W, bf16* X, float* Yw, int warp, int lane, bool keep) {
-  for (int l = 0; l < kNrcLayers; ++l) {
-    const bf16* Xl = X + (keep ? l : (l & 1)) * kTileX;
-    layer_forward(Xl, W + woff(l), l, Yw, warp);
+    wmma::store_matrix_sync(S, acc, kLdS, wmma::mem_row_major);
     __syncwarp();
-    if (l < kNrcHidden) relu_store(Yw, X + (keep ? l + 1 : ((l + 1) & 1)) * kTileX, warp, lane);
-    __syncwarp();
+    if (l < kNrcHidden) {  // lane: row lane/2, 8 columns
+      const int r = lane >> 1, c0 = (lane & 1) * 8;
+      const float4 y0 = *reinterpret_cast<const float4*>(S + r * kLdS + c0);
+      const float4 y1 = *reinterpret_cast<const float4*>(S + r * kLdS + c0 + 4);
+      __nv_bfloat162* d = reinterpret_cast<__nv_bfloat162*>(Xn + (warp * 16 + r) * kLdX + nt * 16 + c0);
+      d[0] = __floats2bfloat162_rn(fmaxf(y0.x, 0.0f), fmaxf(y0.y, 0.0f));
+      d[1] = __floats2bfloat162_rn(fmaxf(y0.z, 0.0f), fmaxf(y0.w, 0.0f));
+      d[2] = __floats2bfloat162_rn(fmaxf(y1.x, 0.0f), fmaxf(y1.y, 0.0f));
+      d[3] = __floats2bfloat162_rn(fmaxf(y1.z, 0.0f), fmaxf(y1.w, 0.0f));
+      __syncwarp();
+    }
   }
 }
 
@@ -181,20 +174,28 @@ __global__ void __launch_bounds__(kInferThreads, 3) nrc_infer_kernel(NrcView v, 
 // ---------------------------------------------------------------------------
 // training: relative L2 loss sum_c (y - t)^2 / (sg(y)^2 + 0.01) / (3 B)
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kNrcThreads) nrc_train_kernel(NrcView v, const NrcRecord* __restrict__ recs,
-                                                                const uint32_t* __restrict__ count_ptr,
-                                                                uint32_t capacity, uint32_t first_rec,
-                                                                float* __restrict__ grad, float* __restrict__ loss) {
+__global__ void __launch_bounds__(kTrainThreads, 1) nrc_train_kernel(NrcView v, const NrcRecord* __restrict__ recs,
+                                                                     const uint32_t* __restrict__ count_ptr,
+                                                                     uint32_t capacity, uint32_t first_rec,
+                                                                     float* __restrict__ grad, float* __restrict__ loss) {
   extern __shared__ __align__(128) unsigned char smem[];
   bf16* W = reinterpret_cast<bf16*>(smem);
-  bf16* X = W + kWs;                                        // h_0 .. h_5
-  bf16* D = X + kNrcLayers * kTileX;                         // dY ping-pong: 2 tiles
-  float* Y = reinterpret_cast<float*>(D + 2 * kTileX);       // 4 x 16 x kLdY
-  float* G = Y + 4 * 16 * kLdY;                              // dW accumulator [kGs]
+  bf16* X = W + kWs;                                     // h_0 .. h_5 of the tile
+  bf16* D = X + kNrcLayers * kTileX;                     // dY ping-pong: 2 tiles
+  float* S = reinterpret_cast<float*>(D + 2 * kTileX);  // per warp: 16 x kLdS
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  float* Yw = Y + warp * 16 * kLdY;
+  float* Sw = S + warp * 16 * kLdS;
   load_weights(v.wb, W);
-  for (int i = threadIdx.x; i < kGs; i += blockDim.x) G[i] = 0.0f;
+  // The CTA's weight gradient stays in registers across its tiles: warp w
+  // owns tiles 2w and 2w+1 (row block t/4, column block t%4) of each 64x64
+  // hidden-layer gradient, and warps 0-3 the row blocks of the 64x16 output
+  // layer's.
+  wmma::fragment<wmma::accumulator, 16, 16, 16, float> dw[kNrcLayers][2];
+#pragma unroll
+  for (int l = 0; l < kNrcLayers; ++l) {
+    wmma::fill_fragment(dw[l][0], 0.0f);
+    wmma::fill_fragment(dw[l][1], 0.0f);
+  }
   __syncthreads();
   // records [first_rec, first_rec + capacity) of the *count_ptr written
   const uint32_t total = *count_ptr;
@@ -202,12 +203,13 @@ __global__ void __launch_bounds__(kNrcThreads) nrc_train_kernel(NrcView v, const
   recs += first_rec;
   const float inv_n = 1.0f / (3.0f * (float)max(count, 1u));
   float loss_local = 0.0f;
-  for (uint32_t first = blockIdx.x * kNrcTile; first < count; first += gridDim.x * kNrcTile) {
+  for (uint32_t first = blockIdx.x * kTrainTile; first < count; first += gridDim.x * kTrainTile) {
     encode_rows(recs, first, count, v, X, warp, lane);
     __syncwarp();
-    mlp_forward(W, X, Yw, warp, lane, true);
+#pragma unroll 1
+    for (int l = 0; l < kNrcLayers; ++l)
+      forward_layer(X + l * kTileX, W + woff(l), l, X + (l + 1 < kNrcLayers ? l + 1 : l) * kTileX, Sw, warp, lane);
     // output gradient (cols 0..2), zero elsewhere and for padding rows
-    bf16* d5 = D;  // dY_5 in buffer 0 (cols 0..15 used)
     for (int e = lane; e < 16 * kNrcOutPad; e += 32) {
       int r = e / kNrcOutPad, c = e - r * kNrcOutPad;
       uint32_t idx = first + (uint32_t)(warp * 16 + r);
@@ -215,41 +217,41 @@ __global__ void __launch_bounds__(kNrcThreads) nrc_train_kernel(NrcView v, const
       if (c < kNrcOut && idx < count) {
         const NrcRecord& rec = recs[idx];
         float t = c == 0 ? rec.w0 : (c == 1 ? rec.w1 : rec.w2);
-        float y = Yw[r * kLdY + c];
+        float y = Sw[r * kLdS + c];
         float den = y * y + 0.01f;
         float diff = y - t;
         loss_local += (diff * diff / den) * inv_n;
         gval = (2.0f * diff / den) * inv_n;
       }
-      d5[(warp * 16 + r) * kLdX + c] = __float2bfloat16_rn(gval);
+      D[(warp * 16 + r) * kLdX + c] = __float2bfloat16_rn(gval);  // dY_5 in buffer 0
     }
-    __syncthreads();
-    // backward through layers 5..0
+    // backward through layers 5..0 (unrolled: the gradient fragments are indexed by layer)
+#pragma unroll
     for (int l = kNrcLayers - 1; l >= 0; --l) {
       const int cols = nrc_layer_cols(l);
       const bf16* Xl = X + l * kTileX;
-      bf16* Dl = D + (l & 1 ? 0 : 1) * kTileX;  // l = 5 -> buffer 0
-      if (l == kNrcLayers - 1) Dl = D;
-      // dW_l += X_l^T dY_l : tiles (mt over 64 inputs, nt over cols/16), K = 64 samples
-      const int ntiles = 4 * (cols / 16);
-      for (int tI = warp; tI < ntiles; tI += kNrcThreads / 32) {
-        int mt = tI / (cols / 16), nt = tI - mt * (cols / 16);
-        float* g = G + goff(l) + mt * 16 * ldg(l) + nt * 16;
-        wmma::fragment<wmma::accumulator, 16, 16, 16, float> acc;
-        wmma::load_matrix_sync(acc, g, ldg(l), wmma::mem_row_major);
+      bf16* Dl = D + ((kNrcLayers - 1 - l) & 1) * kTileX;  // dY_5 in buffer 0, dY_4 in 1, ...
+      __syncthreads();                                     // dY_l complete for every row
+      // dW_l += X_l^T dY_l over the tile's rows
 #pragma unroll
-        for (int kt = 0; kt < 4; ++kt) {
-          wmma::fragment<wmma::matrix_a, 16, 16, 16, bf16, wmma::col_major> a;  // X_l^T
-          wmma::load_matrix_sync(a, Xl + kt * 16 * kLdX + mt * 16, kLdX);
-          wmma::fragment<wmma::matrix_b, 16, 16, 16, bf16, wmma::row_major> b;  // dY_l
-          wmma::load_matrix_sync(b, Dl + kt * 16 * kLdX + nt * 16, kLdX);
-          wmma::mma_sync(acc, a, b, acc);
+      for (int j = 0; j < 2; ++j) {
+        const bool own = l < kNrcHidden || (j == 0 && warp < 4);
+        if (own) {
+          const int t = l < kNrcHidden ? 2 * warp + j : 4 * warp;
+          const int mt = t >> 2, nt = t & 3;
+#pragma unroll 4
+          for (int kt = 0; kt < kTrainTile / 16; ++kt) {
+            wmma::fragment<wmma::matrix_a, 16, 16, 16, bf16, wmma::col_major> a;  // X_l^T
+            wmma::load_matrix_sync(a, Xl + kt * 16 * kLdX + mt * 16, kLdX);
+            wmma::fragment<wmma::matrix_b, 16, 16, 16, bf16, wmma::row_major> b;  // dY_l
+            wmma::load_matrix_sync(b, Dl + kt * 16 * kLdX + nt * 16, kLdX);
+            wmma::mma_sync(dw[l][j], a, b, dw[l][j]);
+          }
         }
-        wmma::store_matrix_sync(g, acc, ldg(l), wmma::mem_row_major);
       }
       if (l > 0) {
-        // dY_{l-1} = (dY_l W_l^T) * (h_l > 0), rows of this warp
-        bf16* Dn = (Dl == D) ? D + kTileX : D;
+        // dY_{l-1} = (dY_l W_l^T) * (h_l > 0) for this warp's rows, 16 columns at a time
+        bf16* Dn = D + ((kNrcLayers - l) & 1) * kTileX;
         const bf16* Wl = W + woff(l);
         for (int nt = 0; nt < 4; ++nt) {
           wmma::fragment<wmma::accumulator, 16, 16, 16, float> acc;
@@ -261,31 +263,45 @@ __global__ void __launch_bounds__(kNrcThreads) nrc_train_kernel(NrcView v, const
             wmma::load_matrix_sync(b, Wl + nt * 16 * ldw(l) + kt * 16, ldw(l));
             wmma::mma_sync(acc, a, b, acc);
           }
-          wmma::store_matrix_sync(Yw + nt * 16, acc, kLdY, wmma::mem_row_major);
+          wmma::store_matrix_sync(Sw, acc, kLdS, wmma::mem_row_major);
+          __syncwarp();
+          const int r = lane >> 1, c0 = (lane & 1) * 8, row = warp * 16 + r;
+          const float* y = Sw + r * kLdS + c0;
+          const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(Xl + row * kLdX + nt * 16 + c0);
+          __nv_bfloat162* d = reinterpret_cast<__nv_bfloat162*>(Dn + row * kLdX + nt * 16 + c0);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const __nv_bfloat162 hq = h[q];
+            const float m0 = __low2float(hq) > 0.0f ? 1.0f : 0.0f, m1 = __high2float(hq) > 0.0f ? 1.0f : 0.0f;
+            d[q] = __floats2bfloat162_rn(y[2 * q] * m0, y[2 * q + 1] * m1);
+          }
+          __syncwarp();
         }
+      }
+    }
+    __syncthreads();  // every warp is done with X_0 before the next tile's encoding
+  }
+  // flush the CTA's gradient ([in][out] layout per layer) and loss
+#pragma unroll
+  for (int l = 0; l < kNrcLayers; ++l) {
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      const bool own = l < kNrcHidden || (j == 0 && warp < 4);
+      if (own) {
+        const int t = l < kNrcHidden ? 2 * warp + j : 4 * warp;
+        const int mt = t >> 2, nt = t & 3, cols = nrc_layer_cols(l);
+        wmma::store_matrix_sync(Sw, dw[l][j], kLdS, wmma::mem_row_major);
         __syncwarp();
-#pragma unroll 4
-        for (int e = lane * 2; e < 16 * kNrcWidth; e += 64) {
-          int r = e / kNrcWidth, c = e - r * kNrcWidth;
-          int row = warp * 16 + r;
-          float2 y = *reinterpret_cast<const float2*>(Yw + r * kLdY + c);
-          __nv_bfloat162 h = *reinterpret_cast<const __nv_bfloat162*>(Xl + row * kLdX + c);
-          float m0 = __low2float(h) > 0.0f ? 1.0f : 0.0f, m1 = __high2float(h) > 0.0f ? 1.0f : 0.0f;
-          *reinterpret_cast<__nv_bfloat162*>(Dn + row * kLdX + c) = __floats2bfloat162_rn(y.x * m0, y.y * m1);
+        const int r = lane >> 1, c0 = (lane & 1) * 8;
+        float* gdst = grad + nrc_layer_offset(l) + (mt * 16 + r) * cols + nt * 16 + c0;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+          const float gv = Sw[r * kLdS + c0 + c];
+          if (gv != 0.0f) atomicAdd(gdst + c, gv);
         }
         __syncwarp();
       }
-      __syncthreads();
     }
-  }
-  // flush the CTA's gradient (padded layout -> [in][out]) and loss
-  for (int i = threadIdx.x; i < kNrcWeightCount; i += blockDim.x) {
-    const int l = i < kNrcHidden * kNrcWidth * kNrcWidth ? i / (kNrcWidth * kNrcWidth) : kNrcHidden;
-    const int cols = nrc_layer_cols(l);
-    const int rel = i - nrc_layer_offset(l);
-    const int row = rel / cols, col = rel - row * cols;
-    float gv = G[goff(l) + row * ldg(l) + col];
-    if (gv != 0.0f) atomicAdd(grad + i, gv);
   }
   for (int o = 16; o > 0; o >>= 1) loss_local += __shfl_xor_sync(0xffffffffu, loss_local, o);
   if (lane == 0) atomicAdd(loss, loss_local);
@@ -331,7 +347,7 @@ __global__ void nrc_to_bf16_kernel(const float* __restrict__ w, bf16* __restrict
 // ---------------------------------------------------------------------------
 static size_t infer_smem() { return (size_t)kWtElems * 2 + kNrcPosLevels * 3 * sizeof(float); }
 static size_t train_smem() {
-  return (size_t)kWs * 2 + (size_t)(kNrcLayers + 2) * kTileX * 2 + (size_t)4 * 16 * kLdY * 4 + (size_t)kGs * 4;
+  return (size_t)kWs * 2 + (size_t)(kNrcLayers + 2) * kTileX * 2 + (size_t)kTrainWarps * 16 * kLdS * 4;
 }
 
 NrcView nrc_view(const vcr_ctx* ctx) {
@@ -428,7 +444,7 @@ vcr_status nrc_accumulate_grad(vcr_ctx* ctx, const NrcRecord* recs, const uint32
   VCR_CUDA(ctx, cudaFuncSetAttribute(nrc_train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)train_smem()));
   VCR_CUDA(ctx, cudaMemsetAsync(st->loss, 0, 8, s));
   int blocks = ctx->sm_count;
-  nrc_train_kernel<<<blocks, kNrcThreads, train_smem(), s>>>(nrc_view(ctx), recs, d_count, capacity, first,
+  nrc_train_kernel<<<blocks, kTrainThreads, train_smem(), s>>>(nrc_view(ctx), recs, d_count, capacity, first,
                                                             st->grad, st->loss);
   VCR_CUDA(ctx, cudaGetLastError());
   return VCR_OK;
