@@ -127,3 +127,23 @@ def test_morton_codes_bit_exact(cuda):
             ctx.morton_codes(dp.data_ptr(), len(p), bb0, bb1, bits, out.data_ptr())
             ctx.synchronize()
             np.testing.assert_array_equal(_from_dev(out), orc.morton(p, bb0, bb1, bits))
+
+
+def test_tests_cpp_fixture_keys_on_the_gpu(cuda):
+    """The reference's only sort fixture (Tests.cpp:113-131: 176 keys in
+    [0, 255], sorted on bits 0..7), from the pinned golden array: the GPU
+    sort's permutation is the stable one."""
+    import os
+    import torch
+    golden = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "sort_fixture_keys.txt")
+    keys = np.loadtxt(golden, dtype=np.uint32)
+    n = len(keys)
+    with vcr.Context() as ctx:
+        dk = _to_dev(keys, cuda)
+        ko = torch.empty(n, dtype=torch.int32, device=cuda)
+        vo = torch.empty(n, dtype=torch.int32, device=cuda)
+        ctx.radix_sort_pairs(dk.data_ptr(), None, ko.data_ptr(), vo.data_ptr(), n, 0, 8)
+        ctx.synchronize()
+    perm = np.argsort(keys, kind="stable").astype(np.uint32)
+    np.testing.assert_array_equal(_from_dev(vo), perm)
+    np.testing.assert_array_equal(_from_dev(ko), keys[perm])
