@@ -12,8 +12,9 @@
 // warp-level matrix API (16x16x16) runs the forward, the relative-L2 loss
 // gradient, the backward and X_l^T dY_l over the tile.  The weight gradient
 // stays in the warps' accumulator fragments (each warp owns two 16x16 tiles
-// of every layer) across all the CTA's tiles; one atomic add per weight per
-// CTA flushes it at the end.  Adam
+// of every layer) across all the CTA's tiles; at the end each CTA stores it
+// into its own slot and a small kernel sums the slots in a fixed order (one
+// atomic add per weight per CTA cost as much as the tiles themselves).  Adam
 // runs on FP32 master weights and refreshes the BF16 copies (training
 // weights, and the moving average the queries use).
 #include <mma.h>
@@ -177,7 +178,7 @@ __global__ void __launch_bounds__(kInferThreads, 3) nrc_infer_kernel(NrcView v, 
 __global__ void __launch_bounds__(kTrainThreads, 1) nrc_train_kernel(NrcView v, const NrcRecord* __restrict__ recs,
                                                                      const uint32_t* __restrict__ count_ptr,
                                                                      uint32_t capacity, uint32_t first_rec,
-                                                                     float* __restrict__ grad, float* __restrict__ loss) {
+                                                                     float* __restrict__ gpart, float* __restrict__ loss) {
   extern __shared__ __align__(128) unsigned char smem[];
   bf16* W = reinterpret_cast<bf16*>(smem);
   bf16* X = W + kWs;                                     // h_0 .. h_5 of the tile
@@ -281,7 +282,10 @@ __global__ void __launch_bounds__(kTrainThreads, 1) nrc_train_kernel(NrcView v, 
     }
     __syncthreads();  // every warp is done with X_0 before the next tile's encoding
   }
-  // flush the CTA's gradient ([in][out] layout per layer) and loss
+  // the CTA's gradient ([in][out] layout per layer) into its own slot of
+  // gpart, every weight written (the owned tiles cover each layer once);
+  // nrc_grad_reduce_kernel sums the slots in a fixed order
+  float* slot = gpart + (size_t)blockIdx.x * kNrcWeightCount;
 #pragma unroll
   for (int l = 0; l < kNrcLayers; ++l) {
 #pragma unroll
@@ -293,18 +297,24 @@ __global__ void __launch_bounds__(kTrainThreads, 1) nrc_train_kernel(NrcView v, 
         wmma::store_matrix_sync(Sw, dw[l][j], kLdS, wmma::mem_row_major);
         __syncwarp();
         const int r = lane >> 1, c0 = (lane & 1) * 8;
-        float* gdst = grad + nrc_layer_offset(l) + (mt * 16 + r) * cols + nt * 16 + c0;
-#pragma unroll
-        for (int c = 0; c < 8; ++c) {
-          const float gv = Sw[r * kLdS + c0 + c];
-          if (gv != 0.0f) atomicAdd(gdst + c, gv);
-        }
+        float4* gdst = reinterpret_cast<float4*>(slot + nrc_layer_offset(l) + (mt * 16 + r) * cols + nt * 16 + c0);
+        gdst[0] = *reinterpret_cast<const float4*>(Sw + r * kLdS + c0);
+        gdst[1] = *reinterpret_cast<const float4*>(Sw + r * kLdS + c0 + 4);
         __syncwarp();
       }
     }
   }
   for (int o = 16; o > 0; o >>= 1) loss_local += __shfl_xor_sync(0xffffffffu, loss_local, o);
   if (lane == 0) atomicAdd(loss, loss_local);
+}
+
+// grad[i] += the launch's per-CTA gradients, summed over the CTAs in order.
+__global__ void nrc_grad_reduce_kernel(const float* __restrict__ gpart, int blocks, float* __restrict__ grad) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= kNrcWeightCount) return;
+  float s = 0.0f;
+  for (int b = 0; b < blocks; ++b) s += gpart[(size_t)b * kNrcWeightCount + i];
+  grad[i] += s;
 }
 
 __global__ void nrc_adam_kernel(float* __restrict__ w, bf16* __restrict__ wb, float* __restrict__ m,
@@ -364,7 +374,7 @@ NrcView nrc_view(const vcr_ctx* ctx) {
 void nrc_free(vcr_ctx* ctx) {
   NrcState* st = ctx->nrc;
   if (!st) return;
-  void* ptrs[] = {st->w, st->wb, st->m, st->v, st->grad, st->ema, st->wbi, st->loss, st->train, st->train_count,
+  void* ptrs[] = {st->w, st->wb, st->m, st->v, st->grad, st->gpart, st->ema, st->wbi, st->loss, st->train, st->train_count,
                   st->query, st->query_count};
   for (void* p : ptrs) cudaFree(p);
   delete st;
@@ -407,6 +417,8 @@ vcr_status nrc_setup(vcr_ctx* ctx, const vcr_nrc_params* p) {
   VCR_ALLOC(st->m, kNrcWeightCount * 4);
   VCR_ALLOC(st->v, kNrcWeightCount * 4);
   VCR_ALLOC(st->grad, kNrcWeightCount * 4);
+  st->gpart_blocks = ctx->sm_count;
+  VCR_ALLOC(st->gpart, (size_t)st->gpart_blocks * kNrcWeightCount * 4);
   VCR_ALLOC(st->loss, 8);
   VCR_ALLOC(st->train, (size_t)st->train_cap * sizeof(NrcRecord));
   if (p->ema_decay > 0.0f) {
@@ -443,9 +455,11 @@ vcr_status nrc_accumulate_grad(vcr_ctx* ctx, const NrcRecord* recs, const uint32
   NrcState* st = ctx->nrc;
   VCR_CUDA(ctx, cudaFuncSetAttribute(nrc_train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)train_smem()));
   VCR_CUDA(ctx, cudaMemsetAsync(st->loss, 0, 8, s));
-  int blocks = ctx->sm_count;
+  const int blocks = st->gpart_blocks;
   nrc_train_kernel<<<blocks, kTrainThreads, train_smem(), s>>>(nrc_view(ctx), recs, d_count, capacity, first,
-                                                            st->grad, st->loss);
+                                                               st->gpart, st->loss);
+  VCR_CUDA(ctx, cudaGetLastError());
+  nrc_grad_reduce_kernel<<<(kNrcWeightCount + 255) / 256, 256, 0, s>>>(st->gpart, blocks, st->grad);
   VCR_CUDA(ctx, cudaGetLastError());
   return VCR_OK;
 }

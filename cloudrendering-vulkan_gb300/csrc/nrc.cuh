@@ -52,6 +52,8 @@ struct NrcState {
   float* m = nullptr;        // Adam first moment
   float* v = nullptr;        // Adam second moment
   float* grad = nullptr;     // gradient accumulator [kNrcWeightCount]
+  float* gpart = nullptr;    // per-CTA gradients of one training launch [gpart_blocks][kNrcWeightCount]
+  int gpart_blocks = 0;
   float* ema = nullptr;      // exponential moving average of w (ema_decay > 0)
   void* wbi = nullptr;       // BF16 copy of ema used for inference (ema_decay > 0)
   float* loss = nullptr;     // [2]: loss sum, sample count of the last step
