@@ -76,20 +76,28 @@ __device__ __forceinline__ void encode_rows(const NrcRecord* __restrict__ recs, 
 // bf16(relu(Y)) into Xn; the output layer (16 columns) is left in S.
 __device__ __forceinline__ void forward_layer(const bf16* Xl, const bf16* Wl, int l, bf16* Xn, float* S, int warp,
                                               int lane) {
-  const int cols = nrc_layer_cols(l), ld = ldw(l);
-  wmma::fragment<wmma::matrix_a, 16, 16, 16, bf16, wmma::row_major> a[4];
+  const int ncols = nrc_layer_cols(l) / 16, ld = ldw(l);
+  // the column blocks' MMA chains interleave (k outer), four independent accumulators
+  wmma::fragment<wmma::accumulator, 16, 16, 16, float> acc[4];
 #pragma unroll
-  for (int kt = 0; kt < 4; ++kt) wmma::load_matrix_sync(a[kt], Xl + warp * 16 * kLdX + kt * 16, kLdX);
-  for (int nt = 0; nt < cols / 16; ++nt) {
-    wmma::fragment<wmma::accumulator, 16, 16, 16, float> acc;
-    wmma::fill_fragment(acc, 0.0f);
+  for (int nt = 0; nt < 4; ++nt) wmma::fill_fragment(acc[nt], 0.0f);
 #pragma unroll
-    for (int kt = 0; kt < 4; ++kt) {
-      wmma::fragment<wmma::matrix_b, 16, 16, 16, bf16, wmma::row_major> b;
-      wmma::load_matrix_sync(b, Wl + kt * 16 * ld + nt * 16, ld);
-      wmma::mma_sync(acc, a[kt], b, acc);
+  for (int kt = 0; kt < 4; ++kt) {
+    wmma::fragment<wmma::matrix_a, 16, 16, 16, bf16, wmma::row_major> a;
+    wmma::load_matrix_sync(a, Xl + warp * 16 * kLdX + kt * 16, kLdX);
+#pragma unroll
+    for (int nt = 0; nt < 4; ++nt) {
+      if (nt < ncols) {
+        wmma::fragment<wmma::matrix_b, 16, 16, 16, bf16, wmma::row_major> b;
+        wmma::load_matrix_sync(b, Wl + kt * 16 * ld + nt * 16, ld);
+        wmma::mma_sync(acc[nt], a, b, acc[nt]);
+      }
     }
-    wmma::store_matrix_sync(S, acc, kLdS, wmma::mem_row_major);
+  }
+#pragma unroll
+  for (int nt = 0; nt < 4; ++nt) {
+    if (nt >= ncols) break;
+    wmma::store_matrix_sync(S, acc[nt], kLdS, wmma::mem_row_major);
     __syncwarp();
     if (l < kNrcHidden) {  // lane: row lane/2, 8 columns
       const int r = lane >> 1, c0 = (lane & 1) * 8;
@@ -233,15 +241,16 @@ __global__ void __launch_bounds__(kTrainThreads, 1) nrc_train_kernel(NrcView v, 
       const bf16* Xl = X + l * kTileX;
       bf16* Dl = D + ((kNrcLayers - 1 - l) & 1) * kTileX;  // dY_5 in buffer 0, dY_4 in 1, ...
       __syncthreads();                                     // dY_l complete for every row
-      // dW_l += X_l^T dY_l over the tile's rows
-#pragma unroll
-      for (int j = 0; j < 2; ++j) {
-        const bool own = l < kNrcHidden || (j == 0 && warp < 4);
-        if (own) {
-          const int t = l < kNrcHidden ? 2 * warp + j : 4 * warp;
-          const int mt = t >> 2, nt = t & 3;
+      // dW_l += X_l^T dY_l over the tile's rows; the warp's two tiles'
+      // MMA chains interleave (k outer)
 #pragma unroll 4
-          for (int kt = 0; kt < kTrainTile / 16; ++kt) {
+      for (int kt = 0; kt < kTrainTile / 16; ++kt) {
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+          const bool own = l < kNrcHidden || (j == 0 && warp < 4);
+          if (own) {
+            const int t = l < kNrcHidden ? 2 * warp + j : 4 * warp;
+            const int mt = t >> 2, nt = t & 3;
             wmma::fragment<wmma::matrix_a, 16, 16, 16, bf16, wmma::col_major> a;  // X_l^T
             wmma::load_matrix_sync(a, Xl + kt * 16 * kLdX + mt * 16, kLdX);
             wmma::fragment<wmma::matrix_b, 16, 16, 16, bf16, wmma::row_major> b;  // dY_l
@@ -254,17 +263,24 @@ __global__ void __launch_bounds__(kTrainThreads, 1) nrc_train_kernel(NrcView v, 
         // dY_{l-1} = (dY_l W_l^T) * (h_l > 0) for this warp's rows, 16 columns at a time
         bf16* Dn = D + ((kNrcLayers - l) & 1) * kTileX;
         const bf16* Wl = W + woff(l);
-        for (int nt = 0; nt < 4; ++nt) {
-          wmma::fragment<wmma::accumulator, 16, 16, 16, float> acc;
-          wmma::fill_fragment(acc, 0.0f);
-          for (int kt = 0; kt < cols / 16; ++kt) {
-            wmma::fragment<wmma::matrix_a, 16, 16, 16, bf16, wmma::row_major> a;  // dY_l rows
-            wmma::load_matrix_sync(a, Dl + warp * 16 * kLdX + kt * 16, kLdX);
+        // four independent column-block accumulators, their chains interleaved
+        wmma::fragment<wmma::accumulator, 16, 16, 16, float> acc[4];
+#pragma unroll
+        for (int nt = 0; nt < 4; ++nt) wmma::fill_fragment(acc[nt], 0.0f);
+#pragma unroll
+        for (int kt = 0; kt < cols / 16; ++kt) {
+          wmma::fragment<wmma::matrix_a, 16, 16, 16, bf16, wmma::row_major> a;  // dY_l rows
+          wmma::load_matrix_sync(a, Dl + warp * 16 * kLdX + kt * 16, kLdX);
+#pragma unroll
+          for (int nt = 0; nt < 4; ++nt) {
             wmma::fragment<wmma::matrix_b, 16, 16, 16, bf16, wmma::col_major> b;  // W_l^T
             wmma::load_matrix_sync(b, Wl + nt * 16 * ldw(l) + kt * 16, ldw(l));
-            wmma::mma_sync(acc, a, b, acc);
+            wmma::mma_sync(acc[nt], a, b, acc[nt]);
           }
-          wmma::store_matrix_sync(Sw, acc, kLdS, wmma::mem_row_major);
+        }
+#pragma unroll
+        for (int nt = 0; nt < 4; ++nt) {
+          wmma::store_matrix_sync(Sw, acc[nt], kLdS, wmma::mem_row_major);
           __syncwarp();
           const int r = lane >> 1, c0 = (lane & 1) * 8, row = warp * 16 + r;
           const float* y = Sw + r * kLdS + c0;
