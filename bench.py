@@ -486,6 +486,48 @@ def _divided(sc, div):
                                height=max(1, sc.height // div))
 
 
+def run_display(args):
+    """The display image of the 1920x1080 frame (the swapchain blit's
+    headless form): one thread per pixel reads 3 FP64 sums (24 B) and writes
+    one 8-bit RGBA pixel (4 B); device output, CUDA events, roofline against
+    the measured HBM copy peak."""
+    import torch
+    import vcr
+    from vcr import configs
+
+    sc = configs.C5_NRC
+    stream = torch.cuda.Stream()
+    sh = stream.cuda_stream
+    px = sc.width * sc.height
+    with vcr.Context() as ctx:
+        configs.setup_context(ctx, sc, tracker=vcr.TRACKER_DDA)
+        for k in range(2):
+            ctx.pt_pass(seed=1, pass_index=k, stream=sh)
+        out = torch.empty(px * 4, dtype=torch.uint8, device="cuda")
+        flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # larger than L2, written between launches
+        for k in range(args.warmup):
+            ctx.display_to(out.data_ptr(), stream=sh)
+        ms = []
+        for k in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(k & 0xFF)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            ctx.display_to(out.data_ptr(), stream=sh)
+            b.record(stream)
+            b.synchronize()
+            ms.append(a.elapsed_time(b))
+    t = float(np.median(ms))
+    peak, kind = measured_peaks()
+    algo = px * 28
+    print(json.dumps({
+        "metric": "display image", "workload": f"{sc.width}x{sc.height} FP64 sums -> RGBA8 sRGB", "ms": round(t, 4),
+        "steps": args.steps, "l2": "a 256 MiB buffer written between launches",
+        "roofline": {"bound": "hbm", "achieved": round(algo / (t / 1e3) / 1e9, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(algo / (t / 1e3) / 1e9 / peak, 4), "peak_source": kind,
+                     "bytes_per_pixel": 28}}), flush=True)
+
+
 def run_ppm(args):
     """C2: 256^3 FP32 cloud (sigma_t = 16 rho), 1,048,576 photons a pass, r0
     0.01, alpha 0.7, 960x540; one JSON line of pass time and rates."""
@@ -708,12 +750,13 @@ def main():
                     help="only measure the batched 64-view configuration (CUDA graph, autotuned)")
     ap.add_argument("--ppm", action="store_true", help="only measure the photon-mapping configuration")
     ap.add_argument("--ppb", action="store_true", help="only measure the photon-beam configuration")
+    ap.add_argument("--display", action="store_true", help="only measure the display-image kernel")
     ap.add_argument("--image-div", type=int, default=1,
                     help="divide the --ppm / --ppb image sides (a small case for profiler captures)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.impl == "reference" and not (args.ppm or args.ppb or args.batch or args.nrc_frames):
+    if args.impl == "reference" and not (args.ppm or args.ppb or args.batch or args.nrc_frames or args.display):
         run_reference(args)
         return
     import contextlib
@@ -721,7 +764,9 @@ def main():
     import __graft_entry__ as ge
     with contextlib.redirect_stdout(sys.stderr):  # stdout carries only the JSON line
         ge.build()
-    if args.ppm or args.ppb:
+    if args.display:
+        run_display(args)
+    elif args.ppm or args.ppb:
         run_ppm(args) if args.ppm else run_ppb(args)
     elif args.batch:
         run_batch(args)

@@ -124,6 +124,14 @@ VCR_HD float vexp(float x) {
   return (p * u2f((uint32_t)(k1 + 127) << 23)) * u2f((uint32_t)(k2 + 127) << 23);
 }
 
+// sRGB transfer function (IEC 61966-2-1) of a linear value in [0, 1]:
+// 12.92 v up to 0.0031308, else 1.055 v^(1/2.4) - 0.055, the power taken as
+// exp(log(v) / 2.4) with the functions above (so CPU and GPU agree).
+VCR_HD float srgb_encode(float v) {
+  if (v <= 0.0031308f) return 12.92f * v;
+  return 1.055f * vexp(vlog(v) * (1.0f / 2.4f)) - 0.055f;
+}
+
 // sin(2 pi u) and cos(2 pi u): u = q/4 + r with q = round(4u), x = 2 pi r in
 // [-pi/4, pi/4]; Taylor series of sin to x^11 and cos to x^10, then the
 // quadrant rotation.

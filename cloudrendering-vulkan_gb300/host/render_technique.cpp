@@ -164,6 +164,16 @@ std::vector<float> RenderTechnique::ReadMean() const {
   return out;
 }
 
+std::vector<uint8_t> RenderTechnique::ReadDisplay(float exposure, bool bgra) const {
+  Require(frameSet_, "no frame target");
+  std::vector<uint8_t> out((size_t)width_ * height_ * 4);
+  vcr_display_desc d{};
+  d.exposure = exposure;
+  d.order = bgra ? VCR_ORDER_BGRA : VCR_ORDER_RGBA;
+  Check(vcr_display(Context(), &d, out.data(), out.size(), nullptr), Context());
+  return out;
+}
+
 uint32_t RenderTechnique::PassCount() const {
   uint32_t n = 0;
   Check(vcr_pass_count(Context(), &n), Context());

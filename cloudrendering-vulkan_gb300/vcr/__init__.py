@@ -77,6 +77,27 @@ def xyz_read(path: str):
     return desc, out
 
 
+def write_png(path: str, rgba: np.ndarray) -> None:
+    """8-bit RGBA image [H, W, 4] as a PNG file (zlib from the standard
+    library; filter 0 on every row)."""
+    import struct
+    import zlib
+    img = np.ascontiguousarray(rgba, np.uint8)
+    if img.ndim != 3 or img.shape[2] != 4:
+        raise ValueError("write_png wants an [H, W, 4] uint8 array")
+    h, w = img.shape[:2]
+    raw = b"".join(b"\x00" + img[y].tobytes() for y in range(h))
+
+    def chunk(kind, data):
+        return struct.pack(">I", len(data)) + kind + data + struct.pack(">I", zlib.crc32(kind + data) & 0xFFFFFFFF)
+
+    with open(path, "wb") as f:
+        f.write(b"\x89PNG\r\n\x1a\n")
+        f.write(chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, 6, 0, 0, 0)))
+        f.write(chunk(b"IDAT", zlib.compress(raw, 6)))
+        f.write(chunk(b"IEND", b""))
+
+
 class Context:
     """One vcr_ctx: owns the device grid, frame sums and scratch."""
 
@@ -396,6 +417,20 @@ class Context:
         out = np.empty((n, n, n), np.float32)
         self._ck(lib().vcr_readback(self.h, _abi.BUF_SHADOW_VOLUME, _ptr(out), out.nbytes))
         return out
+
+    def display(self, exposure=1.0, order=_abi.ORDER_RGBA, stream=0) -> np.ndarray:
+        """The display image (uint8 [H, W, 4]): the accumulated mean, clamped,
+        sRGB-encoded, as the reference's swapchain blit shows it."""
+        out = np.empty((self.height, self.width, 4), np.uint8)
+        d = _abi.DisplayDesc(exposure, order)
+        self._ck(lib().vcr_display(self.h, C.byref(d), _ptr(out), out.nbytes, C.c_void_p(stream)))
+        return out
+
+    def display_to(self, d_ptr, exposure=1.0, order=_abi.ORDER_RGBA, stream=0):
+        """The display image into device memory (stream-ordered)."""
+        d = _abi.DisplayDesc(exposure, order)
+        self._ck(lib().vcr_display(self.h, C.byref(d), C.c_void_p(d_ptr), self.width * self.height * 4,
+                                   C.c_void_p(stream)))
 
     def readback_to(self, buf_id, d_ptr, nbytes):
         """Copy a context buffer into caller memory (host or device)."""

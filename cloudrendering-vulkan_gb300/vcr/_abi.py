@@ -21,6 +21,7 @@ NEE_RATIO, NEE_SHADOW_VOLUME = 0, 1
 SKY_CONSTANT, SKY_GRADIENT = 0, 1
 TRACKER_GLOBAL, TRACKER_DDA = 0, 1
 BUF_IMAGE_MEAN, BUF_IMAGE_SUM, BUF_PATH_STATS, BUF_PPM_STATS, BUF_SHADOW_VOLUME = range(5)
+ORDER_RGBA, ORDER_BGRA = range(2)
 PASS_RECORD_STATS, PASS_NO_ACCUMULATE = 1, 2
 
 F3 = C.c_float * 3
@@ -56,6 +57,10 @@ class Params(C.Structure):
 class ShadowVolume(C.Structure):
     _fields_ = [("bounds_min", F3), ("bounds_max", F3), ("light_dir", F3), ("right", F3), ("up", F3),
                 ("basis_change", C.c_float * 9), ("voxel_axis_count", C.c_uint32), ("voxel_size", C.c_float)]
+
+
+class DisplayDesc(C.Structure):
+    _fields_ = [("exposure", C.c_float), ("order", C.c_uint32), ("reserved", C.c_uint32 * 2)]
 
 
 class Tuning(C.Structure):
@@ -188,6 +193,7 @@ SIGNATURES = {
     "vcr_radix_sort_pairs_noalloc": (_S, [_P, _P, _P, _P, _u32, _u32, _u32, _P]),
     "vcr_morton_codes": (_S, [_P, _P, _u32, F3, F3, _u32, _P, _P]),
     "vcr_readback": (_S, [_P, C.c_int, _P, _sz]),
+    "vcr_display": (_S, [_P, C.POINTER(DisplayDesc), _P, _sz, _P]),
     "vcr_pass_count": (_S, [_P, C.POINTER(_u32)]),
     "vcr_image_rel_rmse": (_S, [_P, _P, _P, _P]),
 }

@@ -597,6 +597,26 @@ VCR_API vcr_status vcr_checkpoint_load(vcr_ctx* ctx, const char* path);
 /* Synchronous copy of a context buffer (bytes must match). host_out may be
  * host, pinned or device memory of the context's device. */
 VCR_API vcr_status vcr_readback(vcr_ctx* ctx, vcr_buffer_id id, void* host_out, size_t bytes);
+
+/* ------------------------------------------------------------------------ */
+/* Display image                                                            */
+/* ------------------------------------------------------------------------ */
+/* Replaces the blit of the result image into the swapchain
+ * (RenderTechniquePT.cpp:143-167; the swapchain is B8G8R8A8_SRGB,
+ * VulkanSwapchain.cpp:72, so the blit clamps to [0, 1] and sRGB-encodes):
+ * every pixel's accumulated mean times `exposure` (1 = the reference),
+ * clamped to [0, 1], sRGB-encoded (IEC 61966-2-1) and rounded to 8 bits,
+ * alpha 255, as R G B A bytes or, with VCR_ORDER_BGRA, as the swapchain's
+ * B G R A. */
+typedef enum vcr_pixel_order { VCR_ORDER_RGBA = 0, VCR_ORDER_BGRA = 1 } vcr_pixel_order;
+typedef struct vcr_display_desc {
+  float exposure;
+  uint32_t order; /* vcr_pixel_order */
+  uint32_t reserved[2];
+} vcr_display_desc;
+/* out: W*H*4 bytes.  Device memory of the context's device: written in
+ * stream order.  Host memory: written when the call returns. */
+VCR_API vcr_status vcr_display(vcr_ctx* ctx, const vcr_display_desc* desc, void* out, size_t bytes, void* stream);
 /* Number of passes accumulated into the sums so far. */
 VCR_API vcr_status vcr_pass_count(vcr_ctx* ctx, uint32_t* out);
 /* Relative RMSE of the running mean image I against a reference mean image

@@ -108,6 +108,10 @@ class VCR_API RenderTechnique {
 
   /* The accumulated mean image, float RGB, width * height * 3. */
   std::vector<float> ReadMean() const;
+  /* What the swapchain blit would show (RenderTechniquePT.cpp:143-167 into
+   * the B8G8R8A8_SRGB swapchain): 8-bit sRGB pixels, width * height * 4
+   * bytes, R G B A or (bgra) B G R A, alpha 255. */
+  std::vector<uint8_t> ReadDisplay(float exposure = 1.0f, bool bgra = false) const;
   uint32_t PassCount() const;
   uint32_t Width() const { return width_; }
   uint32_t Height() const { return height_; }

@@ -41,6 +41,8 @@ def lib():
                                          C.c_int]),
             "oracle_sv_build": (None, [P, C.POINTER(_abi.Cloud), C.POINTER(_abi.ShadowVolume), P]),
             "oracle_fbm_fill": (None, [P, C.c_uint64, u32, f, f, f, P, C.c_int]),
+            "oracle_display": (None, [P, C.c_size_t, C.c_double, f, u32, P]),
+            "oracle_srgb_encode": (f, [f]),
             "oracle_log": (f, [f]),
             "oracle_exp": (f, [f]),
             "oracle_sincos2pi": (None, [f, C.POINTER(f), C.POINTER(f)]),
@@ -146,6 +148,20 @@ class Grid:
         out = np.empty((n, n, n), np.float32)
         lib().oracle_sv_build(self.h, C.byref(cloud), C.byref(sv), _p(out))
         return out
+
+
+def display(sum_img: np.ndarray, samples: int, exposure: float = 1.0, order: int = 0) -> np.ndarray:
+    """The oracle's display image (uint8 [H, W, 4]) of FP64 sums [H, W, 3]."""
+    s = np.ascontiguousarray(sum_img, np.float64)
+    h, w = s.shape[:2]
+    out = np.empty((h, w), np.uint32)
+    inv = 1.0 / samples if samples else 0.0
+    lib().oracle_display(_p(s), h * w, inv, exposure, order, _p(out))
+    return out.view(np.uint8).reshape(h, w, 4)
+
+
+def srgb_encode(v: float) -> float:
+    return lib().oracle_srgb_encode(v)
 
 
 def olog(x: float) -> float:

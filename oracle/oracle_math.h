@@ -92,6 +92,13 @@ inline float oexp(float x) {
 }
 
 // sin / cos of 2 pi u: quadrant from round(4u), Taylor on [-pi/4, pi/4].
+// sRGB transfer function (IEC 61966-2-1), the power as exp(log(v) / 2.4)
+// with olog / oexp (the device's srgb_encode, bit for bit).
+inline float osrgb_encode(float v) {
+  if (v <= 0.0031308f) return 12.92f * v;
+  return 1.055f * oexp(olog(v) * (1.0f / 2.4f)) - 0.055f;
+}
+
 inline void osincos2pi(float u, float* s, float* c) {
   float q = std::floor(std::fma(u, 4.0f, 0.5f));
   float r = std::fma(q, -0.25f, u);

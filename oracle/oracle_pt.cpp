@@ -696,6 +696,24 @@ void oracle_fbm_fill(const uint32_t n[3], uint64_t seed, uint32_t octaves, float
             fbm_voxel(perm, n, octaves, lac, gain, f0, i, j, (uint32_t)k);
 }
 
+// Display image (the blit of RenderTechniquePT.cpp:143-167 into an sRGB
+// swapchain, VulkanSwapchain.cpp:72): mean = float(sum * inv), times
+// exposure, clamped to [0, 1], sRGB-encoded, rounded to 8 bits; alpha 255;
+// order 0 writes R G B A bytes, 1 writes B G R A.
+void oracle_display(const double* sum, size_t npx, double inv, float exposure, uint32_t order, uint32_t* out) {
+  for (size_t p = 0; p < npx; ++p) {
+    uint32_t q[3];
+    for (int c = 0; c < 3; ++c) {
+      float v = (float)(sum[3 * p + c] * inv) * exposure;
+      v = std::fmin(std::fmax(v, 0.0f), 1.0f);
+      q[c] = (uint32_t)(osrgb_encode(v) * 255.0f + 0.5f);
+    }
+    const uint32_t r = order ? q[2] : q[0], b = order ? q[0] : q[2];
+    out[p] = r | (q[1] << 8) | (b << 16) | (255u << 24);
+  }
+}
+float oracle_srgb_encode(float v) { return osrgb_encode(v); }
+
 float oracle_log(float x) { return olog(x); }
 float oracle_exp(float x) { return oexp(x); }
 void oracle_sincos2pi(float u, float* s, float* c) { osincos2pi(u, s, c); }
