@@ -24,38 +24,84 @@ __global__ void fbm_kernel(float* __restrict__ out, uint64_t total) {
   }
 }
 
-// One CTA per brick, one thread per texel: brick maximum -> scale, encode.
+// One warp per brick (8 bricks per 256-thread CTA): lane l holds texel rows
+// l and l + 32 of the brick (row r = y + 8 z, 8 texels along x, zero
+// outside the grid), the warp's maximum is the brick's scale, and each row
+// is stored as one 16-byte (FP16 / BF16) or two (FP32) vectors into the
+// brick's contiguous 512 texels.
+constexpr int kBrickWarps = 8;
+
 template <int P>
-__global__ void __launch_bounds__(512) brick_kernel(const float* __restrict__ dense, void* __restrict__ bricks,
-                                                    float* __restrict__ scales, int nx, int ny, int nz,
-                                                    int bx, int by) {
-  __shared__ float red[16];
-  uint32_t b = blockIdx.x;
-  int ib = (int)(b % (uint32_t)bx), jb = (int)((b / (uint32_t)bx) % (uint32_t)by), kb = (int)(b / ((uint32_t)bx * (uint32_t)by));
-  int t = threadIdx.x;
-  int i = ib * kBrick + (t & 7), j = jb * kBrick + ((t >> 3) & 7), k = kb * kBrick + (t >> 6);
-  float v = 0.0f;
-  if (i < nx && j < ny && k < nz) v = dense[(size_t)i + (size_t)nx * ((size_t)j + (size_t)ny * (size_t)k)];
-  size_t off = ((size_t)b << 9) + (size_t)t;
+__global__ void __launch_bounds__(kBrickWarps * 32) brick_kernel(const float* __restrict__ dense,
+                                                                 void* __restrict__ bricks,
+                                                                 float* __restrict__ scales, int nx, int ny, int nz,
+                                                                 int bx, int by, uint32_t nbricks) {
+  const uint32_t b = blockIdx.x * kBrickWarps + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (b >= nbricks) return;  // warp-uniform
+  const int ib = (int)(b % (uint32_t)bx), jb = (int)((b / (uint32_t)bx) % (uint32_t)by);
+  const int kb = (int)(b / ((uint32_t)bx * (uint32_t)by));
+  const int i0 = ib * kBrick;
+  const bool vec = (nx & 3) == 0 && i0 + kBrick <= nx;  // rows 16-byte aligned and whole
+  float v[2][8];
+  float m = -INFINITY;  // the max over the brick's 512 values (out-of-grid texels are 0)
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int r = lane + 32 * h;
+    const int j = jb * kBrick + (r & 7), k = kb * kBrick + (r >> 3);
+    const size_t base = (size_t)i0 + (size_t)nx * ((size_t)j + (size_t)ny * (size_t)k);
+    if (j < ny && k < nz && vec) {
+      const float4 a = __ldg(reinterpret_cast<const float4*>(dense + base));
+      const float4 c = __ldg(reinterpret_cast<const float4*>(dense + base) + 1);
+      v[h][0] = a.x; v[h][1] = a.y; v[h][2] = a.z; v[h][3] = a.w;
+      v[h][4] = c.x; v[h][5] = c.y; v[h][6] = c.z; v[h][7] = c.w;
+    } else {
+#pragma unroll
+      for (int x = 0; x < 8; ++x) v[h][x] = (j < ny && k < nz && i0 + x < nx) ? __ldg(dense + base + x) : 0.0f;
+    }
+#pragma unroll
+    for (int x = 0; x < 8; ++x) m = fmaxf(m, v[h][x]);
+  }
+  const size_t brick = (size_t)b << 9;
   if (P == 0) {
-    reinterpret_cast<float*>(bricks)[off] = v;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      float4* dst = reinterpret_cast<float4*>(reinterpret_cast<float*>(bricks) + brick + 8 * (lane + 32 * h));
+      dst[0] = make_float4(v[h][0], v[h][1], v[h][2], v[h][3]);
+      dst[1] = make_float4(v[h][4], v[h][5], v[h][6], v[h][7]);
+    }
     return;
   }
-  float m = v;
   for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if ((t & 31) == 0) red[t >> 5] = m;
-  __syncthreads();
-  if (t < 32) {
-    m = t < 16 ? red[t] : 0.0f;
-    for (int o = 8; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if (t == 0) red[0] = m;
+  const float s = m;
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    uint32_t w[4];
+#pragma unroll
+    for (int x = 0; x < 8; x += 2) {
+      const float q0 = s > 0.0f ? v[h][x] / s : 0.0f, q1 = s > 0.0f ? v[h][x + 1] / s : 0.0f;
+      if (P == 1) {
+        const __half2 hv = __halves2half2(__float2half_rn(q0), __float2half_rn(q1));
+        w[x / 2] = *reinterpret_cast<const uint32_t*>(&hv);
+      } else {
+        const __nv_bfloat162 bv = __halves2bfloat162(__float2bfloat16_rn(q0), __float2bfloat16_rn(q1));
+        w[x / 2] = *reinterpret_cast<const uint32_t*>(&bv);
+      }
+    }
+    uint16_t* base16 = reinterpret_cast<uint16_t*>(bricks) + brick + 8 * (lane + 32 * h);
+    *reinterpret_cast<uint4*>(base16) = make_uint4(w[0], w[1], w[2], w[3]);
   }
-  __syncthreads();
-  float s = red[0];
-  float q = s > 0.0f ? v / s : 0.0f;
-  if (P == 1) reinterpret_cast<__half*>(bricks)[off] = __float2half_rn(q);
-  else reinterpret_cast<__nv_bfloat16*>(bricks)[off] = __float2bfloat16_rn(q);
-  if (t == 0) scales[b] = s;
+  if (lane == 0) scales[b] = s;
+}
+
+// The stored grid decoded to dense floats, x fastest (texel() per voxel).
+__global__ void decode_kernel(GridView g, float* __restrict__ out, uint64_t total) {
+  const uint64_t nx = (uint64_t)g.n[0], ny = (uint64_t)g.n[1];
+  for (uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t r = idx / nx;
+    out[idx] = texel(g, (int)(idx - r * nx), (int)(r % ny), (int)(r / ny));
+  }
 }
 
 // Brick majorant: max decoded texel over [8b-1, 8b+8] per axis (clamped),
@@ -197,11 +243,14 @@ vcr_status grid_build(vcr_ctx* ctx, const float* d_dense, const vcr_grid_desc* d
   VCR_CUDA(ctx, cudaMemsetAsync(ctx->d_majorants, 0, mtotal * sizeof(float), s));
   VCR_CUDA(ctx, cudaMemsetAsync(ctx->d_scales, 0, nbricks * sizeof(float), s));
   if (precision == 0)
-    brick_kernel<0><<<(unsigned)nbricks, 512, 0, s>>>(d_dense, ctx->d_bricks, ctx->d_scales, n[0], n[1], n[2], nb[0], nb[1]);
+    brick_kernel<0><<<(unsigned)((nbricks + kBrickWarps - 1) / kBrickWarps), kBrickWarps * 32, 0, s>>>(
+        d_dense, ctx->d_bricks, ctx->d_scales, n[0], n[1], n[2], nb[0], nb[1], (uint32_t)nbricks);
   else if (precision == 1)
-    brick_kernel<1><<<(unsigned)nbricks, 512, 0, s>>>(d_dense, ctx->d_bricks, ctx->d_scales, n[0], n[1], n[2], nb[0], nb[1]);
+    brick_kernel<1><<<(unsigned)((nbricks + kBrickWarps - 1) / kBrickWarps), kBrickWarps * 32, 0, s>>>(
+        d_dense, ctx->d_bricks, ctx->d_scales, n[0], n[1], n[2], nb[0], nb[1], (uint32_t)nbricks);
   else
-    brick_kernel<2><<<(unsigned)nbricks, 512, 0, s>>>(d_dense, ctx->d_bricks, ctx->d_scales, n[0], n[1], n[2], nb[0], nb[1]);
+    brick_kernel<2><<<(unsigned)((nbricks + kBrickWarps - 1) / kBrickWarps), kBrickWarps * 32, 0, s>>>(
+        d_dense, ctx->d_bricks, ctx->d_scales, n[0], n[1], n[2], nb[0], nb[1], (uint32_t)nbricks);
   VCR_CUDA(ctx, cudaGetLastError());
   ctx->gdesc = *desc;
   ctx->precision = precision;
@@ -249,3 +298,31 @@ vcr_status dda_trace_launch(vcr_ctx* ctx, const float* d_o, const float* d_d, ui
 }
 
 }  // namespace vcr
+
+using namespace vcr;
+
+// The stored grid (its FP32 / FP16 / BF16 bricks) decoded to dense floats,
+// x fastest; out is host or device memory.  Synchronous.
+extern "C" VCR_API vcr_status vcr_grid_read_dense(vcr_ctx* ctx, float* out, size_t count) {
+  if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  if (!ctx->has_grid) return fail(ctx, VCR_ERR_STATE, "no grid");
+  const uint64_t total = (uint64_t)ctx->gdesc.size[0] * ctx->gdesc.size[1] * ctx->gdesc.size[2];
+  if (!out || count != total) return fail(ctx, VCR_ERR_INVALID, "dense grid count %zu != %llu", count,
+                                          (unsigned long long)total);
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
+  cudaPointerAttributes at{};
+  VCR_CUDA(ctx, cudaPointerGetAttributes(&at, out));
+  const bool on_device = (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) && at.device == ctx->device;
+  float* dst = out;
+  if (!on_device) {
+    vcr_status vs = ensure_scratch(ctx, total * sizeof(float));
+    if (vs) return vs;
+    dst = reinterpret_cast<float*>(ctx->d_scratch);
+  }
+  const unsigned blocks = (unsigned)std::min<uint64_t>((total + 255) / 256, (uint64_t)ctx->sm_count * 64);
+  decode_kernel<<<blocks, 256>>>(grid_view(ctx), dst, total);
+  VCR_CUDA(ctx, cudaGetLastError());
+  if (!on_device) VCR_CUDA(ctx, cudaMemcpy(out, dst, total * sizeof(float), cudaMemcpyDeviceToHost));
+  VCR_CUDA(ctx, cudaDeviceSynchronize());
+  return VCR_OK;
+}

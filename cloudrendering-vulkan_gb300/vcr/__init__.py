@@ -108,6 +108,7 @@ class Context:
         check(L.vcr_create(C.byref(h), C.byref(d)))
         self.h = h
         self.width = self.height = 0
+        self.grid_size = (0, 0, 0)
 
     def close(self):
         if self.h:
@@ -133,9 +134,19 @@ class Context:
     def grid_upload(self, desc, dense: np.ndarray, precision=_abi.PREC_FP32):
         dense = np.ascontiguousarray(dense, np.float32)
         self._ck(lib().vcr_grid_upload(self.h, C.byref(desc), _ptr(dense), precision))
+        self.grid_size = tuple(desc.size)
 
     def grid_generate(self, desc, fbm, precision=_abi.PREC_FP32):
         self._ck(lib().vcr_grid_generate(self.h, C.byref(desc), C.byref(fbm), precision))
+        self.grid_size = tuple(desc.size)
+
+    def grid_read_dense(self) -> np.ndarray:
+        """The stored grid decoded to dense floats [Z, Y, X] (what the
+        trackers sample)."""
+        X, Y, Z = self.grid_size
+        out = np.empty((Z, Y, X), np.float32)
+        self._ck(lib().vcr_grid_read_dense(self.h, _ptr(out), out.size))
+        return out
 
     def grid_info(self):
         m = C.c_float()

@@ -194,6 +194,7 @@ SIGNATURES = {
     "vcr_morton_codes": (_S, [_P, _P, _u32, F3, F3, _u32, _P, _P]),
     "vcr_readback": (_S, [_P, C.c_int, _P, _sz]),
     "vcr_display": (_S, [_P, C.POINTER(DisplayDesc), _P, _sz, _P]),
+    "vcr_grid_read_dense": (_S, [_P, _P, _sz]),
     "vcr_pass_count": (_S, [_P, C.POINTER(_u32)]),
     "vcr_image_rel_rmse": (_S, [_P, _P, _P, _P]),
 }

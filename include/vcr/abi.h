@@ -257,6 +257,10 @@ VCR_API vcr_status vcr_grid_info(vcr_ctx* ctx, float* out_max_density,
  * plus a one-texel halo; level l+1 takes the max over 2x2x2 cells of level
  * l; level l has ceil(bricks / 2^l) cells per axis. */
 VCR_API vcr_status vcr_grid_read_majorants(vcr_ctx* ctx, uint32_t level, float* host_out, size_t count);
+/* The stored grid decoded to dense floats (what the trackers sample: FP16 /
+ * BF16 texels times their brick's scale), x fastest, count = X*Y*Z; out is
+ * host or device memory.  Synchronous. */
+VCR_API vcr_status vcr_grid_read_dense(vcr_ctx* ctx, float* out, size_t count);
 /* Densities at n world positions (device pointers; float3 in, float out),
  * through the same trilinear fetch the trackers use. */
 VCR_API vcr_status vcr_grid_sample(vcr_ctx* ctx, const float* d_pos, float* d_out,
