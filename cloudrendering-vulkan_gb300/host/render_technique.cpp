@@ -77,6 +77,11 @@ void RenderTechnique::BindCloud(const Grid& grid, const vcr_cloud& cloud, int pr
   hasPendingCloud_ = true;
 }
 
+void RenderTechnique::BindCloudProperties(const vcr_cloud& cloud) {
+  pendingCloudProps_ = cloud;
+  hasPendingCloudProps_ = true;
+}
+
 void RenderTechnique::BindCamera(const vcr_camera& camera) {
   pendingCamera_ = camera;
   hasPendingCamera_ = true;
@@ -107,6 +112,11 @@ void RenderTechnique::Commit() {
     Check(vcr_set_cloud(c, &cl), c);
     hasPendingCloud_ = false;
     pendingGrid_ = nullptr;
+    restart = true;
+  }
+  if (hasPendingCloudProps_) {
+    Check(vcr_set_cloud(c, &pendingCloudProps_), c);
+    hasPendingCloudProps_ = false;
     restart = true;
   }
   if (hasPendingCamera_) {

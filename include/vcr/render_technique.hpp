@@ -90,6 +90,9 @@ class VCR_API RenderTechnique {
 
   /* Queue updates; nothing reaches the device before Commit. */
   void BindCloud(const Grid& grid, const vcr_cloud& cloud, int precision = VCR_PREC_FP32);
+  /* The cloud properties alone (QueueUpdateCloudData without the sampler):
+   * bounds and scalings change, the stored grid stays. */
+  void BindCloudProperties(const vcr_cloud& cloud);
   void BindCamera(const vcr_camera& camera);
   void BindParameters(const vcr_params& params);
   void BindShadowVolume(const vcr_shadow_volume& shadowVolume);
@@ -132,6 +135,8 @@ class VCR_API RenderTechnique {
   vcr_cloud pendingCloud_{};
   int pendingPrecision_ = VCR_PREC_FP32;
   bool hasPendingCloud_ = false;
+  vcr_cloud pendingCloudProps_{};
+  bool hasPendingCloudProps_ = false;
   vcr_camera pendingCamera_{};
   bool hasPendingCamera_ = false;
   vcr_params pendingParams_{};
@@ -193,6 +198,72 @@ class VCR_API TechniqueNRC : public RenderTechnique {
  private:
   vcr_nrc_params cache_;
   bool allocated_ = false;
+};
+
+/* The state the reference's window edits (main.cpp:500-596).  Apply clamps
+ * fov and pitch the way CameraProperties::SetFOV / SetRotation clamp the
+ * caller's values (UniformBuffers.h:29-58). */
+struct Settings {
+  uint32_t width = 800, height = 600;
+  float position[3] = {0.0f, 0.0f, -0.4f};
+  float rotation[2] = {0.0f, 0.0f};  /* degrees: pitch about x (|pitch| <= 80), then yaw about y */
+  float fov = 90.0f;                 /* vertical, degrees, [60, 150] */
+  float nearPlane = 0.1f;
+  float phaseG = 0.857f;             /* Parameters::SetPhaseG */
+  float densityScaling = 8.0f;       /* CloudProperties.densityScaling */
+  float sunDirection[3] = {0.0f, -0.5f, 0.866f}; /* direction the sunlight travels (normalised) */
+};
+
+enum class Technique { PathTracing = 0, PhotonMapping = 1, PhotonBeams = 2 };
+
+/* The reference's main.cpp around its techniques, headless: one device, the
+ * three techniques, the current one (the switch of main.cpp:197-221), and
+ * the updates each edit needs.  Every edit that changes the image restarts
+ * the progressive accumulation (frameCount = 1, main.cpp:262).
+ *   LoadCloud  ≙ UpdateCloudData (main.cpp:266-335): grid, bounds, majorant
+ *   Apply      ≙ the Apply button (main.cpp:545-596) + UpdateShadowVolume
+ *                (:223-264): resolution, camera, phase, density, light;
+ *                the shadow volume is rebuilt when the parameters use it,
+ *                lit along the camera's forward for photon beams
+ *   Render     ≙ one frame's RecordDrawCommands of the current technique */
+class VCR_API Renderer {
+ public:
+  Renderer(Device& device, PushConstants* pushConstants, const vcr_params& params,
+           const vcr_ppm_params& photonMap, const vcr_ppb_params& beams, uint32_t shadowVolumeSize = 128);
+  ~Renderer();
+  Renderer(const Renderer&) = delete;
+  Renderer& operator=(const Renderer&) = delete;
+
+  void LoadCloud(const Grid& grid, int precision = VCR_PREC_FP32, float baseScaling = 1.0f);
+  /* Returns whether the accumulation restarted; `settings` receives the
+   * clamped fov and pitch. */
+  bool Apply(Settings& settings);
+  void SetTechnique(Technique technique);
+  void Render(void* stream);
+
+  Technique Current() const { return current_; }
+  RenderTechnique& Active();
+  const vcr_camera& Camera() const { return camera_; }
+  const vcr_params& Parameters() const { return params_; }
+  const vcr_cloud& Cloud() const { return cloud_; }
+  uint32_t PassCount() const;
+
+ private:
+  void Restart();
+
+  Device* device_;
+  PushConstants* pushConstants_;
+  TechniquePT pt_;
+  TechniquePPM ppm_;
+  TechniquePPB ppb_;
+  Technique current_ = Technique::PathTracing;
+  vcr_params params_{};
+  vcr_camera camera_{};
+  vcr_cloud cloud_{};
+  vcr_shadow_volume shadowVolume_{};
+  uint32_t shadowVolumeSize_;
+  bool hasCloud_ = false, hasSettings_ = false, hasShadowVolume_ = false;
+  Settings settings_{};
 };
 
 }  // namespace vcr
