@@ -634,6 +634,7 @@ def run_e2e(args, sc, device, sh):
     dense = vcr.fbm_fill_host(sc.size, sc.fbm())  # the library's host generator (threaded)
     pinned = torch.from_numpy(dense).pin_memory()
     img_bytes = sc.width * sc.height * 3 * 4
+    img = torch.empty(sc.width * sc.height * 3, dtype=torch.float32).pin_memory()  # the result, read every pass
     with vcr.Context(device) as ctx:
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -647,12 +648,12 @@ def run_e2e(args, sc, device, sh):
         ctx.set_frame(sc.width, sc.height)
         for k in range(args.steps):
             ctx.pt_pass(seed=5, pass_index=k, stream=sh)
-            img = ctx.image_mean()
+            ctx.readback_to(vcr.BUF_IMAGE_MEAN, img.data_ptr(), img_bytes)  # waits for the pass
         t1 = time.perf_counter()
     grid_bytes = dense.nbytes
     return {"value": round(sc.width * sc.height * args.steps / (t1 - t0) / 1e6, 3), "unit": UNIT,
             "h2d_bytes_per_step": int(grid_bytes // args.steps), "d2h_bytes_per_step": img_bytes,
-            "note": "grid (FP32, pinned) uploaded once per run; mean image read back every pass"}
+            "note": "grid (FP32, pinned) uploaded once per run; mean image read back into pinned memory every pass"}
 
 
 class OracleScene:
