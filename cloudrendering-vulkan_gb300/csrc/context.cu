@@ -325,17 +325,7 @@ extern "C" VCR_API vcr_status vcr_grid_upload(vcr_ctx* ctx, const vcr_grid_desc*
   if (st) return st;
   if (!host) return fail(ctx, VCR_ERR_INVALID, "null host density");
   VCR_CUDA(ctx, cudaSetDevice(ctx->device));
-  size_t bytes = (size_t)desc->size[0] * desc->size[1] * desc->size[2] * sizeof(float);
-  float* d_dense = nullptr;
-  VCR_CUDA(ctx, cudaMalloc(&d_dense, bytes));
-  cudaError_t e = cudaMemcpy(d_dense, host, bytes, cudaMemcpyHostToDevice);
-  if (e != cudaSuccess) {
-    cudaFree(d_dense);
-    return cuda_fail(ctx, e, "grid upload");
-  }
-  st = grid_build(ctx, d_dense, desc, (int)precision, 0);
-  cudaFree(d_dense);
-  return st;
+  return grid_upload_host(ctx, host, desc, (int)precision);
 }
 
 extern "C" VCR_API vcr_status vcr_grid_generate(vcr_ctx* ctx, const vcr_grid_desc* desc, const vcr_fbm_desc* fbm,

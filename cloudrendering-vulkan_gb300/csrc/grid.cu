@@ -4,6 +4,8 @@
 // Replaces the reference's dense R32F 3D image upload (main.cpp:266-335) and
 // its single global majorant (Grid3D::GetMajorant, Grid3D.h:180-192;
 // main.cpp:152).
+#include <algorithm>
+
 #include "vcr_internal.h"
 #include "vcr_fbm.cuh"
 
@@ -31,14 +33,18 @@ __global__ void fbm_kernel(float* __restrict__ out, uint64_t total) {
 // brick's contiguous 512 texels.
 constexpr int kBrickWarps = 8;
 
+// `dense` holds z planes [8 kb0, ...) of the grid: the whole grid (kb0 = 0)
+// or one slab of brick layers; the launch covers bricks [b0, b0 + count).
 template <int P>
 __global__ void __launch_bounds__(kBrickWarps * 32) brick_kernel(const float* __restrict__ dense,
                                                                  void* __restrict__ bricks,
                                                                  float* __restrict__ scales, int nx, int ny, int nz,
-                                                                 int bx, int by, uint32_t nbricks) {
-  const uint32_t b = blockIdx.x * kBrickWarps + (threadIdx.x >> 5);
+                                                                 int bx, int by, uint32_t b0, uint32_t count,
+                                                                 int kb0) {
+  const uint32_t local = blockIdx.x * kBrickWarps + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
-  if (b >= nbricks) return;  // warp-uniform
+  if (local >= count) return;  // warp-uniform
+  const uint32_t b = b0 + local;
   const int ib = (int)(b % (uint32_t)bx), jb = (int)((b / (uint32_t)bx) % (uint32_t)by);
   const int kb = (int)(b / ((uint32_t)bx * (uint32_t)by));
   const int i0 = ib * kBrick;
@@ -49,7 +55,7 @@ __global__ void __launch_bounds__(kBrickWarps * 32) brick_kernel(const float* __
   for (int h = 0; h < 2; ++h) {
     const int r = lane + 32 * h;
     const int j = jb * kBrick + (r & 7), k = kb * kBrick + (r >> 3);
-    const size_t base = (size_t)i0 + (size_t)nx * ((size_t)j + (size_t)ny * (size_t)k);
+    const size_t base = (size_t)i0 + (size_t)nx * ((size_t)j + (size_t)ny * (size_t)(k - kb0 * kBrick));
     if (j < ny && k < nz && vec) {
       const float4 a = __ldg(reinterpret_cast<const float4*>(dense + base));
       const float4 c = __ldg(reinterpret_cast<const float4*>(dense + base) + 1);
@@ -104,32 +110,82 @@ __global__ void decode_kernel(GridView g, float* __restrict__ out, uint64_t tota
   }
 }
 
-// Brick majorant: max decoded texel over [8b-1, 8b+8] per axis (clamped),
-// which bounds every trilinear sample whose position lies in the brick's
-// cell (a sample at texel coordinate u reads floor(u - 1/2) and the next).
-__global__ void __launch_bounds__(256) majorant_kernel(GridView g, float* __restrict__ maj,
-                                                       unsigned int* __restrict__ gmax) {
-  __shared__ float red[8];
-  uint32_t b = blockIdx.x;
-  int ib = (int)(b % (uint32_t)g.nb[0]), jb = (int)((b / (uint32_t)g.nb[0]) % (uint32_t)g.nb[1]);
-  int kb = (int)(b / ((uint32_t)g.nb[0] * (uint32_t)g.nb[1]));
+// Brick summaries for the majorants: per brick, the maximum decoded texel
+// over each of the 27 sets "x in X, y in Y, z in Z" with each set one of
+// {0} (the low face), {0..7} (the whole brick), {7} (the high face); entry
+// sx + 3 sy + 9 sz with 0 = low face, 1 = whole, 2 = high face.  One warp
+// per brick, lane l holding texel rows l and l + 32 (row r = y + 8 z).
+constexpr int kSumWarps = 8;
+
+__global__ void __launch_bounds__(kSumWarps * 32) brick_summary_kernel(GridView g, float* __restrict__ summary,
+                                                                      uint32_t nbricks) {
+  const uint32_t b = blockIdx.x * kSumWarps + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (b >= nbricks) return;  // warp-uniform
+  float m[27];
+#pragma unroll
+  for (int e = 0; e < 27; ++e) m[e] = 0.0f;
+  const float s = g.precision == 0 ? 1.0f : __ldg(g.scales + b);
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int r = lane + 32 * h, y = r & 7, z = r >> 3;
+    float v[8];
+    const size_t off = ((size_t)b << 9) + 8 * (size_t)r;
+#pragma unroll
+    for (int x = 0; x < 8; ++x) {
+      if (g.precision == 0) v[x] = __ldg(reinterpret_cast<const float*>(g.bricks) + off + x);
+      else if (g.precision == 1) v[x] = __half2float(__ldg(reinterpret_cast<const __half*>(g.bricks) + off + x)) * s;
+      else v[x] = __bfloat162float(__ldg(reinterpret_cast<const __nv_bfloat16*>(g.bricks) + off + x)) * s;
+    }
+    float row = v[0];
+#pragma unroll
+    for (int x = 1; x < 8; ++x) row = fmaxf(row, v[x]);
+    const float sel_x[3] = {v[0], row, v[7]};
+#pragma unroll
+    for (int sz = 0; sz < 3; ++sz) {
+      if (!(sz == 1 || (sz == 0 && z == 0) || (sz == 2 && z == 7))) continue;
+#pragma unroll
+      for (int sy = 0; sy < 3; ++sy) {
+        if (!(sy == 1 || (sy == 0 && y == 0) || (sy == 2 && y == 7))) continue;
+#pragma unroll
+        for (int sx = 0; sx < 3; ++sx) m[sx + 3 * sy + 9 * sz] = fmaxf(m[sx + 3 * sy + 9 * sz], sel_x[sx]);
+      }
+    }
+  }
+#pragma unroll
+  for (int e = 0; e < 27; ++e)
+    for (int o = 16; o > 0; o >>= 1) m[e] = fmaxf(m[e], __shfl_xor_sync(0xffffffffu, m[e], o));
+#pragma unroll
+  for (int e = 0; e < 27; ++e)
+    if (lane == e) summary[(size_t)b * 27 + e] = m[e];
+}
+
+// Brick majorant from the summaries: the texels in [8b-1, 8b+8] per axis
+// (clamped to the grid) are the brick's own and, from each of the 26
+// neighbours inside the grid, its face / edge / corner that touches the
+// brick; so the maximum over them is the maximum over 27 summary entries
+// (the same texels as a scan of the 10^3 block).
+__global__ void majorant_from_summary_kernel(const float* __restrict__ summary, int bx, int by, int bz,
+                                             float* __restrict__ maj, unsigned int* __restrict__ gmax) {
+  const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= (uint32_t)(bx * by * bz)) return;
+  const int ib = (int)(b % (uint32_t)bx), jb = (int)((b / (uint32_t)bx) % (uint32_t)by);
+  const int kb = (int)(b / ((uint32_t)bx * (uint32_t)by));
   float m = 0.0f;
-  for (int t = threadIdx.x; t < 1000; t += blockDim.x) {
-    int di = t % 10, dj = (t / 10) % 10, dk = t / 100;
-    int i = min(max(ib * kBrick - 1 + di, 0), g.n[0] - 1);
-    int j = min(max(jb * kBrick - 1 + dj, 0), g.n[1] - 1);
-    int k = min(max(kb * kBrick - 1 + dk, 0), g.n[2] - 1);
-    m = fmaxf(m, texel(g, i, j, k));
-  }
-  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = fmaxf(m, red[w]);
-    m = fmaxf(m, red[0]);
-    maj[b] = m;
-    atomicMax(gmax, __float_as_uint(m));  // non-negative floats order as integers
-  }
+#pragma unroll
+  for (int dz = -1; dz <= 1; ++dz)
+#pragma unroll
+    for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+      for (int dx = -1; dx <= 1; ++dx) {
+        const int i = ib + dx, j = jb + dy, k = kb + dz;
+        if (i < 0 || j < 0 || k < 0 || i >= bx || j >= by || k >= bz) continue;
+        // a neighbour below on an axis gives its high face there, above its low face
+        const int e = (1 - dx) + 3 * (1 - dy) + 9 * (1 - dz);
+        m = fmaxf(m, __ldg(summary + ((size_t)i + (size_t)bx * ((size_t)j + (size_t)by * k)) * 27 + e));
+      }
+  maj[b] = m;
+  atomicMax(gmax, __float_as_uint(m));  // non-negative floats order as integers
 }
 
 // Level l+1 of the majorant pyramid: max over the (up to) 2x2x2 cells of
@@ -211,16 +267,17 @@ vcr_status grid_fbm_device(vcr_ctx* ctx, float* d_dense, const vcr_grid_desc* de
   return VCR_OK;
 }
 
-vcr_status grid_build(vcr_ctx* ctx, const float* d_dense, const vcr_grid_desc* desc, int precision,
-                      cudaStream_t s) {
-  int n[3] = {(int)desc->size[0], (int)desc->size[1], (int)desc->size[2]};
+// Releases the previous grid and allocates the bricks, scales and majorant
+// pyramid of `desc` (levels l = 0..3 with ceil(nb / 2^l) cells per axis,
+// each level starting on a 16-byte boundary for the bulk copies into shared
+// memory).
+static vcr_status grid_alloc(vcr_ctx* ctx, const vcr_grid_desc* desc, int precision, cudaStream_t s) {
   int nb[3];
-  for (int a = 0; a < 3; ++a) nb[a] = (n[a] + kBrick - 1) / kBrick;
+  for (int a = 0; a < 3; ++a) nb[a] = ((int)desc->size[a] + kBrick - 1) / kBrick;
   uint64_t nbricks = (uint64_t)nb[0] * nb[1] * nb[2];
   if (nbricks > (1ull << 22)) return fail(ctx, VCR_ERR_UNSUPPORTED, "grid too large: %llu bricks (max 2^22)",
                                           (unsigned long long)nbricks);
   size_t esz = precision == 0 ? 4 : 2;
-  // release the previous grid
   cudaFree(ctx->d_bricks);
   cudaFree(ctx->d_scales);
   cudaFree(ctx->d_majorants);
@@ -230,8 +287,6 @@ vcr_status grid_build(vcr_ctx* ctx, const float* d_dense, const vcr_grid_desc* d
   ctx->has_grid = false;
   VCR_CUDA(ctx, cudaMalloc(&ctx->d_bricks, nbricks * kBrickVoxels * esz));
   VCR_CUDA(ctx, cudaMalloc(&ctx->d_scales, nbricks * sizeof(float)));
-  // majorant pyramid: level l has ceil(nb / 2^l) cells per axis; each level
-  // starts on a 16-byte boundary (bulk copies into shared memory need it)
   size_t mtotal = 0;
   for (int l = 0; l < 4; ++l) {
     for (int a = 0; a < 3; ++a) ctx->mnb[l][a] = l == 0 ? nb[a] : (ctx->mnb[l - 1][a] + 1) / 2;
@@ -242,23 +297,48 @@ vcr_status grid_build(vcr_ctx* ctx, const float* d_dense, const vcr_grid_desc* d
   VCR_CUDA(ctx, cudaMalloc(&ctx->d_majorants, mtotal * sizeof(float)));
   VCR_CUDA(ctx, cudaMemsetAsync(ctx->d_majorants, 0, mtotal * sizeof(float), s));
   VCR_CUDA(ctx, cudaMemsetAsync(ctx->d_scales, 0, nbricks * sizeof(float), s));
+  return VCR_OK;
+}
+
+// Bricks [b0, b0 + count) from `dense`, which holds z planes [8 kb0, ...).
+static vcr_status brick_launch(vcr_ctx* ctx, const float* dense, const vcr_grid_desc* desc, int precision,
+                               uint32_t b0, uint32_t count, int kb0, cudaStream_t s) {
+  const int n[3] = {(int)desc->size[0], (int)desc->size[1], (int)desc->size[2]};
+  const int bx = (n[0] + kBrick - 1) / kBrick, by = (n[1] + kBrick - 1) / kBrick;
+  const unsigned blocks = (count + kBrickWarps - 1) / kBrickWarps;
+  if (count == 0) return VCR_OK;
   if (precision == 0)
-    brick_kernel<0><<<(unsigned)((nbricks + kBrickWarps - 1) / kBrickWarps), kBrickWarps * 32, 0, s>>>(
-        d_dense, ctx->d_bricks, ctx->d_scales, n[0], n[1], n[2], nb[0], nb[1], (uint32_t)nbricks);
+    brick_kernel<0><<<blocks, kBrickWarps * 32, 0, s>>>(dense, ctx->d_bricks, ctx->d_scales, n[0], n[1], n[2], bx,
+                                                         by, b0, count, kb0);
   else if (precision == 1)
-    brick_kernel<1><<<(unsigned)((nbricks + kBrickWarps - 1) / kBrickWarps), kBrickWarps * 32, 0, s>>>(
-        d_dense, ctx->d_bricks, ctx->d_scales, n[0], n[1], n[2], nb[0], nb[1], (uint32_t)nbricks);
+    brick_kernel<1><<<blocks, kBrickWarps * 32, 0, s>>>(dense, ctx->d_bricks, ctx->d_scales, n[0], n[1], n[2], bx,
+                                                         by, b0, count, kb0);
   else
-    brick_kernel<2><<<(unsigned)((nbricks + kBrickWarps - 1) / kBrickWarps), kBrickWarps * 32, 0, s>>>(
-        d_dense, ctx->d_bricks, ctx->d_scales, n[0], n[1], n[2], nb[0], nb[1], (uint32_t)nbricks);
+    brick_kernel<2><<<blocks, kBrickWarps * 32, 0, s>>>(dense, ctx->d_bricks, ctx->d_scales, n[0], n[1], n[2], bx,
+                                                         by, b0, count, kb0);
   VCR_CUDA(ctx, cudaGetLastError());
+  return VCR_OK;
+}
+
+// Once every brick is written: brick summaries, majorant pyramid, global
+// maximum (synchronises on s).
+static vcr_status grid_finish(vcr_ctx* ctx, const vcr_grid_desc* desc, int precision, cudaStream_t s) {
+  int nb[3];
+  for (int a = 0; a < 3; ++a) nb[a] = ((int)desc->size[a] + kBrick - 1) / kBrick;
+  const uint64_t nbricks = (uint64_t)nb[0] * nb[1] * nb[2];
   ctx->gdesc = *desc;
   ctx->precision = precision;
   for (int a = 0; a < 3; ++a) ctx->nb[a] = nb[a];
   unsigned int* d_gmax = reinterpret_cast<unsigned int*>(ctx->d_counters + 5);
   VCR_CUDA(ctx, cudaMemsetAsync(d_gmax, 0, sizeof(unsigned int), s));
   GridView g = grid_view(ctx);
-  majorant_kernel<<<(unsigned)nbricks, 256, 0, s>>>(g, ctx->d_majorants, d_gmax);
+  vcr_status ss = ensure_scratch(ctx, nbricks * 27 * sizeof(float));
+  if (ss) return ss;
+  float* summary = reinterpret_cast<float*>(ctx->d_scratch);
+  brick_summary_kernel<<<(unsigned)((nbricks + kSumWarps - 1) / kSumWarps), kSumWarps * 32, 0, s>>>(
+      g, summary, (uint32_t)nbricks);
+  majorant_from_summary_kernel<<<(unsigned)((nbricks + 255) / 256), 256, 0, s>>>(summary, nb[0], nb[1], nb[2],
+                                                                                ctx->d_majorants, d_gmax);
   VCR_CUDA(ctx, cudaGetLastError());
   for (int l = 1; l < 4; ++l) {
     const int* sdim = ctx->mnb[l - 1];
@@ -278,6 +358,72 @@ vcr_status grid_build(vcr_ctx* ctx, const float* d_dense, const vcr_grid_desc* d
   ctx->max_density = f;
   ctx->has_grid = true;
   return VCR_OK;
+}
+
+vcr_status grid_build(vcr_ctx* ctx, const float* d_dense, const vcr_grid_desc* desc, int precision,
+                      cudaStream_t s) {
+  vcr_status st = grid_alloc(ctx, desc, precision, s);
+  if (st) return st;
+  uint32_t nbricks = 1;
+  for (int a = 0; a < 3; ++a) nbricks *= ((uint32_t)desc->size[a] + kBrick - 1) / kBrick;
+  st = brick_launch(ctx, d_dense, desc, precision, 0u, nbricks, 0, s);
+  if (st) return st;
+  return grid_finish(ctx, desc, precision, s);
+}
+
+namespace {
+// Streams, events and the slab ring of one streamed upload.
+struct UploadRing {
+  static constexpr int kSlabs = 3;
+  float* buf = nullptr;
+  cudaStream_t copy = nullptr, brick = nullptr;
+  cudaEvent_t copied[kSlabs] = {}, done[kSlabs] = {};
+  ~UploadRing() {
+    if (copy) cudaStreamSynchronize(copy);
+    if (brick) cudaStreamSynchronize(brick);
+    for (int r = 0; r < kSlabs; ++r) {
+      if (copied[r]) cudaEventDestroy(copied[r]);
+      if (done[r]) cudaEventDestroy(done[r]);
+    }
+    if (copy) cudaStreamDestroy(copy);
+    if (brick) cudaStreamDestroy(brick);
+    cudaFree(buf);
+  }
+};
+}  // namespace
+
+// A host grid uploaded one brick layer (8 z planes) at a time through a
+// ring of three device slabs: the copy of layer k overlaps the bricking of
+// layer k - 1, and no device copy of the whole dense grid is made.
+vcr_status grid_upload_host(vcr_ctx* ctx, const float* host, const vcr_grid_desc* desc, int precision) {
+  vcr_status st = grid_alloc(ctx, desc, precision, 0);
+  if (st) return st;
+  VCR_CUDA(ctx, cudaDeviceSynchronize());  // the allocations' clears are done
+  const size_t nx = desc->size[0], ny = desc->size[1], nz = desc->size[2], plane = nx * ny;
+  const uint32_t bx = (uint32_t)((nx + kBrick - 1) / kBrick), by = (uint32_t)((ny + kBrick - 1) / kBrick);
+  const int layers = (int)((nz + kBrick - 1) / kBrick);
+  UploadRing ring;
+  VCR_CUDA(ctx, cudaMalloc(&ring.buf, (size_t)UploadRing::kSlabs * kBrick * plane * sizeof(float)));
+  VCR_CUDA(ctx, cudaStreamCreateWithFlags(&ring.copy, cudaStreamNonBlocking));
+  VCR_CUDA(ctx, cudaStreamCreateWithFlags(&ring.brick, cudaStreamNonBlocking));
+  for (int r = 0; r < UploadRing::kSlabs; ++r) {
+    VCR_CUDA(ctx, cudaEventCreateWithFlags(&ring.copied[r], cudaEventDisableTiming));
+    VCR_CUDA(ctx, cudaEventCreateWithFlags(&ring.done[r], cudaEventDisableTiming));
+  }
+  for (int kb = 0; kb < layers; ++kb) {
+    const int r = kb % UploadRing::kSlabs;
+    float* slab = ring.buf + (size_t)r * kBrick * plane;
+    if (kb >= UploadRing::kSlabs) VCR_CUDA(ctx, cudaStreamWaitEvent(ring.copy, ring.done[r], 0));
+    const size_t z0 = (size_t)kb * kBrick, planes = std::min<size_t>(kBrick, nz - z0);
+    VCR_CUDA(ctx, cudaMemcpyAsync(slab, host + z0 * plane, planes * plane * sizeof(float), cudaMemcpyHostToDevice,
+                                  ring.copy));
+    VCR_CUDA(ctx, cudaEventRecord(ring.copied[r], ring.copy));
+    VCR_CUDA(ctx, cudaStreamWaitEvent(ring.brick, ring.copied[r], 0));
+    st = brick_launch(ctx, slab, desc, precision, (uint32_t)kb * bx * by, bx * by, kb, ring.brick);
+    if (st) return st;
+    VCR_CUDA(ctx, cudaEventRecord(ring.done[r], ring.brick));
+  }
+  return grid_finish(ctx, desc, precision, ring.brick);
 }
 
 vcr_status grid_sample_launch(vcr_ctx* ctx, const float* d_pos, float* d_out, uint32_t n, cudaStream_t s) {

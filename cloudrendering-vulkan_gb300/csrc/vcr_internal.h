@@ -93,6 +93,8 @@ GridView grid_view(const vcr_ctx* ctx);
 SceneView scene_view(const vcr_ctx* ctx);
 
 // grid.cu
+// A host grid, uploaded and bricked one brick layer at a time.
+vcr_status grid_upload_host(vcr_ctx* ctx, const float* host, const vcr_grid_desc* desc, int precision);
 vcr_status grid_build(vcr_ctx* ctx, const float* d_dense, const vcr_grid_desc* desc, int precision,
                       cudaStream_t s);
 vcr_status grid_fbm_device(vcr_ctx* ctx, float* d_dense, const vcr_grid_desc* desc,
