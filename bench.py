@@ -246,7 +246,7 @@ def run_vcr(args):
 
 CONV = {"ref_passes": 4000, "plain_passes": 1000, "warm_steps": 6000, "warm_more": 19, "warm_batch": 16384,
         "train_every": 3, "reuse_steps": 1, "max_frames": 8000, "chunk": 500, "spp": 1, "train_samples": 65536,
-        "learning_rate": 1e-3, "ema_decay": 0.99, "nrc_events": 2}
+        "learning_rate": 1e-3, "ema_decay": 0.99, "nrc_events": 2, "repeats": 3}
 
 
 class Reference:
@@ -387,7 +387,12 @@ def convergence(ctx, sc, stream, args, overrides=None):
     cfg = dict(CONV, **(overrides or {}))
     ref = Reference(ctx, sc, stream, cfg["ref_passes"])
     plain = plain_time_to_1pct(ctx, sc, stream, ref, cfg["plain_passes"])
-    nrc = cached_time_to_1pct(ctx, sc, stream, ref, cfg)
+    # the cache's training trajectory varies from run to run (the order of
+    # its training records follows atomic appends): the median of a few runs
+    runs = [cached_time_to_1pct(ctx, sc, stream, ref, cfg) for _ in range(cfg["repeats"])]
+    done = [r for r in runs if r["time_s"] is not None]
+    nrc = sorted(done, key=lambda r: r["time_s"])[len(done) // 2] if done else runs[0]
+    nrc = dict(nrc, runs_s=[r["time_s"] for r in runs])
     return {"plain": plain, "nrc": nrc,
             "speedup": round(plain["time_s"] / nrc["time_s"], 2) if nrc["time_s"] else None,
             "reference": {"passes": 2 * ref.passes, "own_relrmse": round(float(np.sqrt(ref.noise2)), 5),
