@@ -244,7 +244,7 @@ def run_vcr(args):
     print(json.dumps(line), flush=True)
 
 
-CONV = {"ref_passes": 4000, "plain_passes": 1000, "warm_steps": 6000, "warm_more": 19, "warm_batch": 16384,
+CONV = {"ref_passes": 4000, "plain_passes": 1000, "warm_steps": 6000, "warm_sets": 16, "warm_more": 19, "warm_batch": 16384,
         "train_every": 3, "reuse_steps": 1, "max_frames": 8000, "chunk": 500, "spp": 1, "train_samples": 65536,
         "learning_rate": 1e-3, "ema_decay": 0.99, "nrc_events": 2, "repeats": 3}
 
@@ -316,9 +316,10 @@ def plain_time_to_1pct(ctx, sc, stream, ref, passes):
 
 
 def cached_time_to_1pct(ctx, sc, stream, ref, cfg):
-    """Warm-up (training steps, each optionally followed by cfg["warm_more"]
-    extra Adam steps on the same records), then frames of cfg["spp"]
-    samples per pixel until the corrected relRMSE reaches 1 %."""
+    """Warm-up (training launches of cfg["warm_sets"] record sets, each set
+    feeding 1 + cfg["warm_more"] Adam steps on batches of its records), then
+    frames of cfg["spp"] samples per pixel until the corrected relRMSE
+    reaches 1 %."""
     import torch
     import vcr
 
@@ -330,13 +331,15 @@ def cached_time_to_1pct(ctx, sc, stream, ref, cfg):
     ctx.set_params(prm)
     ctx.nrc_setup(train_samples=cfg["train_samples"], learning_rate=cfg["learning_rate"], query_capacity=px * spp,
                   seed=1, ema_decay=cfg["ema_decay"], tail_survival=cfg.get("tail_survival", 0.0))
-    batches = max(1, cfg["warm_steps"] // (1 + cfg["warm_more"]))
+    sets = cfg.get("warm_sets", 1)
+    per_launch = sets * (1 + cfg["warm_more"])  # Adam steps a training launch feeds
+    batches = max(1, cfg["warm_steps"] // per_launch)
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     a.record(stream)
     for k in range(batches):
-        ctx.nrc_train_step(seed=400, pass_index=k, stream=sh)
-        if cfg["warm_more"]:
-            ctx.nrc_train_more(cfg["warm_more"], max_records=cfg.get("warm_batch", 0), stream=sh)
+        ctx.nrc_train_step(seed=400, pass_index=k, stream=sh, sets=sets)
+        if per_launch > 1:
+            ctx.nrc_train_more(per_launch - 1, max_records=cfg.get("warm_batch", 0), stream=sh)
     b.record(stream)
     b.synchronize()
     warm_ms = a.elapsed_time(b)

@@ -194,6 +194,12 @@ __global__ void __launch_bounds__(kTrainThreads, 1) nrc_train_kernel(NrcView v, 
   float* S = reinterpret_cast<float*>(D + 2 * kTileX);  // per warp: 16 x kLdS
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   float* Sw = S + warp * 16 * kLdS;
+  // records [first_rec, first_rec + capacity) of the *count_ptr written; a
+  // CTA without a tile leaves its slot alone (the reduction reads the slots
+  // of the first ceil(count / kTrainTile) CTAs only)
+  const uint32_t total = *count_ptr;
+  const uint32_t count = total > first_rec ? min(total - first_rec, capacity) : 0u;
+  if (blockIdx.x * kTrainTile >= count) return;
   load_weights(v.wb, W);
   // The CTA's weight gradient stays in registers across its tiles: warp w
   // owns tiles 2w and 2w+1 (row block t/4, column block t%4) of each 64x64
@@ -206,9 +212,6 @@ __global__ void __launch_bounds__(kTrainThreads, 1) nrc_train_kernel(NrcView v, 
     wmma::fill_fragment(dw[l][1], 0.0f);
   }
   __syncthreads();
-  // records [first_rec, first_rec + capacity) of the *count_ptr written
-  const uint32_t total = *count_ptr;
-  const uint32_t count = total > first_rec ? min(total - first_rec, capacity) : 0u;
   recs += first_rec;
   const float inv_n = 1.0f / (3.0f * (float)max(count, 1u));
   float loss_local = 0.0f;
@@ -324,34 +327,78 @@ __global__ void __launch_bounds__(kTrainThreads, 1) nrc_train_kernel(NrcView v, 
   if (lane == 0) atomicAdd(loss, loss_local);
 }
 
-// grad[i] += the launch's per-CTA gradients, summed over the CTAs in order.
-__global__ void nrc_grad_reduce_kernel(const float* __restrict__ gpart, int blocks, float* __restrict__ grad) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= kNrcWeightCount) return;
-  float s = 0.0f;
-  for (int b = 0; b < blocks; ++b) s += gpart[(size_t)b * kNrcWeightCount + i];
-  grad[i] += s;
-}
+// The optimiser state Adam updates, and the hyper-parameters of one step
+// (bias corrections c1 = 1 - b1^t, c2 = 1 - b2^t; moving-average decay).
+struct AdamView {
+  float* w;
+  bf16* wb;
+  float* m;
+  float* v;
+  float* ema;
+  bf16* wbi;
+};
+struct AdamStep {
+  float lr, b1, b2, eps, c1, c2, decay;
+};
 
-__global__ void nrc_adam_kernel(float* __restrict__ w, bf16* __restrict__ wb, float* __restrict__ m,
-                                float* __restrict__ vv, float* __restrict__ g, float lr, float b1, float b2,
-                                float eps, float c1, float c2, float* __restrict__ ema, bf16* __restrict__ wbi,
-                                float decay) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= kNrcWeightCount) return;
-  float gi = g[i];
-  float mi = b1 * m[i] + (1.0f - b1) * gi;
-  float vi = b2 * vv[i] + (1.0f - b2) * gi * gi;
-  m[i] = mi;
-  vv[i] = vi;
-  float wi = w[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
-  w[i] = wi;
-  wb[i] = __float2bfloat16_rn(wi);
-  g[i] = 0.0f;
-  if (ema) {
-    float e = decay * ema[i] + (1.0f - decay) * wi;
-    ema[i] = e;
-    wbi[i] = __float2bfloat16_rn(e);
+constexpr int kReduceCols = 64;    // weights per reduction CTA
+constexpr int kReduceGroups = 4;   // slot groups per weight (b mod 4)
+constexpr int kReduceUnroll = 8;   // independent loads in flight per thread
+static_assert(kNrcWeightCount % kReduceCols == 0, "reduction tiling");
+
+// Sums the slots of the CTAs that had records (the first
+// ceil(count / kTrainTile)) in a fixed order: thread group g adds slots
+// g, g+4, g+8, ... into eight partial sums (slot g + 4u + 32k into sum u),
+// combined pairwise, then the four groups in order.  Without kAdam the sum
+// is added to grad; with kAdam the Adam step follows on grad + sum and grad
+// is cleared.  One launch of kNrcWeightCount / 64 CTAs: every weight's 152
+// loads are spread over four threads with eight in flight each.
+template <bool kAdam>
+__global__ void __launch_bounds__(kReduceCols * kReduceGroups)
+    nrc_grad_reduce_kernel(const float* __restrict__ gpart, int blocks, const uint32_t* __restrict__ count_ptr,
+                           uint32_t capacity, uint32_t first_rec, float* __restrict__ grad, AdamView a, AdamStep h) {
+  __shared__ float part[kReduceGroups][kReduceCols];
+  const int col = threadIdx.x % kReduceCols, grp = threadIdx.x / kReduceCols;
+  const int i = blockIdx.x * kReduceCols + col;
+  const uint32_t total = *count_ptr;
+  const uint32_t count = total > first_rec ? min(total - first_rec, capacity) : 0u;
+  const int active = (int)min((uint32_t)blocks, (count + kTrainTile - 1) / kTrainTile);
+  float s[kReduceUnroll];
+#pragma unroll
+  for (int u = 0; u < kReduceUnroll; ++u) s[u] = 0.0f;
+  constexpr int kStride = kReduceGroups * kReduceUnroll;
+  int b = grp;
+  for (; b + kStride - kReduceGroups < active; b += kStride) {
+    float x[kReduceUnroll];
+#pragma unroll
+    for (int u = 0; u < kReduceUnroll; ++u) x[u] = gpart[(size_t)(b + kReduceGroups * u) * kNrcWeightCount + i];
+#pragma unroll
+    for (int u = 0; u < kReduceUnroll; ++u) s[u] += x[u];
+  }
+#pragma unroll
+  for (int u = 0; u < kReduceUnroll; ++u)  // the last slots of the group: < 8 of them
+    if (b + kReduceGroups * u < active) s[u] += gpart[(size_t)(b + kReduceGroups * u) * kNrcWeightCount + i];
+  part[grp][col] = ((s[0] + s[1]) + (s[2] + s[3])) + ((s[4] + s[5]) + (s[6] + s[7]));
+  __syncthreads();
+  if (grp != 0) return;
+  const float sum = (part[0][col] + part[1][col]) + (part[2][col] + part[3][col]);
+  if (!kAdam) {
+    grad[i] += sum;
+    return;
+  }
+  const float gi = grad[i] + sum;
+  const float mi = h.b1 * a.m[i] + (1.0f - h.b1) * gi;
+  const float vi = h.b2 * a.v[i] + (1.0f - h.b2) * gi * gi;
+  a.m[i] = mi;
+  a.v[i] = vi;
+  const float wi = a.w[i] - h.lr * (mi / h.c1) / (sqrtf(vi / h.c2) + h.eps);
+  a.w[i] = wi;
+  a.wb[i] = __float2bfloat16_rn(wi);
+  grad[i] = 0.0f;
+  if (a.ema) {
+    const float e = h.decay * a.ema[i] + (1.0f - h.decay) * wi;
+    a.ema[i] = e;
+    a.wbi[i] = __float2bfloat16_rn(e);
   }
 }
 
@@ -465,9 +512,10 @@ vcr_status nrc_setup(vcr_ctx* ctx, const vcr_nrc_params* p) {
 }
 
 // Gradient of the loss over records [first, first + capacity) of the
-// *d_count written (device), accumulated into grad.
-vcr_status nrc_accumulate_grad(vcr_ctx* ctx, const NrcRecord* recs, const uint32_t* d_count, uint32_t capacity,
-                               cudaStream_t s, uint32_t first = 0) {
+// *d_count written (device): added to grad, or (adam) followed by one Adam
+// step in the same reduction launch.
+static vcr_status nrc_grad(vcr_ctx* ctx, const NrcRecord* recs, const uint32_t* d_count, uint32_t capacity,
+                           cudaStream_t s, uint32_t first, bool adam) {
   NrcState* st = ctx->nrc;
   VCR_CUDA(ctx, cudaFuncSetAttribute(nrc_train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)train_smem()));
   VCR_CUDA(ctx, cudaMemsetAsync(st->loss, 0, 8, s));
@@ -475,22 +523,24 @@ vcr_status nrc_accumulate_grad(vcr_ctx* ctx, const NrcRecord* recs, const uint32
   nrc_train_kernel<<<blocks, kTrainThreads, train_smem(), s>>>(nrc_view(ctx), recs, d_count, capacity, first,
                                                                st->gpart, st->loss);
   VCR_CUDA(ctx, cudaGetLastError());
-  nrc_grad_reduce_kernel<<<(kNrcWeightCount + 255) / 256, 256, 0, s>>>(st->gpart, blocks, st->grad);
-  VCR_CUDA(ctx, cudaGetLastError());
-  return VCR_OK;
-}
-
-vcr_status nrc_adam(vcr_ctx* ctx, cudaStream_t s) {
-  NrcState* st = ctx->nrc;
-  st->step += 1;
-  const float b1 = 0.9f, b2 = 0.99f, eps = 1e-8f;
-  float c1 = 1.0f - (float)std::pow(0.9, (double)st->step);
-  float c2 = 1.0f - (float)std::pow(0.99, (double)st->step);
-  // moving-average decay ramps up over the first steps: min(d, (1+k)/(10+k))
-  float decay = std::min(st->prm.ema_decay, (1.0f + (float)st->step) / (10.0f + (float)st->step));
-  nrc_adam_kernel<<<(kNrcWeightCount + 255) / 256, 256, 0, s>>>(
-      st->w, reinterpret_cast<bf16*>(st->wb), st->m, st->v, st->grad, st->prm.learning_rate, b1, b2, eps, c1, c2,
-      st->ema, reinterpret_cast<bf16*>(st->wbi), decay);
+  AdamView a{st->w, reinterpret_cast<bf16*>(st->wb), st->m, st->v, st->ema, reinterpret_cast<bf16*>(st->wbi)};
+  AdamStep h{};
+  if (adam) {
+    st->step += 1;
+    h.lr = st->prm.learning_rate;
+    h.b1 = 0.9f;
+    h.b2 = 0.99f;
+    h.eps = 1e-8f;
+    h.c1 = 1.0f - (float)std::pow(0.9, (double)st->step);
+    h.c2 = 1.0f - (float)std::pow(0.99, (double)st->step);
+    // moving-average decay ramps up over the first steps: min(d, (1+k)/(10+k))
+    h.decay = std::min(st->prm.ema_decay, (1.0f + (float)st->step) / (10.0f + (float)st->step));
+  }
+  const dim3 grid(kNrcWeightCount / kReduceCols), block(kReduceCols * kReduceGroups);
+  if (adam)
+    nrc_grad_reduce_kernel<true><<<grid, block, 0, s>>>(st->gpart, blocks, d_count, capacity, first, st->grad, a, h);
+  else
+    nrc_grad_reduce_kernel<false><<<grid, block, 0, s>>>(st->gpart, blocks, d_count, capacity, first, st->grad, a, h);
   VCR_CUDA(ctx, cudaGetLastError());
   return VCR_OK;
 }
@@ -549,7 +599,10 @@ static bool nrc_calibrated(const vcr_ctx* ctx) {
 // where their long paths overlap the pass's short ones.  The first step for
 // a camera/cloud/frame calibrates the path count so that a step yields
 // about train_samples records (synchronises once; deterministic, as the
-// yield of a seeded launch is).
+// yield of a seeded launch is).  A step with pass.spp = S > 1 traces S
+// sets of paths in its one launch: a training-only launch is as long as
+// its longest path, so S sets take far less than S launches (0.95 ms for
+// four sets against 0.65 ms for one on the 1920x1080 cloud scene).
 static NrcTrainSink nrc_sink(vcr_ctx* ctx) {
   NrcState* st = ctx->nrc;
   return NrcTrainSink{st->train, st->train_count, st->train_cap, st->npaths, st->prm.tail_survival};
@@ -584,9 +637,23 @@ static vcr_status nrc_calibrate(vcr_ctx* ctx, const PassView& pv, cudaStream_t s
 // Loss gradient over the step's records, then Adam.
 static vcr_status nrc_update(vcr_ctx* ctx, cudaStream_t s, uint32_t first = 0, uint32_t limit = 0) {
   NrcState* st = ctx->nrc;
-  vcr_status vs = nrc_accumulate_grad(ctx, st->train, st->train_count, limit ? limit : st->train_cap, s, first);
-  if (vs) return vs;
-  return nrc_adam(ctx, s);
+  return nrc_grad(ctx, st->train, st->train_count, limit ? limit : st->train_cap, s, first, true);
+}
+
+// Record room for `sets` training sets; growing the buffer synchronises.
+static vcr_status nrc_reserve_sets(vcr_ctx* ctx, uint32_t sets) {
+  NrcState* st = ctx->nrc;
+  const uint64_t cap = 2ull * st->prm.train_samples * sets;
+  if (sets > kNrcMaxSets || cap > (1ull << 25))
+    return fail(ctx, VCR_ERR_INVALID, "training sets (pass.spp) 1..%u with sets x train_samples <= 2^24", kNrcMaxSets);
+  if (cap <= st->train_cap) return VCR_OK;
+  VCR_CUDA(ctx, cudaDeviceSynchronize());
+  VCR_CUDA(ctx, cudaFree(st->train));
+  st->train = nullptr;
+  st->train_cap = 0;
+  VCR_CUDA(ctx, cudaMalloc(reinterpret_cast<void**>(&st->train), (size_t)cap * sizeof(NrcRecord)));
+  st->train_cap = (uint32_t)cap;
+  return VCR_OK;
 }
 
 vcr_status nrc_train_step(vcr_ctx* ctx, const vcr_pass_desc* pass, cudaStream_t s) {
@@ -595,9 +662,18 @@ vcr_status nrc_train_step(vcr_ctx* ctx, const vcr_pass_desc* pass, cudaStream_t 
   PassView pv;
   vs = make_pass_view(ctx, pass, pv);
   if (vs) return vs;
-  if (!nrc_calibrated(ctx)) vs = nrc_calibrate(ctx, pv, s);  // its records serve this step
-  else vs = nrc_launch_training(ctx, pv, ctx->nrc->npaths, s);
+  const uint32_t sets = pv.spp;
+  vs = nrc_reserve_sets(ctx, sets);
   if (vs) return vs;
+  NrcState* st = ctx->nrc;
+  if (!nrc_calibrated(ctx)) {
+    vs = nrc_calibrate(ctx, pv, s);  // its records serve a one-set step
+    if (!vs && sets > 1) vs = nrc_launch_training(ctx, pv, st->npaths * sets, s);
+  } else {
+    vs = nrc_launch_training(ctx, pv, st->npaths * sets, s);
+  }
+  if (vs) return vs;
+  st->sets = sets;
   vs = nrc_update(ctx, s);
   if (vs) return vs;
   VCR_CUDA(ctx, cudaEventRecord(ctx->work_done, s));
@@ -627,6 +703,7 @@ vcr_status nrc_frame(vcr_ctx* ctx, const vcr_pass_desc* pass, cudaStream_t s) {
     vs = pt_pass_launch(ctx, pass, s, &ts);
   }
   if (vs) return vs;
+  ctx->nrc->sets = 1;
   vs = nrc_update(ctx, s);
   if (vs) return vs;
   VCR_CUDA(ctx, cudaEventRecord(ctx->work_done, s));
@@ -665,7 +742,7 @@ extern "C" VCR_API vcr_status vcr_nrc_train_more(vcr_ctx* ctx, uint32_t steps, u
   if (!ctx->nrc) return fail(ctx, VCR_ERR_STATE, "no radiance cache");
   if (ctx->nrc->step == 0) return fail(ctx, VCR_ERR_STATE, "no training records yet (vcr_nrc_train_step)");
   cudaStream_t s = (cudaStream_t)stream;
-  const uint32_t want = ctx->nrc->prm.train_samples;
+  const uint32_t want = ctx->nrc->prm.train_samples * ctx->nrc->sets;
   const uint32_t batch = (max_records && max_records < want) ? max_records : 0u;
   const uint32_t subsets = batch ? want / batch : 1u;
   for (uint32_t k = 0; k < steps; ++k) {
@@ -762,9 +839,7 @@ extern "C" VCR_API vcr_status vcr_nrc_fit(vcr_ctx* ctx, const void* d_records, u
   uint32_t* d_n = reinterpret_cast<uint32_t*>(ctx->d_scratch);
   VCR_CUDA(ctx, cudaMemcpyAsync(d_n, &n, 4, cudaMemcpyHostToDevice, s));
   for (uint32_t k = 0; k < steps; ++k) {
-    vs = nrc_accumulate_grad(ctx, reinterpret_cast<const NrcRecord*>(d_records), d_n, n, s);
-    if (vs) return vs;
-    vs = nrc_adam(ctx, s);
+    vs = nrc_grad(ctx, reinterpret_cast<const NrcRecord*>(d_records), d_n, n, s, 0, true);
     if (vs) return vs;
   }
   VCR_CUDA(ctx, cudaEventRecord(ctx->work_done, s));
@@ -785,7 +860,7 @@ extern "C" VCR_API vcr_status vcr_nrc_gradient(vcr_ctx* ctx, const void* d_recor
   uint32_t* d_n = reinterpret_cast<uint32_t*>(ctx->d_scratch);
   VCR_CUDA(ctx, cudaMemcpy(d_n, &n, 4, cudaMemcpyHostToDevice));
   VCR_CUDA(ctx, cudaMemset(ctx->nrc->grad, 0, kNrcWeightCount * 4));
-  vs = nrc_accumulate_grad(ctx, reinterpret_cast<const NrcRecord*>(d_records), d_n, n, 0);
+  vs = nrc_grad(ctx, reinterpret_cast<const NrcRecord*>(d_records), d_n, n, 0, 0, false);
   if (vs) return vs;
   VCR_CUDA(ctx, cudaDeviceSynchronize());
   VCR_CUDA(ctx, cudaMemcpy(host_grad, ctx->nrc->grad, count * 4, cudaMemcpyDeviceToHost));

@@ -34,6 +34,8 @@ static_assert(sizeof(NrcRecord) == 64, "record size");
 // scattering vertices.  They run as the first work items of a wavefront
 // launch, ahead of the pass's camera paths.
 constexpr int kNrcRecordEvents = 4;
+// training sets one vcr_nrc_train_step may trace in its launch (pass.spp)
+constexpr uint32_t kNrcMaxSets = 64;
 constexpr uint32_t kNrcTrainSalt = 0x3C6EF372u;  // RNG stream salt of training paths
 constexpr uint32_t kNrcNoSlot = 0xFFFFFFFFu;
 
@@ -59,7 +61,8 @@ struct NrcState {
   float* loss = nullptr;     // [2]: loss sum, sample count of the last step
   NrcRecord* train = nullptr;  // training records [train_cap]
   uint32_t* train_count = nullptr;
-  uint32_t train_cap = 0;      // 2 x train_samples: room for the yield's spread
+  uint32_t train_cap = 0;      // 2 x train_samples x sets: room for the yield's spread
+  uint32_t sets = 1;           // training sets (of ~train_samples records) in the buffer
   NrcRecord* query = nullptr;  // cache queries of one pass [query_capacity]
   uint32_t* query_count = nullptr;
   uint32_t query_capacity = 0;

@@ -233,9 +233,9 @@ class Context:
     def nrc_free(self):
         self._ck(lib().vcr_nrc_free(self.h))
 
-    def nrc_train_step(self, seed=0, pass_index=0, stream=0):
+    def nrc_train_step(self, seed=0, pass_index=0, stream=0, sets=1):
         p = _abi.PassDesc()
-        p.seed, p.pass_index, p.spp = seed, pass_index, 1
+        p.seed, p.pass_index, p.spp = seed, pass_index, sets
         self._ck(lib().vcr_nrc_train_step(self.h, C.byref(p), C.c_void_p(stream)))
 
     def nrc_frame(self, seed=0, pass_index=0, spp=1, stream=0):

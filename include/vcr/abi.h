@@ -367,7 +367,11 @@ VCR_API vcr_status vcr_nrc_free(vcr_ctx* ctx);
  * scattering vertices; the fused kernel computes the relative L2 loss
  * gradient; Adam updates the weights.  With vcr_params.nrc_events = k > 0,
  * vcr_pt_pass (DDA tracker) ends paths at their k-th scattering event and
- * adds throughput x cache prediction there. */
+ * adds throughput x cache prediction there.  pass.spp = S > 1 traces S
+ * training sets (about S x train_samples records) in the one launch, for
+ * vcr_nrc_train_more to walk: a training-only launch lasts as long as its
+ * longest path, so S sets cost far less than S steps (S <= 64,
+ * S x train_samples <= 2^24; the record buffer grows on first use). */
 VCR_API vcr_status vcr_nrc_train_step(vcr_ctx* ctx, const vcr_pass_desc* pass, void* stream);
 /* One frame of the cached tracker, the same as vcr_pt_pass followed by
  * vcr_nrc_train_step with the same pass: one wavefront launch runs the
@@ -378,7 +382,8 @@ VCR_API vcr_status vcr_nrc_train_step(vcr_ctx* ctx, const vcr_pass_desc* pass, v
  * Needs the DDA tracker and params.nrc_events > 0. */
 VCR_API vcr_status vcr_nrc_frame(vcr_ctx* ctx, const vcr_pass_desc* pass, void* stream);
 /* `steps` further gradient + Adam steps on the records of the last training
- * step or frame (a cheap warm-up: the records are reused, not re-traced).
+ * step (all its sets) or frame (a cheap warm-up: the records are reused,
+ * not re-traced).
  * max_records > 0 makes each step use a batch of that many records, the
  * steps walking through the records batch by batch; 0 uses them all. */
 VCR_API vcr_status vcr_nrc_train_more(vcr_ctx* ctx, uint32_t steps, uint32_t max_records, void* stream);

@@ -145,6 +145,31 @@ def test_training_paths_are_calibrated_to_the_record_budget(cuda):
         assert 0.7 * 16384 <= c <= 1.4 * 16384, counts
 
 
+def test_a_step_traces_several_training_sets_in_one_launch(cuda):
+    sc = configs.C1_PT
+    with vcr.Context() as ctx:
+        configs.setup_context(ctx, sc, width=128, height=128)
+        prm = sc.params(vcr.TRACKER_DDA)
+        prm.nrc_events = 2
+        ctx.set_params(prm)
+        ctx.nrc_setup(train_samples=8192, seed=3)
+        ctx.nrc_train_step(seed=5, pass_index=0, sets=4)  # calibrates, then traces four sets
+        four = ctx.nrc_info()["train_records"]
+        w0 = ctx.nrc_get_weights()
+        ctx.nrc_train_more(15, max_records=2048)  # walks the four sets batch by batch
+        info = ctx.nrc_info()
+        assert info["steps"] == 16 and np.isfinite(info["last_loss"])
+        assert not np.array_equal(w0, ctx.nrc_get_weights())
+        ctx.nrc_train_step(seed=5, pass_index=1)
+        one = ctx.nrc_info()["train_records"]
+        ctx.nrc_frame(seed=6, pass_index=2)
+        frame = ctx.nrc_info()["train_records"]
+        with pytest.raises(vcr.VcrError):
+            ctx.nrc_train_step(seed=5, pass_index=3, sets=65)
+    assert 0.7 * 4 * 8192 <= four <= 1.4 * 4 * 8192, four
+    assert 0.7 * 8192 <= one <= 1.4 * 8192 and 0.7 * 8192 <= frame <= 1.4 * 8192, (one, frame)
+
+
 def test_frame_equals_pass_then_train_step(cuda):
     """vcr_nrc_frame overlaps the training paths with the pass; its result
     is the sequential pass + train step (up to the order of the gradient's
