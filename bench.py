@@ -244,7 +244,7 @@ def run_vcr(args):
     print(json.dumps(line), flush=True)
 
 
-CONV = {"ref_passes": 4000, "plain_passes": 1000, "warm_steps": 6000, "warm_sets": 16, "warm_more": 19, "warm_batch": 16384,
+CONV = {"ref_passes": 4000, "plain_passes": 1000, "warm_steps": 6000, "warm_sets": 32, "warm_more": 19, "warm_batch": 16384,
         "train_every": 3, "reuse_steps": 1, "max_frames": 8000, "chunk": 500, "spp": 1, "train_samples": 65536,
         "learning_rate": 1e-3, "ema_decay": 0.99, "nrc_events": 2, "repeats": 3}
 

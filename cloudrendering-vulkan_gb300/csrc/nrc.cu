@@ -8,17 +8,16 @@
 // runs 16-sample tiles whose activations stay in the MMA fragments, the CTA
 // shares only the transposed BF16 weights.  Training: one 8-warp CTA per
 // SM holds the BF16 weights and, for a 128-sample tile, the six activation
-// tiles and the gradient ping-pong in padded shared memory (202 KB); the
-// warp-level matrix API (16x16x16) runs the forward, the relative-L2 loss
-// gradient, the backward and X_l^T dY_l over the tile.  The weight gradient
-// stays in the warps' accumulator fragments (each warp owns two 16x16 tiles
-// of every layer) across all the CTA's tiles; at the end each CTA stores it
-// into its own slot and a small kernel sums the slots in a fixed order (one
-// atomic add per weight per CTA cost as much as the tiles themselves).  Adam
-// runs on FP32 master weights and refreshes the BF16 copies (training
-// weights, and the moving average the queries use).
-#include <mma.h>
-
+// tiles and the gradient ping-pong in padded shared memory (197 KB); the
+// forward and the backward's dY_l W_l^T run register-resident on the same
+// mma.sync fragments, and ldmatrix.trans feeds X_l^T dY_l over the tile.
+// The weight gradient stays in the warps' accumulator fragments (each warp
+// owns a 16x32 block of every hidden layer) across all the CTA's tiles; at
+// the end each CTA stores it into its own slot and one kernel sums the
+// slots in a fixed order and takes the Adam step (one atomic add per
+// weight per CTA cost as much as the tiles themselves).  Adam runs on FP32
+// master weights and refreshes the BF16 copies (training weights, and the
+// moving average the queries use).
 #include <cstring>
 
 #include "nrc.cuh"
@@ -27,7 +26,6 @@
 
 namespace vcr {
 
-using namespace nvcuda;
 using bf16 = __nv_bfloat16;
 
 // Training CTA: 8 warps, 16 records each, one 128-record tile at a time.
@@ -38,7 +36,6 @@ constexpr int kTrainTile = kTrainWarps * 16;
 // Shared-memory row strides are padded off powers of two, so the 16 rows of
 // a matrix fragment load or store fall on different banks.
 constexpr int kLdX = kNrcWidth + 8;  // BF16 activation / gradient tiles: 144-byte rows
-constexpr int kLdS = 16 + 4;         // FP32 staging of one 16x16 accumulator: 80-byte rows
 __host__ __device__ constexpr int ldw(int l) { return nrc_layer_cols(l) + 8; }  // BF16 weights of layer l
 __host__ __device__ constexpr int woff(int l) { return l * kNrcWidth * (kNrcWidth + 8); }
 constexpr int kWs = woff(kNrcLayers - 1) + kNrcWidth * (kNrcOutPad + 8);  // BF16 weights in shared memory
@@ -49,69 +46,6 @@ struct NrcView {
   const bf16* wbi;  // inference weights (the moving average, or wb)
   f3 b0, inv_ext;
 };
-
-// Encode 16 samples (rows) of a warp into X0 rows [16w, 16w+16): lane 2s+h
-// writes half h of sample s (h = 0: position; h = 1: both SH blocks).
-__device__ __forceinline__ void encode_rows(const NrcRecord* __restrict__ recs, uint32_t first, uint32_t count,
-                                            const NrcView& v, bf16* X0, int warp, int lane) {
-  int s = lane >> 1, h = lane & 1;
-  uint32_t idx = first + (uint32_t)(warp * 16 + s);
-  float e[32];
-  if (idx < count) {
-    NrcRecord r = recs[idx];
-    if (h == 0) nrc_encode_position(r, v.b0, v.inv_ext, e);
-    else nrc_encode_directions(r, e);
-  } else {
-#pragma unroll
-    for (int i = 0; i < 32; ++i) e[i] = 0.0f;
-  }
-  bf16* row = X0 + (warp * 16 + s) * kLdX + h * 32;
-#pragma unroll
-  for (int i = 0; i < 32; i += 2)
-    *reinterpret_cast<__nv_bfloat162*>(row + i) = __floats2bfloat162_rn(e[i], e[i + 1]);
-}
-
-// Layer l for the warp's rows [16w, 16w + 16): Y = X_l W_l, 16 columns at a
-// time through the warp's 16x16 FP32 staging block S.  Hidden layers store
-// bf16(relu(Y)) into Xn; the output layer (16 columns) is left in S.
-__device__ __forceinline__ void forward_layer(const bf16* Xl, const bf16* Wl, int l, bf16* Xn, float* S, int warp,
-                                              int lane) {
-  const int ncols = nrc_layer_cols(l) / 16, ld = ldw(l);
-  // the column blocks' MMA chains interleave (k outer), four independent accumulators
-  wmma::fragment<wmma::accumulator, 16, 16, 16, float> acc[4];
-#pragma unroll
-  for (int nt = 0; nt < 4; ++nt) wmma::fill_fragment(acc[nt], 0.0f);
-#pragma unroll
-  for (int kt = 0; kt < 4; ++kt) {
-    wmma::fragment<wmma::matrix_a, 16, 16, 16, bf16, wmma::row_major> a;
-    wmma::load_matrix_sync(a, Xl + warp * 16 * kLdX + kt * 16, kLdX);
-#pragma unroll
-    for (int nt = 0; nt < 4; ++nt) {
-      if (nt < ncols) {
-        wmma::fragment<wmma::matrix_b, 16, 16, 16, bf16, wmma::row_major> b;
-        wmma::load_matrix_sync(b, Wl + kt * 16 * ld + nt * 16, ld);
-        wmma::mma_sync(acc[nt], a, b, acc[nt]);
-      }
-    }
-  }
-#pragma unroll
-  for (int nt = 0; nt < 4; ++nt) {
-    if (nt >= ncols) break;
-    wmma::store_matrix_sync(S, acc[nt], kLdS, wmma::mem_row_major);
-    __syncwarp();
-    if (l < kNrcHidden) {  // lane: row lane/2, 8 columns
-      const int r = lane >> 1, c0 = (lane & 1) * 8;
-      const float4 y0 = *reinterpret_cast<const float4*>(S + r * kLdS + c0);
-      const float4 y1 = *reinterpret_cast<const float4*>(S + r * kLdS + c0 + 4);
-      __nv_bfloat162* d = reinterpret_cast<__nv_bfloat162*>(Xn + (warp * 16 + r) * kLdX + nt * 16 + c0);
-      d[0] = __floats2bfloat162_rn(fmaxf(y0.x, 0.0f), fmaxf(y0.y, 0.0f));
-      d[1] = __floats2bfloat162_rn(fmaxf(y0.z, 0.0f), fmaxf(y0.w, 0.0f));
-      d[2] = __floats2bfloat162_rn(fmaxf(y1.x, 0.0f), fmaxf(y1.y, 0.0f));
-      d[3] = __floats2bfloat162_rn(fmaxf(y1.z, 0.0f), fmaxf(y1.w, 0.0f));
-      __syncwarp();
-    }
-  }
-}
 
 // Global [in][out] BF16 weights (ld = cols) into the padded shared layout,
 // 16 bytes at a time.
@@ -183,17 +117,65 @@ __global__ void __launch_bounds__(kInferThreads, 3) nrc_infer_kernel(NrcView v, 
 // ---------------------------------------------------------------------------
 // training: relative L2 loss sum_c (y - t)^2 / (sg(y)^2 + 0.01) / (3 B)
 // ---------------------------------------------------------------------------
+
+// The lane's four BF16 pairs of an A fragment (rows g, g+8; columns 2t and
+// 8+2t of each 16-column tile kt) to / from a [record][feature] tile with
+// kLdX rows: 4-byte accesses on 32 distinct banks.
+__device__ __forceinline__ void store_a(bf16* T, int row, int t, const uint32_t (&a)[4][4], int tiles) {
+#pragma unroll
+  for (int kt = 0; kt < 4; ++kt) {
+    if (kt >= tiles) break;
+    uint32_t* p0 = reinterpret_cast<uint32_t*>(T + row * kLdX + kt * 16 + 2 * t);
+    uint32_t* p1 = reinterpret_cast<uint32_t*>(T + (row + 8) * kLdX + kt * 16 + 2 * t);
+    p0[0] = a[kt][0];
+    p1[0] = a[kt][1];
+    p0[4] = a[kt][2];
+    p1[4] = a[kt][3];
+  }
+}
+
+// acc = X W_l for the NT 8-column output tiles of layer l: X the A
+// fragments a[kt] (4 input tiles), W_l the [in][out] rows of ldw(l); the B
+// fragments come from ldmatrix.trans, two output tiles per load.
+template <int NT>
+__device__ __forceinline__ void mma_layer_in_out(const bf16* Wl, int ld, const uint32_t (&a)[4][4],
+                                                 float (&acc)[NT][4], int lane) {
+  const int rr = lane & 7, q = lane >> 3;
+#pragma unroll
+  for (int nt = 0; nt < NT; ++nt) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
+#pragma unroll
+  for (int kt = 0; kt < 4; ++kt) {
+#pragma unroll
+    for (int np = 0; np < NT / 2; ++np) {
+      uint32_t b[4];  // (in 16kt.., out 16np..), (in +8, out), (in, out +8), (in +8, out +8)
+      ldsm_x4_t(b, Wl + (kt * 16 + rr + 8 * (q & 1)) * ld + np * 16 + 8 * (q >> 1));
+      mma_bf16(acc[2 * np], a[kt], b[0], b[1]);
+      mma_bf16(acc[2 * np + 1], a[kt], b[2], b[3]);
+    }
+  }
+}
+
+// One 8-warp CTA per SM; a 128-record tile at a time, 16 records per warp.
+// The forward keeps a warp's activations in its MMA fragments (as the
+// queries do) and stores each layer's input X_l once, as BF16, into the
+// tile's shared [record][feature] buffers; the backward runs dY_l W_l^T in
+// registers as well (the dY A fragments of one layer are the masked
+// accumulators of the last), so only X_l and dY_l go through shared memory,
+// for the weight gradient dW_l = X_l^T dY_l over all 128 records.  Warp w
+// owns the 16 x 32 block (rows 16(w/2).., columns 32(w%2)..) of every 64x64
+// hidden-layer gradient and the 16 x 8 block (rows 16(w/2).., columns
+// 8(w%2)..) of the 64x16 output layer's, in registers across the CTA's
+// tiles; X_l^T and dY_l fragments come from ldmatrix.trans.  At the end each
+// CTA stores its gradient into its own slot of gpart.
 __global__ void __launch_bounds__(kTrainThreads, 1) nrc_train_kernel(NrcView v, const NrcRecord* __restrict__ recs,
                                                                      const uint32_t* __restrict__ count_ptr,
                                                                      uint32_t capacity, uint32_t first_rec,
                                                                      float* __restrict__ gpart, float* __restrict__ loss) {
   extern __shared__ __align__(128) unsigned char smem[];
-  bf16* W = reinterpret_cast<bf16*>(smem);
-  bf16* X = W + kWs;                                     // h_0 .. h_5 of the tile
+  bf16* W = reinterpret_cast<bf16*>(smem);              // [in][out], rows of ldw(l)
+  bf16* X = W + kWs;                                     // X_0 .. X_5 of the tile
   bf16* D = X + kNrcLayers * kTileX;                     // dY ping-pong: 2 tiles
-  float* S = reinterpret_cast<float*>(D + 2 * kTileX);  // per warp: 16 x kLdS
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  float* Sw = S + warp * 16 * kLdS;
+  float* dirs = reinterpret_cast<float*>(D + 2 * kTileX);  // 16 position-level directions
   // records [first_rec, first_rec + capacity) of the *count_ptr written; a
   // CTA without a tile leaves its slot alone (the reduction reads the slots
   // of the first ceil(count / kTrainTile) CTAs only)
@@ -201,127 +183,148 @@ __global__ void __launch_bounds__(kTrainThreads, 1) nrc_train_kernel(NrcView v, 
   const uint32_t count = total > first_rec ? min(total - first_rec, capacity) : 0u;
   if (blockIdx.x * kTrainTile >= count) return;
   load_weights(v.wb, W);
-  // The CTA's weight gradient stays in registers across its tiles: warp w
-  // owns tiles 2w and 2w+1 (row block t/4, column block t%4) of each 64x64
-  // hidden-layer gradient, and warps 0-3 the row blocks of the 64x16 output
-  // layer's.
-  wmma::fragment<wmma::accumulator, 16, 16, 16, float> dw[kNrcLayers][2];
+  load_level_dirs(dirs);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  const int rr = lane & 7, q = lane >> 3;
+  const int mt = warp >> 1, half = warp & 1;  // the warp's gradient blocks
+  float dwh[kNrcHidden][4][4], dwo[4];
 #pragma unroll
-  for (int l = 0; l < kNrcLayers; ++l) {
-    wmma::fill_fragment(dw[l][0], 0.0f);
-    wmma::fill_fragment(dw[l][1], 0.0f);
-  }
+  for (int l = 0; l < kNrcHidden; ++l)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) dwh[l][j][0] = dwh[l][j][1] = dwh[l][j][2] = dwh[l][j][3] = 0.0f;
+  dwo[0] = dwo[1] = dwo[2] = dwo[3] = 0.0f;
   __syncthreads();
   recs += first_rec;
   const float inv_n = 1.0f / (3.0f * (float)max(count, 1u));
   float loss_local = 0.0f;
+  const int row = warp * 16 + g;  // the lane's tile rows: row and row + 8
   for (uint32_t first = blockIdx.x * kTrainTile; first < count; first += gridDim.x * kTrainTile) {
-    encode_rows(recs, first, count, v, X, warp, lane);
-    __syncwarp();
-#pragma unroll 1
-    for (int l = 0; l < kNrcLayers; ++l)
-      forward_layer(X + l * kTileX, W + woff(l), l, X + (l + 1 < kNrcLayers ? l + 1 : l) * kTileX, Sw, warp, lane);
-    // output gradient (cols 0..2), zero elsewhere and for padding rows
-    for (int e = lane; e < 16 * kNrcOutPad; e += 32) {
-      int r = e / kNrcOutPad, c = e - r * kNrcOutPad;
-      uint32_t idx = first + (uint32_t)(warp * 16 + r);
-      float gval = 0.0f;
-      if (c < kNrcOut && idx < count) {
-        const NrcRecord& rec = recs[idx];
-        float t = c == 0 ? rec.w0 : (c == 1 ? rec.w1 : rec.w2);
-        float y = Sw[r * kLdS + c];
-        float den = y * y + 0.01f;
-        float diff = y - t;
-        loss_local += (diff * diff / den) * inv_n;
-        gval = (2.0f * diff / den) * inv_n;
-      }
-      D[(warp * 16 + r) * kLdX + c] = __float2bfloat16_rn(gval);  // dY_5 in buffer 0
+    const uint32_t i0 = first + (uint32_t)row, i1 = i0 + 8u;
+    uint32_t a[4][4];
+    {
+      NrcRecord r0{}, r1{};
+      if (i0 < count) r0 = recs[i0];
+      if (i1 < count) r1 = recs[i1];
+      encode_a(r0, i0 < count, v.b0, v.inv_ext, dirs, t, 0, a);
+      encode_a(r1, i1 < count, v.b0, v.inv_ext, dirs, t, 1, a);
     }
-    // backward through layers 5..0 (unrolled: the gradient fragments are indexed by layer)
+    store_a(X, row, t, a, 4);
+#pragma unroll 1
+    for (int l = 0; l < kNrcHidden; ++l) {
+      float acc[8][4];
+      mma_layer_in_out<8>(W + woff(l), ldw(l), a, acc, lane);
+      relu_to_a(acc, a);
+      store_a(X + (l + 1) * kTileX, row, t, a, 4);
+    }
+    // output layer and the loss gradient dY_5 (columns 0..2 of 16)
+    uint32_t da[4][4];
+    {
+      float out[2][4];
+      mma_layer_in_out<2>(W + woff(kNrcHidden), ldw(kNrcHidden), a, out, lane);
+      float d5[4];  // (row, 2t), (row, 2t+1), (row+8, 2t), (row+8, 2t+1)
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const uint32_t idx = h ? i1 : i0;
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+          const int c = 2 * t + e;
+          float gval = 0.0f;
+          if (c < kNrcOut && idx < count) {
+            const NrcRecord& rec = recs[idx];
+            const float tv = c == 0 ? rec.w0 : (c == 1 ? rec.w1 : rec.w2);
+            const float y = out[0][2 * h + e];
+            const float den = y * y + 0.01f;
+            const float diff = y - tv;
+            loss_local += (diff * diff / den) * inv_n;
+            gval = (2.0f * diff / den) * inv_n;
+          }
+          d5[2 * h + e] = gval;
+        }
+      }
+      da[0][0] = pack_bf16(d5[0], d5[1]);
+      da[0][1] = pack_bf16(d5[2], d5[3]);
+      da[0][2] = 0u;  // columns 8..15: padding
+      da[0][3] = 0u;
+      store_a(D, row, t, da, 1);  // dY_5 in buffer 0
+    }
+    // backward through layers 5..0 (unrolled: the gradient blocks are indexed by layer)
 #pragma unroll
     for (int l = kNrcLayers - 1; l >= 0; --l) {
-      const int cols = nrc_layer_cols(l);
       const bf16* Xl = X + l * kTileX;
-      bf16* Dl = D + ((kNrcLayers - 1 - l) & 1) * kTileX;  // dY_5 in buffer 0, dY_4 in 1, ...
-      __syncthreads();                                     // dY_l complete for every row
-      // dW_l += X_l^T dY_l over the tile's rows; the warp's two tiles'
-      // MMA chains interleave (k outer)
-#pragma unroll 4
+      const bf16* Dl = D + ((kNrcLayers - 1 - l) & 1) * kTileX;  // dY_5 in buffer 0, dY_4 in 1, ...
+      __syncthreads();                                           // X_l and dY_l complete for every row
+      // dW_l += X_l^T dY_l over the tile's 128 records (k)
+#pragma unroll 2
       for (int kt = 0; kt < kTrainTile / 16; ++kt) {
+        uint32_t xa[4];  // X_l^T rows 16mt.. (features), columns 16kt.. (records)
+        ldsm_x4_t(xa, Xl + (kt * 16 + rr + 8 * (q >> 1)) * kLdX + mt * 16 + 8 * (q & 1));
+        if (l == kNrcLayers - 1) {
+          uint32_t b[2];  // dY_5 records 16kt.., columns 8 half..
+          ldsm_x2_t(b, Dl + (kt * 16 + rr + 8 * (q & 1)) * kLdX + half * 8);
+          mma_bf16(dwo, xa, b[0], b[1]);
+        } else {
 #pragma unroll
-        for (int j = 0; j < 2; ++j) {
-          const bool own = l < kNrcHidden || (j == 0 && warp < 4);
-          if (own) {
-            const int t = l < kNrcHidden ? 2 * warp + j : 4 * warp;
-            const int mt = t >> 2, nt = t & 3;
-            wmma::fragment<wmma::matrix_a, 16, 16, 16, bf16, wmma::col_major> a;  // X_l^T
-            wmma::load_matrix_sync(a, Xl + kt * 16 * kLdX + mt * 16, kLdX);
-            wmma::fragment<wmma::matrix_b, 16, 16, 16, bf16, wmma::row_major> b;  // dY_l
-            wmma::load_matrix_sync(b, Dl + kt * 16 * kLdX + nt * 16, kLdX);
-            wmma::mma_sync(dw[l][j], a, b, dw[l][j]);
+          for (int np = 0; np < 2; ++np) {
+            uint32_t b[4];  // dY_l records 16kt.., columns 32 half + 16 np ..
+            ldsm_x4_t(b, Dl + (kt * 16 + rr + 8 * (q & 1)) * kLdX + half * 32 + np * 16 + 8 * (q >> 1));
+            mma_bf16(dwh[l < kNrcHidden ? l : 0][2 * np], xa, b[0], b[1]);
+            mma_bf16(dwh[l < kNrcHidden ? l : 0][2 * np + 1], xa, b[2], b[3]);
           }
         }
       }
       if (l > 0) {
-        // dY_{l-1} = (dY_l W_l^T) * (h_l > 0) for this warp's rows, 16 columns at a time
-        bf16* Dn = D + ((kNrcLayers - l) & 1) * kTileX;
+        // dY_{l-1} = (dY_l W_l^T) * (X_l > 0) for the warp's rows, in registers
         const bf16* Wl = W + woff(l);
-        // four independent column-block accumulators, their chains interleaved
-        wmma::fragment<wmma::accumulator, 16, 16, 16, float> acc[4];
+        const int ld = ldw(l), ktiles = nrc_layer_cols(l) / 16;
+        float acc[8][4];
 #pragma unroll
-        for (int nt = 0; nt < 4; ++nt) wmma::fill_fragment(acc[nt], 0.0f);
+        for (int nt = 0; nt < 8; ++nt) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
 #pragma unroll
-        for (int kt = 0; kt < cols / 16; ++kt) {
-          wmma::fragment<wmma::matrix_a, 16, 16, 16, bf16, wmma::row_major> a;  // dY_l rows
-          wmma::load_matrix_sync(a, Dl + warp * 16 * kLdX + kt * 16, kLdX);
+        for (int kt = 0; kt < 4; ++kt) {
+          if (kt >= ktiles) break;
 #pragma unroll
-          for (int nt = 0; nt < 4; ++nt) {
-            wmma::fragment<wmma::matrix_b, 16, 16, 16, bf16, wmma::col_major> b;  // W_l^T
-            wmma::load_matrix_sync(b, Wl + nt * 16 * ldw(l) + kt * 16, ldw(l));
-            wmma::mma_sync(acc[nt], a, b, acc[nt]);
+          for (int np = 0; np < 4; ++np) {
+            uint32_t b[4];  // W_l rows (in) 16np.., columns (out) 16kt..: (in, out), (in, out+8), (in+8, out), (in+8, out+8)
+            ldsm_x4(b, Wl + (np * 16 + rr + 8 * (q >> 1)) * ld + kt * 16 + 8 * (q & 1));
+            mma_bf16(acc[2 * np], da[kt], b[0], b[1]);
+            mma_bf16(acc[2 * np + 1], da[kt], b[2], b[3]);
           }
         }
+        bf16* Dn = D + ((kNrcLayers - l) & 1) * kTileX;
 #pragma unroll
-        for (int nt = 0; nt < 4; ++nt) {
-          wmma::store_matrix_sync(Sw, acc[nt], kLdS, wmma::mem_row_major);
-          __syncwarp();
-          const int r = lane >> 1, c0 = (lane & 1) * 8, row = warp * 16 + r;
-          const float* y = Sw + r * kLdS + c0;
-          const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(Xl + row * kLdX + nt * 16 + c0);
-          __nv_bfloat162* d = reinterpret_cast<__nv_bfloat162*>(Dn + row * kLdX + nt * 16 + c0);
+        for (int kt = 0; kt < 4; ++kt) {
+          const uint32_t* h0 = reinterpret_cast<const uint32_t*>(Xl + row * kLdX + kt * 16 + 2 * t);
+          const uint32_t* h1 = reinterpret_cast<const uint32_t*>(Xl + (row + 8) * kLdX + kt * 16 + 2 * t);
+          const uint32_t hv[4] = {h0[0], h1[0], h0[4], h1[4]};
 #pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const __nv_bfloat162 hq = h[q];
+          for (int p = 0; p < 4; ++p) {
+            const __nv_bfloat162 hq = *reinterpret_cast<const __nv_bfloat162*>(&hv[p]);
+            const float* y = &acc[2 * kt + (p >> 1)][2 * (p & 1)];
             const float m0 = __low2float(hq) > 0.0f ? 1.0f : 0.0f, m1 = __high2float(hq) > 0.0f ? 1.0f : 0.0f;
-            d[q] = __floats2bfloat162_rn(y[2 * q] * m0, y[2 * q + 1] * m1);
+            da[kt][p] = pack_bf16(y[0] * m0, y[1] * m1);
           }
-          __syncwarp();
         }
+        store_a(Dn, row, t, da, 4);
       }
     }
-    __syncthreads();  // every warp is done with X_0 before the next tile's encoding
+    __syncthreads();  // every warp is done with X_0 and dY_0 before the next tile's
   }
   // the CTA's gradient ([in][out] layout per layer) into its own slot of
-  // gpart, every weight written (the owned tiles cover each layer once);
+  // gpart, every weight written (the warps' blocks cover each layer once);
   // nrc_grad_reduce_kernel sums the slots in a fixed order
   float* slot = gpart + (size_t)blockIdx.x * kNrcWeightCount;
 #pragma unroll
-  for (int l = 0; l < kNrcLayers; ++l) {
+  for (int l = 0; l < kNrcHidden; ++l)
 #pragma unroll
-    for (int j = 0; j < 2; ++j) {
-      const bool own = l < kNrcHidden || (j == 0 && warp < 4);
-      if (own) {
-        const int t = l < kNrcHidden ? 2 * warp + j : 4 * warp;
-        const int mt = t >> 2, nt = t & 3, cols = nrc_layer_cols(l);
-        wmma::store_matrix_sync(Sw, dw[l][j], kLdS, wmma::mem_row_major);
-        __syncwarp();
-        const int r = lane >> 1, c0 = (lane & 1) * 8;
-        float4* gdst = reinterpret_cast<float4*>(slot + nrc_layer_offset(l) + (mt * 16 + r) * cols + nt * 16 + c0);
-        gdst[0] = *reinterpret_cast<const float4*>(Sw + r * kLdS + c0);
-        gdst[1] = *reinterpret_cast<const float4*>(Sw + r * kLdS + c0 + 4);
-        __syncwarp();
-      }
+    for (int j = 0; j < 4; ++j) {
+      float* base = slot + nrc_layer_offset(l) + (mt * 16 + g) * kNrcWidth + half * 32 + j * 8 + 2 * t;
+      *reinterpret_cast<float2*>(base) = make_float2(dwh[l][j][0], dwh[l][j][1]);
+      *reinterpret_cast<float2*>(base + 8 * kNrcWidth) = make_float2(dwh[l][j][2], dwh[l][j][3]);
     }
+  {
+    float* base = slot + nrc_layer_offset(kNrcHidden) + (mt * 16 + g) * kNrcOutPad + half * 8 + 2 * t;
+    *reinterpret_cast<float2*>(base) = make_float2(dwo[0], dwo[1]);
+    *reinterpret_cast<float2*>(base + 8 * kNrcOutPad) = make_float2(dwo[2], dwo[3]);
   }
   for (int o = 16; o > 0; o >>= 1) loss_local += __shfl_xor_sync(0xffffffffu, loss_local, o);
   if (lane == 0) atomicAdd(loss, loss_local);
@@ -420,7 +423,7 @@ __global__ void nrc_to_bf16_kernel(const float* __restrict__ w, bf16* __restrict
 // ---------------------------------------------------------------------------
 static size_t infer_smem() { return (size_t)kWtElems * 2 + kNrcPosLevels * 3 * sizeof(float); }
 static size_t train_smem() {
-  return (size_t)kWs * 2 + (size_t)(kNrcLayers + 2) * kTileX * 2 + (size_t)kTrainWarps * 16 * kLdS * 4;
+  return (size_t)kWs * 2 + (size_t)(kNrcLayers + 2) * kTileX * 2 + kNrcPosLevels * 3 * sizeof(float);
 }
 
 NrcView nrc_view(const vcr_ctx* ctx) {
