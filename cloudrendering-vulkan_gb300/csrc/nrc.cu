@@ -6,7 +6,7 @@
 // Tensor cores, BF16 operands, FP32 accumulation.  Queries: a
 // register-resident forward (mma.sync m16n8k16, nrc_mma.cuh) — each warp
 // runs 16-sample tiles whose activations stay in the MMA fragments, the CTA
-// shares only the transposed BF16 weights.  Training: one 8-warp CTA per
+// shares only the BF16 weights.  Training: one 8-warp CTA per
 // SM holds the BF16 weights and, for a 128-sample tile, the six activation
 // tiles and the gradient ping-pong in padded shared memory (197 KB); the
 // forward and the backward's dY_l W_l^T run register-resident on the same
@@ -33,12 +33,6 @@ constexpr int kTrainWarps = 8;
 constexpr int kTrainThreads = kTrainWarps * 32;
 constexpr int kTrainTile = kTrainWarps * 16;
 
-// Shared-memory row strides are padded off powers of two, so the 16 rows of
-// a matrix fragment load or store fall on different banks.
-constexpr int kLdX = kNrcWidth + 8;  // BF16 activation / gradient tiles: 144-byte rows
-__host__ __device__ constexpr int ldw(int l) { return nrc_layer_cols(l) + 8; }  // BF16 weights of layer l
-__host__ __device__ constexpr int woff(int l) { return l * kNrcWidth * (kNrcWidth + 8); }
-constexpr int kWs = woff(kNrcLayers - 1) + kNrcWidth * (kNrcOutPad + 8);  // BF16 weights in shared memory
 constexpr int kTileX = kTrainTile * kLdX;                                  // one activation tile
 
 struct NrcView {
@@ -46,20 +40,6 @@ struct NrcView {
   const bf16* wbi;  // inference weights (the moving average, or wb)
   f3 b0, inv_ext;
 };
-
-// Global [in][out] BF16 weights (ld = cols) into the padded shared layout,
-// 16 bytes at a time.
-__device__ __forceinline__ void load_weights(const bf16* __restrict__ g, bf16* s) {
-  const uint4* src = reinterpret_cast<const uint4*>(g);
-  for (int c = threadIdx.x; c < kNrcWeightCount / 8; c += blockDim.x) {
-    const int e = c * 8;
-    const int l = e < kNrcHidden * kNrcWidth * kNrcWidth ? e / (kNrcWidth * kNrcWidth) : kNrcHidden;
-    const int cols = nrc_layer_cols(l);
-    const int rel = e - nrc_layer_offset(l);
-    const int row = rel / cols, col = rel - row * cols;
-    *reinterpret_cast<uint4*>(s + woff(l) + row * ldw(l) + col) = src[c];
-  }
-}
 
 // ---------------------------------------------------------------------------
 // inference: sum[pix] += throughput * max(cache(x, view, sun), 0); out (if
@@ -73,9 +53,9 @@ __global__ void __launch_bounds__(kInferThreads, 3) nrc_infer_kernel(NrcView v, 
                                                                      uint32_t capacity, double* __restrict__ sum,
                                                                      float* __restrict__ out) {
   extern __shared__ __align__(128) unsigned char smem[];
-  bf16* Wt = reinterpret_cast<bf16*>(smem);
-  float* dirs = reinterpret_cast<float*>(Wt + kWtElems);  // 16 level directions
-  load_weights_transposed(v.wbi, Wt);
+  bf16* W = reinterpret_cast<bf16*>(smem);
+  float* dirs = reinterpret_cast<float*>(W + kWs);  // 16 level directions
+  load_weights(v.wbi, W);
   load_level_dirs(dirs);
   __syncthreads();
   const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
@@ -90,7 +70,7 @@ __global__ void __launch_bounds__(kInferThreads, 3) nrc_infer_kernel(NrcView v, 
     encode_a(r0, i0 < count, v.b0, v.inv_ext, dirs, t, 0, a);
     encode_a(r1, i1 < count, v.b0, v.inv_ext, dirs, t, 1, a);
     float yg[3], yh[3];
-    mlp_forward_mma(Wt, a, g, t, yg, yh);
+    mlp_forward_mma(W, a, lane, yg, yh);
     if (t == 0) {
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
@@ -131,27 +111,6 @@ __device__ __forceinline__ void store_a(bf16* T, int row, int t, const uint32_t 
     p1[0] = a[kt][1];
     p0[4] = a[kt][2];
     p1[4] = a[kt][3];
-  }
-}
-
-// acc = X W_l for the NT 8-column output tiles of layer l: X the A
-// fragments a[kt] (4 input tiles), W_l the [in][out] rows of ldw(l); the B
-// fragments come from ldmatrix.trans, two output tiles per load.
-template <int NT>
-__device__ __forceinline__ void mma_layer_in_out(const bf16* Wl, int ld, const uint32_t (&a)[4][4],
-                                                 float (&acc)[NT][4], int lane) {
-  const int rr = lane & 7, q = lane >> 3;
-#pragma unroll
-  for (int nt = 0; nt < NT; ++nt) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
-#pragma unroll
-  for (int kt = 0; kt < 4; ++kt) {
-#pragma unroll
-    for (int np = 0; np < NT / 2; ++np) {
-      uint32_t b[4];  // (in 16kt.., out 16np..), (in +8, out), (in, out +8), (in +8, out +8)
-      ldsm_x4_t(b, Wl + (kt * 16 + rr + 8 * (q & 1)) * ld + np * 16 + 8 * (q >> 1));
-      mma_bf16(acc[2 * np], a[kt], b[0], b[1]);
-      mma_bf16(acc[2 * np + 1], a[kt], b[2], b[3]);
-    }
   }
 }
 
@@ -421,7 +380,7 @@ __global__ void nrc_to_bf16_kernel(const float* __restrict__ w, bf16* __restrict
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
-static size_t infer_smem() { return (size_t)kWtElems * 2 + kNrcPosLevels * 3 * sizeof(float); }
+static size_t infer_smem() { return (size_t)kWs * 2 + kNrcPosLevels * 3 * sizeof(float); }
 static size_t train_smem() {
   return (size_t)kWs * 2 + (size_t)(kNrcLayers + 2) * kTileX * 2 + kNrcPosLevels * 3 * sizeof(float);
 }

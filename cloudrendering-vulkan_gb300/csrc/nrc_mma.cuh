@@ -5,8 +5,9 @@
 // each 8-column tile, g = lane/4, t = lane%4) is, after ReLU and BF16
 // packing, exactly the A fragment of the next layer (rows g and g+8,
 // columns 2t, 2t+1 and 2t+8, 2t+9 of each 16-column tile).  Only the
-// weights live in shared memory, transposed to [out][in] with 144-byte rows
-// so that the B-fragment loads (column g, rows 2t..2t+1) of a warp touch 32
+// weights live in shared memory, in their [in][out] layout with padded
+// rows (144 bytes for the hidden layers), copied 16 bytes at a time; the B
+// fragments come from ldmatrix.trans, two 8-column tiles per load, on 32
 // distinct banks.
 #pragma once
 
@@ -14,8 +15,12 @@
 
 namespace vcr {
 
-constexpr int kLdT = kNrcWidth + 8;                                      // [out][in] rows: 72 BF16
-constexpr int kWtElems = kNrcHidden * kNrcWidth * kLdT + kNrcOutPad * kLdT;  // 24,192 BF16
+// Shared-memory row strides are padded off powers of two, so the 16 rows of
+// a matrix fragment load or store fall on different banks.
+constexpr int kLdX = kNrcWidth + 8;  // BF16 activation / gradient tiles: 144-byte rows
+__host__ __device__ constexpr int ldw(int l) { return nrc_layer_cols(l) + 8; }  // BF16 weights of layer l
+__host__ __device__ constexpr int woff(int l) { return l * kNrcWidth * (kNrcWidth + 8); }
+constexpr int kWs = woff(kNrcLayers - 1) + kNrcWidth * (kNrcOutPad + 8);  // BF16 weights in shared memory
 
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
   __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
@@ -56,32 +61,37 @@ __device__ __forceinline__ void ldsm_x2_t(uint32_t (&r)[2], const void* p) {
                : "memory");
 }
 
-// Global [in][out] BF16 weights (row length = the layer's columns) into
-// shared [out][in] rows of kLdT.
-__device__ __forceinline__ void load_weights_transposed(const __nv_bfloat16* __restrict__ g, __nv_bfloat16* s) {
-  for (int e = threadIdx.x; e < kNrcWeightCount; e += blockDim.x) {
+// Global [in][out] BF16 weights (ld = cols) into the padded shared layout,
+// 16 bytes at a time.
+__device__ __forceinline__ void load_weights(const __nv_bfloat16* __restrict__ g, __nv_bfloat16* s) {
+  const uint4* src = reinterpret_cast<const uint4*>(g);
+  for (int c = threadIdx.x; c < kNrcWeightCount / 8; c += blockDim.x) {
+    const int e = c * 8;
     const int l = e < kNrcHidden * kNrcWidth * kNrcWidth ? e / (kNrcWidth * kNrcWidth) : kNrcHidden;
     const int cols = nrc_layer_cols(l);
     const int rel = e - nrc_layer_offset(l);
-    const int i = rel / cols, o = rel - i * cols;
-    s[l * kNrcWidth * kLdT + o * kLdT + i] = g[e];
+    const int row = rel / cols, col = rel - row * cols;
+    *reinterpret_cast<uint4*>(s + woff(l) + row * ldw(l) + col) = src[c];
   }
 }
 
-// acc[nt] = X W_l for the NT 8-column output tiles; X is the A fragments
-// a[kt] of the 4 16-column input tiles, Wt the layer's [out][in] rows.
+// acc = X W_l for the NT 8-column output tiles of layer l: X the A
+// fragments a[kt] (4 input tiles), W_l the [in][out] rows of ldw(l); the B
+// fragments come from ldmatrix.trans, two output tiles per load.
 template <int NT>
-__device__ __forceinline__ void mma_layer(const __nv_bfloat16* Wt, const uint32_t (&a)[4][4], float (&acc)[NT][4],
-                                          int g, int t) {
+__device__ __forceinline__ void mma_layer_in_out(const __nv_bfloat16* Wl, int ld, const uint32_t (&a)[4][4],
+                                                 float (&acc)[NT][4], int lane) {
+  const int rr = lane & 7, q = lane >> 3;
 #pragma unroll
-  for (int nt = 0; nt < NT; ++nt) {
-    acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
-    const __nv_bfloat16* row = Wt + (nt * 8 + g) * kLdT + 2 * t;
+  for (int nt = 0; nt < NT; ++nt) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
 #pragma unroll
-    for (int kt = 0; kt < 4; ++kt) {
-      const uint32_t b0 = *reinterpret_cast<const uint32_t*>(row + kt * 16);
-      const uint32_t b1 = *reinterpret_cast<const uint32_t*>(row + kt * 16 + 8);
-      mma_bf16(acc[nt], a[kt], b0, b1);
+  for (int kt = 0; kt < 4; ++kt) {
+#pragma unroll
+    for (int np = 0; np < NT / 2; ++np) {
+      uint32_t b[4];  // (in 16kt.., out 16np..), (in +8, out), (in, out +8), (in +8, out +8)
+      ldsm_x4_t(b, Wl + (kt * 16 + rr + 8 * (q & 1)) * ld + np * 16 + 8 * (q >> 1));
+      mma_bf16(acc[2 * np], a[kt], b[0], b[1]);
+      mma_bf16(acc[2 * np + 1], a[kt], b[2], b[3]);
     }
   }
 }
@@ -148,16 +158,17 @@ __device__ __forceinline__ void encode_a(const NrcRecord& r, bool valid, f3 b0, 
 
 // Forward of rows g and g+8 of one 16-sample tile: outputs y (cols 0..2)
 // land in lanes with t == 0 (row g in yg, row g + 8 in yh).
-__device__ __forceinline__ void mlp_forward_mma(const __nv_bfloat16* Wt, uint32_t (&a)[4][4], int g, int t,
+// W holds the weights in the shared [in][out] layout (load_weights).
+__device__ __forceinline__ void mlp_forward_mma(const __nv_bfloat16* W, uint32_t (&a)[4][4], int lane,
                                                 float (&yg)[3], float (&yh)[3]) {
 #pragma unroll 1
   for (int l = 0; l < kNrcHidden; ++l) {
     float acc[8][4];
-    mma_layer<8>(Wt + l * kNrcWidth * kLdT, a, acc, g, t);
+    mma_layer_in_out<8>(W + woff(l), ldw(l), a, acc, lane);
     relu_to_a(acc, a);
   }
   float out[2][4];
-  mma_layer<2>(Wt + kNrcHidden * kNrcWidth * kLdT, a, out, g, t);
+  mma_layer_in_out<2>(W + woff(kNrcHidden), ldw(kNrcHidden), a, out, lane);
   // tile 0 holds cols 2t, 2t+1: lane t = 0 has cols 0, 1 and lane t = 1 col 2
   const float c2g = __shfl_down_sync(0xffffffffu, out[0][0], 1);
   const float c2h = __shfl_down_sync(0xffffffffu, out[0][2], 1);
