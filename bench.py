@@ -24,13 +24,16 @@ time_to_1pct: the headline comparison on the same scene.  R is an FP64
          the per-sample relative variance measured from R's halves (the
          measured curve is reported beside it); time = passes to 1 % x
          measured pass time.  Cached tracker (paths end in the radiance
-         cache after 2 events, 65,536 training records a frame, Adam lr
-         1e-3, moving-average weights for queries): a warm-up of 6,000 Adam
-         steps (300 training launches, each followed by 19 more steps on
-         16,384-record batches of the same records), then frames until its
-         corrected error reaches 1 %: every 3rd frame traces new training
-         paths in its launch and steps on them, the others render and step
-         once more on those records; time = warm-up + frames, device-timed.
+         cache after 2 events, Adam lr 1e-3, moving-average weights for
+         queries): a warm-up of 6,000 Adam steps on 16,384-record batches
+         (9 training launches of 32 sets of ~65,536 records each; a
+         training-only launch lasts as long as its longest path, so one
+         launch of 32 sets costs about 3 of one set), then frames until its
+         corrected error reaches 1 %: each frame renders and takes one Adam
+         step on the next 65,536 records of a pool of 32 training sets,
+         traced in one launch every 96 frames (training paths never read
+         the weights, so the pool is as good as per-frame paths); time =
+         warm-up + frames, device-timed.
 --impl reference: the CPU restatement of the reference's tracker (the
          oracle) on all host cores, on a bounded sample of the same passes.
 """
@@ -245,7 +248,7 @@ def run_vcr(args):
 
 
 CONV = {"ref_passes": 4000, "plain_passes": 1000, "warm_steps": 6000, "warm_sets": 32, "warm_more": 19, "warm_batch": 16384,
-        "train_every": 3, "reuse_steps": 1, "max_frames": 8000, "chunk": 500, "spp": 1, "train_samples": 65536,
+        "pool_sets": 32, "pool_every": 96, "max_frames": 8000, "chunk": 500, "spp": 1, "train_samples": 65536,
         "learning_rate": 1e-3, "ema_decay": 0.99, "nrc_events": 2, "repeats": 3}
 
 
@@ -351,8 +354,18 @@ def cached_time_to_1pct(ctx, sc, stream, ref, cfg):
     done = 0
     more = cfg.get("frame_more", 0)
     every = cfg.get("train_every", 1)  # frames between training frames (0: none after the warm-up)
+    pool = cfg.get("pool_sets", 0)
 
     def frame(k):
+        if pool:
+            # render-only frames; their Adam steps walk a pool of pool_sets
+            # training sets, traced in one launch every pool_every frames
+            ctx.pt_pass(seed=500 ^ 0x5bd1e995, pass_index=batches + k, spp=spp, stream=sh)
+            if k % cfg["pool_every"] == 0:
+                ctx.nrc_train_step(seed=600, pass_index=k // cfg["pool_every"], stream=sh, sets=pool)
+            else:
+                ctx.nrc_train_more(1, max_records=cfg.get("frame_batch", cfg["train_samples"]), stream=sh)
+            return
         if every and k % every == 0:
             ctx.nrc_frame(seed=500, pass_index=batches + k, spp=spp, stream=sh)
             if more:

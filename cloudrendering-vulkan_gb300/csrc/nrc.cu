@@ -636,8 +636,11 @@ vcr_status nrc_train_step(vcr_ctx* ctx, const vcr_pass_desc* pass, cudaStream_t 
   }
   if (vs) return vs;
   st->sets = sets;
-  vs = nrc_update(ctx, s);
+  // one set: a step over all its records; several: over the first
+  // train_samples, and vcr_nrc_train_more continues after them
+  vs = sets == 1 ? nrc_update(ctx, s) : nrc_update(ctx, s, 0, st->prm.train_samples);
   if (vs) return vs;
+  st->cursor = sets == 1 ? 0u : st->prm.train_samples;
   VCR_CUDA(ctx, cudaEventRecord(ctx->work_done, s));
   return VCR_OK;
 }
@@ -666,6 +669,7 @@ vcr_status nrc_frame(vcr_ctx* ctx, const vcr_pass_desc* pass, cudaStream_t s) {
   }
   if (vs) return vs;
   ctx->nrc->sets = 1;
+  ctx->nrc->cursor = 0;
   vs = nrc_update(ctx, s);
   if (vs) return vs;
   VCR_CUDA(ctx, cudaEventRecord(ctx->work_done, s));
@@ -704,13 +708,16 @@ extern "C" VCR_API vcr_status vcr_nrc_train_more(vcr_ctx* ctx, uint32_t steps, u
   if (!ctx->nrc) return fail(ctx, VCR_ERR_STATE, "no radiance cache");
   if (ctx->nrc->step == 0) return fail(ctx, VCR_ERR_STATE, "no training records yet (vcr_nrc_train_step)");
   cudaStream_t s = (cudaStream_t)stream;
-  const uint32_t want = ctx->nrc->prm.train_samples * ctx->nrc->sets;
+  NrcState* st = ctx->nrc;
+  const uint32_t want = st->prm.train_samples * st->sets;
   const uint32_t batch = (max_records && max_records < want) ? max_records : 0u;
-  const uint32_t subsets = batch ? want / batch : 1u;
   for (uint32_t k = 0; k < steps; ++k) {
-    // consecutive steps walk through the records batch by batch
-    vcr_status vs = batch ? nrc_update(ctx, s, (k % subsets) * batch, batch) : nrc_update(ctx, s);
+    // consecutive steps, and consecutive calls, walk through the records
+    // batch by batch, from the start again after the last whole batch
+    if (batch && st->cursor + batch > want) st->cursor = 0;
+    vcr_status vs = batch ? nrc_update(ctx, s, st->cursor, batch) : nrc_update(ctx, s);
     if (vs) return vs;
+    if (batch) st->cursor += batch;
   }
   VCR_CUDA(ctx, cudaEventRecord(ctx->work_done, s));
   return VCR_OK;

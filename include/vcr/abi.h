@@ -383,9 +383,11 @@ VCR_API vcr_status vcr_nrc_train_step(vcr_ctx* ctx, const vcr_pass_desc* pass, v
 VCR_API vcr_status vcr_nrc_frame(vcr_ctx* ctx, const vcr_pass_desc* pass, void* stream);
 /* `steps` further gradient + Adam steps on the records of the last training
  * step (all its sets) or frame (a cheap warm-up: the records are reused,
- * not re-traced).
+ * not re-traced).  A step of several sets takes its own Adam step on their
+ * first train_samples records.
  * max_records > 0 makes each step use a batch of that many records, the
- * steps walking through the records batch by batch; 0 uses them all. */
+ * steps (and the next calls) walking through the records batch by batch
+ * until new records are traced; 0 uses them all. */
 VCR_API vcr_status vcr_nrc_train_more(vcr_ctx* ctx, uint32_t steps, uint32_t max_records, void* stream);
 VCR_API vcr_status vcr_nrc_info(vcr_ctx* ctx, vcr_nrc_info_t* out);
 VCR_API vcr_status vcr_nrc_get_weights(vcr_ctx* ctx, float* host_out, size_t count);
