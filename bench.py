@@ -332,7 +332,8 @@ def cached_time_to_1pct(ctx, sc, stream, ref, cfg):
     prm = sc.params(vcr.TRACKER_DDA)
     prm.nrc_events = cfg["nrc_events"]
     ctx.set_params(prm)
-    ctx.nrc_setup(train_samples=cfg["train_samples"], learning_rate=cfg["learning_rate"], query_capacity=px * spp,
+    ctx.nrc_setup(train_samples=cfg["train_samples"], learning_rate=cfg.get("warm_lr", cfg["learning_rate"]),
+                  query_capacity=px * spp,
                   seed=1, ema_decay=cfg["ema_decay"], tail_survival=cfg.get("tail_survival", 0.0))
     sets = cfg.get("warm_sets", 1)
     per_launch = sets * (1 + cfg["warm_more"])  # Adam steps a training launch feeds
@@ -346,6 +347,7 @@ def cached_time_to_1pct(ctx, sc, stream, ref, cfg):
     b.record(stream)
     b.synchronize()
     warm_ms = a.elapsed_time(b)
+    ctx.nrc_set_learning_rate(cfg["learning_rate"])
     ctx.reset()
     nmax, chunk = cfg["max_frames"], cfg["chunk"]
     errs = torch.zeros(nmax, dtype=torch.float64, device="cuda")

@@ -18,6 +18,7 @@
 // weight per CTA cost as much as the tiles themselves).  Adam runs on FP32
 // master weights and refreshes the BF16 copies (training weights, and the
 // moving average the queries use).
+#include <cmath>
 #include <cstring>
 
 #include "nrc.cuh"
@@ -720,6 +721,15 @@ extern "C" VCR_API vcr_status vcr_nrc_train_more(vcr_ctx* ctx, uint32_t steps, u
     if (batch) st->cursor += batch;
   }
   VCR_CUDA(ctx, cudaEventRecord(ctx->work_done, s));
+  return VCR_OK;
+}
+
+extern "C" VCR_API vcr_status vcr_nrc_set_learning_rate(vcr_ctx* ctx, float learning_rate) {
+  if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  if (!ctx->nrc) return fail(ctx, VCR_ERR_STATE, "no radiance cache");
+  if (!(learning_rate > 0.0f) || !std::isfinite(learning_rate))
+    return fail(ctx, VCR_ERR_INVALID, "learning rate must be finite and > 0");
+  ctx->nrc->prm.learning_rate = learning_rate;  // read on the host when the next step is enqueued
   return VCR_OK;
 }
 

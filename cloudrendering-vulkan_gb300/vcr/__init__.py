@@ -246,6 +246,9 @@ class Context:
     def nrc_train_more(self, steps, max_records=0, stream=0):
         self._ck(lib().vcr_nrc_train_more(self.h, steps, max_records, C.c_void_p(stream)))
 
+    def nrc_set_learning_rate(self, learning_rate):
+        self._ck(lib().vcr_nrc_set_learning_rate(self.h, learning_rate))
+
     def nrc_info(self) -> dict:
         i = _abi.NrcInfo()
         self._ck(lib().vcr_nrc_info(self.h, C.byref(i)))

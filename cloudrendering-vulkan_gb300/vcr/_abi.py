@@ -161,6 +161,7 @@ SIGNATURES = {
     "vcr_nrc_train_step": (_S, [_P, C.POINTER(PassDesc), _P]),
     "vcr_nrc_frame": (_S, [_P, C.POINTER(PassDesc), _P]),
     "vcr_nrc_train_more": (_S, [_P, _u32, _u32, _P]),
+    "vcr_nrc_set_learning_rate": (_S, [_P, C.c_float]),
     "vcr_nrc_info": (_S, [_P, C.POINTER(NrcInfo)]),
     "vcr_nrc_get_weights": (_S, [_P, _P, _sz]),
     "vcr_nrc_set_weights": (_S, [_P, _P, _sz]),

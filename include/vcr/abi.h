@@ -389,6 +389,8 @@ VCR_API vcr_status vcr_nrc_frame(vcr_ctx* ctx, const vcr_pass_desc* pass, void* 
  * steps (and the next calls) walking through the records batch by batch
  * until new records are traced; 0 uses them all. */
 VCR_API vcr_status vcr_nrc_train_more(vcr_ctx* ctx, uint32_t steps, uint32_t max_records, void* stream);
+/* Adam step size for the following steps (> 0); the moments are kept. */
+VCR_API vcr_status vcr_nrc_set_learning_rate(vcr_ctx* ctx, float learning_rate);
 VCR_API vcr_status vcr_nrc_info(vcr_ctx* ctx, vcr_nrc_info_t* out);
 VCR_API vcr_status vcr_nrc_get_weights(vcr_ctx* ctx, float* host_out, size_t count);
 VCR_API vcr_status vcr_nrc_set_weights(vcr_ctx* ctx, const float* host, size_t count);

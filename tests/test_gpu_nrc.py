@@ -166,6 +166,10 @@ def test_a_step_traces_several_training_sets_in_one_launch(cuda):
         frame = ctx.nrc_info()["train_records"]
         with pytest.raises(vcr.VcrError):
             ctx.nrc_train_step(seed=5, pass_index=3, sets=65)
+        with pytest.raises(vcr.VcrError):
+            ctx.nrc_set_learning_rate(0.0)
+        ctx.nrc_set_learning_rate(5e-4)
+        ctx.nrc_train_more(1)
     assert 0.7 * 4 * 8192 <= four <= 1.4 * 4 * 8192, four
     assert 0.7 * 8192 <= one <= 1.4 * 8192 and 0.7 * 8192 <= frame <= 1.4 * 8192, (one, frame)
 
