@@ -56,7 +56,7 @@ __global__ void __launch_bounds__(kInferThreads, 3) nrc_infer_kernel(NrcView v, 
   extern __shared__ __align__(128) unsigned char smem[];
   bf16* W = reinterpret_cast<bf16*>(smem);
   float* dirs = reinterpret_cast<float*>(W + kWs);  // 16 level directions
-  load_weights(v.wbi, W);
+  load_weights<kInferThreads>(v.wbi, W);
   load_level_dirs(dirs);
   __syncthreads();
   const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
@@ -142,7 +142,7 @@ __global__ void __launch_bounds__(kTrainThreads, 1) nrc_train_kernel(NrcView v, 
   const uint32_t total = *count_ptr;
   const uint32_t count = total > first_rec ? min(total - first_rec, capacity) : 0u;
   if (blockIdx.x * kTrainTile >= count) return;
-  load_weights(v.wb, W);
+  load_weights<kTrainThreads>(v.wb, W);
   load_level_dirs(dirs);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
   const int rr = lane & 7, q = lane >> 3;
@@ -315,12 +315,19 @@ static_assert(kNrcWeightCount % kReduceCols == 0, "reduction tiling");
 // combined pairwise, then the four groups in order.  Without kAdam the sum
 // is added to grad; with kAdam the Adam step follows on grad + sum and grad
 // is cleared.  One launch of kNrcWeightCount / 64 CTAs: every weight's 152
-// loads are spread over four threads with eight in flight each.
+// loads are spread over four threads with eight in flight each.  Its first
+// thread also moves the step's loss sum to loss[1] and clears loss[0] for
+// the next step's training kernel.
 template <bool kAdam>
 __global__ void __launch_bounds__(kReduceCols * kReduceGroups)
     nrc_grad_reduce_kernel(const float* __restrict__ gpart, int blocks, const uint32_t* __restrict__ count_ptr,
-                           uint32_t capacity, uint32_t first_rec, float* __restrict__ grad, AdamView a, AdamStep h) {
+                           uint32_t capacity, uint32_t first_rec, float* __restrict__ grad, AdamView a, AdamStep h,
+                           float* __restrict__ loss) {
   __shared__ float part[kReduceGroups][kReduceCols];
+  if (blockIdx.x == 0 && threadIdx.x == 0) {  // the step's loss, and a zero sum for the next step
+    loss[1] = loss[0];
+    loss[0] = 0.0f;
+  }
   const int col = threadIdx.x % kReduceCols, grp = threadIdx.x / kReduceCols;
   const int i = blockIdx.x * kReduceCols + col;
   const uint32_t total = *count_ptr;
@@ -456,6 +463,7 @@ vcr_status nrc_setup(vcr_ctx* ctx, const vcr_nrc_params* p) {
   VCR_ALLOC(st->query_count, 4);
 #undef VCR_ALLOC
   VCR_CUDA(ctx, cudaMemset(st->train_count, 0, 4));
+  VCR_CUDA(ctx, cudaMemset(st->loss, 0, 8));
   std::vector<float> w;
   nrc_init_weights(w, p->seed);
   VCR_CUDA(ctx, cudaMemcpy(st->w, w.data(), kNrcWeightCount * 4, cudaMemcpyHostToDevice));
@@ -481,7 +489,6 @@ static vcr_status nrc_grad(vcr_ctx* ctx, const NrcRecord* recs, const uint32_t* 
                            cudaStream_t s, uint32_t first, bool adam) {
   NrcState* st = ctx->nrc;
   VCR_CUDA(ctx, cudaFuncSetAttribute(nrc_train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)train_smem()));
-  VCR_CUDA(ctx, cudaMemsetAsync(st->loss, 0, 8, s));
   const int blocks = st->gpart_blocks;
   nrc_train_kernel<<<blocks, kTrainThreads, train_smem(), s>>>(nrc_view(ctx), recs, d_count, capacity, first,
                                                                st->gpart, st->loss);
@@ -501,9 +508,11 @@ static vcr_status nrc_grad(vcr_ctx* ctx, const NrcRecord* recs, const uint32_t* 
   }
   const dim3 grid(kNrcWeightCount / kReduceCols), block(kReduceCols * kReduceGroups);
   if (adam)
-    nrc_grad_reduce_kernel<true><<<grid, block, 0, s>>>(st->gpart, blocks, d_count, capacity, first, st->grad, a, h);
+    nrc_grad_reduce_kernel<true><<<grid, block, 0, s>>>(st->gpart, blocks, d_count, capacity, first, st->grad, a, h,
+                                                        st->loss);
   else
-    nrc_grad_reduce_kernel<false><<<grid, block, 0, s>>>(st->gpart, blocks, d_count, capacity, first, st->grad, a, h);
+    nrc_grad_reduce_kernel<false><<<grid, block, 0, s>>>(st->gpart, blocks, d_count, capacity, first, st->grad, a, h,
+                                                         st->loss);
   VCR_CUDA(ctx, cudaGetLastError());
   return VCR_OK;
 }
@@ -746,7 +755,7 @@ extern "C" VCR_API vcr_status vcr_nrc_info(vcr_ctx* ctx, vcr_nrc_info_t* out) {
   VCR_CUDA(ctx, cudaEventSynchronize(ctx->work_done));
   float loss = 0.0f;
   uint32_t ntrain = 0, nq = 0;
-  VCR_CUDA(ctx, cudaMemcpy(&loss, st->loss, 4, cudaMemcpyDeviceToHost));
+  VCR_CUDA(ctx, cudaMemcpy(&loss, st->loss + 1, 4, cudaMemcpyDeviceToHost));
   VCR_CUDA(ctx, cudaMemcpy(&ntrain, st->train_count, 4, cudaMemcpyDeviceToHost));
   VCR_CUDA(ctx, cudaMemcpy(&nq, st->query_count, 4, cudaMemcpyDeviceToHost));
   out->steps = st->step;
@@ -843,7 +852,7 @@ extern "C" VCR_API vcr_status vcr_nrc_gradient(vcr_ctx* ctx, const void* d_recor
   if (vs) return vs;
   VCR_CUDA(ctx, cudaDeviceSynchronize());
   VCR_CUDA(ctx, cudaMemcpy(host_grad, ctx->nrc->grad, count * 4, cudaMemcpyDeviceToHost));
-  if (out_loss) VCR_CUDA(ctx, cudaMemcpy(out_loss, ctx->nrc->loss, 4, cudaMemcpyDeviceToHost));
+  if (out_loss) VCR_CUDA(ctx, cudaMemcpy(out_loss, ctx->nrc->loss + 1, 4, cudaMemcpyDeviceToHost));
   VCR_CUDA(ctx, cudaMemset(ctx->nrc->grad, 0, kNrcWeightCount * 4));
   return VCR_OK;
 }

@@ -58,7 +58,7 @@ struct NrcState {
   int gpart_blocks = 0;
   float* ema = nullptr;      // exponential moving average of w (ema_decay > 0)
   void* wbi = nullptr;       // BF16 copy of ema used for inference (ema_decay > 0)
-  float* loss = nullptr;     // [2]: loss sum, sample count of the last step
+  float* loss = nullptr;     // [2]: the running step's loss sum (zeroed by the reduction), the last step's loss
   NrcRecord* train = nullptr;  // training records [train_cap]
   uint32_t* train_count = nullptr;
   uint32_t train_cap = 0;      // 2 x train_samples x sets: room for the yield's spread

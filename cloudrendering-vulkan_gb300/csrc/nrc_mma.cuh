@@ -62,16 +62,30 @@ __device__ __forceinline__ void ldsm_x2_t(uint32_t (&r)[2], const void* p) {
 }
 
 // Global [in][out] BF16 weights (ld = cols) into the padded shared layout,
-// 16 bytes at a time.
+// 16 bytes at a time by a CTA of kThreads threads: all of a thread's loads
+// are issued before its stores, so the copy costs one L2 round trip, not
+// eleven.
+template <int kThreads>
 __device__ __forceinline__ void load_weights(const __nv_bfloat16* __restrict__ g, __nv_bfloat16* s) {
+  constexpr int kPieces = kNrcWeightCount / 8;
+  constexpr int kIters = (kPieces + kThreads - 1) / kThreads;
   const uint4* src = reinterpret_cast<const uint4*>(g);
-  for (int c = threadIdx.x; c < kNrcWeightCount / 8; c += blockDim.x) {
+  uint4 v[kIters];
+#pragma unroll
+  for (int k = 0; k < kIters; ++k) {
+    const int c = (int)threadIdx.x + k * kThreads;
+    if (c < kPieces) v[k] = src[c];
+  }
+#pragma unroll
+  for (int k = 0; k < kIters; ++k) {
+    const int c = (int)threadIdx.x + k * kThreads;
+    if (c >= kPieces) break;
     const int e = c * 8;
     const int l = e < kNrcHidden * kNrcWidth * kNrcWidth ? e / (kNrcWidth * kNrcWidth) : kNrcHidden;
     const int cols = nrc_layer_cols(l);
     const int rel = e - nrc_layer_offset(l);
     const int row = rel / cols, col = rel - row * cols;
-    *reinterpret_cast<uint4*>(s + woff(l) + row * ldw(l) + col) = src[c];
+    *reinterpret_cast<uint4*>(s + woff(l) + row * ldw(l) + col) = v[k];
   }
 }
 
