@@ -332,6 +332,10 @@ def cached_time_to_1pct(ctx, sc, stream, ref, cfg):
     prm = sc.params(vcr.TRACKER_DDA)
     prm.nrc_events = cfg["nrc_events"]
     ctx.set_params(prm)
+    plain_tuning = ctx.get_tuning()
+    if cfg.get("tune_cached"):  # the autotuner on the cached pass itself (untimed set-up, as for the plain one)
+        ctx.nrc_setup(train_samples=cfg["train_samples"], query_capacity=px * spp, seed=1)
+        ctx.autotune(seed=998, spp=spp, stream=sh)
     ctx.nrc_setup(train_samples=cfg["train_samples"], learning_rate=cfg.get("warm_lr", cfg["learning_rate"]),
                   query_capacity=px * spp,
                   seed=1, ema_decay=cfg["ema_decay"], tail_survival=cfg.get("tail_survival", 0.0))
@@ -386,7 +390,9 @@ def cached_time_to_1pct(ctx, sc, stream, ref, cfg):
                 hit = i
                 break
     info = ctx.nrc_info()
+    cached_tuning = ctx.get_tuning()
     ctx.set_params(sc.params(vcr.TRACKER_DDA))
+    ctx.set_tuning(**plain_tuning)
     e = errs[:done].cpu().numpy()
     frames_ms = np.cumsum(ms)
     return {"frames": (hit + 1) if hit is not None else None, "spp_per_frame": spp,
@@ -396,7 +402,7 @@ def cached_time_to_1pct(ctx, sc, stream, ref, cfg):
             "relrmse_last": round(ref.corrected(e[-1]), 5), "frames_run": done,
             "curve": {str(i + 1): round(ref.corrected(e[i]), 5) for i in (0, 9, 99, 499, 999, 1999, 3999, done - 1)
                       if i < done},
-            "train_records": info["train_records"], "loss": round(info["last_loss"], 4)}
+            "train_records": info["train_records"], "loss": round(info["last_loss"], 4), "tuning": cached_tuning}
 
 
 def convergence(ctx, sc, stream, args, overrides=None):
