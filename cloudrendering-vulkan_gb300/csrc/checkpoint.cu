@@ -221,6 +221,7 @@ extern "C" VCR_API vcr_status vcr_checkpoint_load(vcr_ctx* ctx, const char* path
       float* parts[] = {st->w, st->m, st->v, st->ema};
       for (int i = 0; i < 3 + (int)has_avg; ++i) VCR_CUDA(ctx, cudaMemcpy(parts[i], r.p + i * nb, nb, cudaMemcpyHostToDevice));
       st->step = step;
+      st->records = false;  // the records are not part of a checkpoint
       // the calibrated training-path count applies to the scene bound now
       st->npaths = npaths;
       st->calib_cam = ctx->cam;

@@ -645,6 +645,7 @@ vcr_status nrc_train_step(vcr_ctx* ctx, const vcr_pass_desc* pass, cudaStream_t 
     vs = nrc_launch_training(ctx, pv, st->npaths * sets, s);
   }
   if (vs) return vs;
+  st->records = true;
   st->sets = sets;
   // one set: a step over all its records; several: over the first
   // train_samples, and vcr_nrc_train_more continues after them
@@ -678,6 +679,7 @@ vcr_status nrc_frame(vcr_ctx* ctx, const vcr_pass_desc* pass, cudaStream_t s) {
     vs = pt_pass_launch(ctx, pass, s, &ts);
   }
   if (vs) return vs;
+  ctx->nrc->records = true;
   ctx->nrc->sets = 1;
   ctx->nrc->cursor = 0;
   vs = nrc_update(ctx, s);
@@ -716,7 +718,8 @@ extern "C" VCR_API vcr_status vcr_nrc_train_more(vcr_ctx* ctx, uint32_t steps, u
                                                  void* stream) {
   if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
   if (!ctx->nrc) return fail(ctx, VCR_ERR_STATE, "no radiance cache");
-  if (ctx->nrc->step == 0) return fail(ctx, VCR_ERR_STATE, "no training records yet (vcr_nrc_train_step)");
+  if (!ctx->nrc->records)
+    return fail(ctx, VCR_ERR_STATE, "no training records (vcr_nrc_train_step or vcr_nrc_frame first)");
   cudaStream_t s = (cudaStream_t)stream;
   NrcState* st = ctx->nrc;
   const uint32_t want = st->prm.train_samples * st->sets;

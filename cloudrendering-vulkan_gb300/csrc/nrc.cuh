@@ -64,6 +64,7 @@ struct NrcState {
   uint32_t train_cap = 0;      // 2 x train_samples x sets: room for the yield's spread
   uint32_t sets = 1;           // training sets (of ~train_samples records) in the buffer
   uint32_t cursor = 0;         // first record of the next vcr_nrc_train_more batch
+  bool records = false;        // the buffer holds a training step's or frame's records
   NrcRecord* query = nullptr;  // cache queries of one pass [query_capacity]
   uint32_t* query_count = nullptr;
   uint32_t query_capacity = 0;

@@ -153,6 +153,8 @@ def test_a_step_traces_several_training_sets_in_one_launch(cuda):
         prm.nrc_events = 2
         ctx.set_params(prm)
         ctx.nrc_setup(train_samples=8192, seed=3)
+        with pytest.raises(vcr.VcrError):  # nothing traced yet
+            ctx.nrc_train_more(1)
         ctx.nrc_train_step(seed=5, pass_index=0, sets=4)  # calibrates, then traces four sets
         four = ctx.nrc_info()["train_records"]
         w0 = ctx.nrc_get_weights()
