@@ -282,8 +282,15 @@ void TechniquePPB::RecordPass(void* stream, uint32_t passIndex) {
 // ---------------------------------------------------------------------------
 // TechniqueNRC
 // ---------------------------------------------------------------------------
-TechniqueNRC::TechniqueNRC(Device& device, PushConstants* pushConstants, const vcr_nrc_params& cache)
-    : RenderTechnique(device, pushConstants), cache_(cache) {}
+TechniqueNRC::TechniqueNRC(Device& device, PushConstants* pushConstants, const vcr_nrc_params& cache,
+                           const NrcSchedule& schedule)
+    : RenderTechnique(device, pushConstants), cache_(cache), schedule_(schedule) {}
+
+namespace {
+// Seeds of the training-set launches: a stream of their own, apart from
+// the camera passes' and from each other's (pass index = launch count).
+constexpr uint32_t kTrainSetSeedSalt = 0x6A09E667u;
+}  // namespace
 
 TechniqueNRC::~TechniqueNRC() {
   if (allocated_) vcr_nrc_free(Context());
@@ -292,6 +299,24 @@ TechniqueNRC::~TechniqueNRC() {
 void TechniqueNRC::AllocateResources() {
   Check(vcr_nrc_setup(Context(), &cache_), Context());
   allocated_ = true;
+  passes_ = 0;
+  launches_ = 0;
+}
+
+void TechniqueNRC::Warmup(void* stream, uint32_t steps, uint32_t sets, uint32_t batch) {
+  Require(allocated_, "TechniqueNRC::AllocateResources first");
+  Require(sets >= 1, "TechniqueNRC::Warmup needs sets >= 1");
+  const uint32_t records = batch ? batch : cache_.train_samples;
+  // steps per launch: every set walked about as often as the bench's warm-up walks it
+  const uint32_t perLaunch = std::max(1u, sets * (cache_.train_samples / std::max(records, 1u)) * 5u);
+  for (uint32_t done = 0; done < steps;) {
+    vcr_pass_desc t = PassDesc(launches_++, sets);
+    t.seed ^= kTrainSetSeedSalt;
+    Check(vcr_nrc_train_step(Context(), &t, stream), Context());
+    const uint32_t more = std::min(perLaunch, steps - done) - 1u;
+    if (more) Check(vcr_nrc_train_more(Context(), more, records, stream), Context());
+    done += more + 1u;
+  }
 }
 
 void TechniqueNRC::FreeResources() {
@@ -302,7 +327,20 @@ void TechniqueNRC::FreeResources() {
 void TechniqueNRC::RecordPass(void* stream, uint32_t passIndex) {
   Require(allocated_, "TechniqueNRC::AllocateResources first");
   vcr_pass_desc p = PassDesc(passIndex);
-  Check(vcr_nrc_frame(Context(), &p, stream), Context());
+  if (schedule_.poolSets == 0) {
+    Check(vcr_nrc_frame(Context(), &p, stream), Context());
+  } else {
+    Check(vcr_pt_pass(Context(), &p, stream), Context());
+    if (passes_ % std::max(schedule_.poolEvery, 1u) == 0) {
+      vcr_pass_desc t = PassDesc(launches_++, schedule_.poolSets);
+      t.seed ^= kTrainSetSeedSalt;
+      Check(vcr_nrc_train_step(Context(), &t, stream), Context());
+    } else {
+      const uint32_t records = schedule_.batch ? schedule_.batch : cache_.train_samples;
+      Check(vcr_nrc_train_more(Context(), 1, records, stream), Context());
+    }
+  }
+  ++passes_;
   Advance();
 }
 

@@ -185,18 +185,41 @@ class VCR_API TechniquePPB : public RenderTechnique {
   bool allocated_ = false;
 };
 
+/* How TechniqueNRC trains while it renders.  poolSets = 0: every pass is a
+ * vcr_nrc_frame (its training paths run in the pass's own launch, whose
+ * length their deepest path sets).  poolSets = S > 0: every pass is a
+ * vcr_pt_pass ending in the cache plus one Adam step on the next `batch`
+ * records (0: train_samples) of a pool of S training sets, traced in one
+ * launch every poolEvery passes.  Training paths never read the weights, so
+ * pooled records train as well as per-pass ones, and one launch of S sets
+ * costs about as much as three of one set. */
+struct NrcSchedule {
+  uint32_t poolSets = 0;
+  uint32_t poolEvery = 96;
+  uint32_t batch = 0;
+};
+
 /* The DDA tracker with the learned radiance cache: paths end in the cache
  * after params.nrc_events events; every pass also trains it. */
 class VCR_API TechniqueNRC : public RenderTechnique {
  public:
-  TechniqueNRC(Device& device, PushConstants* pushConstants, const vcr_nrc_params& cache);
+  TechniqueNRC(Device& device, PushConstants* pushConstants, const vcr_nrc_params& cache,
+               const NrcSchedule& schedule = NrcSchedule());
   ~TechniqueNRC() override;
   void AllocateResources() override;
   void FreeResources() override;
   void RecordPass(void* stream, uint32_t passIndex) override;
+  /* Training before the first pass: at least `steps` Adam steps, from
+   * launches of `sets` training sets (vcr_nrc_train_step with pass.spp =
+   * sets), each walked by vcr_nrc_train_more in batches of `batch` records
+   * (0: train_samples).  Needs the camera, cloud and frame bound. */
+  void Warmup(void* stream, uint32_t steps, uint32_t sets, uint32_t batch);
 
  private:
   vcr_nrc_params cache_;
+  NrcSchedule schedule_;
+  uint32_t passes_ = 0;    // passes since AllocateResources
+  uint32_t launches_ = 0;  // training-set launches since AllocateResources
   bool allocated_ = false;
 };
 

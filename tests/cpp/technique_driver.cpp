@@ -7,7 +7,7 @@
 //   [u32 passes][f32 pmRadius][f32 mean image w*h*3]
 // to the output file, so a test can re-render the same structs through
 // the C-ABI and compare.
-//   technique_driver <pt|ppm|ppb|nrc|misuse> <out> [passes]
+//   technique_driver <pt|ppm|ppb|nrc|nrcpool|misuse> <out> [passes]
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -35,7 +35,7 @@ static vcr_params scene_params() {
 
 int main(int argc, char** argv) {
   if (argc < 3) {
-    std::fprintf(stderr, "usage: %s <pt|ppm|ppb|nrc|misuse> <out> [passes]\n", argv[0]);
+    std::fprintf(stderr, "usage: %s <pt|ppm|ppb|nrc|nrcpool|misuse> <out> [passes]\n", argv[0]);
     return 2;
   }
   const std::string mode = argv[1];
@@ -69,10 +69,16 @@ int main(int argc, char** argv) {
     vcr::TechniquePPB ppb(device, &pc, pb);
     vcr_nrc_params nc{4096, 1e-3f, W * H, 1, 0.0f};
     vcr::TechniqueNRC nrc(device, &pc, nc);
+    vcr::NrcSchedule pool;  // a pool of 4 sets re-traced every 2nd pass, 1,024-record steps
+    pool.poolSets = 4;
+    pool.poolEvery = 2;
+    pool.batch = 1024;
+    vcr::TechniqueNRC nrcpool(device, &pc, nc, pool);
     if (mode == "pt") tech = &pt;
     else if (mode == "ppm") tech = &ppm;
     else if (mode == "ppb") tech = &ppb;
     else if (mode == "nrc") tech = &nrc;
+    else if (mode == "nrcpool") tech = &nrcpool;
     else if (mode == "misuse") {
       // a pass before the frame target and before AllocateResources must
       // throw vcr::Error (the reference aborts instead)
@@ -87,7 +93,7 @@ int main(int argc, char** argv) {
       std::fprintf(stderr, "unknown technique %s\n", mode.c_str());
       return 2;
     }
-    if (mode == "nrc") prm.nrc_events = 2;
+    if (mode == "nrc" || mode == "nrcpool") prm.nrc_events = 2;
 
     tech->BindCloud(grid, cloud, VCR_PREC_FP32);
     tech->BindCamera(cam);
@@ -95,6 +101,7 @@ int main(int argc, char** argv) {
     tech->SetFrameTarget(W, H);
     tech->Commit();
     tech->AllocateResources();
+    if (mode == "nrcpool") nrcpool.Warmup(nullptr, 40, 4, 1024);  // 40 steps from 4-set launches
     for (int k = 0; k < passes; ++k) tech->RecordPass(nullptr, (uint32_t)k);
     device.Synchronize();
     std::vector<float> img = tech->ReadMean();

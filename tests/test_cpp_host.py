@@ -90,7 +90,7 @@ def test_technique_pt_equals_the_c_abi_path(cuda, tmp_path):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("mode", ["ppm", "ppb", "nrc"])
+@pytest.mark.parametrize("mode", ["ppm", "ppb", "nrc", "nrcpool"])
 def test_other_techniques_render(cuda, tmp_path, mode):
     exe = _build(tmp_path)
     _run(exe, mode, tmp_path / f"{mode}.bin", 3)
