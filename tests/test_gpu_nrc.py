@@ -50,10 +50,11 @@ def test_forward_matches_oracle(cuda):
     assert np.abs(got - ref).mean() <= 3e-3 * scale
 
 
-def test_gradient_matches_oracle(cuda):
+@pytest.mark.parametrize("n", [4096, 20037])  # whole tiles; a ragged last tile and two tiles on some CTAs
+def test_gradient_matches_oracle(cuda, n):
     desc, cloud = _cloud()
     rng = np.random.default_rng(2)
-    recs = onrc.random_records(4096, cloud, rng)
+    recs = onrc.random_records(n, cloud, rng)
     with vcr.Context() as ctx:
         _ctx_with_cloud(ctx, desc, cloud)
         ctx.nrc_setup(train_samples=4096, seed=11)
