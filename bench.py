@@ -44,6 +44,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -103,8 +104,8 @@ class Clocks:
     """nvidia-smi sampling during the timed region."""
 
     def __init__(self, index: int):
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
-        os.makedirs(os.path.dirname(self.path), exist_ok=True)
+        fd, self.path = tempfile.mkstemp(prefix="vcr_clocks_", suffix=".csv")
+        os.close(fd)
         q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -138,6 +139,10 @@ class Clocks:
             for n, v in zip(names, parts[5:9]):
                 if v.lower().startswith("active"):
                     reasons.add(n)
+        try:
+            os.remove(self.path)
+        except OSError:
+            pass
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": sorted(reasons), "samples": len(sm)}
 
@@ -690,8 +695,8 @@ class OracleScene:
     benchmark scene, generated by the oracle's own fBm on all host cores."""
 
     def __init__(self, sc, threads=None):
-        import vcr
         from oracle import oracle as orc
+        from vcr import _abi
 
         self.sc = sc
         self.threads = threads or os.cpu_count() or 1
@@ -700,9 +705,10 @@ class OracleScene:
         self.g = orc.Grid(dense, sc.precision)
         del dense
         self.setup_s = time.perf_counter() - t0
-        self.cloud = sc.cloud()
+        # the scene's structs from the oracle's restatement of the reference's
+        # set-up: this leg loads no product library
+        _, self.cloud, self.cam, self.prm = orc.scene_structs(sc, _abi.TRACKER_DDA)
         self.cloud.max_extinction = max(self.g.max_density(), 0.01)
-        self.cam, self.prm = sc.camera(), sc.params(vcr.TRACKER_DDA)
 
     def pass_rows(self, rows, pass_index):
         """One pass over `rows` full-width image rows in (up to) 8 bands

@@ -130,6 +130,7 @@ static vcr_status batch_table(vcr_ctx* ctx, uint32_t spp, cudaStream_t s) {
 
 extern "C" VCR_API vcr_status vcr_batch_pass(vcr_ctx* ctx, const vcr_pass_desc* pass, void* stream) {
   if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
   PassView pv;
   vcr_status vs = batch_check(ctx, pass, pv);
   if (vs) return vs;
@@ -147,6 +148,7 @@ extern "C" VCR_API vcr_status vcr_batch_pass(vcr_ctx* ctx, const vcr_pass_desc* 
 
 extern "C" VCR_API vcr_status vcr_batch_graph_record(vcr_ctx* ctx, const vcr_pass_desc* pass) {
   if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
   PassView pv;
   vcr_status vs = batch_check(ctx, pass, pv);
   if (vs) return vs;
@@ -181,6 +183,7 @@ extern "C" VCR_API vcr_status vcr_batch_graph_record(vcr_ctx* ctx, const vcr_pas
 
 extern "C" VCR_API vcr_status vcr_batch_graph_replay(vcr_ctx* ctx, uint32_t count, void* stream) {
   if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
   BatchState* b = ctx->batch;
   if (!b || !b->exec) return fail(ctx, VCR_ERR_STATE, "no recorded batch graph");
   cudaStream_t s = (cudaStream_t)stream;
@@ -196,6 +199,7 @@ extern "C" VCR_API vcr_status vcr_batch_graph_replay(vcr_ctx* ctx, uint32_t coun
 extern "C" VCR_API vcr_status vcr_batch_autotune(vcr_ctx* ctx, const vcr_pass_desc* pass, vcr_tuning* out,
                                                  void* stream) {
   if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
   PassView pv;
   vcr_status vs = batch_check(ctx, pass, pv);
   if (vs) return vs;
@@ -239,6 +243,7 @@ extern "C" VCR_API vcr_status vcr_batch_autotune(vcr_ctx* ctx, const vcr_pass_de
 
 extern "C" VCR_API vcr_status vcr_batch_read(vcr_ctx* ctx, uint32_t view, double* out, size_t bytes) {
   if (!ctx || !out) return fail(ctx, VCR_ERR_INVALID, "null argument");
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
   BatchState* b = ctx->batch;
   if (!b) return fail(ctx, VCR_ERR_STATE, "no batch");
   if (view >= b->views.size()) return fail(ctx, VCR_ERR_INVALID, "view %u of %zu", view, b->views.size());
@@ -262,6 +267,7 @@ extern "C" VCR_API vcr_status vcr_batch_info(vcr_ctx* ctx, vcr_batch_info_t* out
 
 extern "C" VCR_API vcr_status vcr_batch_reset(vcr_ctx* ctx) {
   if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
   if (!ctx->batch) return fail(ctx, VCR_ERR_STATE, "no batch");
   VCR_CUDA(ctx, cudaEventSynchronize(ctx->work_done));
   return batch_clear(ctx);
@@ -269,6 +275,7 @@ extern "C" VCR_API vcr_status vcr_batch_reset(vcr_ctx* ctx) {
 
 extern "C" VCR_API vcr_status vcr_batch_free(vcr_ctx* ctx) {
   if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
   cudaDeviceSynchronize();
   batch_free(ctx);
   return VCR_OK;

@@ -4,18 +4,26 @@
 // of the process (frameCount and the accumulated image, main.cpp:262,
 // PathTracer.comp:420-424; pmRadius, RenderTechniquePPM.cpp:302-312).
 //
-// File: "VCRCKPT\0", u32 version (1), u32 section count, then sections of
+// File: "VCRCKPT\0", u32 version (2), u32 section count, then sections of
 // { char tag[4]; u32 zero; u64 bytes; payload }:
+//   SCEN  u64 scene hash (always first): FNV-1a over the grid description
+//         and precision, the level-0 majorants (per-brick maxima of the
+//         density, a fingerprint of its content), the cloud, camera and
+//         parameter structs, and the batch's views and the photon-map
+//         parameters when those are set up
 //   FRAM  u32 width, height, passes, 0; u64 samples; f64 sums [w*h*3]
 //   PPMS  u64 pixels; f64 statistics [pixels*8] (N, R, tau rgb, bg rgb)
 //   NRCW  u32 step, has_average, training paths per step, weight count;
 //         f32 weights, Adam m, Adam v [, moving average]
 //   BTCH  u64 pixels; u32 passes, 0; u64 samples; f64 sums [pixels*3]
-// Loading checks every section against the context's current setup (same
-// frame size, the technique set up with the same sizes) and leaves the
-// rest of the context as it is; unknown tags are skipped.
+// Loading checks every section against the context's current setup (the
+// same scene hash, frame size, the technique set up with the same sizes)
+// and leaves the rest of the context as it is; unknown tags are skipped.
+// Section lengths are checked against the bytes left in the file, so a
+// truncated or corrupt file is an I/O error, not an allocation failure.
 #include <cstring>
 #include <fstream>
+#include <new>
 
 #include "batch.cuh"
 #include "nrc.cuh"
@@ -24,7 +32,7 @@
 namespace vcr {
 
 static const char kMagic[8] = {'V', 'C', 'R', 'C', 'K', 'P', 'T', '\0'};
-constexpr uint32_t kCkptVersion = 1;
+constexpr uint32_t kCkptVersion = 2;
 
 struct Section {
   char tag[4];
@@ -44,7 +52,58 @@ static vcr_status put_device(vcr_ctx* ctx, std::vector<uint8_t>& v, const void* 
   return VCR_OK;
 }
 
+// FNV-1a, 64 bits.
+struct Fnv {
+  uint64_t h = 1469598103934665603ull;
+  void add(const void* p, size_t n) {
+    const uint8_t* b = static_cast<const uint8_t*>(p);
+    for (size_t i = 0; i < n; ++i) h = (h ^ b[i]) * 1099511628211ull;
+  }
+  template <typename T>
+  void add(const T& x) { add(&x, sizeof(T)); }
+};
+
+// Hash of what the progressive state was rendered from (see the file
+// header).  A part not bound hashes as a marker, so "no camera" differs
+// from any camera.
+static vcr_status scene_hash(vcr_ctx* ctx, uint64_t& out) {
+  Fnv f;
+  f.add((uint32_t)ctx->has_grid);
+  if (ctx->has_grid) {
+    for (int a = 0; a < 3; ++a) {
+      f.add(ctx->gdesc.size[a]);
+      f.add(ctx->gdesc.voxel_size[a]);
+    }
+    f.add(ctx->precision);
+    const size_t cells = (size_t)ctx->mnb[0][0] * ctx->mnb[0][1] * ctx->mnb[0][2];
+    std::vector<float> maj(cells);
+    VCR_CUDA(ctx, cudaMemcpy(maj.data(), ctx->d_majorants + ctx->moff[0], cells * sizeof(float),
+                             cudaMemcpyDeviceToHost));
+    f.add(maj.data(), cells * sizeof(float));
+  }
+  f.add((uint32_t)ctx->has_cloud);
+  if (ctx->has_cloud) f.add(ctx->cloud);
+  f.add((uint32_t)ctx->has_cam);
+  if (ctx->has_cam) f.add(ctx->cam);
+  f.add((uint32_t)ctx->has_params);
+  if (ctx->has_params) f.add(ctx->params);
+  f.add((uint32_t)(ctx->batch != nullptr));
+  if (ctx->batch) f.add(ctx->batch->views.data(), ctx->batch->views.size() * sizeof(vcr_view_desc));
+  f.add((uint32_t)(ctx->ppm != nullptr));
+  if (ctx->ppm) f.add(ctx->ppm->prm);
+  out = f.h;
+  return VCR_OK;
+}
+
 static vcr_status save_sections(vcr_ctx* ctx, std::vector<Section>& out) {
+  {
+    Section s{{'S', 'C', 'E', 'N'}, {}};
+    uint64_t h = 0;
+    vcr_status vs = scene_hash(ctx, h);
+    if (vs) return vs;
+    put(s.data, h);
+    out.push_back(std::move(s));
+  }
   if (ctx->d_sum) {
     Section s{{'F', 'R', 'A', 'M'}, {}};
     put(s.data, ctx->width);
@@ -155,15 +214,26 @@ extern "C" VCR_API vcr_status vcr_checkpoint_load(vcr_ctx* ctx, const char* path
   if (!f.read(magic, 8) || std::memcmp(magic, kMagic, 8) != 0 || !f.read(reinterpret_cast<char*>(hdr), 8))
     return fail(ctx, VCR_ERR_IO, "%s is not a vcr checkpoint", path);
   if (hdr[0] != kCkptVersion) return fail(ctx, VCR_ERR_UNSUPPORTED, "checkpoint version %u", hdr[0]);
+  const std::streamoff here = f.tellg();
+  f.seekg(0, std::ios::end);
+  const std::streamoff end = f.tellg();
+  f.seekg(here);
+  if (here < 0 || end < here || !f) return fail(ctx, VCR_ERR_IO, "cannot size %s", path);
+  uint64_t left = (uint64_t)(end - here);
   std::vector<Section> secs;
   for (uint32_t i = 0; i < hdr[1]; ++i) {
     Section s;
     uint32_t zero;
     uint64_t n;
-    if (!f.read(s.tag, 4) || !f.read(reinterpret_cast<char*>(&zero), 4) || !f.read(reinterpret_cast<char*>(&n), 8) ||
-        n > (1ull << 40))
+    if (left < 16 || !f.read(s.tag, 4) || !f.read(reinterpret_cast<char*>(&zero), 4) ||
+        !f.read(reinterpret_cast<char*>(&n), 8) || n > left - 16)
       return fail(ctx, VCR_ERR_IO, "truncated checkpoint %s", path);
-    s.data.resize(n);
+    left -= 16 + n;
+    try {
+      s.data.resize(n);
+    } catch (const std::bad_alloc&) {
+      return fail(ctx, VCR_ERR_IO, "checkpoint section of %llu bytes does not fit in host memory", (unsigned long long)n);
+    }
     if (!f.read(reinterpret_cast<char*>(s.data.data()), (std::streamsize)n))
       return fail(ctx, VCR_ERR_IO, "truncated checkpoint %s", path);
     secs.push_back(std::move(s));
@@ -171,6 +241,19 @@ extern "C" VCR_API vcr_status vcr_checkpoint_load(vcr_ctx* ctx, const char* path
   VCR_CUDA(ctx, cudaSetDevice(ctx->device));
   VCR_CUDA(ctx, cudaDeviceSynchronize());
   // validate every section before changing anything
+  if (secs.empty() || std::memcmp(secs[0].tag, "SCEN", 4) != 0 || secs[0].data.size() != sizeof(uint64_t))
+    return fail(ctx, VCR_ERR_IO, "%s has no scene hash", path);
+  {
+    uint64_t saved = 0, now = 0;
+    std::memcpy(&saved, secs[0].data.data(), sizeof saved);
+    vcr_status vs = scene_hash(ctx, now);
+    if (vs) return vs;
+    if (saved != now)
+      return fail(ctx, VCR_ERR_STATE,
+                  "checkpoint %s was saved for another scene (grid, cloud, camera, parameters, batch views or "
+                  "photon-map parameters differ)",
+                  path);
+  }
   for (const Section& s : secs) {
     Reader r{s.data.data(), s.data.size()};
     if (!std::memcmp(s.tag, "FRAM", 4)) {

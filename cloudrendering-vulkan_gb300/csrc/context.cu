@@ -4,6 +4,7 @@
 #include <cstring>
 #include <fstream>
 #include <cmath>
+#include <atomic>
 #include <thread>
 
 #include "vcr_internal.h"
@@ -193,6 +194,25 @@ extern "C" VCR_API vcr_status vcr_synchronize(vcr_ctx* ctx) {
   return VCR_OK;
 }
 
+namespace vcr {
+static std::atomic<uint32_t> g_sort_lookback{kDefaultSortLookback};
+static std::atomic<uint32_t> g_stage_wait{kDefaultStageWait};
+
+vcr_wait_limits wait_limits() { return vcr_wait_limits{g_sort_lookback.load(), g_stage_wait.load()}; }
+}  // namespace vcr
+
+extern "C" VCR_API vcr_status vcr_set_wait_limits(const vcr_wait_limits* limits) {
+  g_sort_lookback.store(limits ? limits->sort_lookback : kDefaultSortLookback);
+  g_stage_wait.store(limits ? limits->stage_wait : kDefaultStageWait);
+  return VCR_OK;
+}
+
+extern "C" VCR_API vcr_status vcr_get_wait_limits(vcr_wait_limits* out) {
+  if (!out) return fail(nullptr, VCR_ERR_INVALID, "null wait limits");
+  *out = wait_limits();
+  return VCR_OK;
+}
+
 // ---------------------------------------------------------------------------
 // parameter helpers (host restatements of UniformBuffers.h / main.cpp logic)
 // ---------------------------------------------------------------------------
@@ -346,6 +366,7 @@ extern "C" VCR_API vcr_status vcr_grid_generate(vcr_ctx* ctx, const vcr_grid_des
 
 extern "C" VCR_API vcr_status vcr_grid_info(vcr_ctx* ctx, float* out_max, uint32_t out_bricks[3]) {
   if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
   if (!ctx->has_grid) return fail(ctx, VCR_ERR_STATE, "no grid");
   if (out_max) *out_max = ctx->max_density;
   if (out_bricks)
@@ -355,6 +376,7 @@ extern "C" VCR_API vcr_status vcr_grid_info(vcr_ctx* ctx, float* out_max, uint32
 
 extern "C" VCR_API vcr_status vcr_grid_read_majorants(vcr_ctx* ctx, uint32_t level, float* host, size_t count) {
   if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
   if (!ctx->has_grid) return fail(ctx, VCR_ERR_STATE, "no grid");
   if (level > 3) return fail(ctx, VCR_ERR_INVALID, "majorant level %u (0..3)", level);
   const int* m = ctx->mnb[level];
@@ -366,6 +388,7 @@ extern "C" VCR_API vcr_status vcr_grid_read_majorants(vcr_ctx* ctx, uint32_t lev
 
 extern "C" VCR_API vcr_status vcr_set_tuning(vcr_ctx* ctx, const vcr_tuning* t) {
   if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
   if (!t || t->majorant_level > 3 || t->dda_steps == 0 || t->dda_steps > 4096 ||
       (t->block_threads != 128 && t->block_threads != 256))
     return fail(ctx, VCR_ERR_INVALID, "tuning: level 0..3, dda_steps 1..4096, block_threads 128 or 256");
@@ -382,6 +405,7 @@ extern "C" VCR_API vcr_status vcr_get_tuning(vcr_ctx* ctx, vcr_tuning* out) {
 extern "C" VCR_API vcr_status vcr_grid_sample(vcr_ctx* ctx, const float* d_pos, float* d_out, uint32_t n,
                                               void* stream) {
   if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
   if (!ctx->has_grid || !ctx->has_cloud) return fail(ctx, VCR_ERR_STATE, "sampling needs a grid and a cloud");
   if (n && (!d_pos || !d_out)) return fail(ctx, VCR_ERR_INVALID, "null buffer");
   return grid_sample_launch(ctx, d_pos, d_out, n, (cudaStream_t)stream);
@@ -462,6 +486,7 @@ extern "C" VCR_API vcr_status vcr_xyz_write(const char* path, const vcr_grid_des
 // ---------------------------------------------------------------------------
 extern "C" VCR_API vcr_status vcr_set_cloud(vcr_ctx* ctx, const vcr_cloud* cloud) {
   if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
   if (!cloud) return fail(ctx, VCR_ERR_INVALID, "null cloud");
   for (int a = 0; a < 3; ++a)
     if (!(cloud->bounds_max[a] > cloud->bounds_min[a])) return fail(ctx, VCR_ERR_INVALID, "empty cloud bounds");
@@ -477,6 +502,7 @@ extern "C" VCR_API vcr_status vcr_set_cloud(vcr_ctx* ctx, const vcr_cloud* cloud
 
 extern "C" VCR_API vcr_status vcr_set_camera(vcr_ctx* ctx, const vcr_camera* cam) {
   if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
   if (!cam) return fail(ctx, VCR_ERR_INVALID, "null camera");
   ctx->cam = *cam;
   ctx->has_cam = true;
@@ -485,6 +511,7 @@ extern "C" VCR_API vcr_status vcr_set_camera(vcr_ctx* ctx, const vcr_camera* cam
 
 extern "C" VCR_API vcr_status vcr_set_params(vcr_ctx* ctx, const vcr_params* p) {
   if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
   if (!p) return fail(ctx, VCR_ERR_INVALID, "null params");
   if (p->rng_mode > 1 || p->nee_mode > 1 || p->sky_mode > 1 || p->tracker > 1)
     return fail(ctx, VCR_ERR_INVALID, "bad mode enum");
@@ -515,6 +542,7 @@ extern "C" VCR_API vcr_status vcr_set_frame(vcr_ctx* ctx, uint32_t width, uint32
 
 extern "C" VCR_API vcr_status vcr_reset_accumulation(vcr_ctx* ctx) {
   if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
   if (!ctx->d_sum) return fail(ctx, VCR_ERR_STATE, "no frame");
   size_t px = (size_t)ctx->width * ctx->height;
   VCR_CUDA(ctx, cudaMemset(ctx->d_sum, 0, px * 3 * sizeof(double)));
@@ -526,18 +554,21 @@ extern "C" VCR_API vcr_status vcr_reset_accumulation(vcr_ctx* ctx) {
 
 extern "C" VCR_API vcr_status vcr_shadow_volume_build(vcr_ctx* ctx, const vcr_shadow_volume* sv, void* stream) {
   if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
   if (!sv) return fail(ctx, VCR_ERR_INVALID, "null shadow volume");
   return sv_build_launch(ctx, sv, (cudaStream_t)stream);
 }
 
 extern "C" VCR_API vcr_status vcr_pt_pass(vcr_ctx* ctx, const vcr_pass_desc* pass, void* stream) {
   if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
   if (!pass) return fail(ctx, VCR_ERR_INVALID, "null pass");
   return pt_pass_launch(ctx, pass, (cudaStream_t)stream);
 }
 
 extern "C" VCR_API vcr_status vcr_pt_counters(vcr_ctx* ctx, uint64_t out[4]) {
   if (!ctx || !out) return fail(ctx, VCR_ERR_INVALID, "null argument");
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
   unsigned long long c[4];
   VCR_CUDA(ctx, cudaEventSynchronize(ctx->work_done));
   VCR_CUDA(ctx, cudaMemcpy(c, ctx->d_counters, sizeof(c), cudaMemcpyDeviceToHost));
@@ -549,6 +580,7 @@ extern "C" VCR_API vcr_status vcr_dda_trace(vcr_ctx* ctx, const float* d_o, cons
                                             uint32_t max_cells, uint32_t* d_cells, float* d_t, uint32_t* d_count,
                                             void* stream) {
   if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
   if (!ctx->has_grid || !ctx->has_cloud) return fail(ctx, VCR_ERR_STATE, "DDA needs a grid and a cloud");
   if (n && (!d_o || !d_d || !d_cells || !d_t || !d_count || max_cells == 0))
     return fail(ctx, VCR_ERR_INVALID, "bad DDA buffers");
@@ -598,6 +630,7 @@ extern "C" VCR_API vcr_status vcr_readback(vcr_ctx* ctx, vcr_buffer_id id, void*
 
 extern "C" VCR_API vcr_status vcr_image_rel_rmse(vcr_ctx* ctx, const double* d_ref, double* d_out, void* stream) {
   if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
   if (!d_ref || !d_out) return fail(ctx, VCR_ERR_INVALID, "null reference or output");
   if (!ctx->d_sum) return fail(ctx, VCR_ERR_STATE, "no frame");
   cudaStream_t s = (cudaStream_t)stream;

@@ -703,6 +703,7 @@ extern "C" VCR_API vcr_status vcr_nrc_setup(vcr_ctx* ctx, const vcr_nrc_params* 
 
 extern "C" VCR_API vcr_status vcr_nrc_free(vcr_ctx* ctx) {
   if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
   cudaDeviceSynchronize();
   nrc_free(ctx);
   return VCR_OK;
@@ -710,6 +711,7 @@ extern "C" VCR_API vcr_status vcr_nrc_free(vcr_ctx* ctx) {
 
 extern "C" VCR_API vcr_status vcr_nrc_train_step(vcr_ctx* ctx, const vcr_pass_desc* pass, void* stream) {
   if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
   if (!pass) return fail(ctx, VCR_ERR_INVALID, "null pass");
   return nrc_train_step(ctx, pass, (cudaStream_t)stream);
 }
@@ -717,6 +719,7 @@ extern "C" VCR_API vcr_status vcr_nrc_train_step(vcr_ctx* ctx, const vcr_pass_de
 extern "C" VCR_API vcr_status vcr_nrc_train_more(vcr_ctx* ctx, uint32_t steps, uint32_t max_records,
                                                  void* stream) {
   if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
   if (!ctx->nrc) return fail(ctx, VCR_ERR_STATE, "no radiance cache");
   if (!ctx->nrc->records)
     return fail(ctx, VCR_ERR_STATE, "no training records (vcr_nrc_train_step or vcr_nrc_frame first)");
@@ -738,6 +741,7 @@ extern "C" VCR_API vcr_status vcr_nrc_train_more(vcr_ctx* ctx, uint32_t steps, u
 
 extern "C" VCR_API vcr_status vcr_nrc_set_learning_rate(vcr_ctx* ctx, float learning_rate) {
   if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
   if (!ctx->nrc) return fail(ctx, VCR_ERR_STATE, "no radiance cache");
   if (!(learning_rate > 0.0f) || !std::isfinite(learning_rate))
     return fail(ctx, VCR_ERR_INVALID, "learning rate must be finite and > 0");
@@ -747,6 +751,7 @@ extern "C" VCR_API vcr_status vcr_nrc_set_learning_rate(vcr_ctx* ctx, float lear
 
 extern "C" VCR_API vcr_status vcr_nrc_frame(vcr_ctx* ctx, const vcr_pass_desc* pass, void* stream) {
   if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
   if (!pass) return fail(ctx, VCR_ERR_INVALID, "null pass");
   return nrc_frame(ctx, pass, (cudaStream_t)stream);
 }
@@ -772,6 +777,7 @@ extern "C" VCR_API vcr_status vcr_nrc_info(vcr_ctx* ctx, vcr_nrc_info_t* out) {
 // Weights: FP32 master copy in the layer layout of vcr_nrc_params.
 extern "C" VCR_API vcr_status vcr_nrc_get_weights(vcr_ctx* ctx, float* host, size_t count) {
   if (!ctx || !host) return fail(ctx, VCR_ERR_INVALID, "null argument");
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
   if (!ctx->nrc) return fail(ctx, VCR_ERR_STATE, "no radiance cache");
   if (count != (size_t)kNrcWeightCount) return fail(ctx, VCR_ERR_INVALID, "the cache has %d weights", kNrcWeightCount);
   VCR_CUDA(ctx, cudaEventSynchronize(ctx->work_done));
@@ -781,6 +787,7 @@ extern "C" VCR_API vcr_status vcr_nrc_get_weights(vcr_ctx* ctx, float* host, siz
 
 extern "C" VCR_API vcr_status vcr_nrc_set_weights(vcr_ctx* ctx, const float* host, size_t count) {
   if (!ctx || !host) return fail(ctx, VCR_ERR_INVALID, "null argument");
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
   if (!ctx->nrc) return fail(ctx, VCR_ERR_STATE, "no radiance cache");
   if (count != (size_t)kNrcWeightCount) return fail(ctx, VCR_ERR_INVALID, "the cache has %d weights", kNrcWeightCount);
   VCR_CUDA(ctx, cudaMemcpy(ctx->nrc->w, host, count * 4, cudaMemcpyHostToDevice));
@@ -800,6 +807,7 @@ extern "C" VCR_API vcr_status vcr_nrc_set_weights(vcr_ctx* ctx, const float* hos
 extern "C" VCR_API vcr_status vcr_nrc_forward(vcr_ctx* ctx, const void* d_records, uint32_t n, float* d_out,
                                               void* stream) {
   if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
   if (!ctx->nrc) return fail(ctx, VCR_ERR_STATE, "no radiance cache");
   if (n == 0) return VCR_OK;
   if (!d_records || !d_out) return fail(ctx, VCR_ERR_INVALID, "null buffer");
@@ -821,6 +829,7 @@ extern "C" VCR_API vcr_status vcr_nrc_forward(vcr_ctx* ctx, const void* d_record
 extern "C" VCR_API vcr_status vcr_nrc_fit(vcr_ctx* ctx, const void* d_records, uint32_t n, uint32_t steps,
                                           void* stream) {
   if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
   if (!ctx->nrc) return fail(ctx, VCR_ERR_STATE, "no radiance cache");
   if (!d_records || n == 0) return fail(ctx, VCR_ERR_INVALID, "bad fit arguments");
   if (!ctx->has_cloud) return fail(ctx, VCR_ERR_STATE, "the encoding needs the cloud box (vcr_set_cloud)");
@@ -842,6 +851,7 @@ extern "C" VCR_API vcr_status vcr_nrc_fit(vcr_ctx* ctx, const void* d_records, u
 extern "C" VCR_API vcr_status vcr_nrc_gradient(vcr_ctx* ctx, const void* d_records, uint32_t n, float* host_grad,
                                                size_t count, float* out_loss) {
   if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
   if (!ctx->nrc) return fail(ctx, VCR_ERR_STATE, "no radiance cache");
   if (!d_records || !host_grad || count != (size_t)kNrcWeightCount || n == 0)
     return fail(ctx, VCR_ERR_INVALID, "bad gradient arguments");

@@ -571,6 +571,7 @@ extern "C" VCR_API vcr_status vcr_ppb_setup(vcr_ctx* ctx, const vcr_ppb_params* 
 
 extern "C" VCR_API vcr_status vcr_ppb_free(vcr_ctx* ctx) {
   if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
   cudaDeviceSynchronize();
   ppb_free(ctx);
   return VCR_OK;
@@ -578,6 +579,7 @@ extern "C" VCR_API vcr_status vcr_ppb_free(vcr_ctx* ctx) {
 
 extern "C" VCR_API vcr_status vcr_ppb_pass(vcr_ctx* ctx, const vcr_pass_desc* pass, void* stream) {
   if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
   if (!pass) return fail(ctx, VCR_ERR_INVALID, "null pass");
   return ppb_pass_launch(ctx, pass, (cudaStream_t)stream);
 }
@@ -595,6 +597,7 @@ extern "C" VCR_API vcr_status vcr_ppb_info(vcr_ctx* ctx, vcr_ppb_info_t* out) {
 // Copies of the last pass's beam data (test and debug access).
 extern "C" VCR_API vcr_status vcr_ppb_read(vcr_ctx* ctx, vcr_ppb_buffer which, void* host, size_t bytes) {
   if (!ctx || !host) return fail(ctx, VCR_ERR_INVALID, "null argument");
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
   PpbState* st = ctx->ppb;
   if (!st) return fail(ctx, VCR_ERR_STATE, "no photon-beam state");
   VCR_CUDA(ctx, cudaEventSynchronize(ctx->work_done));

@@ -384,6 +384,7 @@ extern "C" VCR_API vcr_status vcr_ppm_setup(vcr_ctx* ctx, const vcr_ppm_params* 
 
 extern "C" VCR_API vcr_status vcr_ppm_free(vcr_ctx* ctx) {
   if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
   cudaDeviceSynchronize();
   ppm_free(ctx);
   return VCR_OK;
@@ -391,6 +392,7 @@ extern "C" VCR_API vcr_status vcr_ppm_free(vcr_ctx* ctx) {
 
 extern "C" VCR_API vcr_status vcr_ppm_pass(vcr_ctx* ctx, const vcr_pass_desc* pass, void* stream) {
   if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
   if (!pass) return fail(ctx, VCR_ERR_INVALID, "null pass");
   return ppm_pass_launch(ctx, pass, (cudaStream_t)stream);
 }
@@ -405,6 +407,7 @@ extern "C" VCR_API vcr_status vcr_ppm_info(vcr_ctx* ctx, vcr_ppm_info_t* out) {
 
 extern "C" VCR_API vcr_status vcr_ppm_read(vcr_ctx* ctx, vcr_ppm_buffer which, void* host, size_t bytes) {
   if (!ctx || !host) return fail(ctx, VCR_ERR_INVALID, "null argument");
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
   PpmState* st = ctx->ppm;
   if (!st) return fail(ctx, VCR_ERR_STATE, "no photon-map state");
   VCR_CUDA(ctx, cudaEventSynchronize(ctx->work_done));

@@ -34,7 +34,7 @@ struct NrcSink {
   uint32_t capacity;
 };
 
-constexpr uint32_t kMbarSpin = 1u << 24;  // bounded mbarrier wait
+constexpr uint32_t kMbarDrain = kDefaultStageWait;  // wait for a copy in flight after a timeout
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -49,9 +49,12 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t phase) {
 }
 
 // Copy `bytes` (multiple of 16, 16-byte aligned both sides) from global to
-// this CTA's shared memory with one bulk copy; every thread waits (bounded).
-// Returns false (error word set) if the copy did not complete in time.
-__device__ bool stage_to_smem(void* dst, const void* src, uint32_t bytes, uint64_t* bar, int* err) {
+// this CTA's shared memory with one bulk copy; every thread waits (at most
+// `polls` polls).  Returns false (error word set) if the copy did not
+// complete in time; the copy in flight is then waited for once more (at
+// most kMbarDrain polls) so that no copy lands after the CTA stops using
+// the buffer, and the caller reads the majorants from global memory.
+__device__ bool stage_to_smem(void* dst, const void* src, uint32_t bytes, uint64_t* bar, uint32_t polls, int* err) {
   const uint32_t b = smem_u32(bar);
   if (threadIdx.x == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b) : "memory");
@@ -66,7 +69,7 @@ __device__ bool stage_to_smem(void* dst, const void* src, uint32_t bytes, uint64
                  : "memory");
   }
   bool ok = false;
-  for (uint32_t i = 0; i < kMbarSpin; ++i) {
+  for (uint32_t i = 0; i < polls; ++i) {
     if (mbar_try_wait(b, 0u)) {
       ok = true;
       break;
@@ -74,7 +77,7 @@ __device__ bool stage_to_smem(void* dst, const void* src, uint32_t bytes, uint64
   }
   if (!ok) {
     atomicExch(err, 3);  // staging wait ran out; wait (bounded) once more for the copy in flight
-    for (uint32_t i = 0; i < kMbarSpin; ++i)
+    for (uint32_t i = 0; i < kMbarDrain; ++i)
       if (mbar_try_wait(b, 0u)) break;
   }
   return __syncthreads_and(ok ? 1 : 0) != 0;
@@ -210,14 +213,15 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
     pt_wavefront_kernel(const __grid_constant__ GridView g, const __grid_constant__ SceneView s,
                         const __grid_constant__ CamView cam, const __grid_constant__ PassView pv,
                         double* __restrict__ sum, uint32_t* __restrict__ stats, Counters cnt, uint32_t total,
-                        uint32_t dda_steps, uint32_t maj_bytes, const __grid_constant__ NrcSink nq,
+                        uint32_t dda_steps, uint32_t maj_bytes, uint32_t stage_polls,
+                        const __grid_constant__ NrcSink nq,
                         const __grid_constant__ NrcTrainSink ts, const __grid_constant__ BatchSink bt,
                         int* __restrict__ err) {
   extern __shared__ __align__(16) float s_maj[];
   __shared__ __align__(8) uint64_t s_bar;
   const float* maj = g.majorants;
   if (kStage) {
-    if (stage_to_smem(s_maj, g.majorants, maj_bytes, &s_bar, err)) maj = s_maj;
+    if (stage_to_smem(s_maj, g.majorants, maj_bytes, &s_bar, stage_polls, err)) maj = s_maj;
   }
   BatchView* s_views = reinterpret_cast<BatchView*>(reinterpret_cast<char*>(s_maj) + (kStage ? align16(maj_bytes) : 0u));
   uint32_t pass = pv.pass;
@@ -476,8 +480,8 @@ static vcr_status launch_t(vcr_ctx* ctx, const GridView& g, const SceneView& s, 
   if (blocks == 0) return VCR_OK;
   NrcSink nq{nullptr, nullptr, 0u};
   if (s.nrc_events && ctx->nrc) nq = NrcSink{ctx->nrc->query, ctx->nrc->query_count, ctx->nrc->query_capacity};
-  kern<<<blocks, kThreads, smem, st>>>(g, s, cam, pv, sum, stats, cnt, total, ctx->tuning.dda_steps, maj_bytes, nq,
-                                       ts, bt, ctx->d_error);
+  kern<<<blocks, kThreads, smem, st>>>(g, s, cam, pv, sum, stats, cnt, total, ctx->tuning.dda_steps, maj_bytes,
+                                       wait_limits().stage_wait, nq, ts, bt, ctx->d_error);
   VCR_CUDA(ctx, cudaGetLastError());
   return VCR_OK;
 }
@@ -522,6 +526,7 @@ using namespace vcr;
 extern "C" VCR_API vcr_status vcr_autotune_pt(vcr_ctx* ctx, const vcr_pass_desc* pass, vcr_tuning* out,
                                               void* stream) {
   if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
   if (!pass) return fail(ctx, VCR_ERR_INVALID, "null pass");
   if (ctx->params.tracker != VCR_TRACKER_DDA) return fail(ctx, VCR_ERR_STATE, "autotune applies to the DDA tracker");
   cudaStream_t st = (cudaStream_t)stream;

@@ -26,7 +26,6 @@ constexpr int kSortTile = kSortThreads * kSortItems;  // 2048 keys
 constexpr uint32_t kFlagA = 1u << 30;                 // tile aggregate published
 constexpr uint32_t kFlagP = 2u << 30;                 // inclusive prefix published
 constexpr uint32_t kCountMask = (1u << 30) - 1u;
-constexpr uint32_t kSpinLimit = 1u << 22;
 
 struct SortScratch {
   uint32_t* hist;     // [8][16] digit counts per pass
@@ -50,16 +49,24 @@ static SortScratch carve(void* base, uint32_t n) {
   return s;
 }
 
+// Mask of pass p's digit: 4 bits, or the bits left below end_bit in the
+// last pass (so bits at or above end_bit never decide the order).
+__host__ __device__ __forceinline__ uint32_t digit_mask(uint32_t begin_bit, uint32_t end_bit, uint32_t p) {
+  const uint32_t w = end_bit - (begin_bit + 4u * p);
+  return w >= 4u ? 15u : (1u << w) - 1u;
+}
+
 // Digit counts of all passes in one read of the keys.
 __global__ void __launch_bounds__(256) sort_hist_kernel(const uint32_t* __restrict__ keys, uint32_t n,
-                                                        uint32_t begin_bit, uint32_t passes,
+                                                        uint32_t begin_bit, uint32_t end_bit, uint32_t passes,
                                                         uint32_t* __restrict__ hist) {
   __shared__ uint32_t h[8][16];
   for (int i = threadIdx.x; i < 8 * 16; i += blockDim.x) (&h[0][0])[i] = 0;
   __syncthreads();
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     uint32_t k = keys[i];
-    for (uint32_t p = 0; p < passes; ++p) atomicAdd(&h[p][(k >> (begin_bit + 4 * p)) & 15u], 1u);
+    for (uint32_t p = 0; p < passes; ++p)
+      atomicAdd(&h[p][(k >> (begin_bit + 4 * p)) & digit_mask(begin_bit, end_bit, p)], 1u);
   }
   __syncthreads();
   for (int i = threadIdx.x; i < (int)(passes * 16); i += blockDim.x) {
@@ -72,8 +79,9 @@ __global__ void __launch_bounds__(kSortThreads) sort_pass_kernel(const uint32_t*
                                                                  const uint32_t* __restrict__ vin,
                                                                  uint32_t* __restrict__ kout,
                                                                  uint32_t* __restrict__ vout, uint32_t n,
-                                                                 uint32_t shift, uint32_t pass,
-                                                                 SortScratch sc, int* __restrict__ err) {
+                                                                 uint32_t shift, uint32_t dmask, uint32_t pass,
+                                                                 SortScratch sc, uint32_t spin_limit,
+                                                                 int* __restrict__ err) {
   __shared__ uint32_t s_tile;
   __shared__ uint32_t s_cnt[kSortThreads / 32][16];
   __shared__ uint32_t s_tile_start[16];  // digit start inside the tile
@@ -99,7 +107,7 @@ __global__ void __launch_bounds__(kSortThreads) sort_pass_kernel(const uint32_t*
     key[j] = ok ? kin[idx] : 0u;
     val[j] = ok ? (vin ? vin[idx] : idx) : 0u;
     uint32_t valid = __ballot_sync(0xffffffffu, ok);
-    uint32_t d = (key[j] >> shift) & 15u;
+    uint32_t d = (key[j] >> shift) & dmask;
     uint32_t peers = __match_any_sync(0xffffffffu, ok ? d : 16u) & valid;
     uint32_t base = ok ? s_cnt[warp][d] : 0u;
     __syncwarp();
@@ -141,7 +149,7 @@ __global__ void __launch_bounds__(kSortThreads) sort_pass_kernel(const uint32_t*
         uint32_t w = desc[(size_t)t * 16 + d];
         uint32_t flag = w & ~kCountMask;
         if (flag == 0u) {
-          if (++spins > kSpinLimit) {
+          if (++spins > spin_limit) {
             atomicExch(err, 2);  // look-back wait ran out
             break;
           }
@@ -161,7 +169,7 @@ __global__ void __launch_bounds__(kSortThreads) sort_pass_kernel(const uint32_t*
   for (int j = 0; j < kSortItems; ++j) {
     uint32_t local = warp * (32 * kSortItems) + j * 32 + lane;
     if (local < count) {
-      uint32_t d = (key[j] >> shift) & 15u;
+      uint32_t d = (key[j] >> shift) & dmask;
       uint32_t pos = s_tile_start[d] + s_cnt[warp][d] + rank[j];
       s_keys[pos] = key[j];
       s_vals[pos] = val[j];
@@ -170,7 +178,7 @@ __global__ void __launch_bounds__(kSortThreads) sort_pass_kernel(const uint32_t*
   __syncthreads();
   for (uint32_t i = threadIdx.x; i < count; i += kSortThreads) {
     uint32_t k = s_keys[i];
-    uint32_t d = (k >> shift) & 15u;
+    uint32_t d = (k >> shift) & dmask;
     uint32_t o = s_base[d] + (i - s_tile_start[d]);
     if (o < n) {  // always true unless a look-back wait ran out (error word set)
       kout[o] = k;
@@ -179,7 +187,8 @@ __global__ void __launch_bounds__(kSortThreads) sort_pass_kernel(const uint32_t*
   }
 }
 
-// Runs the passes for bits [begin_bit, end_bit) in 4-bit digits.  The pass
+// Runs the passes for bits [begin_bit, end_bit) in 4-bit digits (the last
+// digit narrower when the range is not a multiple of 4 bits).  The pass
 // chain ping-pongs between `out` and the scratch copy so the last pass
 // lands in `out`; in-place calls (in == out) with an odd pass count start
 // from a copy.
@@ -188,12 +197,13 @@ cudaError_t sort_pairs_enqueue(int sm_count, int* d_err, void* scratch, const ui
                                cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   uint32_t passes = (end_bit - begin_bit + 3) / 4;
+  const uint32_t spins = wait_limits().sort_lookback;
   SortScratch sc = carve(scratch, n);
   uint32_t ntiles = (n + kSortTile - 1) / kSortTile;
   cudaError_t e = cudaMemsetAsync(scratch, 0, sort_scratch_header_bytes(n), st);
   if (e != cudaSuccess) return e;
   int hb = (int)std::min<uint32_t>((n + 255) / 256, (uint32_t)std::max(sm_count, 1) * 4);
-  sort_hist_kernel<<<hb, 256, 0, st>>>(kin, n, begin_bit, passes, sc.hist);
+  sort_hist_kernel<<<hb, 256, 0, st>>>(kin, n, begin_bit, end_bit, passes, sc.hist);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   const uint32_t* ck = kin;
   const uint32_t* cv = vin;
@@ -206,7 +216,8 @@ cudaError_t sort_pairs_enqueue(int sm_count, int* d_err, void* scratch, const ui
     bool to_out = ((p % 2u) == 0u) == first_to_out;
     uint32_t* nk = to_out ? kout : sc.keys_tmp;
     uint32_t* nv = to_out ? vout : sc.vals_tmp;
-    sort_pass_kernel<<<ntiles, kSortThreads, 0, st>>>(ck, cv, nk, nv, n, begin_bit + 4 * p, p, sc, d_err);
+    sort_pass_kernel<<<ntiles, kSortThreads, 0, st>>>(ck, cv, nk, nv, n, begin_bit + 4 * p,
+                                                      digit_mask(begin_bit, end_bit, p), p, sc, spins, d_err);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     ck = nk;
     cv = nv;
@@ -294,6 +305,7 @@ extern "C" VCR_API vcr_status vcr_morton_codes(vcr_ctx* ctx, const float* d_poin
                                                const float bounds_min[3], const float bounds_max[3],
                                                uint32_t bits, uint32_t* d_codes, void* stream) {
   if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
   if (n && (!d_points || !d_codes || !bounds_min || !bounds_max)) return fail(ctx, VCR_ERR_INVALID, "null argument");
   if (bits != 30 && bits != 24) return fail(ctx, VCR_ERR_INVALID, "Morton bits must be 30 or 24");
   return morton_launch(ctx, d_points, n, bounds_min, bounds_max, (int)bits, d_codes, (cudaStream_t)stream);

@@ -20,7 +20,9 @@
 //    (cudaGetSymbolAddress) with that device current; make that first call
 //    before any stream capture;
 //  - the array keeps the last call's contents; each call clears the parts
-//    that must start at zero before its kernels run.
+//    that must start at zero before its kernels run;
+//  - a look-back wait that runs out sets the array's error word, which
+//    vcr_sort_noalloc_status reads back and clears.
 #include <mutex>
 
 #include "vcr_internal.h"
@@ -95,5 +97,28 @@ extern "C" VCR_API vcr_status vcr_radix_sort_pairs_noalloc(const uint32_t* d_key
     e = sort_pairs_enqueue(g_sm_count[dev], g_error_ptr[dev], g_scratch_ptr[dev], d_keys_in, d_vals_in, d_keys_out,
                            d_vals_out, n, begin_bit, end_bit, st);
   if (e != cudaSuccess) return cuda_fail(nullptr, e, "vcr_radix_sort_pairs_noalloc");
+  return VCR_OK;
+}
+
+// The sort's kernels set the device error word when a look-back wait runs
+// out; this call is how a caller without a context learns of it.  It waits
+// for the stream, copies the word into a host variable (no allocation) and
+// clears it.
+extern "C" VCR_API vcr_status vcr_sort_noalloc_status(void* stream) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaGetDevice");
+  if (dev < 0 || dev >= kMaxDevices) return fail(nullptr, VCR_ERR_UNSUPPORTED, "device ordinal %d", dev);
+  e = setup_device(dev);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaGetSymbolAddress(sort error word)");
+  cudaStream_t st = (cudaStream_t)stream;
+  int word = 0;
+  e = cudaStreamSynchronize(st);
+  if (e == cudaSuccess) e = cudaMemcpy(&word, g_error_ptr[dev], sizeof(int), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && word) e = cudaMemset(g_error_ptr[dev], 0, sizeof(int));
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "vcr_sort_noalloc_status");
+  if (word)
+    return fail(nullptr, VCR_ERR_TIMEOUT, "vcr_radix_sort_pairs_noalloc: device error word %d (a look-back wait ran out)",
+                word);
   return VCR_OK;
 }

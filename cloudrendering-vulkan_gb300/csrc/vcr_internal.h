@@ -86,6 +86,11 @@ vcr_status cuda_fail(vcr_ctx* ctx, cudaError_t e, const char* what);
     if (e_ != cudaSuccess) return ::vcr::cuda_fail((ctx), e_, #call); \
   } while (0)
 
+// Process-wide limits of the device-side waits (vcr_set_wait_limits).
+constexpr uint32_t kDefaultSortLookback = 1u << 22;
+constexpr uint32_t kDefaultStageWait = 1u << 24;
+vcr_wait_limits wait_limits();
+
 // Scratch buffer owned by the context (grown, never shrunk).
 vcr_status ensure_scratch(vcr_ctx* ctx, size_t bytes);
 

@@ -41,6 +41,24 @@ def fbm_fill_host(size, fbm: _abi.FbmDesc) -> np.ndarray:
     return out
 
 
+def set_wait_limits(sort_lookback=None, stage_wait=None) -> None:
+    """Process-wide limits of the device-side waits (vcr_set_wait_limits);
+    no arguments restore the defaults."""
+    if sort_lookback is None and stage_wait is None:
+        check(lib().vcr_set_wait_limits(None))
+        return
+    cur = wait_limits()
+    w = _abi.WaitLimits(cur["sort_lookback"] if sort_lookback is None else sort_lookback,
+                        cur["stage_wait"] if stage_wait is None else stage_wait)
+    check(lib().vcr_set_wait_limits(C.byref(w)))
+
+
+def wait_limits() -> dict:
+    w = _abi.WaitLimits()
+    check(lib().vcr_get_wait_limits(C.byref(w)))
+    return {"sort_lookback": w.sort_lookback, "stage_wait": w.stage_wait}
+
+
 def params_set_phase_g(p: _abi.Params, g: float) -> None:
     check(lib().vcr_params_set_phase_g(C.byref(p), g))
 

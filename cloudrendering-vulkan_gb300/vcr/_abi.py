@@ -115,6 +115,10 @@ class PassDesc(C.Structure):
                 ("crop", C.c_uint32 * 4), ("flags", C.c_uint32)]
 
 
+class WaitLimits(C.Structure):
+    _fields_ = [("sort_lookback", C.c_uint32), ("stage_wait", C.c_uint32)]
+
+
 class FbmDesc(C.Structure):
     _fields_ = [("seed", C.c_uint64), ("octaves", C.c_uint32), ("lacunarity", C.c_float), ("gain", C.c_float),
                 ("base_frequency", C.c_float)]
@@ -132,6 +136,8 @@ SIGNATURES = {
     "vcr_last_error": (C.c_char_p, [_P]),
     "vcr_version": (_u32, []),
     "vcr_synchronize": (_S, [_P]),
+    "vcr_set_wait_limits": (_S, [C.POINTER(WaitLimits)]),
+    "vcr_get_wait_limits": (_S, [C.POINTER(WaitLimits)]),
     "vcr_params_set_phase_g": (_S, [C.POINTER(Params), _f]),
     "vcr_cloud_from_grid": (_S, [C.POINTER(GridDesc), _f, _f, C.POINTER(Cloud)]),
     "vcr_camera_look": (_S, [C.POINTER(Camera), F3, F3, _f, _f, C.c_int32, C.c_int32]),
@@ -192,6 +198,7 @@ SIGNATURES = {
     "vcr_lbvh_build": (_S, [_P, _P, _P, _P, _P, _u32, _P, _P, _P, _P, _P, _P, _P]),
     "vcr_radix_sort_pairs": (_S, [_P, _P, _P, _P, _P, _u32, _u32, _u32, _P]),
     "vcr_radix_sort_pairs_noalloc": (_S, [_P, _P, _P, _P, _u32, _u32, _u32, _P]),
+    "vcr_sort_noalloc_status": (_S, [_P]),
     "vcr_morton_codes": (_S, [_P, _P, _u32, F3, F3, _u32, _P, _P]),
     "vcr_readback": (_S, [_P, C.c_int, _P, _sz]),
     "vcr_display": (_S, [_P, C.POINTER(DisplayDesc), _P, _sz, _P]),

@@ -57,14 +57,26 @@ class Scene:
         c = cloud_from_grid(self.grid_desc(), 1.0, self.density_scaling)
         return c
 
+    @staticmethod
+    def camera_pose():
+        """(position, forward, vertical FOV in degrees, near plane)."""
+        return (0.0, 0.0, -0.4), (0.0, 0.0, 1.0), 90.0, 0.1
+
     def camera(self, width=None, height=None):
-        return camera_look((0.0, 0.0, -0.4), (0.0, 0.0, 1.0), 90.0, 0.1, width or self.width, height or self.height)
+        pos, fwd, fov, near = self.camera_pose()
+        return camera_look(pos, fwd, fov, near, width or self.width, height or self.height)
 
     def params(self, tracker=_abi.TRACKER_DDA):
+        p = self.params_fields(tracker)
+        params_set_phase_g(p, self.g)
+        return p
+
+    def params_fields(self, tracker=_abi.TRACKER_DDA):
+        """The parameter struct without the phase function (set by
+        params_set_phase_g): plain field values, no library call."""
         p = _abi.Params()
         p.max_events = self.max_events
         p.light_intensity = 1.0
-        params_set_phase_g(p, self.g)
         p.albedo = self.albedo
         sd = sun_travel_dir()
         for i in range(3):

@@ -216,6 +216,25 @@ VCR_API uint32_t vcr_version(void);
  * main.cpp:269); also reports any device-side error word. */
 VCR_API vcr_status vcr_synchronize(vcr_ctx* ctx);
 
+/* Limits of the device-side waits (the reference waits without a limit,
+ * vkWaitForFences with UINT64_MAX, main.cpp:606).  sort_lookback: polls of
+ * a predecessor tile's look-back word before a radix-sort tile gives up
+ * (default 1<<22); stage_wait: mbarrier polls for the copy that stages a
+ * majorant level in shared memory (default 1<<24).  A wait that runs out
+ * sets the device error word, which vcr_synchronize (or, for the
+ * allocation-free sort, vcr_sort_noalloc_status) reports as
+ * VCR_ERR_TIMEOUT; a sort whose wait ran out has an unspecified order (it
+ * stays inside its output buffers), a pass whose staging wait ran out reads
+ * the majorants from global memory and renders the same image.  The limits
+ * are process-wide and apply to launches queued after the call; NULL
+ * restores the defaults.  Small limits exist to test the timeout path. */
+typedef struct vcr_wait_limits {
+  uint32_t sort_lookback;
+  uint32_t stage_wait;
+} vcr_wait_limits;
+VCR_API vcr_status vcr_set_wait_limits(const vcr_wait_limits* limits);
+VCR_API vcr_status vcr_get_wait_limits(vcr_wait_limits* out);
+
 /* ------------------------------------------------------------------------ */
 /* Host-side helpers for the reference's parameter structs                 */
 /* ------------------------------------------------------------------------ */
@@ -531,11 +550,18 @@ VCR_API vcr_status vcr_radix_sort_pairs(vcr_ctx* ctx, const uint32_t* d_keys_in,
  * n returns VCR_ERR_CAPACITY).  Calls share that array: calls that overlap
  * on the GPU race, so serialise them.  The first call on each device looks
  * up the array's address with that device current; make it before any
- * stream capture.  Errors are reported through vcr_last_error(NULL). */
+ * stream capture.  Argument errors are reported through
+ * vcr_last_error(NULL); a device-side wait that ran out is reported by
+ * vcr_sort_noalloc_status. */
 #define VCR_SORT_NOALLOC_MAX_KEYS (1u << 20)
 VCR_API vcr_status vcr_radix_sort_pairs_noalloc(const uint32_t* d_keys_in, const uint32_t* d_vals_in,
                                                 uint32_t* d_keys_out, uint32_t* d_vals_out, uint32_t n,
                                                 uint32_t begin_bit, uint32_t end_bit, void* stream);
+/* Waits for `stream`, then reads and clears the device error word of the
+ * allocation-free sort on the current device: VCR_ERR_TIMEOUT if a
+ * look-back wait of a sort queued before ran out (its output order is then
+ * unspecified), else VCR_OK.  Allocates nothing. */
+VCR_API vcr_status vcr_sort_noalloc_status(void* stream);
 /* Morton codes of n points (device float3): bits == 30 quantises each axis
  * to 1024 cells of [bounds_min, bounds_max] and interleaves x<<2|y<<1|z;
  * bits == 24 is the reference's getMortonCode (PPB_PT.comp:317-333:
@@ -601,7 +627,12 @@ VCR_API vcr_status vcr_batch_reset(vcr_ctx* ctx);
 VCR_API vcr_status vcr_checkpoint_save(vcr_ctx* ctx, const char* path);
 /* Restores a checkpoint into a context set up the same way (frame size,
  * techniques and their sizes); the grid, cloud, camera and params are the
- * caller's to bind.  Every section is checked before anything changes. */
+ * caller's to bind.  The file carries a hash of the scene it was rendered
+ * from (grid description, precision and per-brick majorants; cloud,
+ * camera and params; batch views and photon-map parameters when set up):
+ * a context bound to another scene gets VCR_ERR_STATE.  Every section is
+ * checked before anything changes; a truncated or corrupt file is
+ * VCR_ERR_IO. */
 VCR_API vcr_status vcr_checkpoint_load(vcr_ctx* ctx, const char* path);
 
 /* ------------------------------------------------------------------------ */

@@ -13,7 +13,8 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liboracle.so")
-SOURCES = ["oracle_pt.cpp", "oracle_sort.cpp", "oracle_ppb.cpp", "oracle_ppm.cpp", "oracle_nrc.cpp"]
+SOURCES = ["oracle_pt.cpp", "oracle_sort.cpp", "oracle_ppb.cpp", "oracle_ppm.cpp", "oracle_nrc.cpp",
+           "oracle_structs.cpp"]
 HEADERS = ["oracle_math.h", "oracle_scene.h", "oracle_lbvh.h"]
 
 

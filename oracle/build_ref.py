@@ -1,7 +1,8 @@
 """Build the reference's own host C++ that compiles as it lies: Grid3D<float>
 (.xyz Load/Save, GetMajorant) behind oracle/ref_grid3d.cpp, into
 oracle/_ref/ (git-ignored).  Test infrastructure only; it needs the
-reference tree at /root/reference and is skipped where that is absent.
+reference tree, found at $VCR_REFERENCE_DIR (default /root/reference), and
+is skipped where that is absent.
 
 Not built, and why:
   * Tests.cpp (the CPU radix-sort fixture): needs an MSVC-only cast fixed
@@ -16,7 +17,7 @@ import os
 import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = "/root/reference"
+REF = os.environ.get("VCR_REFERENCE_DIR", "/root/reference")
 OUT = os.path.join(HERE, "_ref")
 EXE = os.path.join(OUT, "ref_grid3d")
 

@@ -53,6 +53,10 @@ def lib():
             "oracle_split_sort": (None, [P, u32, u32, u32]),
             "oracle_lsd_sort_pairs": (None, [P, P, u32, u32, u32, P, P]),
             "oracle_morton": (None, [P, u32, P, P, u32, P]),
+            "oracle_params_set_phase_g": (C.c_int, [C.POINTER(_abi.Params), f]),
+            "oracle_cloud_from_grid": (C.c_int, [C.POINTER(_abi.GridDesc), f, f, C.POINTER(_abi.Cloud)]),
+            "oracle_camera_look": (C.c_int, [C.POINTER(_abi.Camera), _abi.F3, _abi.F3, f, f, C.c_int32,
+                                             C.c_int32]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -60,6 +64,27 @@ def lib():
             fn.argtypes = args
         _lib = L
     return _lib
+
+
+def scene_structs(sc, tracker=_abi.TRACKER_DDA):
+    """(grid desc, cloud, camera, params) of a scene configuration, built by
+    the oracle's restatement of the reference's set-up (no product code):
+    the same bytes as the library's vcr_cloud_from_grid / vcr_camera_look /
+    vcr_params_set_phase_g on the same arguments."""
+    L = lib()
+    n = max(sc.size)
+    desc = _abi.GridDesc()
+    for a in range(3):
+        desc.size[a] = sc.size[a]
+        desc.voxel_size[a] = 1.0 / n
+    cloud = _abi.Cloud()
+    assert L.oracle_cloud_from_grid(C.byref(desc), 1.0, sc.density_scaling, C.byref(cloud)) == 0
+    cam = _abi.Camera()
+    pos, fwd, fov, near = sc.camera_pose()
+    assert L.oracle_camera_look(C.byref(cam), _abi.F3(*pos), _abi.F3(*fwd), fov, near, sc.width, sc.height) == 0
+    p = sc.params_fields(tracker)
+    assert L.oracle_params_set_phase_g(C.byref(p), sc.g) == 0
+    return desc, cloud, cam, p
 
 
 def _p(a: np.ndarray):

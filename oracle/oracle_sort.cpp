@@ -66,8 +66,12 @@ static void split_pass(std::vector<uint32_t>& keys, std::vector<uint32_t>& vals,
   vals.swap(v2);
 }
 
-static void local_sort(std::vector<uint32_t>& keys, std::vector<uint32_t>& vals, uint32_t base_shift) {
-  for (uint32_t b = 0; b < 4; ++b) split_pass(keys, vals, base_shift + b);
+// A digit of `width` (<= 4) bits from base_shift up: one 1-bit split pass
+// per bit (LocalSort.comp:154-252 runs four); a last digit narrower than 4
+// bits keeps bits at or above the sort's end out of the order.
+static void local_sort(std::vector<uint32_t>& keys, std::vector<uint32_t>& vals, uint32_t base_shift,
+                       uint32_t width) {
+  for (uint32_t b = 0; b < width; ++b) split_pass(keys, vals, base_shift + b);
 }
 
 }  // namespace oracle
@@ -100,17 +104,19 @@ void oracle_lsd_sort_pairs(const uint32_t* kin, const uint32_t* vin, uint32_t n,
   std::vector<uint32_t> k(kin, kin + n), v(n);
   for (uint32_t i = 0; i < n; ++i) v[i] = vin ? vin[i] : i;
   for (uint32_t shift = begin; shift < end; shift += 4) {
+    const uint32_t width = std::min(4u, end - shift);
+    const uint32_t dmask = (1u << width) - 1u;
     uint32_t groups = (n + wg - 1) / wg;
     std::vector<uint32_t> hist((size_t)16 * groups, 0u);
     std::vector<uint32_t> lk(n), lv(n);
     for (uint32_t g = 0; g < groups; ++g) {
       uint32_t a = g * wg, b = std::min(n, a + wg);
       std::vector<uint32_t> bk(k.begin() + a, k.begin() + b), bv(v.begin() + a, v.begin() + b);
-      local_sort(bk, bv, shift);
+      local_sort(bk, bv, shift, width);
       for (uint32_t i = 0; i < b - a; ++i) {
         lk[a + i] = bk[i];
         lv[a + i] = bv[i];
-        hist[(size_t)((bk[i] >> shift) & 15u) * groups + g] += 1;  // digit-major
+        hist[(size_t)((bk[i] >> shift) & dmask) * groups + g] += 1;  // digit-major
       }
     }
     // exclusive scan of the digit-major histogram
@@ -125,7 +131,7 @@ void oracle_lsd_sort_pairs(const uint32_t* kin, const uint32_t* vin, uint32_t n,
       uint32_t a = g * wg, b = std::min(n, a + wg);
       uint32_t seen[16] = {0};
       for (uint32_t i = a; i < b; ++i) {
-        uint32_t d = (lk[i] >> shift) & 15u;
+        uint32_t d = (lk[i] >> shift) & dmask;
         uint32_t o = scan[(size_t)d * groups + g] + seen[d]++;
         k[o] = lk[i];
         v[o] = lv[i];

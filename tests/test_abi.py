@@ -128,3 +128,17 @@ def test_create_without_gpu_fails_cleanly():
         pytest.skip("a GPU is present")
     with pytest.raises(vcr.VcrError):
         vcr.Context()
+
+
+def test_wait_limits_round_trip_and_defaults():
+    d = vcr.wait_limits()
+    assert d == {"sort_lookback": 1 << 22, "stage_wait": 1 << 24}
+    try:
+        vcr.set_wait_limits(sort_lookback=0)
+        assert vcr.wait_limits() == {"sort_lookback": 0, "stage_wait": 1 << 24}
+        vcr.set_wait_limits(stage_wait=7)
+        assert vcr.wait_limits() == {"sort_lookback": 0, "stage_wait": 7}
+    finally:
+        vcr.set_wait_limits()
+    assert vcr.wait_limits() == d
+    assert vcr.lib().vcr_get_wait_limits(None) == vcr.ERR_INVALID

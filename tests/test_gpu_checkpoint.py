@@ -127,3 +127,59 @@ def test_batch_resume_and_refusals(cuda, tmp_path):
             ctx.checkpoint_load(path)
         with pytest.raises(vcr.VcrError):
             ctx.checkpoint_load(str(tmp_path / "missing.ckpt"))
+
+
+def test_checkpoint_of_another_scene_is_refused(cuda, tmp_path):
+    """The scene hash: a checkpoint loads only into a context bound to the
+    grid, cloud, camera and parameters it was rendered from."""
+    path = str(tmp_path / "scene.ckpt")
+    sc = configs.C1_PT
+    with vcr.Context() as ctx:
+        _scene(ctx)
+        ctx.pt_pass(seed=2, pass_index=0)
+        ctx.checkpoint_save(path)
+    with vcr.Context() as ctx:  # other phase g
+        _scene(ctx)
+        prm = sc.params(vcr.TRACKER_DDA)
+        vcr.params_set_phase_g(prm, 0.5)
+        ctx.set_params(prm)
+        with pytest.raises(vcr.VcrError, match="another scene"):
+            ctx.checkpoint_load(path)
+        ctx.set_params(sc.params(vcr.TRACKER_DDA))
+        ctx.checkpoint_load(path)  # the same scene again: accepted
+        assert ctx.pass_count() == 1
+    with vcr.Context() as ctx:  # other grid seed, same sizes
+        ctx.grid_generate(sc.grid_desc(), vcr.fbm_desc(seed=2, octaves=sc.octaves), sc.precision)
+        ctx.set_cloud(sc.cloud())
+        ctx.set_camera(sc.camera(W, H))
+        ctx.set_params(sc.params(vcr.TRACKER_DDA))
+        ctx.set_frame(W, H)
+        with pytest.raises(vcr.VcrError, match="another scene"):
+            ctx.checkpoint_load(path)
+    with vcr.Context() as ctx:  # other camera
+        _scene(ctx)
+        ctx.set_camera(vcr.camera_look((0.0, 0.1, -0.4), (0.0, 0.0, 1.0), 90.0, 0.1, W, H))
+        with pytest.raises(vcr.VcrError, match="another scene"):
+            ctx.checkpoint_load(path)
+
+
+def test_truncated_and_corrupt_checkpoints_are_io_errors(cuda, tmp_path):
+    path = str(tmp_path / "full.ckpt")
+    with vcr.Context() as ctx:
+        _scene(ctx)
+        ctx.pt_pass(seed=2, pass_index=0)
+        ctx.checkpoint_save(path)
+        data = open(path, "rb").read()
+        cut = tmp_path / "cut.ckpt"
+        cut.write_bytes(data[: len(data) // 2])
+        with pytest.raises(vcr.VcrError) as e:
+            ctx.checkpoint_load(str(cut))
+        assert e.value.status == vcr.ERR_IO
+        # a section length far beyond the file (first section's u64 at byte 24)
+        bad = bytearray(data)
+        bad[24:32] = (1 << 39).to_bytes(8, "little")
+        (tmp_path / "bad.ckpt").write_bytes(bytes(bad))
+        with pytest.raises(vcr.VcrError) as e:
+            ctx.checkpoint_load(str(tmp_path / "bad.ckpt"))
+        assert e.value.status == vcr.ERR_IO
+        ctx.checkpoint_load(path)  # the intact file still loads

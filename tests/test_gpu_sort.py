@@ -58,8 +58,10 @@ def test_sort_permutation_bit_exact(cuda, n, kind):
         np.testing.assert_array_equal(_from_dev(vo)[:n], ov)
 
 
-@pytest.mark.parametrize("bits", [(0, 30), (4, 12), (0, 4), (28, 32)])
+@pytest.mark.parametrize("bits", [(0, 30), (4, 12), (0, 4), (28, 32), (3, 13), (5, 6), (0, 31)])
 def test_sort_bit_ranges_and_payload(cuda, bits):
+    """Only the bits [begin, end) decide the order, also when the range is
+    not a multiple of the 4-bit digit (the keys' other bits are random)."""
     import torch
     n = 50001
     rng = np.random.default_rng(bits[0])
@@ -74,6 +76,9 @@ def test_sort_bit_ranges_and_payload(cuda, bits):
         ctx.synchronize()
     np.testing.assert_array_equal(_from_dev(ko), ok)
     np.testing.assert_array_equal(_from_dev(vo), ov)
+    mask = np.uint32(((1 << (bits[1] - bits[0])) - 1) << bits[0])
+    perm = np.argsort(keys & mask, kind="stable")
+    np.testing.assert_array_equal(_from_dev(vo), vals[perm])
 
 
 @pytest.mark.parametrize("bits", [(0, 32), (0, 28)])

@@ -27,14 +27,14 @@ def test_split_passes_are_stable_partitions(n):
 
 
 @pytest.mark.parametrize("n,hi", [(0, 10), (1, 10), (1023, 7), (1025, 3), (5000, 1 << 30), (20000, 1 << 32)])
-@pytest.mark.parametrize("bits", [(0, 32), (0, 30), (4, 12)])
+@pytest.mark.parametrize("bits", [(0, 32), (0, 30), (4, 12), (3, 13), (5, 6)])
 def test_lsd_pipeline_equals_stable_argsort(n, hi, bits):
     rng = np.random.default_rng(n + bits[0])
     keys = rng.integers(0, hi, n, dtype=np.uint64).astype(np.uint32)
     ko, vo = orc.lsd_sort_pairs(keys, None, *bits)
-    # the range is rounded up to whole 4-bit digits
-    width = 4 * ((bits[1] - bits[0] + 3) // 4)
-    mask = np.uint32(((1 << min(width, 32 - bits[0])) - 1) << bits[0])
+    # only the bits [begin, end) decide the order (the last digit is narrower
+    # when the range is not a multiple of 4 bits)
+    mask = np.uint32(((1 << (bits[1] - bits[0])) - 1) << bits[0])
     perm = np.argsort(keys & mask, kind="stable")
     np.testing.assert_array_equal(vo, perm)
     np.testing.assert_array_equal(ko, keys[perm])
