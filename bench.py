@@ -184,25 +184,30 @@ def run_vcr(args):
         ctx.synchronize()
         tuning = ctx.autotune(seed=999, stream=sh)  # picks majorant level / DDA steps / CTA size
         seed = replica_seed(rank)
+        # The timed steps are the K passes rendered by one persistent launch
+        # (vcr_pt_passes): the same paths and streams as K single-pass
+        # launches, without each launch's tail of long paths.
         for k in range(args.warmup):
             ctx.pt_pass(seed=seed, pass_index=k, stream=sh)
+        ctx.pt_passes(seed=seed, first=0, count=args.warmup, stream=sh)
         barrier()
         clk = Clocks(local)
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         barrier()
         ev0.record(stream)
-        for k in range(args.steps):
-            ctx.pt_pass(seed=seed, pass_index=args.warmup + k, stream=sh)
+        ctx.pt_passes(seed=seed, first=args.warmup, count=args.steps, stream=sh)
         ev1.record(stream)
         barrier()
         clocks = clk.stop()
         ms_total = max_over_ranks(ev0.elapsed_time(ev1), device="cuda")
-        # per-launch kernel durations and lookups (for the roofline)
+        c = ctx.counters()
+        launch = {"passes": args.steps, "lookups": c[1], "events": c[2], "paths": c[0], "ms": ms_total}
+        # the same passes with one launch per pass, for comparison
         durs, looks, events, paths = [], [], [], []
-        for k in range(min(args.steps, 3)):
+        for k in range(min(args.steps, 5)):
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record(stream)
-            ctx.pt_pass(seed=seed + 7, pass_index=k, stream=sh)
+            ctx.pt_pass(seed=seed, pass_index=args.warmup + k, stream=sh)
             b.record(stream)
             b.synchronize()
             durs.append(a.elapsed_time(b))
@@ -214,9 +219,12 @@ def run_vcr(args):
     value = whole_job_rate(ws, samples_per_step, args.steps, ms_total)
     peak, peak_kind = measured_peaks()
     bpl = BYTES_PER_LOOKUP[prec]
-    lookups = float(np.mean(looks))
-    dur_ms = float(np.mean(durs))
+    # the dominant kernel's launch in the timed region: K passes, its lookups, its CUDA-event time
+    lookups = float(launch["lookups"])
+    dur_ms = float(launch["ms"])
     achieved = lookups * bpl / (dur_ms / 1e3) / 1e9
+    single_ms = float(np.mean(durs))
+    single_lookups = float(np.mean(looks))
     tpl = traffic_per_lookup()
 
     # e2e through the C-ABI with host buffers
@@ -235,48 +243,58 @@ def run_vcr(args):
                    "tuning": tuning,
                    "l2": "inputs larger than L2 (1 GiB FP16 grid), no flush",
                    "parallelism": f"replicas{ws}"},
-        "gpu_launches": args.steps,
+        "gpu_launches": 1,
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "peak_source": peak_kind,
                      "traffic": (round(tpl * lookups) if tpl else None),
                      "kernel": "pt_wavefront_kernel", "bytes_per_lookup": bpl,
+                     "passes_per_launch": args.steps,
                      "lookups_per_launch": int(lookups), "launch_ms": round(dur_ms, 4),
                      "lookups_per_s": round(lookups / (dur_ms / 1e3), 1)},
+        "single_pass_launches": {"ms_per_pass": round(single_ms, 4),
+                                 "value": round(samples_per_step / (single_ms / 1e3) / 1e6, 3),
+                                 "lookups_per_pass": int(single_lookups),
+                                 "frac": round(single_lookups * bpl / (single_ms / 1e3) / 1e9 / peak, 4),
+                                 "note": "one vcr_pt_pass launch per pass (each ends in its own tail of long paths)"},
         "clocks": clocks,
         "time_to_1pct": conv,
         "e2e": e2e,
         "cpu_baseline": cpu,
         "stats": {"events_per_path": round(float(np.sum(events)) / max(1, float(np.sum(paths))), 3),
-                  "lookups_per_path": round(lookups / samples_per_step, 2), "image_mean": float(img.mean())},
+                  "lookups_per_path": round(single_lookups / samples_per_step, 2), "image_mean": float(img.mean())},
     }
     print(json.dumps(line), flush=True)
 
 
-CONV = {"ref_passes": 4000, "plain_passes": 1000, "warm_steps": 6000, "warm_sets": 32, "warm_more": 19, "warm_batch": 16384,
+PLAIN_PASSES_PER_LAUNCH = 25  # the plain tracker's error curve: one launch of 25 passes per point
+
+CONV = {"ref_samples": 147456, "ref_spp": 16, "plain_max_passes": 30000, "warm_steps": 6000, "warm_sets": 32, "warm_more": 19, "warm_batch": 16384,
         "pool_sets": 32, "pool_every": 96, "max_frames": 8000, "chunk": 500, "spp": 1, "train_samples": 65536,
         "learning_rate": 1e-3, "ema_decay": 0.99, "nrc_events": 2, "repeats": 3}
 
 
 class Reference:
     """FP64 high-spp image R of the plain tracker from two independent
-    halves; their difference gives R's own relative MSE (noise2) and the
-    per-sample relative variance V of the plain tracker."""
+    halves (each `launches` passes of `spp` samples per pixel); their
+    difference gives R's own relative MSE (noise2) and the per-sample
+    relative variance V of the plain tracker."""
 
-    def __init__(self, ctx, sc, stream, passes):
+    def __init__(self, ctx, sc, stream, samples, spp):
         import torch
         import vcr
 
         sh = stream.cuda_stream
         px = sc.width * sc.height
+        launches = max(1, samples // (2 * spp))
 
         def render(seed):
             ctx.reset()
-            for k in range(passes):
-                ctx.pt_pass(seed=seed, pass_index=k, stream=sh)
+            for k in range(0, launches, 8):  # 8 passes of spp samples a launch
+                ctx.pt_passes(seed=seed, first=k, count=min(8, launches - k), spp=spp, stream=sh)
             ctx.synchronize()
             buf = torch.empty(px * 3, dtype=torch.float64, device="cuda")
             ctx.readback_to(vcr.BUF_IMAGE_SUM, buf.data_ptr(), px * 24)
-            return buf / passes
+            return buf / (launches * spp)
 
         t0 = time.perf_counter()
         ra, rb = render(100), render(200)
@@ -284,8 +302,9 @@ class Reference:
         self.R = (ra + rb) / 2
         e_ab = torch.sqrt(torch.sum((ra - rb) ** 2 / (self.R ** 2 + 1e-2)) / px).item()
         self.noise2 = e_ab ** 2 / 4
-        self.V = e_ab ** 2 * passes / 2
-        self.passes = passes
+        self.samples = 2 * launches * spp  # per pixel, both halves
+        self.V = e_ab ** 2 * (launches * spp) / 2
+        self.spp = spp
 
     def corrected(self, e):
         return float(np.sqrt(max(e * e - self.noise2, 0.0)))
@@ -306,24 +325,51 @@ def _error_curve(ctx, stream, ref, n, frame, errs, ms, first):
     ms.extend(a.elapsed_time(b) for a, b in evs)
 
 
-def plain_time_to_1pct(ctx, sc, stream, ref, passes):
+def plain_time_to_1pct(ctx, sc, stream, ref, max_passes, chunk=500):
+    """The plain tracker's measured error curve, pass by pass, until its
+    corrected relRMSE reaches 1 % (at most max_passes); time = the device
+    time of the passes run.  The unbiased prediction sqrt(V / passes) is
+    reported beside it."""
     import torch
 
-    errs = torch.zeros(passes, dtype=torch.float64, device="cuda")
+    errs = torch.zeros(max_passes, dtype=torch.float64, device="cuda")
     ms = []
     ctx.reset()
-    _error_curve(ctx, stream, ref, passes, lambda k: ctx.pt_pass(seed=300, pass_index=k, stream=stream.cuda_stream),
-                 errs, ms, 0)
-    e = errs.cpu().numpy()
-    pass_ms = float(np.mean(ms))
+    done, hit = 0, None
+    group = PLAIN_PASSES_PER_LAUNCH
+
+    def frame(k):  # a launch of `group` passes; its error is recorded at the last of them
+        ctx.pt_passes(seed=300, first=k * group, count=group, stream=stream.cuda_stream)
+
+    chunk_launches = max(1, chunk // group)
+    max_launches = max_passes // group
+    while done < max_launches and hit is None:
+        n = min(chunk_launches, max_launches - done)
+        _error_curve(ctx, stream, ref, n, frame, errs, ms, done)
+        done += n
+        e = errs[:done].cpu().numpy()
+        for i in range(done - n, done):
+            if ref.corrected(e[i]) <= 0.01:
+                hit = i
+                break
+    e = errs[:done].cpu().numpy()
+    cum = np.cumsum(ms)
+    pass_ms = float(np.mean(ms)) / group
     need = ref.V / 1e-4
-    return {"time_s": round(need * pass_ms / 1e3, 3), "passes": int(np.ceil(need)), "pass_ms": round(pass_ms, 4),
-            "basis": "unbiased: relRMSE = sqrt(V/passes), V from the reference halves",
-            "check": {"passes": passes, "measured": round(ref.corrected(e[-1]), 5),
-                      "predicted": round(float(np.sqrt(ref.V / passes)), 5)}}
+    marks = sorted({i for i in (0, 3, 39, 399, 799, 1599, done - 1) if i < done} | ({hit} if hit else set()))
+    return {"time_s": round(cum[hit] / 1e3, 3) if hit is not None else None,
+            "passes": (hit + 1) * group if hit is not None else None, "pass_ms": round(pass_ms, 4),
+            "passes_per_launch": group,
+            "basis": "measured: device time of the launches until the corrected relRMSE, checked after every "
+                     f"launch of {group} passes, first reaches 1 %",
+            "predicted": {"passes": int(np.ceil(need)), "time_s": round(need * pass_ms / 1e3, 3),
+                          "basis": "unbiased: relRMSE = sqrt(V/passes), V from the reference halves"},
+            "curve": {str((i + 1) * group): {"measured": round(ref.corrected(e[i]), 5),
+                                             "predicted": round(float(np.sqrt(ref.V / ((i + 1) * group))), 5)}
+                      for i in marks}}
 
 
-def cached_time_to_1pct(ctx, sc, stream, ref, cfg):
+def cached_time_to_1pct(ctx, sc, stream, ref, cfg, to_end=False):
     """Warm-up (training launches of cfg["warm_sets"] record sets, each set
     feeding 1 + cfg["warm_more"] Adam steps on batches of its records), then
     frames of cfg["spp"] samples per pixel until the corrected relRMSE
@@ -386,12 +432,12 @@ def cached_time_to_1pct(ctx, sc, stream, ref, cfg):
             if cfg.get("reuse_steps", 0):  # and train on the last frame's records again
                 ctx.nrc_train_more(cfg["reuse_steps"], stream=sh)
 
-    while done < nmax and hit is None:
+    while done < nmax and (hit is None or to_end):
         _error_curve(ctx, stream, ref, chunk, frame, errs, ms, done)
         done += chunk
         e = errs[:done].cpu().numpy()
         for i in range(done - chunk, done):
-            if ref.corrected(e[i]) <= 0.01:
+            if hit is None and ref.corrected(e[i]) <= 0.01:
                 hit = i
                 break
     info = ctx.nrc_info()
@@ -405,6 +451,10 @@ def cached_time_to_1pct(ctx, sc, stream, ref, cfg):
             "warm_training_launches": batches, "warm_s": round(warm_ms / 1e3, 3),
             "time_s": round((warm_ms + frames_ms[hit]) / 1e3, 3) if hit is not None else None,
             "relrmse_last": round(ref.corrected(e[-1]), 5), "frames_run": done,
+            "floor": ({"frames": done, "relrmse": round(ref.corrected(e[-1]), 5),
+                       "relrmse_min": round(min(ref.corrected(x) for x in e[done // 2:]), 5),
+                       "basis": "the cache's error left after max_frames frames (bias plus the frames' noise)"}
+                      if to_end else None),
             "curve": {str(i + 1): round(ref.corrected(e[i]), 5) for i in (0, 9, 99, 499, 999, 1999, 3999, done - 1)
                       if i < done},
             "train_records": info["train_records"], "loss": round(info["last_loss"], 4), "tuning": cached_tuning}
@@ -414,18 +464,21 @@ def convergence(ctx, sc, stream, args, overrides=None):
     """Time to 1 % relRMSE against an FP64 high-spp image: plain tracker
     and radiance-cached tracker on the bound scene (see the module text)."""
     cfg = dict(CONV, **(overrides or {}))
-    ref = Reference(ctx, sc, stream, cfg["ref_passes"])
-    plain = plain_time_to_1pct(ctx, sc, stream, ref, cfg["plain_passes"])
+    ref = Reference(ctx, sc, stream, cfg["ref_samples"], cfg["ref_spp"])
+    plain = plain_time_to_1pct(ctx, sc, stream, ref, cfg["plain_max_passes"])
     # the cache's training trajectory varies from run to run (the order of
-    # its training records follows atomic appends): the median of a few runs
-    runs = [cached_time_to_1pct(ctx, sc, stream, ref, cfg) for _ in range(cfg["repeats"])]
+    # its training records follows atomic appends): the median of a few
+    # runs; the first run goes on to max_frames for the cache's error floor
+    runs = [cached_time_to_1pct(ctx, sc, stream, ref, cfg, to_end=(i == 0)) for i in range(cfg["repeats"])]
     done = [r for r in runs if r["time_s"] is not None]
     nrc = sorted(done, key=lambda r: r["time_s"])[len(done) // 2] if done else runs[0]
-    nrc = dict(nrc, runs_s=[r["time_s"] for r in runs])
+    nrc = dict(nrc, runs_s=[r["time_s"] for r in runs], floor=runs[0]["floor"])
+    nrc.pop("floor_run", None)
     return {"plain": plain, "nrc": nrc,
-            "speedup": round(plain["time_s"] / nrc["time_s"], 2) if nrc["time_s"] else None,
-            "reference": {"passes": 2 * ref.passes, "own_relrmse": round(float(np.sqrt(ref.noise2)), 5),
-                          "render_s": round(ref.render_s, 2), "per_sample_rel_variance": round(ref.V, 4)},
+            "speedup": round(plain["time_s"] / nrc["time_s"], 2) if (nrc["time_s"] and plain["time_s"]) else None,
+            "reference": {"samples_per_pixel": ref.samples, "spp_per_launch": ref.spp,
+                          "own_relrmse": round(float(np.sqrt(ref.noise2)), 5), "render_s": round(ref.render_s, 2),
+                          "per_sample_rel_variance": round(ref.V, 4)},
             "settings": cfg}
 
 
@@ -467,23 +520,7 @@ def run_batch(args):
         ctx.batch_pass(seed=2, pass_index=0, spp=spp, stream=sh)
         ctx.synchronize()
         c = ctx.counters()
-        # precision: same streams on FP32 (oracle), FP16 and BF16 grids
-        imgs = {}
-        for name, prec in (("fp32", vcr.PREC_FP32), ("fp16", vcr.PREC_FP16), ("bf16", vcr.PREC_BF16)):
-            ctx.grid_generate(sc.grid_desc(), sc.fbm(), prec)
-            ctx.set_cloud(sc.cloud())
-            ctx.batch_reset()
-            for k in range(4):
-                ctx.batch_pass(seed=3, pass_index=k, spp=spp, stream=sh)
-            ctx.synchronize()
-            imgs[name] = [ctx.batch_read(v) for v in range(len(views))]
-    err = {}
-    for name in ("fp16", "bf16"):
-        num = den = 0.0
-        for I, R in zip(imgs[name], imgs["fp32"]):
-            num += float(np.sum((I - R) ** 2 / (R ** 2 + 1e-2)))
-            den += R.shape[0] * R.shape[1]
-        err[name] = round(float(np.sqrt(num / den)), 6)
+        prec = precision_vs_fp32(ctx, sc, views[0], sh)
     samples = info["pixels"] * spp
     peak, peak_kind = measured_peaks()
     achieved = c[1] * BYTES_PER_LOOKUP[vcr.PREC_FP16] / (ms / 1e3) / 1e9
@@ -495,7 +532,85 @@ def run_batch(args):
                    "l2": "inputs larger than L2 (256 MiB FP16 grid + 670 MB sums), no flush"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "peak_source": peak_kind, "lookups_per_launch": c[1]},
-        "precision_relrmse_vs_fp32": err, "precision_passes": 4, "clocks": clocks}), flush=True)
+        "precision_vs_fp32": prec, "clocks": clocks}), flush=True)
+
+
+def precision_vs_fp32(ctx, sc, view, sh, side=160, launches=4000, spp=16):
+    """Error of the FP16 and BF16 bricks against the FP32 grid (the
+    precision oracle) on one view of the scene, two ways:
+      agreement: one pass at the view's full size with the same streams on
+        every grid; the fraction of paths whose decisions (scatter events,
+        density lookups) are identical, and the relRMSE over those paths
+        (quantisation moves the radiance of a path that decides the same);
+      converged: FP64 images of each grid at side x side, launches x spp
+        samples per pixel with the same streams on every grid (common random
+        numbers: the paths that decide alike cancel), and the relRMSE
+        between the FP16 (BF16) and the FP32 image.  It is an upper bound of
+        the quantisation's bias (what remains is the bias plus the noise of
+        the few paths that decide differently, which falls with the sample
+        count); each image's own noise, from its two halves, is given beside
+        it for scale.
+    relRMSE = sqrt(mean_p sum_c (I - R)^2 / (R^2 + 1e-2))."""
+    import torch
+    import vcr
+
+    cam, w, h, sun = view
+    prm = sc.params(vcr.TRACKER_DDA)
+    for a in range(3):
+        prm.sun_dir[a] = sun[a]
+    pos = tuple(cam.position)
+    fwd = tuple(cam.forward)
+    small = vcr.camera_look(pos, fwd, 60.0, 0.1, side, side)
+    stats, passes, conv = {}, {}, {}
+    t0 = time.perf_counter()
+    for name, prec in (("fp32", vcr.PREC_FP32), ("fp16", vcr.PREC_FP16), ("bf16", vcr.PREC_BF16)):
+        ctx.grid_generate(sc.grid_desc(), sc.fbm(), prec)
+        ctx.set_cloud(sc.cloud())
+        ctx.set_params(prm)
+        ctx.set_camera(cam)
+        ctx.set_frame(w, h)
+        ctx.pt_pass(seed=3, pass_index=0, flags=vcr.PASS_RECORD_STATS, stream=sh)
+        ctx.synchronize()
+        stats[name], passes[name] = ctx.path_stats(), ctx.image_sum()
+        ctx.set_camera(small)
+        ctx.set_frame(side, side)
+        halves = []
+        for seed in (11, 12):
+            ctx.reset()
+            for k in range(launches // 2):
+                ctx.pt_pass(seed=seed, pass_index=k, spp=spp, stream=sh)
+            ctx.synchronize()
+            halves.append(ctx.image_sum() / ((launches // 2) * spp))
+        conv[name] = halves
+
+    def rel2(a, b, R):
+        return float(np.mean(np.sum((a - b) ** 2 / (R ** 2 + 1e-2), axis=-1)))
+
+    out = {}
+    R32 = (conv["fp32"][0] + conv["fp32"][1]) / 2
+    noise32 = rel2(conv["fp32"][0], conv["fp32"][1], R32) / 4
+    for name in ("fp16", "bf16"):
+        agree = np.all(stats[name][..., :2] == stats["fp32"][..., :2], axis=-1)
+        a, b = passes[name][agree], passes["fp32"][agree]
+        I = (conv[name][0] + conv[name][1]) / 2
+        noise = rel2(conv[name][0], conv[name][1], R32) / 4
+        out[name] = {"paths_agreeing": round(float(agree.mean()), 5),
+                     "relrmse_agreeing_paths": round(float(np.sqrt(np.mean(np.sum((a - b) ** 2 / (b ** 2 + 1e-2),
+                                                                                    axis=-1)))), 7),
+                     "converged_relrmse_common_streams": round(float(np.sqrt(rel2(I, R32, R32))), 6),
+                     "own_noise_relrmse": round(float(np.sqrt(noise)), 5)}
+    out["fp32_own_noise_relrmse"] = round(float(np.sqrt(noise32)), 5)
+    out["setup"] = {"agreement_view": [w, h], "converged_view": [side, side],
+                    "samples_per_pixel": launches * spp, "seconds": round(time.perf_counter() - t0, 1)}
+    return out
+
+
+def _gather_roofline(kernel, units, bytes_per_unit, ms, basis):
+    peak, peak_kind = measured_peaks()
+    achieved = units * bytes_per_unit / (ms / 1e3) / 1e9 if ms > 0 else 0.0
+    return {"bound": "hbm", "kernel": kernel, "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "peak_source": peak_kind, "units_per_launch": units,
+            "bytes_per_unit": bytes_per_unit, "launch_ms": round(ms, 4), "basis": basis}
 
 
 def _timed_passes(stream, fn, steps):
@@ -518,6 +633,47 @@ def _divided(sc, div):
         return sc
     return dataclasses.replace(sc, name=f"{sc.name}/{div}", width=max(1, sc.width // div),
                                height=max(1, sc.height // div))
+
+
+def run_sort(args):
+    """The stable 4-bit LSD radix sort of (u32 key, u32 value) pairs: the C3
+    pass's 10.3 M segments with 30-bit Morton keys (8 digit passes, the last
+    of 2 bits), and 64 M pairs with 32-bit keys; inputs larger than L2
+    except the ping-pong of the C3 case (82 MB each way).  Algorithmic
+    bytes: 8 B read + 8 B written per pair and digit pass (128 B a pair
+    for 8 passes) plus the one histogram read of the keys (4 B a pair)."""
+    import torch
+    import vcr
+
+    stream = torch.cuda.Stream()
+    sh = stream.cuda_stream
+    peak, peak_kind = measured_peaks()
+    cases = []
+    with vcr.Context() as ctx:
+        for n, bits in ((10301598, 30), (1 << 26, 32)):
+            g = torch.Generator(device="cuda").manual_seed(n)
+            hi = (1 << bits) - 1 if bits < 32 else (1 << 31) - 1
+            keys = torch.randint(0 if bits < 32 else -(1 << 31), hi, (n,), dtype=torch.int32, device="cuda",
+                                 generator=g)
+            vals = torch.arange(n, dtype=torch.int32, device="cuda")
+            ko, vo = torch.empty_like(keys), torch.empty_like(keys)
+            for _ in range(args.warmup):
+                ctx.radix_sort_pairs(keys.data_ptr(), vals.data_ptr(), ko.data_ptr(), vo.data_ptr(), n, 0, bits,
+                                     stream=sh)
+            ms = _timed_passes(stream, lambda k: ctx.radix_sort_pairs(keys.data_ptr(), vals.data_ptr(), ko.data_ptr(),
+                                                                        vo.data_ptr(), n, 0, bits, stream=sh),
+                               args.steps)
+            ctx.synchronize()
+            passes = (bits + 3) // 4
+            alg = n * (16 * passes + 4)
+            achieved = alg / (ms / 1e3) / 1e9
+            cases.append({"pairs": n, "key_bits": bits, "digit_passes": passes, "ms": round(ms, 4),
+                          "pairs_per_s": round(n / (ms / 1e3), 1),
+                          "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                                       "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                                       "algorithmic_bytes": alg}})
+    print(json.dumps({"metric": "radix sort pairs/s", "steps": args.steps, "warmup": args.warmup, "cases": cases}),
+          flush=True)
 
 
 def run_display(args):
@@ -582,12 +738,16 @@ def run_ppm(args):
         ms = _timed_passes(stream, lambda k: ctx.ppm_pass(seed=1, pass_index=args.warmup + k, stream=sh), args.steps)
         info = ctx.ppm_info()
         stats = ctx.ppm_read("stats")
+        tested, gather_ms = ctx.gather_stats("ppm")  # the last pass's gather kernel
     print(json.dumps({
         "metric": "PPM pass", "workload": sc.name, "ms_per_pass": round(ms, 4), "steps": args.steps,
         "photons_emitted_per_s": round(ex["photons"] / (ms / 1e3), 1),
         "photons_stored": info["photons_stored"], "dropped": info["dropped"],
         "pixel_gathers_per_s": round(sc.width * sc.height / (ms / 1e3), 1),
-        "mean_radius": float(stats[..., 1].mean()), "mean_photon_count": float(stats[..., 0].mean())}), flush=True)
+        "mean_radius": float(stats[..., 1].mean()), "mean_photon_count": float(stats[..., 0].mean()),
+        "roofline": _gather_roofline("ppm_gather_kernel", tested, 32, gather_ms,
+                                     "leaf photons tested x 32 B (position + power, direction packed)")}),
+          flush=True)
 
 
 def run_ppb(args):
@@ -618,11 +778,15 @@ def run_ppb(args):
         ms = _timed_passes(stream, lambda k: ctx.ppb_pass(seed=1, pass_index=args.warmup + k, stream=sh), args.steps)
         info = ctx.ppb_info()
         beams = int(ctx.ppb_read("nbeams", photons).sum())
+        evaluated, gather_ms = ctx.gather_stats("ppb")  # the last pass's gather kernel
     print(json.dumps({
         "metric": "PPB pass", "workload": sc.name, "ms_per_pass": round(ms, 4), "steps": args.steps,
         "photons": photons, "beams": beams, "segments": info["segments"], "dropped": info["dropped"],
         "segments_per_s": round(info["segments"] / (ms / 1e3), 1),
-        "pixel_gathers_per_s": round(sc.width * sc.height / (ms / 1e3), 1), "radius": info["radius"]}), flush=True)
+        "pixel_gathers_per_s": round(sc.width * sc.height / (ms / 1e3), 1), "radius": info["radius"],
+        "roofline": _gather_roofline("ppb_gather_kernel", evaluated, 32 + 112, gather_ms,
+                                     "(pixel, segment) pairs evaluated x (32 B segment + 112 B beam slot)")}),
+          flush=True)
 
 
 def run_nrc_frames(args):
@@ -792,12 +956,14 @@ def main():
     ap.add_argument("--ppm", action="store_true", help="only measure the photon-mapping configuration")
     ap.add_argument("--ppb", action="store_true", help="only measure the photon-beam configuration")
     ap.add_argument("--display", action="store_true", help="only measure the display-image kernel")
+    ap.add_argument("--sort", action="store_true", help="only measure the radix sort")
     ap.add_argument("--image-div", type=int, default=1,
                     help="divide the --ppm / --ppb image sides (a small case for profiler captures)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.impl == "reference" and not (args.ppm or args.ppb or args.batch or args.nrc_frames or args.display):
+    if args.impl == "reference" and not (args.ppm or args.ppb or args.batch or args.nrc_frames or args.display
+                                         or args.sort):
         run_reference(args)
         return
     import contextlib
@@ -805,7 +971,9 @@ def main():
     import __graft_entry__ as ge
     with contextlib.redirect_stdout(sys.stderr):  # stdout carries only the JSON line
         ge.build()
-    if args.display:
+    if args.sort:
+        run_sort(args)
+    elif args.display:
         run_display(args)
     elif args.ppm or args.ppb:
         run_ppm(args) if args.ppm else run_ppb(args)

@@ -195,6 +195,42 @@ extern "C" VCR_API vcr_status vcr_synchronize(vcr_ctx* ctx) {
 }
 
 namespace vcr {
+vcr_status probe_begin(vcr_ctx* ctx, GatherProbe& p, cudaStream_t s) {
+  if (!p.d_count) {
+    VCR_CUDA(ctx, cudaMalloc(&p.d_count, sizeof(unsigned long long)));
+    VCR_CUDA(ctx, cudaEventCreate(&p.start));
+    VCR_CUDA(ctx, cudaEventCreate(&p.stop));
+  }
+  VCR_CUDA(ctx, cudaMemsetAsync(p.d_count, 0, sizeof(unsigned long long), s));
+  VCR_CUDA(ctx, cudaEventRecord(p.start, s));
+  return VCR_OK;
+}
+
+vcr_status probe_end(vcr_ctx* ctx, GatherProbe& p, cudaStream_t s) {
+  VCR_CUDA(ctx, cudaEventRecord(p.stop, s));
+  p.recorded = true;
+  return VCR_OK;
+}
+
+vcr_status probe_read(vcr_ctx* ctx, GatherProbe& p, uint64_t& count, float& ms) {
+  count = 0;
+  ms = 0.0f;
+  if (!p.recorded) return VCR_OK;
+  VCR_CUDA(ctx, cudaEventSynchronize(p.stop));
+  VCR_CUDA(ctx, cudaEventElapsedTime(&ms, p.start, p.stop));
+  unsigned long long c = 0;
+  VCR_CUDA(ctx, cudaMemcpy(&c, p.d_count, sizeof c, cudaMemcpyDeviceToHost));
+  count = c;
+  return VCR_OK;
+}
+
+void probe_free(GatherProbe& p) {
+  cudaFree(p.d_count);
+  if (p.start) cudaEventDestroy(p.start);
+  if (p.stop) cudaEventDestroy(p.stop);
+  p = GatherProbe{};
+}
+
 static std::atomic<uint32_t> g_sort_lookback{kDefaultSortLookback};
 static std::atomic<uint32_t> g_stage_wait{kDefaultStageWait};
 
@@ -564,6 +600,14 @@ extern "C" VCR_API vcr_status vcr_pt_pass(vcr_ctx* ctx, const vcr_pass_desc* pas
   VCR_CUDA(ctx, cudaSetDevice(ctx->device));
   if (!pass) return fail(ctx, VCR_ERR_INVALID, "null pass");
   return pt_pass_launch(ctx, pass, (cudaStream_t)stream);
+}
+
+extern "C" VCR_API vcr_status vcr_pt_passes(vcr_ctx* ctx, const vcr_pass_desc* first, uint32_t count,
+                                            void* stream) {
+  if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
+  if (!first) return fail(ctx, VCR_ERR_INVALID, "null pass");
+  return pt_pass_launch(ctx, first, (cudaStream_t)stream, nullptr, count);
 }
 
 extern "C" VCR_API vcr_status vcr_pt_counters(vcr_ctx* ctx, uint64_t out[4]) {

@@ -434,10 +434,10 @@ static void nrc_init_weights(std::vector<float>& w, uint32_t seed) {
 vcr_status nrc_setup(vcr_ctx* ctx, const vcr_nrc_params* p) {
   if (!p || p->train_samples == 0 || p->train_samples > (1u << 22) || !(p->learning_rate > 0.0f) ||
       p->query_capacity == 0 || !(p->ema_decay >= 0.0f && p->ema_decay < 1.0f) ||
-      !(p->tail_survival >= 0.0f && p->tail_survival < 1.0f))
+      !(p->tail_survival >= 0.0f && p->tail_survival < 1.0f) || p->query_kernel > VCR_NRC_QUERY_TCGEN05)
     return fail(ctx, VCR_ERR_INVALID,
                 "nrc params: train_samples 1..2^22, learning_rate > 0, query_capacity > 0, ema_decay and "
-                "tail_survival in [0,1)");
+                "tail_survival in [0,1), query_kernel a VCR_NRC_QUERY_* value");
   nrc_free(ctx);
   NrcState* st = new NrcState();
   ctx->nrc = st;
@@ -537,8 +537,16 @@ vcr_status nrc_reset_queries(vcr_ctx* ctx, cudaStream_t s) {
   return VCR_OK;
 }
 
+// Which kernel serves the queries (vcr_nrc_params.query_kernel).
+static bool use_tc(const NrcState* st) { return st->prm.query_kernel == VCR_NRC_QUERY_TCGEN05; }
+
 vcr_status nrc_infer_queries(vcr_ctx* ctx, cudaStream_t s) {
   NrcState* st = ctx->nrc;
+  if (use_tc(st)) {
+    const NrcView v = nrc_view(ctx);
+    return nrc_infer_tc_launch(ctx, v.wbi, v.b0, v.inv_ext, st->query, st->query_count, st->query_capacity,
+                               ctx->d_sum, nullptr, s);
+  }
   VCR_CUDA(ctx, cudaFuncSetAttribute(nrc_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)infer_smem()));
   int per_sm = 0;
   VCR_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, nrc_infer_kernel, kInferThreads, infer_smem()));
@@ -817,10 +825,18 @@ extern "C" VCR_API vcr_status vcr_nrc_forward(vcr_ctx* ctx, const void* d_record
   if (vs) return vs;
   uint32_t* d_n = reinterpret_cast<uint32_t*>(ctx->d_scratch);
   VCR_CUDA(ctx, cudaMemcpyAsync(d_n, &n, 4, cudaMemcpyHostToDevice, s));
-  VCR_CUDA(ctx, cudaFuncSetAttribute(nrc_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)infer_smem()));
-  nrc_infer_kernel<<<ctx->sm_count * 3, kInferThreads, infer_smem(), s>>>(
-      nrc_view(ctx), reinterpret_cast<const NrcRecord*>(d_records), d_n, n, nullptr, d_out);
-  VCR_CUDA(ctx, cudaGetLastError());
+  if (use_tc(ctx->nrc)) {
+    const NrcView v = nrc_view(ctx);
+    vs = nrc_infer_tc_launch(ctx, v.wbi, v.b0, v.inv_ext, reinterpret_cast<const NrcRecord*>(d_records), d_n, n,
+                             nullptr, d_out, s);
+    if (vs) return vs;
+  } else {
+    VCR_CUDA(ctx, cudaFuncSetAttribute(nrc_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)infer_smem()));
+    nrc_infer_kernel<<<ctx->sm_count * 3, kInferThreads, infer_smem(), s>>>(
+        nrc_view(ctx), reinterpret_cast<const NrcRecord*>(d_records), d_n, n, nullptr, d_out);
+    VCR_CUDA(ctx, cudaGetLastError());
+  }
   VCR_CUDA(ctx, cudaStreamSynchronize(s));
   return VCR_OK;
 }

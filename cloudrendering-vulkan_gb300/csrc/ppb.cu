@@ -347,14 +347,15 @@ constexpr int kGatherThreads = 128;
 
 __global__ void __launch_bounds__(kGatherThreads) ppb_gather_kernel(GridView g, SceneView s, CamView cam, PassView pv,
                                                                     PpbGatherView v, double* __restrict__ sum,
-                                                                    Counters cnt) {
+                                                                    Counters cnt,
+                                                                    unsigned long long* __restrict__ evaluated) {
   __shared__ uint2 s_stack[kGatherThreads / 32][kGatherStack];
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t tiles_x = (pv.cw + 7u) / 8u;
   const uint32_t cx = (wid % tiles_x) * 8u + (lane & 7u), cy = (wid / tiles_x) * 4u + (lane >> 3);
   const bool valid = cx < pv.cw && cy < pv.ch;
-  uint32_t lookups = 0, cells = 0;
+  uint32_t lookups = 0, cells = 0, segs = 0;
   uint32_t pix = 0;
   f3 o = mk(0.f, 0.f, 0.f), rd = mk(0.f, 0.f, 1.f), L = mk(0.f, 0.f, 0.f);
   float t_in = 0.0f, t_out = 0.0f;
@@ -393,8 +394,10 @@ __global__ void __launch_bounds__(kGatherThreads) ppb_gather_kernel(GridView g, 
       if (node & kLeafBit) {
         const uint32_t lf = node & ~kLeafBit;
         const float4 lo = v.leaf_lo[lf], hi = v.leaf_hi[lf];
-        if (mine && ray_box(o, inv, t_in, t_out, lo, hi))
+        if (mine && ray_box(o, inv, t_in, t_out, lo, hi)) {
           L = L + beam_contribution(g, s, v, v.order[lf], o, rd, t_in, t_out, cam_d, lookups);
+          ++segs;
+        }
       } else {
         const float4 lo = v.node_lo[node], hi = v.node_hi[node];
         const uint32_t hit = __ballot_sync(0xffffffffu, mine && ray_box(o, inv, t_in, t_out, lo, hi));
@@ -420,6 +423,7 @@ __global__ void __launch_bounds__(kGatherThreads) ppb_gather_kernel(GridView g, 
   }
   if (valid) write_result(pv, sum, pix, L);
   flush_counters(cnt, valid ? 1ull : 0ull, lookups, 0, cells);
+  warp_count(evaluated, segs);
 }
 
 // ---------------------------------------------------------------------------
@@ -431,6 +435,7 @@ static void ppb_release(PpbState* st) {
                   st->idx_sorted, st->left, st->right, st->parent_int, st->parent_leaf, st->flags, st->leaf_lo,
                   st->leaf_hi, st->node_lo, st->node_hi};
   for (void* p : ptrs) cudaFree(p);
+  probe_free(st->gather);
 }
 
 void ppb_free(vcr_ctx* ctx) {
@@ -548,9 +553,13 @@ vcr_status ppb_pass_launch(vcr_ctx* ctx, const vcr_pass_desc* pass, cudaStream_t
   // one warp per 8x4 pixel tile
   uint32_t tiles = ((pv.cw + 7u) / 8u) * ((pv.ch + 3u) / 4u);
   uint32_t warps_per_block = kGatherThreads / 32;
+  vcr_status ps = probe_begin(ctx, st->gather, st_);
+  if (ps) return ps;
   ppb_gather_kernel<<<(tiles + warps_per_block - 1) / warps_per_block, kGatherThreads, 0, st_>>>(
-      g, s, cam_view(ctx->cam), pv, gv, ctx->d_sum, cnt);
+      g, s, cam_view(ctx->cam), pv, gv, ctx->d_sum, cnt, st->gather.d_count);
   VCR_CUDA(ctx, cudaGetLastError());
+  ps = probe_end(ctx, st->gather, st_);
+  if (ps) return ps;
   VCR_CUDA(ctx, cudaEventRecord(ctx->work_done, st_));
   if (!(pv.flags & VCR_PASS_NO_ACCUMULATE)) {
     ctx->passes += 1;
@@ -592,6 +601,13 @@ extern "C" VCR_API vcr_status vcr_ppb_info(vcr_ctx* ctx, vcr_ppb_info_t* out) {
   out->radius = ctx->ppb->radius;
   out->beam_slots = ctx->ppb->K;
   return VCR_OK;
+}
+
+extern "C" VCR_API vcr_status vcr_ppb_gather_stats(vcr_ctx* ctx, uint64_t* count, float* ms) {
+  if (!ctx || !count || !ms) return fail(ctx, VCR_ERR_INVALID, "null argument");
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
+  if (!ctx->ppb) return fail(ctx, VCR_ERR_STATE, "no photon-beam state");
+  return probe_read(ctx, ctx->ppb->gather, *count, *ms);
 }
 
 // Copies of the last pass's beam data (test and debug access).

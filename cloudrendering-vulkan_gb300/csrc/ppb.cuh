@@ -30,6 +30,7 @@ struct PpbState {
   uint32_t *seg_beam = nullptr, *codes = nullptr, *idx = nullptr, *codes_sorted = nullptr, *idx_sorted = nullptr;
   uint32_t *left = nullptr, *right = nullptr, *parent_int = nullptr, *parent_leaf = nullptr, *flags = nullptr;
   float4 *leaf_lo = nullptr, *leaf_hi = nullptr, *node_lo = nullptr, *node_hi = nullptr;
+  GatherProbe gather;  // segments the last gather evaluated, its device time
 };
 
 // Spread the low 10 bits of v so two zeros separate each bit (Karras 2012;

@@ -163,9 +163,10 @@ __device__ __forceinline__ float box_dist2(f3 x, float4 lo, float4 hi) {
 }
 
 __global__ void __launch_bounds__(128) ppm_gather_kernel(GridView g, SceneView s, CamView cam, PassView pv,
-                                                         PpmGatherView v, double* __restrict__ sum, Counters cnt) {
+                                                         PpmGatherView v, double* __restrict__ sum, Counters cnt,
+                                                         unsigned long long* __restrict__ tested) {
   uint32_t id = blockIdx.x * blockDim.x + threadIdx.x;
-  uint32_t lookups = 0, cells = 0, found = 0;
+  uint32_t lookups = 0, cells = 0, found = 0, cand = 0;
   if (id < pv.cw * pv.ch) {
     uint32_t cy = id / pv.cw, cx = id - cy * pv.cw;
     int x = (int)(pv.x0 + cx), y = (int)(pv.y0 + cy);
@@ -197,6 +198,7 @@ __global__ void __launch_bounds__(128) ppm_gather_kernel(GridView g, SceneView s
         while (true) {
           if (node & kLeafBit) {
             uint32_t lf = node & ~kLeafBit;
+            ++cand;
             float4 q = v.leaf_lo[lf];
             f3 dq = mk(q.x, q.y, q.z) - xm;
             if (dot(dq, dq) <= r2) {
@@ -247,6 +249,7 @@ __global__ void __launch_bounds__(128) ppm_gather_kernel(GridView g, SceneView s
     found = M;
   }
   flush_counters(cnt, id < pv.cw * pv.ch ? 1ull : 0ull, lookups, found, cells);
+  warp_count(tested, cand);
 }
 
 __global__ void ppm_init_stats_kernel(double* __restrict__ stats, size_t pixels, double r0) {
@@ -265,6 +268,7 @@ void ppm_free(vcr_ctx* ctx) {
                   st->codes_sorted, st->order, st->left, st->right, st->parent_int, st->parent_leaf, st->flags,
                   st->leaf_lo, st->leaf_hi, st->node_lo, st->node_hi, st->stats, st->iota};
   for (void* p : ptrs) cudaFree(p);
+  probe_free(st->gather);
   delete st;
   ctx->ppm = nullptr;
 }
@@ -360,8 +364,13 @@ vcr_status ppm_pass_launch(vcr_ctx* ctx, const vcr_pass_desc* pass, cudaStream_t
   PpmGatherView gv{st->pos, st->pw, st->dir, st->order, st->left, st->right, st->leaf_lo, st->node_lo, st->node_hi,
                    (int)n, st->stats, st->prm.alpha, pass->seed, pass->pass_index};
   uint32_t pixels = pv.cw * pv.ch;
-  ppm_gather_kernel<<<(pixels + 127) / 128, 128, 0, cs>>>(g, s, cam_view(ctx->cam), pv, gv, ctx->d_sum, cnt);
+  vcr_status ps = probe_begin(ctx, st->gather, cs);
+  if (ps) return ps;
+  ppm_gather_kernel<<<(pixels + 127) / 128, 128, 0, cs>>>(g, s, cam_view(ctx->cam), pv, gv, ctx->d_sum, cnt,
+                                                          st->gather.d_count);
   VCR_CUDA(ctx, cudaGetLastError());
+  ps = probe_end(ctx, st->gather, cs);
+  if (ps) return ps;
   VCR_CUDA(ctx, cudaEventRecord(ctx->work_done, cs));
   // the sums hold the running estimate times the pass count
   ctx->passes += 1;
@@ -403,6 +412,13 @@ extern "C" VCR_API vcr_status vcr_ppm_info(vcr_ctx* ctx, vcr_ppm_info_t* out) {
   out->photons_stored = ctx->ppm->photons_stored;
   out->dropped = ctx->ppm->dropped;
   return VCR_OK;
+}
+
+extern "C" VCR_API vcr_status vcr_ppm_gather_stats(vcr_ctx* ctx, uint64_t* count, float* ms) {
+  if (!ctx || !count || !ms) return fail(ctx, VCR_ERR_INVALID, "null argument");
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
+  if (!ctx->ppm) return fail(ctx, VCR_ERR_STATE, "no photon-map state");
+  return probe_read(ctx, ctx->ppm->gather, *count, *ms);
 }
 
 extern "C" VCR_API vcr_status vcr_ppm_read(vcr_ctx* ctx, vcr_ppm_buffer which, void* host, size_t bytes) {

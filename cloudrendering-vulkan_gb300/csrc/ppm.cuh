@@ -20,6 +20,7 @@ struct PpmState {
   uint32_t *left = nullptr, *right = nullptr, *parent_int = nullptr, *parent_leaf = nullptr, *flags = nullptr;
   float4 *leaf_lo = nullptr, *leaf_hi = nullptr, *node_lo = nullptr, *node_hi = nullptr;
   double* stats = nullptr;  // per pixel: N, R, tau rgb, background rgb
+  GatherProbe gather;       // photons the last gather tested, its device time
 };
 
 }  // namespace vcr

@@ -24,6 +24,7 @@ struct PassView {
   uint32_t x0, y0, cw, ch;  // crop
   uint32_t width, height;   // frame
   uint32_t padded_w;        // 32 * (W/32 + 1): the reference's dispatch width
+  uint32_t passes;          // consecutive passes in one DDA wavefront launch (0 or 1: one)
 };
 
 struct Counters {

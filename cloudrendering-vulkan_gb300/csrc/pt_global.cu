@@ -122,18 +122,29 @@ __global__ void __launch_bounds__(256) pt_global_kernel(GridView g, SceneView s,
 // host launch
 // ---------------------------------------------------------------------------
 
-vcr_status pt_pass_launch(vcr_ctx* ctx, const vcr_pass_desc* pass, cudaStream_t st, const NrcTrainSink* train) {
+vcr_status pt_pass_launch(vcr_ctx* ctx, const vcr_pass_desc* pass, cudaStream_t st, const NrcTrainSink* train,
+                          uint32_t count) {
   if (!ctx->has_grid || !ctx->has_cloud || !ctx->has_cam || !ctx->has_params || !ctx->d_sum)
     return fail(ctx, VCR_ERR_STATE, "vcr_pt_pass needs a grid, cloud, camera, params and frame");
   PassView pv;
   vcr_status vs = make_pass_view(ctx, pass, pv);
   if (vs) return vs;
   const vcr_params& P = ctx->params;
+  if (count == 0) return fail(ctx, VCR_ERR_INVALID, "a launch of zero passes");
+  if (count > 1) {
+    if (P.tracker != VCR_TRACKER_DDA || P.nrc_events || train)
+      return fail(ctx, VCR_ERR_UNSUPPORTED, "several passes per launch need the DDA tracker without the cache");
+    if (pv.flags & (VCR_PASS_RECORD_STATS | VCR_PASS_NO_ACCUMULATE))
+      return fail(ctx, VCR_ERR_INVALID, "several passes per launch accumulate and record no path statistics");
+    if ((uint64_t)pass->pass_index + count > 0xFFFFFFFFull)
+      return fail(ctx, VCR_ERR_INVALID, "pass indices past 2^32");
+  }
+  pv.passes = count;
   if (P.rng_mode == VCR_RNG_XORSHIFT && pv.spp != 1)
     return fail(ctx, VCR_ERR_UNSUPPORTED, "the xorshift parity mode renders 1 spp per pass");
   if (P.nee_mode == VCR_NEE_SHADOW_VOLUME && !ctx->has_sv)
     return fail(ctx, VCR_ERR_STATE, "shadow-volume NEE needs vcr_shadow_volume_build first");
-  uint64_t total64 = (uint64_t)pv.cw * pv.ch * pv.spp;
+  uint64_t total64 = (uint64_t)pv.cw * pv.ch * pv.spp * count;
   uint64_t pixels = (uint64_t)ctx->width * ctx->height * pv.spp;
   if (total64 > 0x7FFFFFFFull || pixels > 0xFFFFFFFFull)
     return fail(ctx, VCR_ERR_UNSUPPORTED, "more than 2^31 paths in one pass");
@@ -178,8 +189,8 @@ vcr_status pt_pass_launch(vcr_ctx* ctx, const vcr_pass_desc* pass, cudaStream_t 
   VCR_CUDA(ctx, cudaGetLastError());
   VCR_CUDA(ctx, cudaEventRecord(ctx->work_done, st));
   if (!(pv.flags & VCR_PASS_NO_ACCUMULATE)) {
-    ctx->passes += 1;
-    ctx->samples += pv.spp;
+    ctx->passes += count;
+    ctx->samples += (uint64_t)pv.spp * count;
   }
   return VCR_OK;
 }

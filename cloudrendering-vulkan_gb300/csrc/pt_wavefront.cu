@@ -8,7 +8,11 @@
 //
 // Schedule: persistent CTAs; every lane owns one path at a time and refills
 // itself from a global cursor with one atomic per warp (ballot + popc), so
-// lanes never idle while paths remain.  A wavefront step is one bounded DDA
+// lanes never idle while paths remain.  One launch may render several
+// consecutive passes (pv.passes): its work items run through the passes in
+// order, each with its pass's random streams, so the lanes that would sit
+// idle while a pass's longest paths finish (a third of a pass on a dense
+// cloud) already run the next pass's paths.  A wavefront step is one bounded DDA
 // walk (at most `dda_steps` majorant cells, resumable: the optical depth
 // left over is kept) followed by at most one density lookup, so a lane
 // crossing many empty cells cannot hold its warp for a whole flight.  The
@@ -234,6 +238,7 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
     __syncthreads();
   }
   const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t per_pass = pv.cw * pv.ch * pv.spp;  // camera paths of one pass
   const float k = s.k_sigma;
   const f3 lsun0 = -s.sun;
   uint32_t mode = kIdle;
@@ -301,13 +306,19 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
           }
         } else {
           id -= ts.paths;
+          uint32_t pq = pass;  // a launch of several passes: item id / per_pass is the pass offset
+          if (pv.passes > 1u) {
+            const uint32_t q = id / per_pass;
+            id -= q * per_pass;
+            pq += q;
+          }
           pid = id;
           uint32_t per_row = pv.cw * pv.spp;
           uint32_t cy = id / per_row, rem = id - cy * per_row;
           uint32_t cx = rem / pv.spp, sp = rem - cx * pv.spp;
           int x = (int)(pv.x0 + cx), y = (int)(pv.y0 + cy);
           pix = (uint32_t)y * pv.width + (uint32_t)x;
-          rng = rng_pcg(pv.seed, pix * pv.spp + sp, pass);
+          rng = rng_pcg(pv.seed, pix * pv.spp + sp, pq);
           L = mk(0.f, 0.f, 0.f);
           beta = 1.0f;
           events = lookups = cells = 0;

@@ -8,8 +8,9 @@
 // from expandBits/getMortonCode (PPB_PT.comp:317-333).
 //
 // GB300 design: one histogram kernel computes the digit counts of every
-// pass at once; each digit pass is then ONE kernel over 2048-key tiles:
-// stable in-tile ranking with warp match_any, a decoupled look-back across
+// pass at once; each digit pass is then ONE kernel over 4096-key tiles:
+// stable in-tile ranking from four warp ballots of the digit bits (no
+// shared-memory counters inside the ranking), a decoupled look-back across
 // tiles (tile ids taken in launch order from an atomic counter, so every
 // tile waits only on tiles already running), shared-memory staging and a
 // coalesced scatter.  Each pass reads and writes every pair once (16 B/key
@@ -21,8 +22,8 @@
 namespace vcr {
 
 constexpr int kSortThreads = 256;
-constexpr int kSortItems = 8;
-constexpr int kSortTile = kSortThreads * kSortItems;  // 2048 keys
+constexpr int kSortItems = 16;
+constexpr int kSortTile = kSortThreads * kSortItems;  // 4096 keys
 constexpr uint32_t kFlagA = 1u << 30;                 // tile aggregate published
 constexpr uint32_t kFlagP = 2u << 30;                 // inclusive prefix published
 constexpr uint32_t kCountMask = (1u << 30) - 1u;
@@ -75,6 +76,15 @@ __global__ void __launch_bounds__(256) sort_hist_kernel(const uint32_t* __restri
   }
 }
 
+// Per-lane mask of the warp's lanes whose digit equals `d`, from the four
+// ballots of the digit bits (bit_i = ballot of bit i of every lane's digit).
+__device__ __forceinline__ uint32_t digit_peers(const uint32_t bit[4], uint32_t d) {
+  uint32_t m = 0xffffffffu;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) m &= ((d >> i) & 1u) ? bit[i] : ~bit[i];
+  return m;
+}
+
 __global__ void __launch_bounds__(kSortThreads) sort_pass_kernel(const uint32_t* __restrict__ kin,
                                                                  const uint32_t* __restrict__ vin,
                                                                  uint32_t* __restrict__ kout,
@@ -92,55 +102,59 @@ __global__ void __launch_bounds__(kSortThreads) sort_pass_kernel(const uint32_t*
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
   const uint32_t lt = (1u << lane) - 1u;
   if (threadIdx.x == 0) s_tile = atomicAdd(sc.tiles + pass, 1u);
-  if (threadIdx.x < 16 * (kSortThreads / 32)) (&s_cnt[0][0])[threadIdx.x] = 0;
   __syncthreads();
   const uint32_t tile = s_tile;
   const uint32_t tile0 = tile * kSortTile;
   const uint32_t count = min((uint32_t)kSortTile, n - tile0);
 
-  uint32_t key[kSortItems], val[kSortItems], rank[kSortItems];
+  // Stable in-warp ranking: warp w holds keys [w*32*kSortItems, ...) of the
+  // tile in kSortItems rounds of 32 (round j, lane l = key w*32*I + 32j + l).
+  // Lanes 0..15 keep the warp's running count of digit `lane`; an item's
+  // rank is that count before its round plus its peers in lower lanes.
+  uint32_t key[kSortItems], rank[kSortItems];
+  uint32_t run = 0;
 #pragma unroll
   for (int j = 0; j < kSortItems; ++j) {
-    uint32_t local = warp * (32 * kSortItems) + j * 32 + lane;
-    uint32_t idx = tile0 + local;
-    bool ok = local < count;
-    key[j] = ok ? kin[idx] : 0u;
-    val[j] = ok ? (vin ? vin[idx] : idx) : 0u;
-    uint32_t valid = __ballot_sync(0xffffffffu, ok);
-    uint32_t d = (key[j] >> shift) & dmask;
-    uint32_t peers = __match_any_sync(0xffffffffu, ok ? d : 16u) & valid;
-    uint32_t base = ok ? s_cnt[warp][d] : 0u;
-    __syncwarp();
-    if (ok && (peers & lt) == 0u) s_cnt[warp][d] = base + __popc(peers);
-    __syncwarp();
+    const uint32_t local = warp * (32 * kSortItems) + j * 32 + lane;
+    const bool ok = local < count;
+    key[j] = ok ? kin[tile0 + local] : 0u;
+    const uint32_t d = (key[j] >> shift) & dmask;
+    const uint32_t valid = __ballot_sync(0xffffffffu, ok);
+    uint32_t bit[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) bit[i] = __ballot_sync(0xffffffffu, ok && ((d >> i) & 1u));
+    const uint32_t peers = digit_peers(bit, d) & valid;
+    const uint32_t base = __shfl_sync(0xffffffffu, run, d);
     rank[j] = base + __popc(peers & lt);
+    run += __popc(digit_peers(bit, lane & 15u) & valid);  // meaningful in lanes 0..15
   }
+  if (lane < 16) s_cnt[warp][lane] = run;
   __syncthreads();
   if (threadIdx.x < 16) {
     const uint32_t d = threadIdx.x;
-    uint32_t run = 0;
+    uint32_t total = 0;
     for (int w = 0; w < kSortThreads / 32; ++w) {
       uint32_t c = s_cnt[w][d];
-      s_cnt[w][d] = run;  // exclusive prefix over warps
-      run += c;
+      s_cnt[w][d] = total;  // exclusive prefix over warps
+      total += c;
     }
     // digit start inside the tile: exclusive scan over digits (16 lanes)
-    uint32_t incl = run;
+    uint32_t incl = total;
     for (int o = 1; o < 16; o <<= 1) {
       uint32_t v = __shfl_up_sync(0x0000ffffu, incl, o, 16);
       if (d >= (uint32_t)o) incl += v;
     }
-    s_tile_start[d] = incl - run;
+    s_tile_start[d] = incl - total;
     // exclusive global offset of digit d in this pass
     uint32_t g = 0;
     for (uint32_t e = 0; e < d; ++e) g += sc.hist[pass * 16 + e];
     // decoupled look-back
     volatile uint32_t* desc = sc.desc + (size_t)pass * ((size_t)gridDim.x * 16);
     if (tile == 0) {
-      desc[d] = kFlagP | run;
+      desc[d] = kFlagP | total;
       s_base[d] = g;
     } else {
-      desc[(size_t)tile * 16 + d] = kFlagA | run;
+      desc[(size_t)tile * 16 + d] = kFlagA | total;
       __threadfence();
       uint32_t excl = 0;
       int t = (int)tile - 1;
@@ -159,20 +173,20 @@ __global__ void __launch_bounds__(kSortThreads) sort_pass_kernel(const uint32_t*
         if (flag == kFlagP) break;
         --t;
       }
-      desc[(size_t)tile * 16 + d] = kFlagP | (excl + run);
+      desc[(size_t)tile * 16 + d] = kFlagP | (excl + total);
       s_base[d] = g + excl;
     }
   }
   __syncthreads();
-  // stage in tile order
+  // stage in tile order; values are read here, in the same coalesced order
 #pragma unroll
   for (int j = 0; j < kSortItems; ++j) {
-    uint32_t local = warp * (32 * kSortItems) + j * 32 + lane;
+    const uint32_t local = warp * (32 * kSortItems) + j * 32 + lane;
     if (local < count) {
-      uint32_t d = (key[j] >> shift) & dmask;
-      uint32_t pos = s_tile_start[d] + s_cnt[warp][d] + rank[j];
+      const uint32_t d = (key[j] >> shift) & dmask;
+      const uint32_t pos = s_tile_start[d] + s_cnt[warp][d] + rank[j];
       s_keys[pos] = key[j];
-      s_vals[pos] = val[j];
+      s_vals[pos] = vin ? vin[tile0 + local] : tile0 + local;
     }
   }
   __syncthreads();

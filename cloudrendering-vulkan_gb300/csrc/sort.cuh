@@ -8,7 +8,7 @@
 
 namespace vcr {
 
-constexpr uint32_t kSortTileKeys = 2048;  // keys per tile (256 threads x 8)
+constexpr uint32_t kSortTileKeys = 4096;  // keys per tile (256 threads x 16)
 
 constexpr size_t sort_round256(size_t b) { return (b + 255) & ~(size_t)255; }
 constexpr size_t sort_tiles(uint32_t n) { return ((size_t)n + kSortTileKeys - 1) / kSortTileKeys; }

@@ -91,6 +91,29 @@ constexpr uint32_t kDefaultSortLookback = 1u << 22;
 constexpr uint32_t kDefaultStageWait = 1u << 24;
 vcr_wait_limits wait_limits();
 
+// What a gather launch tested (a device counter) and its device time (two
+// events recorded around the launch on its stream), for the techniques'
+// info calls.
+struct GatherProbe {
+  unsigned long long* d_count = nullptr;
+  cudaEvent_t start = nullptr, stop = nullptr;
+  bool recorded = false;
+};
+vcr_status probe_begin(vcr_ctx* ctx, GatherProbe& p, cudaStream_t s);  // allocates on first use
+vcr_status probe_end(vcr_ctx* ctx, GatherProbe& p, cudaStream_t s);
+vcr_status probe_read(vcr_ctx* ctx, GatherProbe& p, uint64_t& count, float& ms);  // waits for the launch
+void probe_free(GatherProbe& p);
+
+// Adds a thread's count to a launch counter, one atomic per warp (every
+// lane of the warp must call it).
+#if defined(__CUDACC__)
+__device__ __forceinline__ void warp_count(unsigned long long* dst, uint32_t v) {
+  unsigned long long t = v;
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  if ((threadIdx.x & 31u) == 0 && t) atomicAdd(dst, t);
+}
+#endif
+
 // Scratch buffer owned by the context (grown, never shrunk).
 vcr_status ensure_scratch(vcr_ctx* ctx, size_t bytes);
 
@@ -114,8 +137,10 @@ vcr_status dda_trace_launch(vcr_ctx* ctx, const float* d_o, const float* d_d, ui
 // pt_global.cu: one pass; with `train`, the radiance cache's training
 // paths run in the same wavefront launch ahead of the camera paths
 struct NrcTrainSink;
+// `count` consecutive passes (pass_index, pass_index + 1, ...) in one DDA
+// wavefront launch when count > 1.
 vcr_status pt_pass_launch(vcr_ctx* ctx, const vcr_pass_desc* pass, cudaStream_t s,
-                          const NrcTrainSink* train = nullptr);
+                          const NrcTrainSink* train = nullptr, uint32_t count = 1);
 
 // ppb.cu / ppm.cu / nrc.cu: release technique state (vcr_destroy)
 void ppb_free(vcr_ctx* ctx);

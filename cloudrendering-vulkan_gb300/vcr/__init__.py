@@ -228,6 +228,14 @@ class Context:
             p.crop[i] = crop[i]
         self._ck(lib().vcr_pt_pass(self.h, C.byref(p), C.c_void_p(stream)))
 
+    def pt_passes(self, seed=0, first=0, count=1, spp=1, crop=(0, 0, 0, 0), stream=0):
+        """`count` consecutive passes (first, first + 1, ...) in one launch."""
+        p = _abi.PassDesc()
+        p.seed, p.pass_index, p.spp, p.flags = seed, first, spp, 0
+        for i in range(4):
+            p.crop[i] = crop[i]
+        self._ck(lib().vcr_pt_passes(self.h, C.byref(p), count, C.c_void_p(stream)))
+
     def counters(self):
         out = (C.c_uint64 * 4)()
         self._ck(lib().vcr_pt_counters(self.h, out))
@@ -244,8 +252,8 @@ class Context:
     NRC_WEIGHTS = 21504
 
     def nrc_setup(self, train_samples=65536, learning_rate=1e-3, query_capacity=1 << 21, seed=1, ema_decay=0.0,
-                  tail_survival=0.0):
-        p = _abi.NrcParams(train_samples, learning_rate, query_capacity, seed, ema_decay, tail_survival)
+                  tail_survival=0.0, query_kernel=0):
+        p = _abi.NrcParams(train_samples, learning_rate, query_capacity, seed, ema_decay, tail_survival, query_kernel)
         self._ck(lib().vcr_nrc_setup(self.h, C.byref(p)))
 
     def nrc_free(self):
@@ -398,6 +406,14 @@ class Context:
         i = _abi.PpbInfo()
         self._ck(lib().vcr_ppb_info(self.h, C.byref(i)))
         return {f: getattr(i, f) for f, _ in _abi.PpbInfo._fields_}
+
+    def gather_stats(self, technique):
+        """(candidates the last pass's gather tested, its device ms) for
+        technique "ppm" (leaf photons) or "ppb" (pixel-segment pairs)."""
+        c, ms = C.c_uint64(), C.c_float()
+        fn = lib().vcr_ppm_gather_stats if technique == "ppm" else lib().vcr_ppb_gather_stats
+        self._ck(fn(self.h, C.byref(c), C.byref(ms)))
+        return int(c.value), float(ms.value)
 
     def ppb_read(self, name, photons=None) -> np.ndarray:
         info = self.ppb_info()

@@ -23,6 +23,7 @@ TRACKER_GLOBAL, TRACKER_DDA = 0, 1
 BUF_IMAGE_MEAN, BUF_IMAGE_SUM, BUF_PATH_STATS, BUF_PPM_STATS, BUF_SHADOW_VOLUME = range(5)
 ORDER_RGBA, ORDER_BGRA = range(2)
 PASS_RECORD_STATS, PASS_NO_ACCUMULATE = 1, 2
+NRC_QUERY_DEFAULT, NRC_QUERY_MMA, NRC_QUERY_TCGEN05 = 0, 1, 2
 
 F3 = C.c_float * 3
 
@@ -79,7 +80,8 @@ class BatchInfo(C.Structure):
 
 class NrcParams(C.Structure):
     _fields_ = [("train_samples", C.c_uint32), ("learning_rate", C.c_float), ("query_capacity", C.c_uint32),
-                ("seed", C.c_uint32), ("ema_decay", C.c_float), ("tail_survival", C.c_float)]
+                ("seed", C.c_uint32), ("ema_decay", C.c_float), ("tail_survival", C.c_float),
+                ("query_kernel", C.c_uint32)]
 
 
 class NrcInfo(C.Structure):
@@ -160,6 +162,7 @@ SIGNATURES = {
     "vcr_reset_accumulation": (_S, [_P]),
     "vcr_shadow_volume_build": (_S, [_P, C.POINTER(ShadowVolume), _P]),
     "vcr_pt_pass": (_S, [_P, C.POINTER(PassDesc), _P]),
+    "vcr_pt_passes": (_S, [_P, C.POINTER(PassDesc), _u32, _P]),
     "vcr_pt_counters": (_S, [_P, C.POINTER(_u64)]),
     "vcr_dda_trace": (_S, [_P, _P, _P, _u32, _u32, _P, _P, _P, _P]),
     "vcr_nrc_setup": (_S, [_P, C.POINTER(NrcParams)]),
@@ -189,11 +192,13 @@ SIGNATURES = {
     "vcr_ppm_free": (_S, [_P]),
     "vcr_ppm_pass": (_S, [_P, C.POINTER(PassDesc), _P]),
     "vcr_ppm_info": (_S, [_P, C.POINTER(PpmInfo)]),
+    "vcr_ppm_gather_stats": (_S, [_P, C.POINTER(_u64), C.POINTER(_f)]),
     "vcr_ppm_read": (_S, [_P, C.c_int, _P, _sz]),
     "vcr_ppb_setup": (_S, [_P, C.POINTER(PpbParams)]),
     "vcr_ppb_free": (_S, [_P]),
     "vcr_ppb_pass": (_S, [_P, C.POINTER(PassDesc), _P]),
     "vcr_ppb_info": (_S, [_P, C.POINTER(PpbInfo)]),
+    "vcr_ppb_gather_stats": (_S, [_P, C.POINTER(_u64), C.POINTER(_f)]),
     "vcr_ppb_read": (_S, [_P, C.c_int, _P, _sz]),
     "vcr_lbvh_build": (_S, [_P, _P, _P, _P, _P, _u32, _P, _P, _P, _P, _P, _P, _P]),
     "vcr_radix_sort_pairs": (_S, [_P, _P, _P, _P, _P, _u32, _u32, _u32, _P]),

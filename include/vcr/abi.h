@@ -324,6 +324,17 @@ VCR_API vcr_status vcr_shadow_volume_build(vcr_ctx* ctx, const vcr_shadow_volume
  * the FP64 sums.  vcr_params.tracker selects the reference per-pixel
  * global-majorant tracker or the persistent DDA wavefront tracker. */
 VCR_API vcr_status vcr_pt_pass(vcr_ctx* ctx, const vcr_pass_desc* pass, void* stream);
+/* `count` consecutive progressive passes (first->pass_index, +1, ...) of the
+ * DDA wavefront tracker in one launch: the same paths, random streams and
+ * per-pass radiance as `count` calls of vcr_pt_pass (the FP64 sums equal
+ * up to the order of their additions).  One persistent launch lets the
+ * lanes that would idle while a pass's longest paths finish run the next
+ * pass's paths.  Needs the DDA tracker without the cache; no
+ * VCR_PASS_RECORD_STATS or VCR_PASS_NO_ACCUMULATE.  vcr_pt_counters then
+ * reports the totals of all `count` passes.  Replaces `count` frames of
+ * RenderTechniquePT::RecordDrawCommands (RenderTechniquePT.cpp:129-168)
+ * whose images are not displayed in between. */
+VCR_API vcr_status vcr_pt_passes(vcr_ctx* ctx, const vcr_pass_desc* first, uint32_t count, void* stream);
 /* Tracker tuning (vcr_tuning).  Defaults: level 2, 4 steps, staging on,
  * 256 threads.  vcr_autotune_pt times one pass of `pass` per candidate on
  * `stream` (the passes are rendered into the sums and then reset), keeps
@@ -369,7 +380,13 @@ typedef struct vcr_nrc_params {
                               continue each event with this probability and
                               weight 1/p (Russian roulette: unbiased targets,
                               a shorter latency tail) */
+  uint32_t query_kernel;   /* VCR_NRC_QUERY_*: which tensor-core kernel
+                              serves the cache's queries */
 } vcr_nrc_params;
+
+#define VCR_NRC_QUERY_DEFAULT 0u  /* the library's choice (the faster measured) */
+#define VCR_NRC_QUERY_MMA 1u      /* warp-level mma.sync, 16-record tiles per warp */
+#define VCR_NRC_QUERY_TCGEN05 2u  /* tcgen05.mma, 128-record tiles, TMEM accumulators */
 
 typedef struct vcr_nrc_info_t {
   uint32_t steps;         /* Adam steps taken */
@@ -464,6 +481,10 @@ VCR_API vcr_status vcr_ppm_free(vcr_ctx* ctx);
  * current estimate times the pass count. */
 VCR_API vcr_status vcr_ppm_pass(vcr_ctx* ctx, const vcr_pass_desc* pass, void* stream);
 VCR_API vcr_status vcr_ppm_info(vcr_ctx* ctx, vcr_ppm_info_t* out);
+/* The last pass's gather kernel: leaf photons it tested against the
+ * pixels' radii and its device time (two events around the launch).
+ * Waits for the gather to finish.  No reference counterpart (measurement). */
+VCR_API vcr_status vcr_ppm_gather_stats(vcr_ctx* ctx, uint64_t* photons_tested, float* ms);
 VCR_API vcr_status vcr_ppm_read(vcr_ctx* ctx, vcr_ppm_buffer which, void* host_out, size_t bytes);
 
 /* ------------------------------------------------------------------------ */
@@ -513,6 +534,10 @@ VCR_API vcr_status vcr_ppb_free(vcr_ctx* ctx);
  * :530-546).  One estimate per pixel is added to the FP64 sums. */
 VCR_API vcr_status vcr_ppb_pass(vcr_ctx* ctx, const vcr_pass_desc* pass, void* stream);
 VCR_API vcr_status vcr_ppb_info(vcr_ctx* ctx, vcr_ppb_info_t* out);
+/* The last pass's gather kernel: (pixel, beam segment) pairs it evaluated
+ * (segments whose box the pixel's ray hit) and its device time.  Waits for
+ * the gather to finish.  No reference counterpart (measurement). */
+VCR_API vcr_status vcr_ppb_gather_stats(vcr_ctx* ctx, uint64_t* segments_evaluated, float* ms);
 /* Synchronous copy of one of the last pass's beam buffers. */
 VCR_API vcr_status vcr_ppb_read(vcr_ctx* ctx, vcr_ppb_buffer which, void* host_out, size_t bytes);
 /* LBVH over n Morton-sorted segments (device buffers): Karras build with

@@ -98,6 +98,33 @@ def test_c5_full_frames_match_the_oracle(cuda, c5_oracle, tuning):
             assert events > W * H  # the frame sees dense cloud
 
 
+def test_c5_passes_in_one_launch_match_the_oracle(cuda, c5_oracle):
+    """Three consecutive passes of the benchmark scene in one launch
+    (vcr_pt_passes, the benchmark's timed form): the sums equal the
+    oracle's three passes up to the order of the FP64 additions."""
+    sc, og = c5_oracle
+    W, H = sc.width, sc.height
+    cloud = sc.cloud()
+    cloud.max_extinction = max(og.max_density(), 0.01)
+    cam, prm = sc.camera(), sc.params(vcr.TRACKER_DDA)
+    with vcr.Context() as ctx:
+        configs.setup_context(ctx, sc)
+        ctx.set_cloud(cloud)
+        ctx.set_tuning(majorant_level=3, dda_steps=16, stage_majorants=1, block_threads=256)
+        ctx.pt_passes(seed=9, first=4, count=3)
+        ctx.synchronize()
+        g_sum = ctx.image_sum()
+        lookups = ctx.counters()[1]
+    o_sum = None
+    o_look = 0
+    for k in range(4, 7):
+        o_sum, o_st = og.pt_pass(cloud, cam, prm, W, H, seed=9, pass_index=k, sum_img=o_sum,
+                                 flags=vcr.PASS_RECORD_STATS, level=3)
+        o_look += int(o_st[..., 1].sum())
+    np.testing.assert_allclose(g_sum, o_sum, rtol=1e-12, atol=0)
+    assert lookups == o_look
+
+
 def test_c5_paths_ending_in_the_cache_match_the_oracle(cuda, c5_oracle):
     """The cached frame's tracker at C5: paths end at their 2nd event in the
     cache; with an all-zero network the image is exactly the oracle's

@@ -31,14 +31,18 @@ def _dev_records(recs, cuda):
     return torch.from_numpy(recs.view(np.uint8).copy()).to(cuda)
 
 
-def test_forward_matches_oracle(cuda):
+@pytest.mark.parametrize("kernel,n", [(vcr.NRC_QUERY_MMA, 1000), (vcr.NRC_QUERY_TCGEN05, 1000),
+                                      (vcr.NRC_QUERY_TCGEN05, 128 * 152 * 3 + 77)])
+def test_forward_matches_oracle(cuda, kernel, n):
+    """Both query kernels (warp mma.sync tiles; tcgen05 128-record tiles
+    with TMEM accumulators, several tiles per CTA and a ragged last one)."""
     import torch
     desc, cloud = _cloud()
     rng = np.random.default_rng(1)
-    recs = onrc.random_records(1000, cloud, rng)
+    recs = onrc.random_records(n, cloud, rng)
     with vcr.Context() as ctx:
         _ctx_with_cloud(ctx, desc, cloud)
-        ctx.nrc_setup(train_samples=4096, seed=7)
+        ctx.nrc_setup(train_samples=4096, seed=7, query_kernel=kernel)
         w = ctx.nrc_get_weights()
         dr = _dev_records(recs, cuda)
         out = torch.zeros(3 * len(recs), dtype=torch.float32, device=cuda)
@@ -48,6 +52,40 @@ def test_forward_matches_oracle(cuda):
     scale = np.abs(ref).mean() + 1e-3
     assert np.abs(got - ref).max() <= 3e-2 * scale, (np.abs(got - ref).max(), scale)
     assert np.abs(got - ref).mean() <= 3e-3 * scale
+
+
+def test_query_kernels_agree_in_a_cached_render(cuda):
+    """A cached frame with trained weights: the tcgen05 queries give the
+    image of the mma.sync queries up to BF16 rounding of the activations
+    (the paths and their queries are identical; only the cache term
+    differs)."""
+    sc = configs.C1_PT
+    W = H = 128
+    prm = sc.params(vcr.TRACKER_DDA)
+    prm.nrc_events = 2
+    with vcr.Context() as ctx:  # trained weights to query with
+        configs.setup_context(ctx, sc, width=W, height=H)
+        ctx.set_params(prm)
+        ctx.nrc_setup(train_samples=8192, learning_rate=3e-3, query_capacity=W * H, seed=2)
+        for k in range(30):
+            ctx.nrc_train_step(seed=4, pass_index=k)
+        ctx.synchronize()
+        w = ctx.nrc_get_weights()
+    imgs = []
+    for kernel in (vcr.NRC_QUERY_MMA, vcr.NRC_QUERY_TCGEN05):
+        with vcr.Context() as ctx:
+            configs.setup_context(ctx, sc, width=W, height=H)
+            ctx.set_params(prm)
+            ctx.nrc_setup(train_samples=8192, query_capacity=W * H, seed=2, query_kernel=kernel)
+            ctx.nrc_set_weights(w)
+            ctx.pt_pass(seed=6, pass_index=0)
+            ctx.synchronize()
+            imgs.append((ctx.image_sum(), ctx.nrc_info()["queries"]))
+    (ia, qa), (ib, qb) = imgs
+    assert qa == qb > 1000
+    d = np.abs(ia - ib)
+    assert d.max() <= 2e-2 * (np.abs(ia).max() + 1e-3), d.max()
+    assert d.mean() <= 1e-3 * (np.abs(ia).mean() + 1e-3), d.mean()
 
 
 @pytest.mark.parametrize("n", [4096, 20037])  # whole tiles; a ragged last tile and two tiles on some CTAs

@@ -94,6 +94,8 @@ def test_ppb_pass_bit_exact(cuda, pass_index, cap):
         info = ctx.ppb_info()
         gb = {k: ctx.ppb_read(k, photons) for k in _abi_buffers()}
         g_sum = ctx.image_sum()
+        evaluated, ms = ctx.gather_stats("ppb")
+    assert evaluated > 0 and ms > 0.0
     o_sum, ob = orc.ppb_pass(g, cloud, cam, prm, photons, cap, r0, alpha, W, H, seed=11, pass_index=pass_index)
     assert info["segments"] == ob["info"]["segments"] and info["dropped"] == ob["info"]["dropped"]
     assert info["radius"] == np.float32(orc.ppb_radius(r0, alpha, pass_index))

@@ -60,6 +60,8 @@ def test_ppm_passes_bit_exact(cuda, level):
             np.testing.assert_array_equal(ctx.ppm_read("right"), o["right"])
             np.testing.assert_array_equal(ctx.ppm_read("stats"), st)
             np.testing.assert_array_equal(ctx.image_sum(), s_o)
+            tested, ms = ctx.gather_stats("ppm")  # leaf photons the gather tested
+            assert tested > 0 and ms > 0.0
         assert ctx.pass_count() == 3
         m = ctx.image_mean()
         np.testing.assert_allclose(m, (s_o / 3).astype(np.float32), rtol=1e-6)

@@ -240,3 +240,36 @@ def test_multi_pass_accumulation_and_mean(cuda):
         m = ctx.image_mean()
         np.testing.assert_allclose(m, (s / 4).astype(np.float32), rtol=1e-7)
         assert np.isfinite(s).all() and s.min() >= 0
+
+
+def test_several_passes_in_one_launch_equal_single_passes(cuda):
+    """vcr_pt_passes: the same paths and random streams as one vcr_pt_pass
+    per pass; the FP64 sums equal up to the order of their additions."""
+    sc = configs.C1_PT
+    W = H = 128
+    with vcr.Context() as ctx:
+        configs.setup_context(ctx, sc, width=W, height=H)
+        ctx.set_tuning(majorant_level=2, dda_steps=8, stage_majorants=1, block_threads=256)
+        tot = np.zeros(4, np.uint64)
+        for k in range(5):
+            ctx.pt_pass(seed=3, pass_index=10 + k)
+            tot += np.array(ctx.counters(), np.uint64)
+        ctx.synchronize()
+        single = ctx.image_sum()
+        ctx.reset()
+        ctx.pt_passes(seed=3, first=10, count=5)
+        ctx.synchronize()
+        multi = ctx.image_sum()
+        assert ctx.pass_count() == 5
+        np.testing.assert_array_equal(np.array(ctx.counters(), np.uint64), tot)
+        with pytest.raises(vcr.VcrError):
+            ctx.pt_passes(seed=3, first=0, count=0)
+        p = vcr._abi.PassDesc()
+        p.seed, p.pass_index, p.spp, p.flags = 3, 0, 1, vcr.PASS_RECORD_STATS
+        assert vcr.lib().vcr_pt_passes(ctx.h, p, 2, None) == vcr.ERR_INVALID
+        prm = sc.params(vcr.TRACKER_GLOBAL)
+        ctx.set_params(prm)
+        with pytest.raises(vcr.VcrError):
+            ctx.pt_passes(seed=3, first=0, count=2)
+    np.testing.assert_allclose(multi, single, rtol=1e-12, atol=0)
+    assert (single > 0).any()
