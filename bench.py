@@ -167,7 +167,7 @@ def run_vcr(args):
     if ws > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    sc = configs.C5_NRC
+    sc = _divided(configs.C5_NRC, args.image_div)  # --image-div: a small case for profiler captures
     W, H = sc.width, sc.height
     prec = sc.precision
     stream = torch.cuda.Stream()
@@ -228,7 +228,7 @@ def run_vcr(args):
     tpl = traffic_per_lookup()
 
     # e2e through the C-ABI with host buffers
-    e2e = run_e2e(args, sc, local, sh) if rank == 0 else None
+    e2e = run_e2e(args, sc, local, sh, tuning) if rank == 0 else None
 
     if rank != 0:
         return
@@ -823,9 +823,10 @@ def run_nrc_frames(args):
                       "train_records": info["train_records"]}), flush=True)
 
 
-def run_e2e(args, sc, device, sh):
+def run_e2e(args, sc, device, sh, tuning=None):
     """Grid upload from pinned host memory + per-pass mean-image read back,
-    all through the C-ABI, wall-clock timed."""
+    all through the C-ABI, wall-clock timed (the tracker's tuning is set
+    before the timed region, as a caller sets it once)."""
     import torch
     import vcr
 
@@ -834,6 +835,8 @@ def run_e2e(args, sc, device, sh):
     img_bytes = sc.width * sc.height * 3 * 4
     img = torch.empty(sc.width * sc.height * 3, dtype=torch.float32).pin_memory()  # the result, read every pass
     with vcr.Context(device) as ctx:
+        if tuning:
+            ctx.set_tuning(**tuning)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         import ctypes as C
@@ -844,6 +847,8 @@ def run_e2e(args, sc, device, sh):
         ctx.set_camera(sc.camera())
         ctx.set_params(sc.params(vcr.TRACKER_DDA))
         ctx.set_frame(sc.width, sc.height)
+        ctx.synchronize()
+        t_up = time.perf_counter()
         for k in range(args.steps):
             ctx.pt_pass(seed=5, pass_index=k, stream=sh)
             ctx.readback_to(vcr.BUF_IMAGE_MEAN, img.data_ptr(), img_bytes)  # waits for the pass
@@ -851,7 +856,9 @@ def run_e2e(args, sc, device, sh):
     grid_bytes = dense.nbytes
     return {"value": round(sc.width * sc.height * args.steps / (t1 - t0) / 1e6, 3), "unit": UNIT,
             "h2d_bytes_per_step": int(grid_bytes // args.steps), "d2h_bytes_per_step": img_bytes,
-            "note": "grid (FP32, pinned) uploaded once per run; mean image read back into pinned memory every pass"}
+            "upload_s": round(t_up - t0, 4), "passes_s": round(t1 - t_up, 4),
+            "note": "grid (FP32, pinned) uploaded once per run; one launch per pass and its mean image read back "
+                    "into pinned memory after every pass"}
 
 
 class OracleScene:
@@ -958,7 +965,7 @@ def main():
     ap.add_argument("--display", action="store_true", help="only measure the display-image kernel")
     ap.add_argument("--sort", action="store_true", help="only measure the radix sort")
     ap.add_argument("--image-div", type=int, default=1,
-                    help="divide the --ppm / --ppb image sides (a small case for profiler captures)")
+                    help="divide the image sides (a small case of the workload for profiler captures)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
