@@ -1,5 +1,6 @@
 // Volumetric progressive photon mapping: photon emission, photon tree,
-// per-pixel gather and the progressive N / R / flux update in FP64.
+// per-pixel gather and the progressive N / R / flux update in FP64, or the
+// reference's ray-marched estimate with one global radius per pass.
 //
 // Reference: PPM_PT.comp (main :452-489, interactWithMedium :393-447,
 // depositPhoton :304-321), PPM_PE.comp (samplePhotonMap :304-375, ray march
@@ -20,6 +21,8 @@
 //   L = background / k + albedo tau / (4/3 pi R^3 k).
 // Photons are stored at every real collision with the power arriving there,
 // so direct and multiple scattering both come from the photon map.
+#include <cmath>
+
 #include "track.cuh"
 #include "sort.cuh"
 #include "ppb.cuh"
@@ -252,6 +255,115 @@ __global__ void __launch_bounds__(128) ppm_gather_kernel(GridView g, SceneView s
   warp_count(tested, cand);
 }
 
+// ---------------------------------------------------------------------------
+// The reference's estimate: a ray march with one global radius
+// (PPM_PE.comp main :443-546, samplePhotonMap :304-375)
+// ---------------------------------------------------------------------------
+constexpr uint32_t kPpmMarchSalt = 0x5F356495u;
+constexpr uint32_t kMarchCap = 1u << 20;  // march and ambient steps of one pixel
+constexpr float kPI4_3 = kPI * 4.0f / 3.0f;
+
+// samplePhotonMap at x: the photons within the global radius r, phase
+// toward wo times power, in the tree's depth-first leaf order, over the
+// sphere volume times sigma_s.  Like the reference it draws one random
+// number when the sum is positive (its unused six-tap density average).
+__device__ f3 march_photon_map(const PpmGatherView& v, const SceneView& s, f3 x, f3 wo, float r, float scatter,
+                               Rng& rng, uint32_t& cand) {
+  f3 phi = mk(0.f, 0.f, 0.f);
+  if (scatter == 0.0f || v.n <= 0) return phi;
+  const float r2 = r * r;
+  uint32_t stack[kGatherStack];
+  int sp = 0;
+  uint32_t node = v.n == 1 ? kLeafBit : 0u;
+  while (true) {
+    if (node & kLeafBit) {
+      const uint32_t lf = node & ~kLeafBit;
+      ++cand;
+      const float4 q = v.leaf_lo[lf];
+      const f3 dq = mk(q.x, q.y, q.z) - x;
+      if (dot(dq, dq) <= r2) {
+        const uint32_t ph = v.order[lf];
+        const float4 w = v.dir[ph], pw = v.pw[ph];
+        const float f = hg_pdf(s.ph, dot(wo, mk(w.x, w.y, w.z)));
+        phi = phi + mk(f * pw.x, f * pw.y, f * pw.z);
+      }
+    } else if (box_dist2(x, v.node_lo[node], v.node_hi[node]) <= r2) {
+      if (sp < kGatherStack) stack[sp++] = v.right[node];
+      node = v.left[node];
+      continue;
+    }
+    if (sp == 0) break;
+    node = stack[--sp];
+  }
+  if ((phi.x + phi.y) + phi.z <= 0.0f) return mk(0.f, 0.f, 0.f);
+  rng_next(rng);
+  const float den = ((kPI4_3 * r) * r2) * scatter;
+  return mk(phi.x / den, phi.y / den, phi.z / den);
+}
+
+__global__ void __launch_bounds__(128) ppm_march_kernel(GridView g, SceneView s, CamView cam, SvView sv, PassView pv,
+                                                        PpmGatherView v, float radius, float step, float amb_step,
+                                                        double* __restrict__ sum, Counters cnt,
+                                                        unsigned long long* __restrict__ tested) {
+  const uint32_t id = blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t lookups = 0, cand = 0;
+  if (id < pv.cw * pv.ch) {
+    const uint32_t cy = id / pv.cw, cx = id - cy * pv.cw;
+    const int x = (int)(pv.x0 + cx), y = (int)(pv.y0 + cy);
+    const uint32_t pix = (uint32_t)y * pv.width + (uint32_t)x;
+    Rng rng = s.rng_mode == 1 ? rng_xorshift(pv.seed * ((uint32_t)x + (uint32_t)y * pv.padded_w))
+                              : rng_pcg(pv.seed ^ kPpmMarchSalt, pix, pv.pass);
+    f3 pos, rd;
+    camera_ray(cam, x, y, pos, rd);
+    f3 L = sky(s, rd);
+    float tmin, tmax;
+    if (slab(pos, rd, s.b0, s.b1, tmin, tmax) && s.ds > 0.0f) {
+      const f3 closest = along(pos, rd, tmin);
+      pos = along(pos, rd, tmax - step * rng_next(rng));
+      const float max_d = length(pos - closest);
+      const f3 wo = -rd;
+      float cur = 0.0f;
+      for (uint32_t it = 0; cur < max_d && it < kMarchCap; ++it) {
+        pos = pos - rd * step;
+        cur = cur + step;
+        const float ext = (density_at(g, s, pos) * s.ds) / s.bs;
+        ++lookups;
+        const float scatter = s.albedo * ext;
+        const float pdf = hg_pdf(s.ph, dot(wo, s.sun));
+        const float dl = (s.light * pdf) * sv_lookup(sv, pos);
+        f3 direct = mk(dl, dl, dl);
+        // ambient: the sky along a phase-sampled direction, attenuated by
+        // the mean extinction of a coarse march to the box
+        const f3 adir = hg_sample(s.ph, rd, rng, false);
+        f3 ap = pos;
+        float acc = 0.0f, adist = 0.0f;
+        uint32_t n = 0;
+        f3 amb = sky(s, adir);
+        while (in_box(ap, s.b0, s.b1) && n < kMarchCap) {
+          ap = ap + adir * amb_step;
+          acc = acc + density_at(g, s, ap);
+          adist = adist + amb_step;
+          ++n;
+        }
+        lookups += n;
+        if (n > 0) {
+          acc = acc * (s.ds / s.bs);
+          const float att = vexp(((-adist) * acc) / (float)n);
+          amb = amb * att;
+          if (amb.x > 0.0f) direct = direct + amb;
+        }
+        const f3 ind = march_photon_map(v, s, pos, wo, radius, scatter, rng, cand) * s.albedo;
+        const float a = vexp((-step) * ext);
+        const f3 src = direct + ind;
+        L = L * a + mk((scatter * src.x) * step, (scatter * src.y) * step, (scatter * src.z) * step);
+      }
+    }
+    write_result(pv, sum, pix, L);
+  }
+  flush_counters(cnt, id < pv.cw * pv.ch ? 1ull : 0ull, lookups, 0, 0);
+  warp_count(tested, cand);
+}
+
 __global__ void ppm_init_stats_kernel(double* __restrict__ stats, size_t pixels, double r0) {
   size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= pixels) return;
@@ -280,8 +392,11 @@ __global__ void iota_kernel(uint32_t* __restrict__ v, uint32_t n) {
 
 vcr_status ppm_setup(vcr_ctx* ctx, const vcr_ppm_params* p) {
   if (!p || p->photons == 0 || p->photons > (1u << 26) || p->capacity < 2 || p->capacity > (1u << 28) ||
-      !(p->radius > 0.0f) || !(p->alpha > 0.0f && p->alpha <= 1.0f))
-    return fail(ctx, VCR_ERR_INVALID, "ppm params: photons 1..2^26, capacity 2..2^28, radius > 0, alpha in (0,1]");
+      !(p->radius > 0.0f) || !(p->alpha > 0.0f && p->alpha <= 1.0f) || p->estimator > VCR_PPM_MARCH ||
+      (p->estimator == VCR_PPM_MARCH && !(p->march_step > 0.0f && p->ambient_step > 0.0f)))
+    return fail(ctx, VCR_ERR_INVALID,
+                "ppm params: photons 1..2^26, capacity 2..2^28, radius > 0, alpha in (0,1], estimator "
+                "VCR_PPM_GATHER or VCR_PPM_MARCH (with march_step > 0, ambient_step > 0)");
   if (!ctx->d_sum) return fail(ctx, VCR_ERR_STATE, "vcr_ppm_setup needs a frame (vcr_set_frame)");
   ppm_free(ctx);
   PpmState* st = new PpmState();
@@ -320,6 +435,27 @@ vcr_status ppm_setup(vcr_ctx* ctx, const vcr_ppm_params* p) {
   return ensure_scratch(ctx, sort_scratch_bytes(p->capacity));
 }
 
+// RenderTechniquePPM::UpdateRadius (:302-312) for frame k + 1 (pass k):
+// r_1 = R0, r_n = r_(n-1) ((n - 1 + alpha) / n)^0.33333, in float.
+float ppm_global_radius(float r0, float alpha, uint32_t pass) {
+  float r = r0;
+  for (uint32_t n = 2; n <= pass + 1; ++n) r = r * std::pow(((float)(n - 1) + alpha) / (float)n, 0.33333f);
+  return r;
+}
+
+static SvView sv_view(const vcr_ctx* ctx) {
+  SvView sv{};
+  sv.tex = ctx->d_sv;
+  sv.n = (int)ctx->sv.voxel_axis_count;
+  sv.b0 = mk(ctx->sv.bounds_min[0], ctx->sv.bounds_min[1], ctx->sv.bounds_min[2]);
+  const f3 e = mk(ctx->sv.bounds_max[0], ctx->sv.bounds_max[1], ctx->sv.bounds_max[2]) - sv.b0;
+  for (int i = 0; i < 9; ++i) sv.B[i] = ctx->sv.basis_change[i];
+  sv.ext.x = (sv.B[0] * e.x + sv.B[1] * e.y) + sv.B[2] * e.z;
+  sv.ext.y = (sv.B[3] * e.x + sv.B[4] * e.y) + sv.B[5] * e.z;
+  sv.ext.z = (sv.B[6] * e.x + sv.B[7] * e.y) + sv.B[8] * e.z;
+  return sv;
+}
+
 vcr_status ppm_pass_launch(vcr_ctx* ctx, const vcr_pass_desc* pass, cudaStream_t cs) {
   PpmState* st = ctx->ppm;
   if (!st) return fail(ctx, VCR_ERR_STATE, "vcr_ppm_pass needs vcr_ppm_setup");
@@ -327,7 +463,11 @@ vcr_status ppm_pass_launch(vcr_ctx* ctx, const vcr_pass_desc* pass, cudaStream_t
     return fail(ctx, VCR_ERR_STATE, "vcr_ppm_pass needs a grid, cloud, camera, params and frame");
   if ((size_t)ctx->width * ctx->height != st->pixels)
     return fail(ctx, VCR_ERR_STATE, "the frame changed since vcr_ppm_setup");
-  if (ctx->params.rng_mode != VCR_RNG_PCG) return fail(ctx, VCR_ERR_UNSUPPORTED, "photon mapping uses PCG streams");
+  const bool march = st->prm.estimator == VCR_PPM_MARCH;
+  if (ctx->params.rng_mode != VCR_RNG_PCG && !march)
+    return fail(ctx, VCR_ERR_UNSUPPORTED, "the gather estimate uses PCG streams");
+  if (march && !ctx->has_sv)
+    return fail(ctx, VCR_ERR_STATE, "the march estimate needs vcr_shadow_volume_build first");
   PassView pv;
   vcr_status vs = make_pass_view(ctx, pass, pv);
   if (vs) return vs;
@@ -366,8 +506,14 @@ vcr_status ppm_pass_launch(vcr_ctx* ctx, const vcr_pass_desc* pass, cudaStream_t
   uint32_t pixels = pv.cw * pv.ch;
   vcr_status ps = probe_begin(ctx, st->gather, cs);
   if (ps) return ps;
-  ppm_gather_kernel<<<(pixels + 127) / 128, 128, 0, cs>>>(g, s, cam_view(ctx->cam), pv, gv, ctx->d_sum, cnt,
-                                                          st->gather.d_count);
+  if (march) {
+    ppm_march_kernel<<<(pixels + 127) / 128, 128, 0, cs>>>(
+        g, s, cam_view(ctx->cam), sv_view(ctx), pv, gv, ppm_global_radius(st->prm.radius, st->prm.alpha, pv.pass),
+        st->prm.march_step, st->prm.ambient_step, ctx->d_sum, cnt, st->gather.d_count);
+  } else {
+    ppm_gather_kernel<<<(pixels + 127) / 128, 128, 0, cs>>>(g, s, cam_view(ctx->cam), pv, gv, ctx->d_sum, cnt,
+                                                            st->gather.d_count);
+  }
   VCR_CUDA(ctx, cudaGetLastError());
   ps = probe_end(ctx, st->gather, cs);
   if (ps) return ps;

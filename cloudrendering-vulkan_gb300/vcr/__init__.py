@@ -358,8 +358,8 @@ class Context:
         self._ck(lib().vcr_batch_reset(self.h))
 
     # photon mapping ---------------------------------------------------------
-    def ppm_setup(self, photons, capacity, radius, alpha=0.7):
-        p = _abi.PpmParams(photons, capacity, radius, alpha)
+    def ppm_setup(self, photons, capacity, radius, alpha=0.7, estimator=0, march_step=0.0, ambient_step=0.0):
+        p = _abi.PpmParams(photons, capacity, radius, alpha, estimator, march_step, ambient_step)
         self._ck(lib().vcr_ppm_setup(self.h, C.byref(p)))
 
     def ppm_free(self):

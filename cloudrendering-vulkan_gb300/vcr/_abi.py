@@ -24,6 +24,7 @@ BUF_IMAGE_MEAN, BUF_IMAGE_SUM, BUF_PATH_STATS, BUF_PPM_STATS, BUF_SHADOW_VOLUME 
 ORDER_RGBA, ORDER_BGRA = range(2)
 PASS_RECORD_STATS, PASS_NO_ACCUMULATE = 1, 2
 NRC_QUERY_DEFAULT, NRC_QUERY_MMA, NRC_QUERY_TCGEN05 = 0, 1, 2
+PPM_GATHER, PPM_MARCH = 0, 1
 
 F3 = C.c_float * 3
 
@@ -90,7 +91,8 @@ class NrcInfo(C.Structure):
 
 
 class PpmParams(C.Structure):
-    _fields_ = [("photons", C.c_uint32), ("capacity", C.c_uint32), ("radius", C.c_float), ("alpha", C.c_float)]
+    _fields_ = [("photons", C.c_uint32), ("capacity", C.c_uint32), ("radius", C.c_float), ("alpha", C.c_float),
+                ("estimator", C.c_uint32), ("march_step", C.c_float), ("ambient_step", C.c_float)]
 
 
 class PpmInfo(C.Structure):

@@ -448,9 +448,31 @@ VCR_API vcr_status vcr_nrc_gradient(vcr_ctx* ctx, const void* d_records, uint32_
 typedef struct vcr_ppm_params {
   uint32_t photons;  /* photons emitted per pass (200 x 64 in RenderTechniquePPM.cpp:253) */
   uint32_t capacity; /* photons stored per pass (every real collision); extra are dropped */
-  float radius;      /* initial per-pixel gather radius R0, world units (initialRadius) */
+  float radius;      /* initial gather radius R0, world units (initialRadius) */
   float alpha;       /* radius reduction (m_alpha, RenderTechniquePPM.h:66) */
+  uint32_t estimator;  /* VCR_PPM_GATHER or VCR_PPM_MARCH */
+  float march_step;    /* VCR_PPM_MARCH: step of the camera-ray march, world units
+                          (stepSize, UniformBuffers.h:221) */
+  float ambient_step;  /* VCR_PPM_MARCH: step of the ambient march toward the sky
+                          (sampleDist, PPM_PE.comp:513) */
 } vcr_ppm_params;
+
+/* The radiance estimate of a pass.
+ * VCR_PPM_GATHER: stochastic progressive photon mapping -- one delta-tracked
+ *   measurement point per pixel, per-pixel radius and flux statistics in
+ *   FP64 (N' = N + alpha M, R' = R ((N + alpha M)/(N + M))^(1/3)).
+ * VCR_PPM_MARCH: the reference's estimate (PPM_PE.comp:443-546): a march
+ *   back to front along the camera ray with march_step (start jittered);
+ *   at each step the shadow volume's transmittance times the phase
+ *   function toward the sun, an ambient term (the sky along a phase-sampled
+ *   direction, attenuated by a march of ambient_step to the box), and the
+ *   photon map within one global radius per pass (RenderTechniquePPM.cpp
+ *   :302-312: r_1 = R0, r_k = r_(k-1) ((k - 1 + alpha) / k)^0.33333);
+ *   L = L exp(-sigma_t step) + sigma_s (direct + indirect) step.  Needs
+ *   vcr_shadow_volume_build; the per-pixel statistics are not used; each
+ *   pass's estimate is added to the sums (the reference's running mean). */
+#define VCR_PPM_GATHER 0u
+#define VCR_PPM_MARCH 1u
 
 typedef struct vcr_ppm_info_t {
   uint32_t photons_stored; /* photons in the last pass's tree */
@@ -570,7 +592,7 @@ VCR_API vcr_status vcr_radix_sort_pairs(vcr_ctx* ctx, const uint32_t* d_keys_in,
  * loop that must not allocate after start-up, a plug-in handed buffers but
  * no allocator).  No counterpart in the reference.  It takes no context and
  * allocates nothing: its working memory is one fixed device array (about
- * 8.3 MB) inside this library, held by every GPU that loads it until the
+ * 8.5 MB) inside this library, held by every GPU that loads it until the
  * process exits.  At most VCR_SORT_NOALLOC_MAX_KEYS pairs per call (larger
  * n returns VCR_ERR_CAPACITY).  Calls share that array: calls that overlap
  * on the GPU race, so serialise them.  The first call on each device looks

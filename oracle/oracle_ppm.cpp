@@ -10,6 +10,9 @@
 //   update   : stochastic progressive photon mapping per pixel in FP64
 //              (instead of the global UpdateRadius, RenderTechniquePPM.cpp
 //              :302-312)
+//   march    : the reference's estimate instead of the gather (PPM_PE.comp
+//              main :443-546, samplePhotonMap :304-375) with the global
+//              radius of UpdateRadius (RenderTechniquePPM.cpp:302-312)
 // The float and double operations follow the CUDA kernels in order.
 #include <algorithm>
 #include <cmath>
@@ -24,6 +27,8 @@ namespace oracle {
 const uint32_t kPpmMaxEvents = 64;
 const uint32_t kPpmEmitSalt = 0x27D4EB2Fu;
 const uint32_t kPpmGatherSalt = 0x165667B1u;
+const uint32_t kPpmMarchSalt = 0x5F356495u;
+const uint32_t kMarchCap = 1u << 20;
 
 struct Photon {
   F4 pos, pw, dir;
@@ -224,6 +229,114 @@ static void gather(const Scene& s, const PhotonTree& T, const vcr_camera& cam, u
   }
 }
 
+// RenderTechniquePPM::UpdateRadius (:302-312) for frame k + 1 (pass k).
+static float global_radius(float r0, float alpha, uint32_t pass) {
+  float r = r0;
+  for (uint32_t n = 2; n <= pass + 1; ++n) r = r * std::pow(((float)(n - 1) + alpha) / (float)n, 0.33333f);
+  return r;
+}
+
+static bool inside(V3 p, V3 b0, V3 b1) {
+  return !(p.x < b0.x || p.y < b0.y || p.z < b0.z || p.x > b1.x || p.y > b1.y || p.z > b1.z);
+}
+
+// samplePhotonMap (PPM_PE.comp:304-375) with the global radius r.
+static V3 photon_map(const Scene& s, const PhotonTree& T, V3 x, V3 wo, float r, float scatter, Rng& rng) {
+  V3 phi = v3(0, 0, 0);
+  int n = (int)T.ph.size();
+  if (scatter == 0.0f || n <= 0) return phi;
+  const float r2 = r * r;
+  uint32_t stack[64];
+  int sp = 0;
+  uint32_t node = n == 1 ? kLeafBit : 0u;
+  while (true) {
+    if (node & kLeafBit) {
+      uint32_t lf = node & ~kLeafBit;
+      F4 q = T.leaf_lo[lf];
+      V3 dq = sub(v3(q.x, q.y, q.z), x);
+      if (dot(dq, dq) <= r2) {
+        const Photon& ph = T.ph[T.order[lf]];
+        float f = hg_pdf(s, dot(wo, v3(ph.dir.x, ph.dir.y, ph.dir.z)));
+        phi = add(phi, v3(f * ph.pw.x, f * ph.pw.y, f * ph.pw.z));
+      }
+    } else if (box_dist2(x, T.node_lo[node], T.node_hi[node]) <= r2) {
+      if (sp < 64) stack[sp++] = T.right[node];
+      node = T.left[node];
+      continue;
+    }
+    if (sp == 0) break;
+    node = stack[--sp];
+  }
+  if ((phi.x + phi.y) + phi.z <= 0.0f) return v3(0, 0, 0);
+  rng.next();  // the reference's unused six-tap density average draws one number
+  const float kPI4_3 = kPI * 4.0f / 3.0f;
+  float den = ((kPI4_3 * r) * r2) * scatter;
+  return v3(phi.x / den, phi.y / den, phi.z / den);
+}
+
+// PPM_PE.comp main (:443-546): back-to-front march, direct light from the
+// shadow volume, an ambient sky term, the photon map; sums += L.
+static void march(const Scene& s, const PhotonTree& T, const vcr_camera& cam, uint32_t W, uint32_t H,
+                  const vcr_pass_desc* pass, float radius, float step, float amb_step, double* sum, int threads) {
+  uint32_t x0 = pass->crop[0], y0 = pass->crop[1];
+  uint32_t cw = pass->crop[2] ? pass->crop[2] : W, ch = pass->crop[2] ? pass->crop[3] : H;
+  const uint32_t padded_w = 32u * (W / 32u + 1u);
+#pragma omp parallel for schedule(dynamic, 1) num_threads(threads > 0 ? threads : 1)
+  for (int64_t row = 0; row < (int64_t)ch; ++row) {
+    for (uint32_t cx = 0; cx < cw; ++cx) {
+      int x = (int)(x0 + cx), y = (int)(y0 + (uint32_t)row);
+      uint32_t pix = (uint32_t)y * W + (uint32_t)x;
+      Rng rng = s.rng_mode == 1 ? rng_xorshift(pass->seed * ((uint32_t)x + (uint32_t)y * padded_w))
+                                : rng_pcg(pass->seed ^ kPpmMarchSalt, pix, pass->pass_index);
+      V3 pos, rd;
+      camera_ray(cam, x, y, pos, rd);
+      V3 L = sky(s, rd);
+      float tmin, tmax;
+      if (slab(pos, rd, s.b0, s.b1, tmin, tmax) && s.ds > 0.0f) {
+        V3 closest = along(pos, rd, tmin);
+        pos = along(pos, rd, tmax - step * rng.next());
+        float max_d = length(sub(pos, closest));
+        V3 wo = neg(rd);
+        float cur = 0.0f;
+        for (uint32_t it = 0; cur < max_d && it < kMarchCap; ++it) {
+          pos = sub(pos, scale(rd, step));
+          cur = cur + step;
+          float ext = (density(s, pos) * s.ds) / s.bs;
+          float scatter = s.albedo * ext;
+          float pdf = hg_pdf(s, dot(wo, s.sun));
+          float dl = (s.light * pdf) * sv_lookup(s, pos);
+          V3 direct = v3(dl, dl, dl);
+          V3 adir = hg_sample(s, rd, rng, false);
+          V3 ap = pos;
+          float acc = 0.0f, adist = 0.0f;
+          uint32_t n = 0;
+          V3 amb = sky(s, adir);
+          while (inside(ap, s.b0, s.b1) && n < kMarchCap) {
+            ap = add(ap, scale(adir, amb_step));
+            acc = acc + density(s, ap);
+            adist = adist + amb_step;
+            ++n;
+          }
+          if (n > 0) {
+            acc = acc * (s.ds / s.bs);
+            float att = oexp(((-adist) * acc) / (float)n);
+            amb = scale(amb, att);
+            if (amb.x > 0.0f) direct = add(direct, amb);
+          }
+          V3 ind = scale(photon_map(s, T, pos, wo, radius, scatter, rng), s.albedo);
+          float a = oexp((-step) * ext);
+          V3 src = add(direct, ind);
+          L = add(scale(L, a), v3((scatter * src.x) * step, (scatter * src.y) * step, (scatter * src.z) * step));
+        }
+      }
+      double* o3 = sum + 3 * (size_t)pix;
+      o3[0] += (double)L.x;
+      o3[1] += (double)L.y;
+      o3[2] += (double)L.z;
+    }
+  }
+}
+
 }  // namespace oracle
 
 using namespace oracle;
@@ -261,6 +374,27 @@ int oracle_ppm_pass(void* h, int level, const vcr_cloud* cl, const vcr_camera* c
   if (order_out) std::copy(T.order.begin(), T.order.end(), order_out);
   if (left_out) std::copy(T.left.begin(), T.left.end(), left_out);
   if (right_out) std::copy(T.right.begin(), T.right.end(), right_out);
+  return 0;
+}
+
+// One pass of the march estimate (VCR_PPM_MARCH): the same photons and tree
+// as oracle_ppm_pass, then the ray march per pixel of the crop; sums +=
+// the pass's estimate.  The shadow volume `sv_tex` is oracle_sv_build's.
+int oracle_ppm_march_pass(void* h, int level, const vcr_cloud* cl, const vcr_camera* cam, const vcr_params* prm,
+                          const vcr_shadow_volume* sv, const float* sv_tex, uint32_t photons, uint32_t cap, float r0,
+                          float alpha, float step, float amb_step, uint32_t W, uint32_t H, const vcr_pass_desc* pass,
+                          double* sum, uint32_t* out_n, float* radius_out, int threads) {
+  Scene s = make_scene(static_cast<Grid*>(h), *cl, *prm, sv, level, sv_tex);
+  PhotonTree T;
+  emit(s, photons, cap, pass->seed, pass->pass_index, T, threads);
+  build(s, T);
+  float r = global_radius(r0, alpha, pass->pass_index);
+  march(s, T, *cam, W, H, pass, r, step, amb_step, sum, threads);
+  if (out_n) {
+    out_n[0] = (uint32_t)T.ph.size();
+    out_n[1] = T.dropped;
+  }
+  if (radius_out) *radius_out = r;
   return 0;
 }
 

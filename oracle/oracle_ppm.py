@@ -22,6 +22,10 @@ def _lib():
         L.oracle_ppm_pass.argtypes = [P, C.c_int, C.POINTER(_abi.Cloud), C.POINTER(_abi.Camera),
                                       C.POINTER(_abi.Params), u32, u32, f, u32, u32, C.POINTER(_abi.PassDesc), P, P,
                                       P, P, P, P, P, P, C.c_int]
+        L.oracle_ppm_march_pass.restype = C.c_int
+        L.oracle_ppm_march_pass.argtypes = [P, C.c_int, C.POINTER(_abi.Cloud), C.POINTER(_abi.Camera),
+                                            C.POINTER(_abi.Params), C.POINTER(_abi.ShadowVolume), P, u32, u32, f, f,
+                                            f, f, u32, u32, C.POINTER(_abi.PassDesc), P, P, C.POINTER(f), C.c_int]
         _bound = True
     return L
 
@@ -63,3 +67,24 @@ def ppm_pass(grid, cloud, cam, params, photons, capacity, alpha, width, height, 
         out["right"] = out["right"][:max(n - 1, 0)]
     out["info"] = info
     return sum_img, out
+
+
+def ppm_march_pass(grid, cloud, cam, params, sv, sv_tex, photons, capacity, r0, alpha, step, ambient_step, width,
+                   height, sum_img=None, seed=0, pass_index=0, crop=(0, 0, 0, 0), level=2, threads=0):
+    """One oracle pass of the reference's march estimate (VCR_PPM_MARCH);
+    adds the pass's estimate to sum_img.  Returns (sum_img, stored photons,
+    the pass's global radius)."""
+    L = _lib()
+    if sum_img is None:
+        sum_img = np.zeros((height, width, 3), np.float64)
+    p = _abi.PassDesc()
+    p.seed, p.pass_index, p.spp = seed, pass_index, 1
+    for i in range(4):
+        p.crop[i] = crop[i]
+    nn = np.zeros(2, np.uint32)
+    r = C.c_float()
+    tex = np.ascontiguousarray(sv_tex, np.float32)
+    L.oracle_ppm_march_pass(grid.h, level, C.byref(cloud), C.byref(cam), C.byref(params), C.byref(sv), _p(tex),
+                            photons, capacity, r0, alpha, step, ambient_step, width, height, C.byref(p),
+                            _p(sum_img), _p(nn), C.byref(r), threads or os.cpu_count() or 1)
+    return sum_img, int(nn[0]), float(r.value)

@@ -74,6 +74,7 @@ float density(const Scene& s, V3 p);
 bool slab(V3 pos, V3 dir, V3 b0, V3 b1, float& tmin, float& tmax);
 V3 sky(const Scene& s, V3 dir);
 float hg_pdf(const Scene& s, float c);
+float sv_lookup(const Scene& s, V3 p);  // sampleShadowVolume (PathTracer.comp:121-127)
 V3 hg_sample(const Scene& s, V3 in, Rng& rng, bool renorm);
 void camera_ray(const vcr_camera& c, int x, int y, V3& pos, V3& dir);
 void track_init(const Scene& s, Track& tr, V3 o, V3 d, Counts& c);
