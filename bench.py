@@ -157,6 +157,28 @@ def traffic_per_lookup():
     return None
 
 
+def set_l2_fetch_granularity(nbytes: int) -> int:
+    """cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity) for this process's
+    context on the current device (a per-process limit; it ends with the
+    process).  Returns the limit read back."""
+    import ctypes
+
+    import torch
+
+    torch.zeros(1, device="cuda")  # the primary context exists
+    rt = ctypes.CDLL(os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "lib64", "libcudart.so"))
+    limit_max_l2_fetch_granularity = 5
+    if rt.cudaDeviceSetLimit(limit_max_l2_fetch_granularity, ctypes.c_size_t(nbytes)) != 0:
+        raise RuntimeError("cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity) failed")
+    got = ctypes.c_size_t(0)
+    rt.cudaDeviceGetLimit(ctypes.byref(got), limit_max_l2_fetch_granularity)
+    return got.value
+
+
+def samples_per_step_of(sc) -> int:
+    return sc.width * sc.height  # one sample per pixel a pass
+
+
 def run_vcr(args):
     import torch
     import vcr
@@ -214,8 +236,23 @@ def run_vcr(args):
             c = ctx.counters()
             paths.append(c[0]); looks.append(c[1]); events.append(c[2])
         img = ctx.image_mean()
+        # the opt-in fast-math build of the same kernel (contracted FMAs,
+        # hardware log / exp / sincos; not bit-exact): the same K passes in
+        # one launch
+        ctx.set_tuning(**dict(tuning, fast_math=1))
+        ctx.pt_passes(seed=seed, first=0, count=args.warmup, stream=sh)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        ctx.pt_passes(seed=seed, first=args.warmup, count=args.steps, stream=sh)
+        b.record(stream)
+        b.synchronize()
+        fast = {"ms_per_pass": round(a.elapsed_time(b) / args.steps, 4),
+                "value": round(samples_per_step_of(sc) / (a.elapsed_time(b) / args.steps / 1e3) / 1e6, 3),
+                "lookups_per_launch": ctx.counters()[1],
+                "note": "opt-in (vcr_tuning.fast_math); path decisions can differ from the oracle's"}
+        ctx.set_tuning(**tuning)
         conv = convergence(ctx, sc, stream, args) if rank == 0 and not args.no_convergence else None
-    samples_per_step = W * H
+    samples_per_step = samples_per_step_of(sc)
     value = whole_job_rate(ws, samples_per_step, args.steps, ms_total)
     peak, peak_kind = measured_peaks()
     bpl = BYTES_PER_LOOKUP[prec]
@@ -242,6 +279,7 @@ def run_vcr(args):
                    "image": [W, H], "spp_per_step": 1, "max_events": sc.max_events, "tracker": "dda-wavefront",
                    "tuning": tuning,
                    "l2": "inputs larger than L2 (1 GiB FP16 grid), no flush",
+                   **({"l2_fetch_bytes": args.l2_fetch} if args.l2_fetch else {}),
                    "parallelism": f"replicas{ws}"},
         "gpu_launches": 1,
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
@@ -256,6 +294,7 @@ def run_vcr(args):
                                  "lookups_per_pass": int(single_lookups),
                                  "frac": round(single_lookups * bpl / (single_ms / 1e3) / 1e9 / peak, 4),
                                  "note": "one vcr_pt_pass launch per pass (each ends in its own tail of long paths)"},
+        "fast_math": fast,
         "clocks": clocks,
         "time_to_1pct": conv,
         "e2e": e2e,
@@ -270,7 +309,8 @@ PLAIN_PASSES_PER_LAUNCH = 25  # the plain tracker's error curve: one launch of 2
 
 CONV = {"ref_samples": 147456, "ref_spp": 16, "plain_max_passes": 30000, "warm_steps": 6000, "warm_sets": 32, "warm_more": 19, "warm_batch": 16384,
         "pool_sets": 32, "pool_every": 96, "max_frames": 8000, "chunk": 500, "spp": 1, "train_samples": 65536,
-        "learning_rate": 1e-3, "ema_decay": 0.99, "nrc_events": 2, "repeats": 3}
+        "learning_rate": 1e-3, "ema_decay": 0.99, "nrc_events": 2, "repeats": 3, "position_levels": 16,
+        "ablation_levels": [8, 0], "frame_group": 8}
 
 
 class Reference:
@@ -384,12 +424,14 @@ def cached_time_to_1pct(ctx, sc, stream, ref, cfg, to_end=False):
     prm.nrc_events = cfg["nrc_events"]
     ctx.set_params(prm)
     plain_tuning = ctx.get_tuning()
+    group = cfg.get("frame_group", 1)  # frames rendered by one launch (vcr_pt_passes)
     if cfg.get("tune_cached"):  # the autotuner on the cached pass itself (untimed set-up, as for the plain one)
         ctx.nrc_setup(train_samples=cfg["train_samples"], query_capacity=px * spp, seed=1)
         ctx.autotune(seed=998, spp=spp, stream=sh)
     ctx.nrc_setup(train_samples=cfg["train_samples"], learning_rate=cfg.get("warm_lr", cfg["learning_rate"]),
-                  query_capacity=px * spp,
-                  seed=1, ema_decay=cfg["ema_decay"], tail_survival=cfg.get("tail_survival", 0.0))
+                  query_capacity=px * spp * group,
+                  seed=1, ema_decay=cfg["ema_decay"], tail_survival=cfg.get("tail_survival", 0.0),
+                  position_levels=cfg.get("position_levels", 16))
     sets = cfg.get("warm_sets", 1)
     per_launch = sets * (1 + cfg["warm_more"])  # Adam steps a training launch feeds
     batches = max(1, cfg["warm_steps"] // per_launch)
@@ -413,7 +455,25 @@ def cached_time_to_1pct(ctx, sc, stream, ref, cfg, to_end=False):
     every = cfg.get("train_every", 1)  # frames between training frames (0: none after the warm-up)
     pool = cfg.get("pool_sets", 0)
 
+    def frame_group(k):
+        # frames k*group .. (k+1)*group - 1 in one launch (their cache
+        # queries all see the weights of the launch's start), then their
+        # `group` Adam steps; a frame at a multiple of pool_every re-traces
+        # the pool with its step
+        f0 = k * group
+        ctx.pt_passes(seed=500 ^ 0x5bd1e995, first=batches + f0, count=group, spp=spp, stream=sh)
+        re = [f for f in range(f0, f0 + group) if f % cfg["pool_every"] == 0]
+        steps = group
+        if re:
+            ctx.nrc_train_step(seed=600, pass_index=re[0] // cfg["pool_every"], stream=sh, sets=pool)
+            steps -= 1
+        if steps:
+            ctx.nrc_train_more(steps, max_records=cfg.get("frame_batch", cfg["train_samples"]), stream=sh)
+
     def frame(k):
+        if group > 1:
+            frame_group(k)
+            return
         if pool:
             # render-only frames; their Adam steps walk a pool of pool_sets
             # training sets, traced in one launch every pool_every frames
@@ -432,6 +492,8 @@ def cached_time_to_1pct(ctx, sc, stream, ref, cfg, to_end=False):
             if cfg.get("reuse_steps", 0):  # and train on the last frame's records again
                 ctx.nrc_train_more(cfg["reuse_steps"], stream=sh)
 
+    assert group == 1 or pool, "several frames a launch need the pooled training schedule"
+    nmax, chunk = nmax // group, max(1, chunk // group)  # counted in launches from here
     while done < nmax and (hit is None or to_end):
         _error_curve(ctx, stream, ref, chunk, frame, errs, ms, done)
         done += chunk
@@ -446,16 +508,18 @@ def cached_time_to_1pct(ctx, sc, stream, ref, cfg, to_end=False):
     ctx.set_tuning(**plain_tuning)
     e = errs[:done].cpu().numpy()
     frames_ms = np.cumsum(ms)
-    return {"frames": (hit + 1) if hit is not None else None, "spp_per_frame": spp,
-            "frame_ms": round(float(np.mean(ms)), 4), "warm_steps": cfg["warm_steps"],
+    return {"frames": (hit + 1) * group if hit is not None else None, "spp_per_frame": spp,
+            "frames_per_launch": group,
+            "frame_ms": round(float(np.mean(ms)) / group, 4), "warm_steps": cfg["warm_steps"],
             "warm_training_launches": batches, "warm_s": round(warm_ms / 1e3, 3),
             "time_s": round((warm_ms + frames_ms[hit]) / 1e3, 3) if hit is not None else None,
-            "relrmse_last": round(ref.corrected(e[-1]), 5), "frames_run": done,
-            "floor": ({"frames": done, "relrmse": round(ref.corrected(e[-1]), 5),
+            "relrmse_last": round(ref.corrected(e[-1]), 5), "frames_run": done * group,
+            "floor": ({"frames": done * group, "relrmse": round(ref.corrected(e[-1]), 5),
                        "relrmse_min": round(min(ref.corrected(x) for x in e[done // 2:]), 5),
                        "basis": "the cache's error left after max_frames frames (bias plus the frames' noise)"}
                       if to_end else None),
-            "curve": {str(i + 1): round(ref.corrected(e[i]), 5) for i in (0, 9, 99, 499, 999, 1999, 3999, done - 1)
+            "curve": {str((i + 1) * group): round(ref.corrected(e[i]), 5)
+                      for i in sorted({max(0, f // group - 1) for f in (1, 10, 100, 500, 1000, 2000, 4000)} | {done - 1})
                       if i < done},
             "train_records": info["train_records"], "loss": round(info["last_loss"], 4), "tuning": cached_tuning}
 
@@ -474,7 +538,13 @@ def convergence(ctx, sc, stream, args, overrides=None):
     nrc = sorted(done, key=lambda r: r["time_s"])[len(done) // 2] if done else runs[0]
     nrc = dict(nrc, runs_s=[r["time_s"] for r in runs], floor=runs[0]["floor"])
     nrc.pop("floor_run", None)
-    return {"plain": plain, "nrc": nrc,
+    # encoding ablation: the same cached run with only the coarsest L
+    # frequency levels of the position encoding (L = 0: no position input)
+    ablation = {}
+    for lv in cfg.get("ablation_levels", ()):
+        r = cached_time_to_1pct(ctx, sc, stream, ref, dict(cfg, position_levels=lv))
+        ablation[str(lv)] = {k: r[k] for k in ("frames", "time_s", "relrmse_last", "frames_run", "loss")}
+    return {"plain": plain, "nrc": nrc, "position_levels_ablation": ablation,
             "speedup": round(plain["time_s"] / nrc["time_s"], 2) if (nrc["time_s"] and plain["time_s"]) else None,
             "reference": {"samples_per_pixel": ref.samples, "spp_per_launch": ref.spp,
                           "own_relrmse": round(float(np.sqrt(ref.noise2)), 5), "render_s": round(ref.render_s, 2),
@@ -833,7 +903,8 @@ def run_e2e(args, sc, device, sh, tuning=None):
     dense = vcr.fbm_fill_host(sc.size, sc.fbm())  # the library's host generator (threaded)
     pinned = torch.from_numpy(dense).pin_memory()
     img_bytes = sc.width * sc.height * 3 * 4
-    img = torch.empty(sc.width * sc.height * 3, dtype=torch.float32).pin_memory()  # the result, read every pass
+    # the result, read back after every pass into alternating pinned buffers
+    imgs = [torch.empty(sc.width * sc.height * 3, dtype=torch.float32).pin_memory() for _ in range(2)]
     with vcr.Context(device) as ctx:
         if tuning:
             ctx.set_tuning(**tuning)
@@ -851,14 +922,16 @@ def run_e2e(args, sc, device, sh, tuning=None):
         t_up = time.perf_counter()
         for k in range(args.steps):
             ctx.pt_pass(seed=5, pass_index=k, stream=sh)
-            ctx.readback_to(vcr.BUF_IMAGE_MEAN, img.data_ptr(), img_bytes)  # waits for the pass
+            # stream-ordered: the copy of pass k overlaps pass k + 1
+            ctx.readback_async(vcr.BUF_IMAGE_MEAN, imgs[k % 2].data_ptr(), img_bytes, stream=sh)
+        ctx.readback_wait()
         t1 = time.perf_counter()
     grid_bytes = dense.nbytes
     return {"value": round(sc.width * sc.height * args.steps / (t1 - t0) / 1e6, 3), "unit": UNIT,
             "h2d_bytes_per_step": int(grid_bytes // args.steps), "d2h_bytes_per_step": img_bytes,
             "upload_s": round(t_up - t0, 4), "passes_s": round(t1 - t_up, 4),
             "note": "grid (FP32, pinned) uploaded once per run; one launch per pass and its mean image read back "
-                    "into pinned memory after every pass"}
+                    "into pinned memory after every pass (vcr_readback_async: the copy of pass k overlaps pass k+1)"}
 
 
 class OracleScene:
@@ -966,6 +1039,9 @@ def main():
     ap.add_argument("--sort", action="store_true", help="only measure the radix sort")
     ap.add_argument("--image-div", type=int, default=1,
                     help="divide the image sides (a small case of the workload for profiler captures)")
+    ap.add_argument("--l2-fetch", type=int, default=0,
+                    help="set this process's maximum L2 fetch granularity in bytes (32/64/128) before the run: "
+                         "how DRAM traffic per lookup depends on the L2's fetch size")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -978,6 +1054,8 @@ def main():
     import __graft_entry__ as ge
     with contextlib.redirect_stdout(sys.stderr):  # stdout carries only the JSON line
         ge.build()
+    if args.l2_fetch:
+        set_l2_fetch_granularity(args.l2_fetch)
     if args.sort:
         run_sort(args)
     elif args.display:

@@ -4,7 +4,8 @@ Every translation unit compiles in parallel with nvcc, then one link step
 produces ``cloudrendering-vulkan_gb300/libvcr.so``.  Float semantics: device
 code is compiled with ``-fmad=false`` (FMAs are written out explicitly) and
 host code with ``-ffp-contract=off``, so the CPU oracle can reproduce results
-bit for bit.
+bit for bit; the one exception is ``pt_wavefront_fast.cu``, the tracker's
+opt-in fast-math instantiation (see FILE_FLAGS).
 """
 from __future__ import annotations
 
@@ -40,6 +41,11 @@ def sources() -> list[str]:
     return out
 
 
+# Per-file flags: the fast-math instantiation of the tracker contracts
+# multiply-adds and uses the hardware transcendental approximations.
+FILE_FLAGS = {"pt_wavefront_fast.cu": (["-fmad=false"], ["-fmad=true", "-DVCR_FAST_MATH"])}
+
+
 def _compile(src: str, extra: list[str]) -> str:
     obj = os.path.join(BUILD, os.path.basename(src) + ".o")
     deps = [src] + [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".cuh", ".h"))]
@@ -49,7 +55,8 @@ def _compile(src: str, extra: list[str]) -> str:
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(d) for d in deps if os.path.exists(d)):
         return obj
     lang = ["-x", "cu"] if src.endswith(".cu") else ["-x", "c++"]
-    cmd = [_nvcc()] + NVCC_FLAGS + extra + lang + ["-c", src, "-o", obj]
+    drop, add = FILE_FLAGS.get(os.path.basename(src), ([], []))
+    cmd = [_nvcc()] + [f for f in NVCC_FLAGS if f not in drop] + add + extra + lang + ["-c", src, "-o", obj]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"nvcc failed for {src}:\n{res.stdout}\n{res.stderr}")

@@ -216,7 +216,7 @@ extern "C" VCR_API vcr_status vcr_batch_autotune(vcr_ctx* ctx, const vcr_pass_de
   for (uint32_t lv : levels)
     for (uint32_t sp : steps)
       for (uint32_t th : threads) {
-        ctx->tuning = vcr_tuning{lv, sp, 1u, th};
+        ctx->tuning = vcr_tuning{lv, sp, 1u, th, saved.corner_blocks, saved.fast_math};
         for (int rep = 0; rep < 2 && !vs; ++rep) {  // the first run warms up
           cudaEventRecord(e0, s);
           vs = batch_launch(ctx, pv, b->d_ctr + 1, s);

@@ -54,6 +54,8 @@ GridView grid_view(const vcr_ctx* ctx) {
     g.mnb[a] = ctx->mnb[lv][a];
   }
   g.precision = ctx->precision;
+  g.corners = (ctx->tuning.corner_blocks && ctx->d_corners && ctx->corners_valid) ? ctx->d_corners : nullptr;
+  for (int a = 0; a < 3; ++a) g.ctiles[a] = ctx->corner_tiles[a];
   return g;
 }
 
@@ -170,13 +172,19 @@ extern "C" VCR_API vcr_status vcr_destroy(vcr_ctx* ctx) {
   cudaSetDevice(ctx->device);
   cudaDeviceSynchronize();
   void* ptrs[] = {ctx->d_bricks, ctx->d_scales, ctx->d_majorants, ctx->d_sum, ctx->d_stats,
-                  ctx->d_counters, ctx->d_error, ctx->d_sv, ctx->d_scratch};
+                  ctx->d_counters, ctx->d_error, ctx->d_sv, ctx->d_scratch, ctx->d_corners};
   for (void* p : ptrs) cudaFree(p);
   ppb_free(ctx);
   ppm_free(ctx);
   nrc_free(ctx);
   batch_free(ctx);
   if (ctx->work_done) cudaEventDestroy(ctx->work_done);
+  for (int i = 0; i < 2; ++i) {
+    cudaFree(ctx->rb.stage[i]);
+    if (ctx->rb.staged[i]) cudaEventDestroy(ctx->rb.staged[i]);
+    if (ctx->rb.copied[i]) cudaEventDestroy(ctx->rb.copied[i]);
+  }
+  if (ctx->rb.copy) cudaStreamDestroy(ctx->rb.copy);
   delete ctx;
   return VCR_OK;
 }
@@ -426,9 +434,16 @@ extern "C" VCR_API vcr_status vcr_set_tuning(vcr_ctx* ctx, const vcr_tuning* t) 
   if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
   VCR_CUDA(ctx, cudaSetDevice(ctx->device));
   if (!t || t->majorant_level > 3 || t->dda_steps == 0 || t->dda_steps > 4096 ||
-      (t->block_threads != 128 && t->block_threads != 256))
-    return fail(ctx, VCR_ERR_INVALID, "tuning: level 0..3, dda_steps 1..4096, block_threads 128 or 256");
+      (t->block_threads != 128 && t->block_threads != 256) || t->corner_blocks > 1 || t->fast_math > 1)
+    return fail(ctx, VCR_ERR_INVALID,
+                "tuning: level 0..3, dda_steps 1..4096, block_threads 128 or 256, corner_blocks and fast_math 0 "
+                "or 1");
   ctx->tuning = *t;
+  if (t->corner_blocks && ctx->has_grid && !ctx->corners_valid) {  // switched on after the grid was bound
+    vcr_status st = corner_build(ctx, 0);
+    if (st) return st;
+    VCR_CUDA(ctx, cudaStreamSynchronize(0));
+  }
   return VCR_OK;
 }
 
@@ -629,6 +644,73 @@ extern "C" VCR_API vcr_status vcr_dda_trace(vcr_ctx* ctx, const float* d_o, cons
   if (n && (!d_o || !d_d || !d_cells || !d_t || !d_count || max_cells == 0))
     return fail(ctx, VCR_ERR_INVALID, "bad DDA buffers");
   return dda_trace_launch(ctx, d_o, d_d, n, max_cells, d_cells, d_t, d_count, (cudaStream_t)stream);
+}
+
+// The copy stream, events and `bytes`-sized staging slots of the
+// stream-ordered read back (created on first use).
+static vcr_status readback_ring(vcr_ctx* ctx, size_t bytes) {
+  vcr_ctx::Readback& r = ctx->rb;
+  if (!r.copy) {
+    VCR_CUDA(ctx, cudaStreamCreateWithFlags(&r.copy, cudaStreamNonBlocking));
+    for (int i = 0; i < 2; ++i) {
+      VCR_CUDA(ctx, cudaEventCreateWithFlags(&r.staged[i], cudaEventDisableTiming));
+      VCR_CUDA(ctx, cudaEventCreateWithFlags(&r.copied[i], cudaEventDisableTiming));
+      VCR_CUDA(ctx, cudaEventRecord(r.copied[i], r.copy));
+    }
+  }
+  if (r.bytes < bytes) {
+    VCR_CUDA(ctx, cudaStreamSynchronize(r.copy));
+    for (int i = 0; i < 2; ++i) {
+      cudaFree(r.stage[i]);
+      r.stage[i] = nullptr;
+    }
+    r.bytes = 0;
+    for (int i = 0; i < 2; ++i) VCR_CUDA(ctx, cudaMalloc(&r.stage[i], bytes));
+    r.bytes = bytes;
+  }
+  return VCR_OK;
+}
+
+extern "C" VCR_API vcr_status vcr_readback_async(vcr_ctx* ctx, vcr_buffer_id id, void* host, size_t bytes,
+                                                 void* stream) {
+  if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  if (!host) return fail(ctx, VCR_ERR_INVALID, "null host buffer");
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
+  if (!ctx->d_sum) return fail(ctx, VCR_ERR_STATE, "no frame");
+  const size_t n = (size_t)ctx->width * ctx->height * 3;
+  if (id == VCR_BUF_IMAGE_MEAN) {
+    if (bytes != n * sizeof(float)) return fail(ctx, VCR_ERR_INVALID, "mean image is %zu bytes", n * 4);
+  } else if (id == VCR_BUF_IMAGE_SUM) {
+    if (bytes != n * sizeof(double)) return fail(ctx, VCR_ERR_INVALID, "sum image is %zu bytes", n * 8);
+  } else {
+    return fail(ctx, VCR_ERR_UNSUPPORTED, "buffer id %d has no stream-ordered read back", (int)id);
+  }
+  vcr_status rs = readback_ring(ctx, bytes);
+  if (rs) return rs;
+  vcr_ctx::Readback& r = ctx->rb;
+  const int k = r.slot;
+  r.slot ^= 1;
+  cudaStream_t st = (cudaStream_t)stream;
+  VCR_CUDA(ctx, cudaStreamWaitEvent(st, r.copied[k], 0));  // the slot's previous copy has landed
+  if (id == VCR_BUF_IMAGE_MEAN) {
+    const double inv = ctx->samples ? 1.0 / (double)ctx->samples : 0.0;  // passes queued so far
+    mean_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(ctx->d_sum, (float*)r.stage[k], n, inv);
+    VCR_CUDA(ctx, cudaGetLastError());
+  } else {
+    VCR_CUDA(ctx, cudaMemcpyAsync(r.stage[k], ctx->d_sum, bytes, cudaMemcpyDeviceToDevice, st));
+  }
+  VCR_CUDA(ctx, cudaEventRecord(r.staged[k], st));
+  VCR_CUDA(ctx, cudaStreamWaitEvent(r.copy, r.staged[k], 0));
+  VCR_CUDA(ctx, cudaMemcpyAsync(host, r.stage[k], bytes, cudaMemcpyDeviceToHost, r.copy));
+  VCR_CUDA(ctx, cudaEventRecord(r.copied[k], r.copy));
+  return VCR_OK;
+}
+
+extern "C" VCR_API vcr_status vcr_readback_wait(vcr_ctx* ctx) {
+  if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
+  VCR_CUDA(ctx, cudaSetDevice(ctx->device));
+  if (ctx->rb.copy) VCR_CUDA(ctx, cudaStreamSynchronize(ctx->rb.copy));
+  return VCR_OK;
 }
 
 extern "C" VCR_API vcr_status vcr_readback(vcr_ctx* ctx, vcr_buffer_id id, void* host, size_t bytes) {

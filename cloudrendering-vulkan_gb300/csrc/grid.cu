@@ -267,6 +267,104 @@ vcr_status grid_fbm_device(vcr_ctx* ctx, float* d_dense, const vcr_grid_desc* de
   return VCR_OK;
 }
 
+// Corner blocks: cell (cx, cy, cz) in 0 .. n per axis holds, for the lower
+// corner floor(u) = c - 1, the 8 texels a trilinear lookup there reads,
+// decoded exactly as the bricks decode them, with the grid-edge clamp
+// already applied.  Cells sit in 8^3-cell tiles, x fastest, so the 64
+// cells of one z plane of a tile are 2 KB of contiguous output.  One warp
+// per such plane (grid-stride over planes, no block barrier): its 9 x 9 x 2
+// texels (clamped) are decoded once into the warp's shared memory, then
+// each of four stores writes 512 contiguous bytes (lane l the half-cell
+// j * 32 + l: the z0 pair block or the z1 pair block of one cell).
+constexpr int kCornerWarps = 8;
+
+__global__ void __launch_bounds__(kCornerWarps * 32) corner_kernel(GridView g, float4* __restrict__ out,
+                                                                    uint32_t p_begin, uint32_t p_end) {
+  __shared__ float tex[kCornerWarps][2 * 81];
+  const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
+  float* tw = tex[w];
+  const uint32_t t0 = (uint32_t)g.ctiles[0], t01 = t0 * (uint32_t)g.ctiles[1];
+  const uint32_t nwarps = gridDim.x * kCornerWarps;
+  for (uint32_t p = p_begin + blockIdx.x * kCornerWarps + w; p < p_end; p += nwarps) {
+    const uint32_t t = p >> 3, lz = p & 7u;  // tile, z plane of the tile
+    const uint32_t tz = t / t01, ty = (t - tz * t01) / t0, tx = t - tz * t01 - ty * t0;
+    const int bx = (int)tx * 8 - 1, by = (int)ty * 8 - 1, bz = (int)(tz * 8u + lz) - 1;
+    for (uint32_t k = lane; k < 162u; k += 32u) {
+      const int i = (int)(k % 9u), j = (int)((k / 9u) % 9u), l = (int)(k / 81u);
+      tw[k] = texel(g, min(max(bx + i, 0), g.n[0] - 1), min(max(by + j, 0), g.n[1] - 1),
+                    min(max(bz + l, 0), g.n[2] - 1));
+    }
+    __syncwarp();
+    const bool plane_in = bz + 1 <= g.n[2];  // not padding of the last tile layer
+    float4* o = out + 2 * ((size_t)t * 512u + lz * 64u);
+#pragma unroll
+    for (uint32_t q = 0; q < 4; ++q) {
+      const uint32_t h = q * 32u + lane, c = h >> 1;  // half-cell h of cell c = lx + 8 ly
+      const int lx = (int)(c & 7u), ly = (int)(c >> 3);
+      const float* s = tw + lx + 9 * ly + 81 * (int)(h & 1u);
+      if (plane_in && bx + 1 + lx <= g.n[0] && by + 1 + ly <= g.n[1]) o[h] = make_float4(s[0], s[1], s[9], s[10]);
+    }
+    __syncwarp();
+  }
+}
+
+// Allocates the corner blocks of the grid description in ctx->gdesc (the
+// buffer of the previous grid is kept when its tiles match: freeing and
+// mapping 17 GB again costs milliseconds); if the allocation fails there
+// are none and lookups gather from the bricks.
+static void corner_alloc(vcr_ctx* ctx) {
+  ctx->corners_valid = false;
+  int tiles3[3];
+  for (int a = 0; a < 3; ++a) tiles3[a] = ((int)ctx->gdesc.size[a] + 1 + 7) / 8;
+  if (ctx->d_corners && tiles3[0] == ctx->corner_tiles[0] && tiles3[1] == ctx->corner_tiles[1] &&
+      tiles3[2] == ctx->corner_tiles[2])
+    return;
+  cudaFree(ctx->d_corners);
+  ctx->d_corners = nullptr;
+  for (int a = 0; a < 3; ++a) ctx->corner_tiles[a] = tiles3[a];
+  const uint32_t tiles = (uint32_t)tiles3[0] * tiles3[1] * tiles3[2];
+  if (cudaMalloc(&ctx->d_corners, (size_t)tiles * 512u * 32u) != cudaSuccess) {
+    cudaGetLastError();
+    ctx->d_corners = nullptr;
+  }
+}
+
+// The corner tiles of tile layers [tz0, tz1): tile layer tz reads the
+// texels of z planes 8 tz - 1 .. 8 tz + 7 (clamped), i.e. brick layers
+// tz - 1 and tz, which must be written.
+static vcr_status corner_layers(vcr_ctx* ctx, uint32_t tz0, uint32_t tz1, cudaStream_t s) {
+  if (!ctx->d_corners || tz0 >= tz1) return VCR_OK;
+  const uint32_t per_layer = (uint32_t)ctx->corner_tiles[0] * ctx->corner_tiles[1] * 8u;  // cell planes
+  const uint32_t p0 = tz0 * per_layer, p1 = tz1 * per_layer;
+  GridView g = grid_view(ctx);
+  g.corners = nullptr;
+  const uint32_t blocks =
+      std::min<uint32_t>((uint32_t)ctx->sm_count * 8u, (p1 - p0 + kCornerWarps - 1) / kCornerWarps);
+  corner_kernel<<<blocks, kCornerWarps * 32, 0, s>>>(g, ctx->d_corners, p0, p1);
+  VCR_CUDA(ctx, cudaGetLastError());
+  return VCR_OK;
+}
+
+vcr_status corner_build(vcr_ctx* ctx, cudaStream_t s) {
+  corner_alloc(ctx);
+  vcr_status st = corner_layers(ctx, 0u, (uint32_t)ctx->corner_tiles[2], s);
+  if (st) return st;
+  ctx->corners_valid = ctx->d_corners != nullptr;
+  return VCR_OK;
+}
+
+// Makes *p a device buffer of `want` bytes: the current one if it has that
+// size, else a new one.
+static vcr_status grid_buffer(vcr_ctx* ctx, void** p, size_t& have, size_t want) {
+  if (*p && have == want) return VCR_OK;
+  cudaFree(*p);
+  *p = nullptr;
+  have = 0;
+  VCR_CUDA(ctx, cudaMalloc(p, want));
+  have = want;
+  return VCR_OK;
+}
+
 // Releases the previous grid and allocates the bricks, scales and majorant
 // pyramid of `desc` (levels l = 0..3 with ceil(nb / 2^l) cells per axis,
 // each level starting on a 16-byte boundary for the bulk copies into shared
@@ -278,15 +376,15 @@ static vcr_status grid_alloc(vcr_ctx* ctx, const vcr_grid_desc* desc, int precis
   if (nbricks > (1ull << 22)) return fail(ctx, VCR_ERR_UNSUPPORTED, "grid too large: %llu bricks (max 2^22)",
                                           (unsigned long long)nbricks);
   size_t esz = precision == 0 ? 4 : 2;
-  cudaFree(ctx->d_bricks);
-  cudaFree(ctx->d_scales);
-  cudaFree(ctx->d_majorants);
-  ctx->d_bricks = nullptr;
-  ctx->d_scales = nullptr;
-  ctx->d_majorants = nullptr;
   ctx->has_grid = false;
-  VCR_CUDA(ctx, cudaMalloc(&ctx->d_bricks, nbricks * kBrickVoxels * esz));
-  VCR_CUDA(ctx, cudaMalloc(&ctx->d_scales, nbricks * sizeof(float)));
+  ctx->corners_valid = false;
+  if (!ctx->tuning.corner_blocks) {  // a same-size buffer is kept only for a grid that builds corners
+    cudaFree(ctx->d_corners);
+    ctx->d_corners = nullptr;
+  }
+  ctx->gdesc = *desc;
+  ctx->precision = precision;
+  for (int a = 0; a < 3; ++a) ctx->nb[a] = nb[a];
   size_t mtotal = 0;
   for (int l = 0; l < 4; ++l) {
     for (int a = 0; a < 3; ++a) ctx->mnb[l][a] = l == 0 ? nb[a] : (ctx->mnb[l - 1][a] + 1) / 2;
@@ -294,7 +392,11 @@ static vcr_status grid_alloc(vcr_ctx* ctx, const vcr_grid_desc* desc, int precis
     size_t cnt = (size_t)ctx->mnb[l][0] * ctx->mnb[l][1] * ctx->mnb[l][2];
     mtotal += (cnt + 3) & ~(size_t)3;
   }
-  VCR_CUDA(ctx, cudaMalloc(&ctx->d_majorants, mtotal * sizeof(float)));
+  // the previous grid's buffers are kept where their sizes match
+  vcr_status st = grid_buffer(ctx, &ctx->d_bricks, ctx->grid_bytes[0], nbricks * kBrickVoxels * esz);
+  if (!st) st = grid_buffer(ctx, reinterpret_cast<void**>(&ctx->d_scales), ctx->grid_bytes[1], nbricks * sizeof(float));
+  if (!st) st = grid_buffer(ctx, reinterpret_cast<void**>(&ctx->d_majorants), ctx->grid_bytes[2], mtotal * sizeof(float));
+  if (st) return st;
   VCR_CUDA(ctx, cudaMemsetAsync(ctx->d_majorants, 0, mtotal * sizeof(float), s));
   VCR_CUDA(ctx, cudaMemsetAsync(ctx->d_scales, 0, nbricks * sizeof(float), s));
   return VCR_OK;
@@ -321,8 +423,10 @@ static vcr_status brick_launch(vcr_ctx* ctx, const float* dense, const vcr_grid_
 }
 
 // Once every brick is written: brick summaries, majorant pyramid, global
-// maximum (synchronises on s).
-static vcr_status grid_finish(vcr_ctx* ctx, const vcr_grid_desc* desc, int precision, cudaStream_t s) {
+// maximum, and the corner blocks unless the caller built them already
+// (synchronises on s).
+static vcr_status grid_finish(vcr_ctx* ctx, const vcr_grid_desc* desc, int precision, cudaStream_t s,
+                              bool corners_built = false) {
   int nb[3];
   for (int a = 0; a < 3; ++a) nb[a] = ((int)desc->size[a] + kBrick - 1) / kBrick;
   const uint64_t nbricks = (uint64_t)nb[0] * nb[1] * nb[2];
@@ -357,6 +461,13 @@ static vcr_status grid_finish(vcr_ctx* ctx, const vcr_grid_desc* desc, int preci
   if (!(f <= 3.0e38f)) return fail(ctx, VCR_ERR_INVALID, "grid holds non-finite densities");
   ctx->max_density = f;
   ctx->has_grid = true;
+  if (ctx->tuning.corner_blocks && !corners_built) {
+    vcr_status cs = corner_build(ctx, s);
+    if (cs) return cs;
+  } else if (corners_built) {
+    ctx->corners_valid = ctx->d_corners != nullptr;
+  }
+  VCR_CUDA(ctx, cudaStreamSynchronize(s));
   return VCR_OK;
 }
 
@@ -394,7 +505,9 @@ struct UploadRing {
 
 // A host grid uploaded one brick layer (8 z planes) at a time through a
 // ring of three device slabs: the copy of layer k overlaps the bricking of
-// layer k - 1, and no device copy of the whole dense grid is made.
+// layer k - 1 and the corner blocks of tile layer k - 1 (which read brick
+// layers k - 2 and k - 1), and no device copy of the whole dense grid is
+// made.
 vcr_status grid_upload_host(vcr_ctx* ctx, const float* host, const vcr_grid_desc* desc, int precision) {
   vcr_status st = grid_alloc(ctx, desc, precision, 0);
   if (st) return st;
@@ -402,6 +515,8 @@ vcr_status grid_upload_host(vcr_ctx* ctx, const float* host, const vcr_grid_desc
   const size_t nx = desc->size[0], ny = desc->size[1], nz = desc->size[2], plane = nx * ny;
   const uint32_t bx = (uint32_t)((nx + kBrick - 1) / kBrick), by = (uint32_t)((ny + kBrick - 1) / kBrick);
   const int layers = (int)((nz + kBrick - 1) / kBrick);
+  const bool corners = ctx->tuning.corner_blocks != 0;
+  if (corners) corner_alloc(ctx);
   UploadRing ring;
   VCR_CUDA(ctx, cudaMalloc(&ring.buf, (size_t)UploadRing::kSlabs * kBrick * plane * sizeof(float)));
   VCR_CUDA(ctx, cudaStreamCreateWithFlags(&ring.copy, cudaStreamNonBlocking));
@@ -422,8 +537,16 @@ vcr_status grid_upload_host(vcr_ctx* ctx, const float* host, const vcr_grid_desc
     st = brick_launch(ctx, slab, desc, precision, (uint32_t)kb * bx * by, bx * by, kb, ring.brick);
     if (st) return st;
     VCR_CUDA(ctx, cudaEventRecord(ring.done[r], ring.brick));
+    if (corners) {
+      st = corner_layers(ctx, (uint32_t)kb, (uint32_t)kb + 1u, ring.brick);
+      if (st) return st;
+    }
   }
-  return grid_finish(ctx, desc, precision, ring.brick);
+  if (corners) {  // the tile layer past the last brick layer (clamped texels)
+    st = corner_layers(ctx, (uint32_t)layers, (uint32_t)ctx->corner_tiles[2], ring.brick);
+    if (st) return st;
+  }
+  return grid_finish(ctx, desc, precision, ring.brick, corners);
 }
 
 vcr_status grid_sample_launch(vcr_ctx* ctx, const float* d_pos, float* d_out, uint32_t n, cudaStream_t s) {

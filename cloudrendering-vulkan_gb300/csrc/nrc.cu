@@ -40,6 +40,7 @@ struct NrcView {
   const bf16* wb;   // training weights
   const bf16* wbi;  // inference weights (the moving average, or wb)
   f3 b0, inv_ext;
+  int levels;       // position-encoding levels the network sees (the rest are 0)
 };
 
 // ---------------------------------------------------------------------------
@@ -68,8 +69,8 @@ __global__ void __launch_bounds__(kInferThreads, 3) nrc_infer_kernel(NrcView v, 
     if (i0 < count) r0 = recs[i0];
     if (i1 < count) r1 = recs[i1];
     uint32_t a[4][4];
-    encode_a(r0, i0 < count, v.b0, v.inv_ext, dirs, t, 0, a);
-    encode_a(r1, i1 < count, v.b0, v.inv_ext, dirs, t, 1, a);
+    encode_a(r0, i0 < count, v.b0, v.inv_ext, dirs, t, 0, a, v.levels);
+    encode_a(r1, i1 < count, v.b0, v.inv_ext, dirs, t, 1, a, v.levels);
     float yg[3], yh[3];
     mlp_forward_mma(W, a, lane, yg, yh);
     if (t == 0) {
@@ -165,8 +166,8 @@ __global__ void __launch_bounds__(kTrainThreads, 1) nrc_train_kernel(NrcView v, 
       NrcRecord r0{}, r1{};
       if (i0 < count) r0 = recs[i0];
       if (i1 < count) r1 = recs[i1];
-      encode_a(r0, i0 < count, v.b0, v.inv_ext, dirs, t, 0, a);
-      encode_a(r1, i1 < count, v.b0, v.inv_ext, dirs, t, 1, a);
+      encode_a(r0, i0 < count, v.b0, v.inv_ext, dirs, t, 0, a, v.levels);
+      encode_a(r1, i1 < count, v.b0, v.inv_ext, dirs, t, 1, a, v.levels);
     }
     store_a(X, row, t, a, 4);
 #pragma unroll 1
@@ -401,6 +402,7 @@ NrcView nrc_view(const vcr_ctx* ctx) {
   v.b0 = mk(c.bounds_min[0], c.bounds_min[1], c.bounds_min[2]);
   v.inv_ext = mk(1.0f / (c.bounds_max[0] - c.bounds_min[0]), 1.0f / (c.bounds_max[1] - c.bounds_min[1]),
                  1.0f / (c.bounds_max[2] - c.bounds_min[2]));
+  v.levels = kNrcPosLevels - (int)ctx->nrc->prm.position_drop;
   return v;
 }
 
@@ -434,10 +436,11 @@ static void nrc_init_weights(std::vector<float>& w, uint32_t seed) {
 vcr_status nrc_setup(vcr_ctx* ctx, const vcr_nrc_params* p) {
   if (!p || p->train_samples == 0 || p->train_samples > (1u << 22) || !(p->learning_rate > 0.0f) ||
       p->query_capacity == 0 || !(p->ema_decay >= 0.0f && p->ema_decay < 1.0f) ||
-      !(p->tail_survival >= 0.0f && p->tail_survival < 1.0f) || p->query_kernel > VCR_NRC_QUERY_TCGEN05)
+      !(p->tail_survival >= 0.0f && p->tail_survival < 1.0f) || p->query_kernel > VCR_NRC_QUERY_TCGEN05 ||
+      p->position_drop > (uint32_t)kNrcPosLevels)
     return fail(ctx, VCR_ERR_INVALID,
                 "nrc params: train_samples 1..2^22, learning_rate > 0, query_capacity > 0, ema_decay and "
-                "tail_survival in [0,1), query_kernel a VCR_NRC_QUERY_* value");
+                "tail_survival in [0,1), query_kernel a VCR_NRC_QUERY_* value, position_drop 0..16");
   nrc_free(ctx);
   NrcState* st = new NrcState();
   ctx->nrc = st;
@@ -544,8 +547,8 @@ vcr_status nrc_infer_queries(vcr_ctx* ctx, cudaStream_t s) {
   NrcState* st = ctx->nrc;
   if (use_tc(st)) {
     const NrcView v = nrc_view(ctx);
-    return nrc_infer_tc_launch(ctx, v.wbi, v.b0, v.inv_ext, st->query, st->query_count, st->query_capacity,
-                               ctx->d_sum, nullptr, s);
+    return nrc_infer_tc_launch(ctx, v.wbi, v.b0, v.inv_ext, v.levels, st->query, st->query_count,
+                               st->query_capacity, ctx->d_sum, nullptr, s);
   }
   VCR_CUDA(ctx, cudaFuncSetAttribute(nrc_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)infer_smem()));
   int per_sm = 0;
@@ -827,8 +830,8 @@ extern "C" VCR_API vcr_status vcr_nrc_forward(vcr_ctx* ctx, const void* d_record
   VCR_CUDA(ctx, cudaMemcpyAsync(d_n, &n, 4, cudaMemcpyHostToDevice, s));
   if (use_tc(ctx->nrc)) {
     const NrcView v = nrc_view(ctx);
-    vs = nrc_infer_tc_launch(ctx, v.wbi, v.b0, v.inv_ext, reinterpret_cast<const NrcRecord*>(d_records), d_n, n,
-                             nullptr, d_out, s);
+    vs = nrc_infer_tc_launch(ctx, v.wbi, v.b0, v.inv_ext, v.levels, reinterpret_cast<const NrcRecord*>(d_records),
+                             d_n, n, nullptr, d_out, s);
     if (vs) return vs;
   } else {
     VCR_CUDA(ctx, cudaFuncSetAttribute(nrc_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -170,7 +170,7 @@ __host__ __device__ constexpr int nrc_layer_cols(int l) { return l < kNrcHidden 
 // nrc_tc.cu: the queries' forward on tcgen05 (128-record tiles, TMEM
 // accumulators): reads the *d_count (<= capacity) records, adds
 // throughput x max(y, 0) to sum[pix] and/or writes y to out.
-vcr_status nrc_infer_tc_launch(vcr_ctx* ctx, const void* wbi, f3 b0, f3 inv_ext, const NrcRecord* recs,
+vcr_status nrc_infer_tc_launch(vcr_ctx* ctx, const void* wbi, f3 b0, f3 inv_ext, int levels, const NrcRecord* recs,
                                const uint32_t* d_count, uint32_t capacity, double* sum, float* out, cudaStream_t s);
 
 }  // namespace vcr

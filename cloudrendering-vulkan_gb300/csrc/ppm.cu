@@ -165,7 +165,7 @@ __device__ __forceinline__ float box_dist2(f3 x, float4 lo, float4 hi) {
   return (dx * dx + dy * dy) + dz * dz;
 }
 
-__global__ void __launch_bounds__(128) ppm_gather_kernel(GridView g, SceneView s, CamView cam, PassView pv,
+__global__ void __launch_bounds__(128, 8) ppm_gather_kernel(GridView g, SceneView s, CamView cam, PassView pv,
                                                          PpmGatherView v, double* __restrict__ sum, Counters cnt,
                                                          unsigned long long* __restrict__ tested) {
   uint32_t id = blockIdx.x * blockDim.x + threadIdx.x;

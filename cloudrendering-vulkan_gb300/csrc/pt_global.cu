@@ -132,8 +132,8 @@ vcr_status pt_pass_launch(vcr_ctx* ctx, const vcr_pass_desc* pass, cudaStream_t 
   const vcr_params& P = ctx->params;
   if (count == 0) return fail(ctx, VCR_ERR_INVALID, "a launch of zero passes");
   if (count > 1) {
-    if (P.tracker != VCR_TRACKER_DDA || P.nrc_events || train)
-      return fail(ctx, VCR_ERR_UNSUPPORTED, "several passes per launch need the DDA tracker without the cache");
+    if (P.tracker != VCR_TRACKER_DDA || train)
+      return fail(ctx, VCR_ERR_UNSUPPORTED, "several passes per launch need the DDA tracker and no training paths");
     if (pv.flags & (VCR_PASS_RECORD_STATS | VCR_PASS_NO_ACCUMULATE))
       return fail(ctx, VCR_ERR_INVALID, "several passes per launch accumulate and record no path statistics");
     if ((uint64_t)pass->pass_index + count > 0xFFFFFFFFull)

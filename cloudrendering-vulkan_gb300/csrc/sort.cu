@@ -85,7 +85,7 @@ __device__ __forceinline__ uint32_t digit_peers(const uint32_t bit[4], uint32_t 
   return m;
 }
 
-__global__ void __launch_bounds__(kSortThreads) sort_pass_kernel(const uint32_t* __restrict__ kin,
+__global__ void __launch_bounds__(kSortThreads, 4) sort_pass_kernel(const uint32_t* __restrict__ kin,
                                                                  const uint32_t* __restrict__ vin,
                                                                  uint32_t* __restrict__ kout,
                                                                  uint32_t* __restrict__ vout, uint32_t n,

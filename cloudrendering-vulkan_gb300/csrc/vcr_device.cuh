@@ -20,6 +20,12 @@ constexpr int kBrickVoxels = kBrick * kBrick * kBrick;
 struct GridView {
   const void* bricks;
   const float* scales;     // per brick (FP16/BF16 only)
+  // Optional per-cell corner blocks: cell (cx, cy, cz) for the lower
+  // trilinear corner floor(u) = cx - 1 in [-1, n-1] holds the 8 decoded
+  // corner texels (clamped to the grid) as two float4, (x, y) pairs of the
+  // z0 plane then of the z1 plane; cells in 8^3 tiles, ctiles tiles per axis.
+  const float4* corners;
+  int ctiles[3];
   const float* majorants;  // the selected pyramid level (max over the cell + halo)
   int n[3];                // voxel counts
   int nb[3];               // brick counts
@@ -67,6 +73,12 @@ __device__ __forceinline__ float texel(const GridView& g, int i, int j, int k) {
 // (i + 1/2)/N in normalised coordinates (the reference's sampler,
 // Initializers.cpp:408-418, sampleCloud PathTracer.comp:115-119).  Lerps are
 // fma(t, b - a, a), x then y then z.
+// Linear index of corner cell (cx, cy, cz) (each in 0 .. n) in its tiles.
+__device__ __forceinline__ uint32_t corner_cell(const GridView& g, uint32_t cx, uint32_t cy, uint32_t cz) {
+  const uint32_t t = (cx >> 3) + (uint32_t)g.ctiles[0] * ((cy >> 3) + (uint32_t)g.ctiles[1] * (cz >> 3));
+  return (t << 9) + (cx & 7u) + ((cy & 7u) << 3) + ((cz & 7u) << 6);
+}
+
 __device__ __forceinline__ float trilinear(const GridView& g, f3 nrm) {
   float ux = nrm.x * (float)g.n[0] - 0.5f;
   float uy = nrm.y * (float)g.n[1] - 0.5f;
@@ -74,6 +86,20 @@ __device__ __forceinline__ float trilinear(const GridView& g, f3 nrm) {
   float fx0 = floorf(ux), fy0 = floorf(uy), fz0 = floorf(uz);
   float tx = ux - fx0, ty = uy - fy0, tz = uz - fz0;
   int x0 = (int)fx0, y0 = (int)fy0, z0 = (int)fz0;
+  if (g.corners) {  // one 32-byte block holds the footprint: the same values, the same lerps
+    const uint32_t cx = (uint32_t)(min(max(x0, -1), g.n[0] - 1) + 1);
+    const uint32_t cy = (uint32_t)(min(max(y0, -1), g.n[1] - 1) + 1);
+    const uint32_t cz = (uint32_t)(min(max(z0, -1), g.n[2] - 1) + 1);
+    const float4* c = g.corners + 2 * (size_t)corner_cell(g, cx, cy, cz);
+    const float4 a = __ldg(c), b = __ldg(c + 1);
+    float c00 = fmaf(tx, a.y - a.x, a.x);
+    float c10 = fmaf(tx, a.w - a.z, a.z);
+    float c01 = fmaf(tx, b.y - b.x, b.x);
+    float c11 = fmaf(tx, b.w - b.z, b.z);
+    float c0 = fmaf(ty, c10 - c00, c00);
+    float c1 = fmaf(ty, c11 - c01, c01);
+    return fmaf(tz, c1 - c0, c0);
+  }
   int x1 = min(max(x0 + 1, 0), g.n[0] - 1);
   int y1 = min(max(y0 + 1, 0), g.n[1] - 1);
   int z1 = min(max(z0 + 1, 0), g.n[2] - 1);

@@ -30,11 +30,16 @@ struct vcr_ctx {
   void* d_bricks = nullptr;
   float* d_scales = nullptr;
   float* d_majorants = nullptr;  // pyramid levels 0..3, each 16-byte aligned
+  size_t grid_bytes[3] = {0, 0, 0};  // allocated bytes of bricks, scales, majorants (kept for a same-size grid)
   float max_density = 0.0f;
   int nb[3] = {0, 0, 0};
   int mnb[4][3] = {};            // cells per axis of each majorant level
   size_t moff[4] = {};           // float offset of each level in d_majorants
-  vcr_tuning tuning{2u, 4u, 1u, 256u};
+  vcr_tuning tuning{2u, 4u, 1u, 256u, 1u, 0u};
+  // per-cell blocks of the 8 decoded trilinear corners (tuning.corner_blocks)
+  float4* d_corners = nullptr;
+  int corner_tiles[3] = {0, 0, 0};  // 8^3-cell tiles per axis over cells -1 .. n-1
+  bool corners_valid = false;       // built from the bound grid (the buffer outlives a re-upload)
 
   vcr_cloud cloud{};
   bool has_cloud = false;
@@ -52,6 +57,15 @@ struct vcr_ctx {
   // recorded on the stream of every queued pass; synchronous reads wait on
   // it (a caller's non-blocking stream does not synchronise with stream 0)
   cudaEvent_t work_done = nullptr;
+  // stream-ordered read back (vcr_readback_async): two device staging slots
+  // copied out on the context's copy stream
+  struct Readback {
+    cudaStream_t copy = nullptr;
+    cudaEvent_t staged[2] = {nullptr, nullptr}, copied[2] = {nullptr, nullptr};
+    void* stage[2] = {nullptr, nullptr};
+    size_t bytes = 0;
+    int slot = 0;
+  } rb;
 
   // device counters: [0] paths [1] lookups [2] events [3] dda cells [4] work cursor
   // [5] grid max (u32 bits) [7] relRMSE accumulator (double bits)
@@ -125,6 +139,8 @@ SceneView scene_view(const vcr_ctx* ctx);
 vcr_status grid_upload_host(vcr_ctx* ctx, const float* host, const vcr_grid_desc* desc, int precision);
 vcr_status grid_build(vcr_ctx* ctx, const float* d_dense, const vcr_grid_desc* desc, int precision,
                       cudaStream_t s);
+// The corner blocks of the bound grid (after the bricks are written).
+vcr_status corner_build(vcr_ctx* ctx, cudaStream_t s);
 vcr_status grid_fbm_device(vcr_ctx* ctx, float* d_dense, const vcr_grid_desc* desc,
                            const vcr_fbm_desc* fbm, cudaStream_t s);
 void fbm_permutation(uint64_t seed, uint8_t perm[256]);

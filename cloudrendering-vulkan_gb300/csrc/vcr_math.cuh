@@ -6,7 +6,9 @@
 // +, -, *, / and sqrtf are IEEE round-to-nearest on both sides.  The
 // transcendental functions below are the project's own, written from the
 // classical series named at each one, so they give the same bits on the CPU
-// and the GPU (CUDA's logf/expf/sinf would not match a host libm).
+// and the GPU (CUDA's logf/expf/sinf would not match a host libm).  A
+// translation unit built with VCR_FAST_MATH (the fast-math tracker) swaps
+// them, in device code only, for CUDA's __logf / __expf / __sincosf.
 #pragma once
 
 #include <stdint.h>
@@ -81,6 +83,9 @@ constexpr float kTWO_PI = 6.28318530717958648f;
 // log(0) = -inf, matching the shaders' log(0) in the xorshift parity mode.
 VCR_HD float vlog(float x) {
   if (!(x > 0.0f)) return -INFINITY;
+#if defined(VCR_FAST_MATH) && defined(__CUDA_ARCH__)
+  return __logf(x);
+#endif
   uint32_t b = f2u(x);
   int e = (int)(b >> 23) - 127;
   float m = u2f((b & 0x007FFFFFu) | 0x3F800000u);
@@ -106,6 +111,9 @@ VCR_HD float vlog(float x) {
 VCR_HD float vexp(float x) {
   if (x < -87.0f) return 0.0f;
   if (x > 88.0f) return INFINITY;
+#if defined(VCR_FAST_MATH) && defined(__CUDA_ARCH__)
+  return __expf(x);
+#endif
   float k = floorf(fmaf(x, kLOG2E, 0.5f));
   float r = fmaf(-k, kLN2_HI, x);
   r = fmaf(-k, kLN2_LO, r);
@@ -136,6 +144,10 @@ VCR_HD float srgb_encode(float v) {
 // [-pi/4, pi/4]; Taylor series of sin to x^11 and cos to x^10, then the
 // quadrant rotation.
 VCR_HD void vsincos2pi(float u, float* s, float* c) {
+#if defined(VCR_FAST_MATH) && defined(__CUDA_ARCH__)
+  __sincosf(kTWO_PI * (u - floorf(u + 0.5f)), s, c);  // argument reduced to [-pi, pi]
+  return;
+#endif
   float q = floorf(fmaf(u, 4.0f, 0.5f));
   float r = fmaf(q, -0.25f, u);
   float x = r * kTWO_PI;

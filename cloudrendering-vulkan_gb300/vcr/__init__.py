@@ -181,8 +181,9 @@ class Context:
         self._ck(lib().vcr_grid_read_majorants(self.h, level, _ptr(out), out.size))
         return out
 
-    def set_tuning(self, majorant_level=2, dda_steps=4, stage_majorants=1, block_threads=256):
-        t = _abi.Tuning(majorant_level, dda_steps, stage_majorants, block_threads)
+    def set_tuning(self, majorant_level=2, dda_steps=4, stage_majorants=1, block_threads=256, corner_blocks=1,
+                   fast_math=0):
+        t = _abi.Tuning(majorant_level, dda_steps, stage_majorants, block_threads, corner_blocks, fast_math)
         self._ck(lib().vcr_set_tuning(self.h, C.byref(t)))
 
     def get_tuning(self) -> dict:
@@ -252,8 +253,9 @@ class Context:
     NRC_WEIGHTS = 21504
 
     def nrc_setup(self, train_samples=65536, learning_rate=1e-3, query_capacity=1 << 21, seed=1, ema_decay=0.0,
-                  tail_survival=0.0, query_kernel=0):
-        p = _abi.NrcParams(train_samples, learning_rate, query_capacity, seed, ema_decay, tail_survival, query_kernel)
+                  tail_survival=0.0, query_kernel=0, position_levels=16):
+        p = _abi.NrcParams(train_samples, learning_rate, query_capacity, seed, ema_decay, tail_survival, query_kernel,
+                           16 - position_levels)
         self._ck(lib().vcr_nrc_setup(self.h, C.byref(p)))
 
     def nrc_free(self):
@@ -483,6 +485,14 @@ class Context:
     def readback_to(self, buf_id, d_ptr, nbytes):
         """Copy a context buffer into caller memory (host or device)."""
         self._ck(lib().vcr_readback(self.h, buf_id, C.c_void_p(d_ptr), nbytes))
+
+    def readback_async(self, buf_id, host_ptr, nbytes, stream=0):
+        """Stream-ordered read back of the mean or sum image into pinned host
+        memory (lands by readback_wait)."""
+        self._ck(lib().vcr_readback_async(self.h, buf_id, C.c_void_p(host_ptr), nbytes, C.c_void_p(stream)))
+
+    def readback_wait(self):
+        self._ck(lib().vcr_readback_wait(self.h))
 
     def image_rel_rmse(self, d_ref, d_out, stream=0):
         self._ck(lib().vcr_image_rel_rmse(self.h, C.c_void_p(d_ref), C.c_void_p(d_out), C.c_void_p(stream)))

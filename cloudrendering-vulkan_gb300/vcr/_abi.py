@@ -67,7 +67,8 @@ class DisplayDesc(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("majorant_level", C.c_uint32), ("dda_steps", C.c_uint32), ("stage_majorants", C.c_uint32),
-                ("block_threads", C.c_uint32)]
+                ("block_threads", C.c_uint32), ("corner_blocks", C.c_uint32),
+                ("fast_math", C.c_uint32)]
 
 
 class ViewDesc(C.Structure):
@@ -82,7 +83,7 @@ class BatchInfo(C.Structure):
 class NrcParams(C.Structure):
     _fields_ = [("train_samples", C.c_uint32), ("learning_rate", C.c_float), ("query_capacity", C.c_uint32),
                 ("seed", C.c_uint32), ("ema_decay", C.c_float), ("tail_survival", C.c_float),
-                ("query_kernel", C.c_uint32)]
+                ("query_kernel", C.c_uint32), ("position_drop", C.c_uint32)]
 
 
 class NrcInfo(C.Structure):
@@ -208,6 +209,8 @@ SIGNATURES = {
     "vcr_sort_noalloc_status": (_S, [_P]),
     "vcr_morton_codes": (_S, [_P, _P, _u32, F3, F3, _u32, _P, _P]),
     "vcr_readback": (_S, [_P, C.c_int, _P, _sz]),
+    "vcr_readback_async": (_S, [_P, C.c_int, _P, _sz, _P]),
+    "vcr_readback_wait": (_S, [_P]),
     "vcr_display": (_S, [_P, C.POINTER(DisplayDesc), _P, _sz, _P]),
     "vcr_grid_read_dense": (_S, [_P, _P, _sz]),
     "vcr_pass_count": (_S, [_P, C.POINTER(_u32)]),

@@ -173,13 +173,23 @@ typedef struct vcr_shadow_volume {
  * the reference uses one global majorant, PathTracer.comp:338).
  * majorant_level selects DDA cells of (8 << level) voxels per axis, 0..3;
  * it changes how random numbers are consumed (not the expected image), so
- * it is part of a render's determinism key.  The other fields change only
- * the schedule, never a result bit. */
+ * it is part of a render's determinism key.  fast_math changes results
+ * (within the floating-point rounding of the functions it swaps); the other
+ * fields change only the schedule, never a result bit. */
 typedef struct vcr_tuning {
   uint32_t majorant_level;  /* 0..3 */
   uint32_t dda_steps;       /* majorant cells a lane may walk per wavefront step, >= 1 */
   uint32_t stage_majorants; /* 1: stage the level's majorants in shared memory (TMA bulk copy) when they fit */
   uint32_t block_threads;   /* wavefront CTA size: 128 or 256 */
+  uint32_t corner_blocks;   /* 1 (default): density lookups read a per-cell block of the 8 decoded trilinear
+                               corners (32 bytes, one sector) built from the bricks, 32 B per voxel of device
+                               memory; 0: they gather the 8 texels from the bricks.  Same values either way. */
+  uint32_t fast_math;       /* 0 (default): the tracker's device arithmetic is the oracle's, operation for
+                               operation (no contracted multiply-adds, the library's own log / exp / sincos
+                               series), so images are bit-exact with it.  1: a second build of the same kernel
+                               with contracted FMAs and the hardware log / exp / sincos approximations; a
+                               path's decisions can then differ from the oracle's where a random number falls
+                               within rounding of a threshold.  The autotuner keeps the caller's choice. */
 } vcr_tuning;
 
 /* PushConstants (UniformBuffers.h:6-13) for one progressive pass. */
@@ -329,7 +339,9 @@ VCR_API vcr_status vcr_pt_pass(vcr_ctx* ctx, const vcr_pass_desc* pass, void* st
  * per-pass radiance as `count` calls of vcr_pt_pass (the FP64 sums equal
  * up to the order of their additions).  One persistent launch lets the
  * lanes that would idle while a pass's longest paths finish run the next
- * pass's paths.  Needs the DDA tracker without the cache; no
+ * pass's paths.  Needs the DDA tracker; with the radiance cache
+ * (nrc_events > 0) the paths of all `count` passes end in the same weights
+ * and the cache's query capacity must hold count x crop x spp queries.  No
  * VCR_PASS_RECORD_STATS or VCR_PASS_NO_ACCUMULATE.  vcr_pt_counters then
  * reports the totals of all `count` passes.  Replaces `count` frames of
  * RenderTechniquePT::RecordDrawCommands (RenderTechniquePT.cpp:129-168)
@@ -382,6 +394,10 @@ typedef struct vcr_nrc_params {
                               a shorter latency tail) */
   uint32_t query_kernel;   /* VCR_NRC_QUERY_*: which tensor-core kernel
                               serves the cache's queries */
+  uint32_t position_drop;  /* 0..16: the finest frequency levels of the
+                              position encoding whose inputs are held at 0
+                              (0: all 16 levels, 16: no position input; for
+                              measuring what the encoding contributes) */
 } vcr_nrc_params;
 
 #define VCR_NRC_QUERY_DEFAULT 0u  /* the library's choice (the faster measured) */
@@ -688,6 +704,18 @@ VCR_API vcr_status vcr_checkpoint_load(vcr_ctx* ctx, const char* path);
 /* Synchronous copy of a context buffer (bytes must match). host_out may be
  * host, pinned or device memory of the context's device. */
 VCR_API vcr_status vcr_readback(vcr_ctx* ctx, vcr_buffer_id id, void* host_out, size_t bytes);
+/* Stream-ordered read back of VCR_BUF_IMAGE_MEAN (FP32 RGB, W*H*12 bytes)
+ * or VCR_BUF_IMAGE_SUM (FP64, W*H*24 bytes): the image as it stands after
+ * the work queued on `stream` is staged on `stream` (into one of two
+ * device slots) and copied to host_out on the context's own copy stream,
+ * so that the next pass queued on `stream` runs while the copy does.
+ * host_out should be pinned (page-locked) memory and must stay untouched
+ * until vcr_readback_wait returns; two calls in flight need two host
+ * buffers.  Replaces the per-frame transfer of the result image
+ * (RenderTechniquePT.cpp:143-167 blits it to the swapchain instead). */
+VCR_API vcr_status vcr_readback_async(vcr_ctx* ctx, vcr_buffer_id id, void* host_out, size_t bytes, void* stream);
+/* Blocks until every copy queued by vcr_readback_async has landed. */
+VCR_API vcr_status vcr_readback_wait(vcr_ctx* ctx);
 
 /* ------------------------------------------------------------------------ */
 /* Display image                                                            */

@@ -22,6 +22,7 @@ struct Rec {
 };
 
 static bool g_exact = false;  // true: no BF16 rounding (finite-difference checks of the analytic gradient)
+static int g_levels = 16;     // position levels encoded; the inputs of the others are 0
 static double bf(double x) { return g_exact ? x : (double)bf16_to_f32(f32_to_bf16((float)x)); }
 static int layer_off(int l) { return l * kW * kW; }
 static int layer_cols(int l) { return l < kHidden ? kW : kOutPad; }
@@ -61,6 +62,10 @@ static void sh16(float x, float y, float z, float* o) {
 static void encode(const Rec& r, const float* b0, const float* inv_ext, float* o) {
   float ux = (r.px - b0[0]) * inv_ext[0], uy = (r.py - b0[1]) * inv_ext[1], uz = (r.pz - b0[2]) * inv_ext[2];
   for (int l = 0; l < 16; ++l) {
+    if (l >= g_levels) {
+      o[2 * l] = o[2 * l + 1] = 0.0f;
+      continue;
+    }
     float dx, dy, dz;
     level_dir(l, dx, dy, dz);
     float f = (float)(1u << (l >> 1)) * ((l & 1) ? 1.41421356f : 1.0f);
@@ -110,6 +115,8 @@ extern "C" {
 int oracle_nrc_weight_count() { return kWeights; }
 
 void oracle_nrc_set_exact(int exact) { g_exact = exact != 0; }
+
+void oracle_nrc_set_levels(int levels) { g_levels = levels < 0 ? 0 : levels > 16 ? 16 : levels; }
 
 void oracle_nrc_encode(const void* recs, uint32_t n, const float* b0, const float* inv_ext, float* out) {
   const Rec* r = static_cast<const Rec*>(recs);

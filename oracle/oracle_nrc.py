@@ -46,6 +46,12 @@ def _box(cloud):
     return b0, inv
 
 
+def set_levels(levels: int) -> None:
+    """Position levels the encoding computes (0..16, default 16), as the
+    cache's 16 - position_drop; the inputs of the other levels are 0."""
+    _lib().oracle_nrc_set_levels(int(levels))
+
+
 def encode(recs: np.ndarray, cloud) -> np.ndarray:
     b0, inv = _box(cloud)
     out = np.zeros((len(recs), 64), np.float32)

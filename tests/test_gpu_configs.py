@@ -125,6 +125,39 @@ def test_c5_passes_in_one_launch_match_the_oracle(cuda, c5_oracle):
     assert lookups == o_look
 
 
+def test_c5_fast_math_frame_against_the_oracle(cuda, c5_oracle):
+    """The opt-in fast-math tracker (vcr_tuning.fast_math: contracted FMAs,
+    hardware log / exp / sincos) on a full C5 frame: the share of paths
+    whose decisions (events, lookups) match the bit-exact oracle's, and the
+    relative radiance difference where they do.  Its figures are printed;
+    the bars are those the fast build measured with margin, not the exact
+    build's bit-exactness."""
+    sc, og = c5_oracle
+    W, H = sc.width, sc.height
+    cloud = sc.cloud()
+    cloud.max_extinction = max(og.max_density(), 0.01)
+    cam, prm = sc.camera(), sc.params(vcr.TRACKER_DDA)
+    with vcr.Context() as ctx:
+        configs.setup_context(ctx, sc)
+        ctx.set_cloud(cloud)
+        ctx.set_tuning(majorant_level=3, dda_steps=16, stage_majorants=1, block_threads=256, fast_math=1)
+        ctx.pt_pass(seed=5, pass_index=0, flags=vcr.PASS_RECORD_STATS)
+        ctx.synchronize()
+        g_sum, g_st = ctx.image_sum(), ctx.path_stats()
+    o_sum, o_st = og.pt_pass(cloud, cam, prm, W, H, seed=5, pass_index=0, flags=vcr.PASS_RECORD_STATS, level=3)
+    agree = np.all(g_st[..., :2] == o_st[..., :2], axis=-1)
+    hit = o_st[..., 1] > 0  # paths with at least one density lookup
+    rel = np.abs(g_sum - o_sum) / np.maximum(np.abs(o_sum), 1e-30)
+    ra = rel[agree & hit]
+    img_rel = abs(g_sum.sum() - o_sum.sum()) / o_sum.sum()
+    print(f"\nfast math: decisions agree on {agree.mean():.5f} of paths ({agree[hit].mean():.5f} of those with a "
+          f"lookup); where they agree, relative radiance difference median {np.median(ra):.2e}, "
+          f"99th pct {np.percentile(ra, 99):.2e}, max {ra.max():.2e}; frame sum differs by {img_rel:.2e}")
+    assert agree.mean() >= 0.95
+    assert np.percentile(ra, 99) <= 1e-4
+    assert img_rel <= 1e-2
+
+
 def test_c5_paths_ending_in_the_cache_match_the_oracle(cuda, c5_oracle):
     """The cached frame's tracker at C5: paths end at their 2nd event in the
     cache; with an all-zero network the image is exactly the oracle's

@@ -54,6 +54,35 @@ def test_forward_matches_oracle(cuda, kernel, n):
     assert np.abs(got - ref).mean() <= 3e-3 * scale
 
 
+@pytest.mark.parametrize("kernel", [vcr.NRC_QUERY_MMA, vcr.NRC_QUERY_TCGEN05])
+@pytest.mark.parametrize("levels", [8, 0])
+def test_forward_with_fewer_position_levels_matches_oracle(cuda, kernel, levels):
+    """position_levels = L (position_drop = 16 - L): both query kernels see
+    only the first L frequency levels, as the oracle encoding with the same
+    L (L = 0: no position input at all)."""
+    import torch
+    desc, cloud = _cloud()
+    recs = onrc.random_records(700, cloud, np.random.default_rng(2))
+    with vcr.Context() as ctx:
+        _ctx_with_cloud(ctx, desc, cloud)
+        ctx.nrc_setup(train_samples=4096, seed=7, query_kernel=kernel, position_levels=levels)
+        w = ctx.nrc_get_weights()
+        dr = _dev_records(recs, cuda)
+        out = torch.zeros(3 * len(recs), dtype=torch.float32, device=cuda)
+        ctx.nrc_forward(dr.data_ptr(), len(recs), out.data_ptr())
+        got = out.cpu().numpy().reshape(-1, 3)
+    try:
+        onrc.set_levels(levels)
+        ref = onrc.forward(w, recs, cloud)
+    finally:
+        onrc.set_levels(16)
+    full = onrc.forward(w, recs, cloud)
+    scale = np.abs(ref).mean() + 1e-3
+    assert np.abs(got - ref).max() <= 3e-2 * scale, (np.abs(got - ref).max(), scale)
+    assert np.abs(got - ref).mean() <= 3e-3 * scale
+    assert np.abs(full - ref).mean() > 10 * np.abs(got - ref).mean()  # the knob changes the output
+
+
 def test_query_kernels_agree_in_a_cached_render(cuda):
     """A cached frame with trained weights: the tcgen05 queries give the
     image of the mma.sync queries up to BF16 rounding of the activations
@@ -241,6 +270,40 @@ def test_frame_equals_pass_then_train_step(cuda):
     assert na["steps"] == nb["steps"] == 4 and na["train_records"] == nb["train_records"]
     np.testing.assert_allclose(wb, wa, rtol=0, atol=1e-5)
     np.testing.assert_allclose(ib, ia, rtol=1e-4, atol=1e-7)
+
+
+@pytest.mark.parametrize("kernel", [vcr.NRC_QUERY_MMA, vcr.NRC_QUERY_TCGEN05])
+def test_cached_passes_in_one_launch_equal_single_passes(cuda, kernel):
+    """vcr_pt_passes with paths ending in the cache: the count passes' queries
+    are answered after the launch with the same weights, so the sums equal
+    count single cached passes up to the order of the FP64 additions; a
+    query buffer too small for all of them is refused."""
+    sc = configs.C1_PT
+    W = H = 96
+    prm = sc.params(vcr.TRACKER_DDA)
+    prm.nrc_events = 2
+    res = []
+    for mode in ("single", "launch"):
+        with vcr.Context() as ctx:
+            configs.setup_context(ctx, sc, width=W, height=H)
+            ctx.set_params(prm)
+            ctx.nrc_setup(train_samples=8192, query_capacity=3 * W * H, seed=2, query_kernel=kernel)
+            for k in range(2):  # train a little so that the cache term is not the initial network's
+                ctx.nrc_train_step(seed=4, pass_index=k)
+            if mode == "launch":
+                ctx.pt_passes(seed=6, first=1, count=3)
+            else:
+                for k in range(1, 4):
+                    ctx.pt_pass(seed=6, pass_index=k)
+            ctx.synchronize()
+            res.append((ctx.image_sum(), ctx.counters()))
+            if mode == "launch":
+                ctx.nrc_setup(train_samples=8192, query_capacity=2 * W * H, seed=2, query_kernel=kernel)
+                with pytest.raises(vcr.VcrError, match="CAPACITY"):
+                    ctx.pt_passes(seed=6, first=1, count=3)
+    (ia, ca), (ib, cb) = res
+    np.testing.assert_allclose(ib, ia, rtol=1e-12, atol=0)
+    assert ia.sum() > 0
 
 
 def _image_mean(ctx, passes, seed):

@@ -273,3 +273,123 @@ def test_several_passes_in_one_launch_equal_single_passes(cuda):
             ctx.pt_passes(seed=3, first=0, count=2)
     np.testing.assert_allclose(multi, single, rtol=1e-12, atol=0)
     assert (single > 0).any()
+
+
+@pytest.mark.parametrize("precision,size", [(vcr.PREC_FP32, (37, 21, 45)), (vcr.PREC_FP16, (37, 21, 45)),
+                                            (vcr.PREC_BF16, (37, 21, 45)), (vcr.PREC_FP16, (24, 16, 40))])
+def test_corner_blocks_give_the_bricks_values(cuda, precision, size):
+    """Lookups through the per-cell corner blocks equal lookups that gather
+    the 8 texels from the bricks, bit for bit: point samples over the whole
+    box and past its faces (the clamp to the grid's edge), and a whole pass
+    with its path statistics.  The blocks are built during the host upload
+    (a tile layer behind each brick layer) or, when switched on after the
+    upload, in one launch.  Odd sizes leave partial bricks and tiles;
+    multiples of 8 add a tile layer past the last brick layer."""
+    import torch
+    dense = orc.fbm_fill(size, seed=9, octaves=4)
+    desc = vcr.grid_desc(size, (1 / 45,) * 3)
+    cloud = vcr.cloud_from_grid(desc, 1.0, 24.0)
+    rng = np.random.default_rng(4)
+    lo, hi = np.array(cloud.bounds_min), np.array(cloud.bounds_max)
+    pts = (lo + (hi - lo) * rng.uniform(-0.02, 1.02, (50000, 3))).astype(np.float32)
+    W = H = 64
+    sc = configs.C1_PT
+    out = []
+    for corners in (1, 0, 2):
+        with vcr.Context() as ctx:
+            ctx.set_tuning(majorant_level=1, dda_steps=4, stage_majorants=1, block_threads=256,
+                           corner_blocks=min(corners, 1))
+            ctx.grid_upload(desc, dense, precision)
+            if corners == 2:  # switched on after the upload
+                ctx.set_tuning(majorant_level=1, dda_steps=4, stage_majorants=1, block_threads=256, corner_blocks=1)
+            assert ctx.get_tuning()["corner_blocks"] == min(corners, 1)
+            ctx.set_cloud(cloud)
+            ctx.set_camera(vcr.camera_look((0.0, 0.0, -0.6), (0.0, 0.0, 1.0), 70.0, 0.1, W, H))
+            ctx.set_params(sc.params(vcr.TRACKER_DDA))
+            ctx.set_frame(W, H)
+            dp = torch.from_numpy(pts).to(cuda)
+            dv = torch.empty(len(pts), dtype=torch.float32, device=cuda)
+            ctx.grid_sample(dp.data_ptr(), dv.data_ptr(), len(pts))
+            ctx.pt_pass(seed=3, pass_index=1, flags=vcr.PASS_RECORD_STATS)
+            ctx.synchronize()
+            out.append((dv.cpu().numpy(), ctx.image_sum(), ctx.path_stats()))
+    (va, ia, sa), (vb, ib, sb), (vc, ic, sc2) = out
+    for v, i, s in ((va, ia, sa), (vc, ic, sc2)):
+        np.testing.assert_array_equal(v, vb)
+        np.testing.assert_array_equal(i, ib)
+        np.testing.assert_array_equal(s, sb)
+    assert (va > 0).mean() > 0.3 and sa[..., 1].sum() > 1000
+
+
+def test_reuploading_a_same_size_grid_replaces_every_buffer(cuda):
+    """A second grid of the same size uploaded into the same context (its
+    brick, scale, majorant and corner buffers are reused) samples exactly
+    as in a fresh context, also when the corner blocks were switched off
+    for the upload and on again afterwards."""
+    import torch
+    size = (40, 24, 32)
+    desc = vcr.grid_desc(size, (1 / 40,) * 3)
+    cloud = vcr.cloud_from_grid(desc, 1.0, 24.0)
+    a = orc.fbm_fill(size, seed=1, octaves=4)
+    b = orc.fbm_fill(size, seed=2, octaves=4) * 1.5
+    lo, hi = np.array(cloud.bounds_min), np.array(cloud.bounds_max)
+    pts = (lo + (hi - lo) * np.random.default_rng(5).uniform(-0.02, 1.02, (20000, 3))).astype(np.float32)
+    dp = torch.from_numpy(pts).to(cuda)
+
+    def sample(ctx):
+        ctx.set_cloud(cloud)
+        dv = torch.empty(len(pts), dtype=torch.float32, device=cuda)
+        ctx.grid_sample(dp.data_ptr(), dv.data_ptr(), len(pts))
+        ctx.synchronize()
+        return dv.cpu().numpy(), [ctx.majorants(lv) for lv in range(4)]
+
+    with vcr.Context() as ctx:
+        ctx.grid_upload(desc, b, vcr.PREC_FP16)
+        want, want_maj = sample(ctx)
+    for switch_off in (False, True):
+        with vcr.Context() as ctx:
+            ctx.grid_upload(desc, a, vcr.PREC_FP16)
+            sample(ctx)
+            if switch_off:
+                ctx.set_tuning(corner_blocks=0)
+            ctx.grid_upload(desc, b, vcr.PREC_FP16)
+            if switch_off:
+                ctx.set_tuning(corner_blocks=1)
+            got, got_maj = sample(ctx)
+        np.testing.assert_array_equal(got, want)
+        for g, w in zip(got_maj, want_maj):
+            np.testing.assert_array_equal(g, w)
+
+
+def test_stream_ordered_readback_gives_each_pass_its_image(cuda):
+    """vcr_readback_async after every pass on a side stream: each pinned
+    host buffer holds the mean (and the FP64 sums) as they stood after its
+    pass, equal to the synchronous read back of the same passes, although
+    the later passes were queued before the copies landed."""
+    import torch
+    sc = configs.C1_PT
+    W = H = 64
+    passes = 4
+    stream = torch.cuda.Stream()
+    want_mean, want_sum = [], []
+    with vcr.Context() as ctx:
+        configs.setup_context(ctx, sc, width=W, height=H, tracker=vcr.TRACKER_DDA)
+        for k in range(passes):
+            ctx.pt_pass(seed=8, pass_index=k)
+            want_mean.append(ctx.image_mean())
+            want_sum.append(ctx.image_sum())
+    means = [torch.empty(W * H * 3, dtype=torch.float32).pin_memory() for _ in range(passes)]
+    sums = [torch.empty(W * H * 3, dtype=torch.float64).pin_memory() for _ in range(passes)]
+    with vcr.Context() as ctx:
+        configs.setup_context(ctx, sc, width=W, height=H, tracker=vcr.TRACKER_DDA)
+        ctx.synchronize()
+        for k in range(passes):
+            ctx.pt_pass(seed=8, pass_index=k, stream=stream.cuda_stream)
+            ctx.readback_async(vcr.BUF_IMAGE_MEAN, means[k].data_ptr(), W * H * 12, stream=stream.cuda_stream)
+            ctx.readback_async(vcr.BUF_IMAGE_SUM, sums[k].data_ptr(), W * H * 24, stream=stream.cuda_stream)
+        ctx.readback_wait()
+        with pytest.raises(vcr.VcrError):
+            ctx.readback_async(vcr.BUF_PATH_STATS, means[0].data_ptr(), W * H * 16)
+    for k in range(passes):
+        np.testing.assert_array_equal(means[k].numpy(), np.asarray(want_mean[k], np.float32).reshape(-1))
+        np.testing.assert_array_equal(sums[k].numpy(), np.asarray(want_sum[k]).reshape(-1))

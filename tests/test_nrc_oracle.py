@@ -2,6 +2,7 @@
 central finite differences of its loss (exact arithmetic mode), and its
 encoding has the documented structure."""
 import numpy as np
+import pytest
 
 import vcr
 from oracle import oracle_nrc as onrc
@@ -56,3 +57,22 @@ def test_encoding_structure():
     np.testing.assert_allclose(e[:, 48], 0.28209479, rtol=1e-6)
     # band 1 is proportional to the direction
     np.testing.assert_allclose(e[:, 34] / 0.48860251, recs["v"][:, 2], rtol=1e-5, atol=1e-6)
+
+
+@pytest.mark.parametrize("levels", [16, 8, 1, 0])
+def test_position_levels_zero_the_finer_levels(levels):
+    """The encoding ablation knob: only levels below `levels` are encoded,
+    the rest of the 32 position inputs are 0 and the SH inputs do not
+    change."""
+    cloud = _cloud()
+    recs = onrc.random_records(40, cloud, np.random.default_rng(3))
+    full = onrc.encode(recs, cloud)
+    try:
+        onrc.set_levels(levels)
+        e = onrc.encode(recs, cloud)
+    finally:
+        onrc.set_levels(16)
+    k = levels
+    np.testing.assert_array_equal(e[:, :2 * k], full[:, :2 * k])
+    assert not e[:, 2 * k:32].any()
+    np.testing.assert_array_equal(e[:, 32:], full[:, 32:])
