@@ -495,10 +495,11 @@ def cached_time_to_1pct(ctx, sc, stream, ref, cfg, to_end=False):
     assert group == 1 or pool, "several frames a launch need the pooled training schedule"
     nmax, chunk = nmax // group, max(1, chunk // group)  # counted in launches from here
     while done < nmax and (hit is None or to_end):
-        _error_curve(ctx, stream, ref, chunk, frame, errs, ms, done)
-        done += chunk
+        n = min(chunk, nmax - done)
+        _error_curve(ctx, stream, ref, n, frame, errs, ms, done)
+        done += n
         e = errs[:done].cpu().numpy()
-        for i in range(done - chunk, done):
+        for i in range(done - n, done):
             if hit is None and ref.corrected(e[i]) <= 0.01:
                 hit = i
                 break
