@@ -96,8 +96,9 @@ __global__ void __launch_bounds__(kSortThreads, 4) sort_pass_kernel(const uint32
   __shared__ uint32_t s_cnt[kSortThreads / 32][16];
   __shared__ uint32_t s_tile_start[16];  // digit start inside the tile
   __shared__ uint32_t s_base[16];        // global output offset of the digit's run
-  __shared__ uint32_t s_keys[kSortTile];
-  __shared__ uint32_t s_vals[kSortTile];
+  __shared__ uint32_t s_keys[kSortTile];  // sorted keys of the tile
+  __shared__ uint32_t s_vals[kSortTile];  // values in tile order (copied in while the tile is ranked)
+  __shared__ uint16_t s_src[kSortTile];   // tile-order index of each sorted key
 
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
   const uint32_t lt = (1u << lane) - 1u;
@@ -106,6 +107,15 @@ __global__ void __launch_bounds__(kSortThreads, 4) sort_pass_kernel(const uint32
   const uint32_t tile = s_tile;
   const uint32_t tile0 = tile * kSortTile;
   const uint32_t count = min((uint32_t)kSortTile, n - tile0);
+  // the tile's values go to shared memory by asynchronous copies, which run
+  // during the ranking and the look-back
+  if (vin) {
+    for (uint32_t i = threadIdx.x; i < count; i += kSortThreads)
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(s_vals + i)),
+                   "l"(vin + tile0 + i)
+                   : "memory");
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  }
 
   // Stable in-warp ranking: warp w holds keys [w*32*kSortItems, ...) of the
   // tile in kSortItems rounds of 32 (round j, lane l = key w*32*I + 32j + l).
@@ -145,9 +155,14 @@ __global__ void __launch_bounds__(kSortThreads, 4) sort_pass_kernel(const uint32
       if (d >= (uint32_t)o) incl += v;
     }
     s_tile_start[d] = incl - total;
-    // exclusive global offset of digit d in this pass
-    uint32_t g = 0;
-    for (uint32_t e = 0; e < d; ++e) g += sc.hist[pass * 16 + e];
+    // exclusive global offset of digit d in this pass: scan of the 16 counts
+    const uint32_t hd = sc.hist[pass * 16 + d];
+    uint32_t g = hd;
+    for (int o = 1; o < 16; o <<= 1) {
+      uint32_t v = __shfl_up_sync(0x0000ffffu, g, o, 16);
+      if (d >= (uint32_t)o) g += v;
+    }
+    g -= hd;
     // decoupled look-back
     volatile uint32_t* desc = sc.desc + (size_t)pass * ((size_t)gridDim.x * 16);
     if (tile == 0) {
@@ -178,7 +193,7 @@ __global__ void __launch_bounds__(kSortThreads, 4) sort_pass_kernel(const uint32
     }
   }
   __syncthreads();
-  // stage in tile order; values are read here, in the same coalesced order
+  // stage the keys in sorted order with the tile-order index they came from
 #pragma unroll
   for (int j = 0; j < kSortItems; ++j) {
     const uint32_t local = warp * (32 * kSortItems) + j * 32 + lane;
@@ -186,17 +201,19 @@ __global__ void __launch_bounds__(kSortThreads, 4) sort_pass_kernel(const uint32
       const uint32_t d = (key[j] >> shift) & dmask;
       const uint32_t pos = s_tile_start[d] + s_cnt[warp][d] + rank[j];
       s_keys[pos] = key[j];
-      s_vals[pos] = vin ? vin[tile0 + local] : tile0 + local;
+      s_src[pos] = (uint16_t)local;
     }
   }
+  if (vin) asm volatile("cp.async.wait_all;" ::: "memory");
   __syncthreads();
   for (uint32_t i = threadIdx.x; i < count; i += kSortThreads) {
     uint32_t k = s_keys[i];
     uint32_t d = (k >> shift) & dmask;
     uint32_t o = s_base[d] + (i - s_tile_start[d]);
     if (o < n) {  // always true unless a look-back wait ran out (error word set)
+      const uint32_t src = s_src[i];
       kout[o] = k;
-      vout[o] = s_vals[i];
+      vout[o] = vin ? s_vals[src] : tile0 + src;
     }
   }
 }
