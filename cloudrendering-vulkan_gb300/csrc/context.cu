@@ -439,6 +439,11 @@ extern "C" VCR_API vcr_status vcr_set_tuning(vcr_ctx* ctx, const vcr_tuning* t) 
                 "tuning: level 0..3, dda_steps 1..4096, block_threads 128 or 256, corner_blocks and fast_math 0 "
                 "or 1");
   ctx->tuning = *t;
+  if (!t->corner_blocks && ctx->d_corners) {  // switched off: the memory goes back (cudaFree waits for the device)
+    cudaFree(ctx->d_corners);
+    ctx->d_corners = nullptr;
+    ctx->corners_valid = false;
+  }
   if (t->corner_blocks && ctx->has_grid && !ctx->corners_valid) {  // switched on after the grid was bound
     vcr_status st = corner_build(ctx, 0);
     if (st) return st;

@@ -183,7 +183,8 @@ typedef struct vcr_tuning {
   uint32_t block_threads;   /* wavefront CTA size: 128 or 256 */
   uint32_t corner_blocks;   /* 1 (default): density lookups read a per-cell block of the 8 decoded trilinear
                                corners (32 bytes, one sector) built from the bricks, 32 B per voxel of device
-                               memory; 0: they gather the 8 texels from the bricks.  Same values either way. */
+                               memory; 0: they gather the 8 texels from the bricks (switching it off frees the
+                               blocks).  Same values either way. */
   uint32_t fast_math;       /* 0 (default): the tracker's device arithmetic is the oracle's, operation for
                                operation (no contracted multiply-adds, the library's own log / exp / sincos
                                series), so images are bit-exact with it.  1: a second build of the same kernel
