@@ -310,7 +310,7 @@ PLAIN_PASSES_PER_LAUNCH = 25  # the plain tracker's error curve: one launch of 2
 CONV = {"ref_samples": 147456, "ref_spp": 16, "plain_max_passes": 30000, "warm_steps": 6000, "warm_sets": 32, "warm_more": 19, "warm_batch": 16384,
         "pool_sets": 32, "pool_every": 96, "max_frames": 8000, "chunk": 500, "spp": 1, "train_samples": 65536,
         "learning_rate": 1e-3, "ema_decay": 0.99, "nrc_events": 2, "repeats": 3, "position_levels": 16,
-        "ablation_levels": [8, 0], "frame_group": 8}
+        "ablation_levels": [8, 0], "ablation_grid": True, "frame_group": 8}
 
 
 class Reference:
@@ -431,7 +431,7 @@ def cached_time_to_1pct(ctx, sc, stream, ref, cfg, to_end=False):
     ctx.nrc_setup(train_samples=cfg["train_samples"], learning_rate=cfg.get("warm_lr", cfg["learning_rate"]),
                   query_capacity=px * spp * group,
                   seed=1, ema_decay=cfg["ema_decay"], tail_survival=cfg.get("tail_survival", 0.0),
-                  position_levels=cfg.get("position_levels", 16))
+                  position_levels=cfg.get("position_levels", 16), encoding=cfg.get("encoding", 0))
     sets = cfg.get("warm_sets", 1)
     per_launch = sets * (1 + cfg["warm_more"])  # Adam steps a training launch feeds
     batches = max(1, cfg["warm_steps"] // per_launch)
@@ -545,7 +545,13 @@ def convergence(ctx, sc, stream, args, overrides=None):
     for lv in cfg.get("ablation_levels", ()):
         r = cached_time_to_1pct(ctx, sc, stream, ref, dict(cfg, position_levels=lv))
         ablation[str(lv)] = {k: r[k] for k in ("frames", "time_s", "relrmse_last", "frames_run", "loss")}
-    return {"plain": plain, "nrc": nrc, "position_levels_ablation": ablation,
+    # the multiresolution grid encoding in place of the frequency one
+    grid = None
+    if cfg.get("ablation_grid"):
+        import vcr
+        r = cached_time_to_1pct(ctx, sc, stream, ref, dict(cfg, encoding=vcr.NRC_ENCODING_GRID))
+        grid = {k: r[k] for k in ("frames", "time_s", "frame_ms", "warm_s", "relrmse_last", "frames_run", "loss")}
+    return {"plain": plain, "nrc": nrc, "position_levels_ablation": ablation, "grid_encoding": grid,
             "speedup": round(plain["time_s"] / nrc["time_s"], 2) if (nrc["time_s"] and plain["time_s"]) else None,
             "reference": {"samples_per_pixel": ref.samples, "spp_per_launch": ref.spp,
                           "own_relrmse": round(float(np.sqrt(ref.noise2)), 5), "render_s": round(ref.render_s, 2),

@@ -15,6 +15,8 @@
 //   PPMS  u64 pixels; f64 statistics [pixels*8] (N, R, tau rgb, bg rgb)
 //   NRCW  u32 step, has_average, training paths per step, weight count;
 //         f32 weights, Adam m, Adam v [, moving average]
+//   NRCG  (grid encoding) u64 table values, u32 has_average; f32 tables,
+//         Adam m, Adam v [, moving average]
 //   BTCH  u64 pixels; u32 passes, 0; u64 samples; f64 sums [pixels*3]
 // Loading checks every section against the context's current setup (the
 // same scene hash, frame size, the technique set up with the same sizes)
@@ -137,6 +139,18 @@ static vcr_status save_sections(vcr_ctx* ctx, std::vector<Section>& out) {
         if (vs) return vs;
       }
     out.push_back(std::move(s));
+    if (st->gw) {  // the grid encoding's tables: values, Adam moments, moving average
+      Section g{{'N', 'R', 'C', 'G'}, {}};
+      put(g.data, (uint64_t)kNrcGridParams);
+      put(g.data, st->gema ? 1u : 0u);
+      const float* gparts[] = {st->gw, st->gm, st->gv, st->gema};
+      for (const float* d : gparts)
+        if (d) {
+          vcr_status vs = put_device(ctx, g.data, d, kNrcGridParams * sizeof(float));
+          if (vs) return vs;
+        }
+      out.push_back(std::move(g));
+    }
   }
   if (ctx->batch) {
     BatchState* b = ctx->batch;
@@ -254,8 +268,11 @@ extern "C" VCR_API vcr_status vcr_checkpoint_load(vcr_ctx* ctx, const char* path
                   "photon-map parameters differ)",
                   path);
   }
+  bool has_nrcw = false, has_nrcg = false;
   for (const Section& s : secs) {
     Reader r{s.data.data(), s.data.size()};
+    has_nrcw = has_nrcw || !std::memcmp(s.tag, "NRCW", 4);
+    has_nrcg = has_nrcg || !std::memcmp(s.tag, "NRCG", 4);
     if (!std::memcmp(s.tag, "FRAM", 4)) {
       uint32_t w, h, passes, z;
       uint64_t samples;
@@ -274,6 +291,15 @@ extern "C" VCR_API vcr_status vcr_checkpoint_load(vcr_ctx* ctx, const char* path
       if (!ctx->nrc || count != (uint32_t)kNrcWeightCount || (has_avg != 0) != (ctx->nrc->ema != nullptr))
         return fail(ctx, VCR_ERR_STATE, "checkpoint holds a radiance cache: vcr_nrc_setup with the same ema_decay first");
       if (r.left != (size_t)count * sizeof(float) * (3u + has_avg)) return fail(ctx, VCR_ERR_IO, "bad NRCW size");
+    } else if (!std::memcmp(s.tag, "NRCG", 4)) {
+      uint64_t count;
+      uint32_t has_avg;
+      if (!r.get(count) || !r.get(has_avg)) return fail(ctx, VCR_ERR_IO, "bad NRCG");
+      if (!ctx->nrc || !ctx->nrc->gw || count != kNrcGridParams || (has_avg != 0) != (ctx->nrc->gema != nullptr))
+        return fail(ctx, VCR_ERR_STATE,
+                    "checkpoint holds a grid-encoded radiance cache: vcr_nrc_setup with the grid encoding and the "
+                    "same ema_decay first");
+      if (r.left != (size_t)count * sizeof(float) * (3u + has_avg)) return fail(ctx, VCR_ERR_IO, "bad NRCG size");
     } else if (!std::memcmp(s.tag, "BTCH", 4)) {
       uint64_t px, samples;
       uint32_t passes, z;
@@ -282,6 +308,8 @@ extern "C" VCR_API vcr_status vcr_checkpoint_load(vcr_ctx* ctx, const char* path
       if (r.left != px * 3 * sizeof(double)) return fail(ctx, VCR_ERR_IO, "bad BTCH size");
     }
   }
+  if (has_nrcw && !has_nrcg && ctx->nrc && ctx->nrc->gw)
+    return fail(ctx, VCR_ERR_STATE, "checkpoint holds a frequency-encoded radiance cache; this one has the grid encoding");
   // apply
   for (const Section& s : secs) {
     Reader r{s.data.data(), s.data.size()};
@@ -313,6 +341,16 @@ extern "C" VCR_API vcr_status vcr_checkpoint_load(vcr_ctx* ctx, const char* path
       st->calib_h = ctx->height;
       vcr_status vs = nrc_refresh_copies(ctx);
       if (vs) return vs;
+    } else if (!std::memcmp(s.tag, "NRCG", 4)) {
+      NrcState* st = ctx->nrc;
+      uint64_t count;
+      uint32_t has_avg;
+      r.get(count);
+      r.get(has_avg);
+      const size_t nb = (size_t)count * sizeof(float);
+      float* gparts[] = {st->gw, st->gm, st->gv, st->gema};
+      for (int i = 0; i < 3 + (int)has_avg; ++i)
+        VCR_CUDA(ctx, cudaMemcpy(gparts[i], r.p + i * nb, nb, cudaMemcpyHostToDevice));
     } else if (!std::memcmp(s.tag, "BTCH", 4)) {
       BatchState* b = ctx->batch;
       uint64_t px, samples;

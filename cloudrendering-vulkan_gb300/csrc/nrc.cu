@@ -41,6 +41,12 @@ struct NrcView {
   const bf16* wbi;  // inference weights (the moving average, or wb)
   f3 b0, inv_ext;
   int levels;       // position-encoding levels the network sees (the rest are 0)
+  // grid encoding (nullptr: the frequency encoding): the tables training
+  // reads, the tables queries read (their moving average, or gtab), and the
+  // tables' gradient accumulator
+  const float* gtab;
+  const float* gtab_i;
+  float* ggrad;
 };
 
 // ---------------------------------------------------------------------------
@@ -69,8 +75,8 @@ __global__ void __launch_bounds__(kInferThreads, 3) nrc_infer_kernel(NrcView v, 
     if (i0 < count) r0 = recs[i0];
     if (i1 < count) r1 = recs[i1];
     uint32_t a[4][4];
-    encode_a(r0, i0 < count, v.b0, v.inv_ext, dirs, t, 0, a, v.levels);
-    encode_a(r1, i1 < count, v.b0, v.inv_ext, dirs, t, 1, a, v.levels);
+    encode_a(r0, i0 < count, v.b0, v.inv_ext, dirs, t, 0, a, v.levels, v.gtab_i);
+    encode_a(r1, i1 < count, v.b0, v.inv_ext, dirs, t, 1, a, v.levels, v.gtab_i);
     float yg[3], yh[3];
     mlp_forward_mma(W, a, lane, yg, yh);
     if (t == 0) {
@@ -128,6 +134,12 @@ __device__ __forceinline__ void store_a(bf16* T, int row, int t, const uint32_t 
 // 8(w%2)..) of the 64x16 output layer's, in registers across the CTA's
 // tiles; X_l^T and dY_l fragments come from ldmatrix.trans.  At the end each
 // CTA stores its gradient into its own slot of gpart.
+//
+// kGrid (the grid encoding): the backward also forms dX_0 = dY_0 W_0^T for
+// the 32 position inputs in registers and adds, for every record, level and
+// feature, the 8 trilinear shares of it into the tables' gradient (float
+// atomics, so their order, and the last bits of the sums, vary).
+template <bool kGrid>
 __global__ void __launch_bounds__(kTrainThreads, 1) nrc_train_kernel(NrcView v, const NrcRecord* __restrict__ recs,
                                                                      const uint32_t* __restrict__ count_ptr,
                                                                      uint32_t capacity, uint32_t first_rec,
@@ -166,8 +178,8 @@ __global__ void __launch_bounds__(kTrainThreads, 1) nrc_train_kernel(NrcView v, 
       NrcRecord r0{}, r1{};
       if (i0 < count) r0 = recs[i0];
       if (i1 < count) r1 = recs[i1];
-      encode_a(r0, i0 < count, v.b0, v.inv_ext, dirs, t, 0, a, v.levels);
-      encode_a(r1, i1 < count, v.b0, v.inv_ext, dirs, t, 1, a, v.levels);
+      encode_a(r0, i0 < count, v.b0, v.inv_ext, dirs, t, 0, a, v.levels, kGrid ? v.gtab : nullptr);
+      encode_a(r1, i1 < count, v.b0, v.inv_ext, dirs, t, 1, a, v.levels, kGrid ? v.gtab : nullptr);
     }
     store_a(X, row, t, a, 4);
 #pragma unroll 1
@@ -266,6 +278,46 @@ __global__ void __launch_bounds__(kTrainThreads, 1) nrc_train_kernel(NrcView v, 
           }
         }
         store_a(Dn, row, t, da, 4);
+      } else if (kGrid) {
+        // dX_0 for inputs 0..31 (n-tiles 0..3): acc[nt] holds (row, 8nt+2t+e)
+        // and (row+8, 8nt+2t+e), i.e. level 4nt+t, feature e
+        const bf16* W0 = W + woff(0);
+        float acc[4][4];
+#pragma unroll
+        for (int nt = 0; nt < 4; ++nt) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
+#pragma unroll
+        for (int kt = 0; kt < 4; ++kt)
+#pragma unroll
+          for (int np = 0; np < 2; ++np) {
+            uint32_t b[4];
+            ldsm_x4(b, W0 + (np * 16 + rr + 8 * (q >> 1)) * ldw(0) + kt * 16 + 8 * (q & 1));
+            mma_bf16(acc[2 * np], da[kt], b[0], b[1]);
+            mma_bf16(acc[2 * np + 1], da[kt], b[2], b[3]);
+          }
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const uint32_t idx = h ? i1 : i0;
+          if (idx >= count) continue;
+          const NrcRecord& rec = recs[idx];
+          float ux, uy, uz;
+          nrc_box_coords(rec, v.b0, v.inv_ext, ux, uy, uz);
+#pragma unroll
+          for (int nt = 0; nt < 4; ++nt) {
+            const int lv = 4 * nt + t;
+            if (lv >= v.levels) continue;
+            const float d0 = acc[nt][2 * h], d1 = acc[nt][2 * h + 1];
+            const int n = nrc_grid_res(lv);
+            const NrcGridCell c = nrc_grid_cell(n, ux, uy, uz);
+            float* gl = v.ggrad + (size_t)lv * kNrcGridTable * 2;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+              const uint32_t e = nrc_grid_index(n, c.x + (k & 1), c.y + ((k >> 1) & 1), c.z + (k >> 2));
+              const float w = nrc_grid_weight(c, k);
+              atomicAdd(gl + 2 * e, w * d0);
+              atomicAdd(gl + 2 * e + 1, w * d1);
+            }
+          }
+        }
       }
     }
     __syncthreads();  // every warp is done with X_0 and dY_0 before the next tile's
@@ -386,12 +438,49 @@ __global__ void nrc_to_bf16_kernel(const float* __restrict__ w, bf16* __restrict
   if (i < kNrcWeightCount) wb[i] = __float2bfloat16_rn(w[i]);
 }
 
+// Adam step on the grid encoding's tables (step size h.lr x
+// kNrcGridLrScale), clearing their gradient; the moving average as for the
+// weights.
+__global__ void nrc_grid_adam_kernel(float* __restrict__ w, float* __restrict__ m, float* __restrict__ v,
+                                     float* __restrict__ grad, float* __restrict__ ema, AdamStep h) {
+  const float lr = h.lr * kNrcGridLrScale;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < kNrcGridParams;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const float gi = grad[i];
+    const float mi = h.b1 * m[i] + (1.0f - h.b1) * gi;
+    const float vi = h.b2 * v[i] + (1.0f - h.b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    const float wi = w[i] - lr * (mi / h.c1) / (sqrtf(vi / h.c2) + h.eps);
+    w[i] = wi;
+    grad[i] = 0.0f;
+    if (ema) ema[i] = h.decay * ema[i] + (1.0f - h.decay) * wi;
+  }
+}
+
+// The tables' initial values: uniform in [-1e-4, 1e-4] from a seeded hash
+// (the moving average starts equal).
+__global__ void nrc_grid_init_kernel(float* __restrict__ w, float* __restrict__ ema, uint32_t seed) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < kNrcGridParams;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const uint32_t hsh = pcg_hash(seed ^ 0x9E3779B9u ^ pcg_hash((uint32_t)i));
+    const float u = (float)(hsh >> 8) * 5.96046448e-08f;  // [0,1)
+    const float x = (2.0f * u - 1.0f) * 1e-4f;
+    w[i] = x;
+    if (ema) ema[i] = x;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
 static size_t infer_smem() { return (size_t)kWs * 2 + kNrcPosLevels * 3 * sizeof(float); }
 static size_t train_smem() {
   return (size_t)kWs * 2 + (size_t)(kNrcLayers + 2) * kTileX * 2 + kNrcPosLevels * 3 * sizeof(float);
+}
+
+size_t nrc_param_count(const NrcState* st) {
+  return (size_t)kNrcWeightCount + (st && st->gw ? kNrcGridParams : 0);
 }
 
 NrcView nrc_view(const vcr_ctx* ctx) {
@@ -403,14 +492,19 @@ NrcView nrc_view(const vcr_ctx* ctx) {
   v.inv_ext = mk(1.0f / (c.bounds_max[0] - c.bounds_min[0]), 1.0f / (c.bounds_max[1] - c.bounds_min[1]),
                  1.0f / (c.bounds_max[2] - c.bounds_min[2]));
   v.levels = kNrcPosLevels - (int)ctx->nrc->prm.position_drop;
+  const NrcState* st = ctx->nrc;
+  v.gtab = st->gw;
+  v.gtab_i = st->gema ? st->gema : st->gw;
+  v.ggrad = st->ggrad;
   return v;
 }
 
 void nrc_free(vcr_ctx* ctx) {
   NrcState* st = ctx->nrc;
   if (!st) return;
-  void* ptrs[] = {st->w, st->wb, st->m, st->v, st->grad, st->gpart, st->ema, st->wbi, st->loss, st->train, st->train_count,
-                  st->query, st->query_count};
+  void* ptrs[] = {st->w,      st->wb,          st->m,     st->v,           st->grad, st->gpart, st->ema,
+                  st->wbi,    st->loss,        st->train, st->train_count, st->query, st->query_count,
+                  st->gw,     st->gm,          st->gv,    st->ggrad,       st->gema};
   for (void* p : ptrs) cudaFree(p);
   delete st;
   ctx->nrc = nullptr;
@@ -437,10 +531,11 @@ vcr_status nrc_setup(vcr_ctx* ctx, const vcr_nrc_params* p) {
   if (!p || p->train_samples == 0 || p->train_samples > (1u << 22) || !(p->learning_rate > 0.0f) ||
       p->query_capacity == 0 || !(p->ema_decay >= 0.0f && p->ema_decay < 1.0f) ||
       !(p->tail_survival >= 0.0f && p->tail_survival < 1.0f) || p->query_kernel > VCR_NRC_QUERY_TCGEN05 ||
-      p->position_drop > (uint32_t)kNrcPosLevels)
+      p->position_drop > (uint32_t)kNrcPosLevels || p->encoding > VCR_NRC_ENCODING_GRID)
     return fail(ctx, VCR_ERR_INVALID,
                 "nrc params: train_samples 1..2^22, learning_rate > 0, query_capacity > 0, ema_decay and "
-                "tail_survival in [0,1), query_kernel a VCR_NRC_QUERY_* value, position_drop 0..16");
+                "tail_survival in [0,1), query_kernel a VCR_NRC_QUERY_* value, position_drop 0..16, encoding a "
+                "VCR_NRC_ENCODING_* value");
   nrc_free(ctx);
   NrcState* st = new NrcState();
   ctx->nrc = st;
@@ -464,6 +559,13 @@ vcr_status nrc_setup(vcr_ctx* ctx, const vcr_nrc_params* p) {
   VCR_ALLOC(st->train_count, 4);
   VCR_ALLOC(st->query, (size_t)p->query_capacity * sizeof(NrcRecord));
   VCR_ALLOC(st->query_count, 4);
+  if (p->encoding == VCR_NRC_ENCODING_GRID) {
+    VCR_ALLOC(st->gw, kNrcGridParams * 4);
+    VCR_ALLOC(st->gm, kNrcGridParams * 4);
+    VCR_ALLOC(st->gv, kNrcGridParams * 4);
+    VCR_ALLOC(st->ggrad, kNrcGridParams * 4);
+    if (p->ema_decay > 0.0f) VCR_ALLOC(st->gema, kNrcGridParams * 4);
+  }
 #undef VCR_ALLOC
   VCR_CUDA(ctx, cudaMemset(st->train_count, 0, 4));
   VCR_CUDA(ctx, cudaMemset(st->loss, 0, 8));
@@ -480,8 +582,18 @@ vcr_status nrc_setup(vcr_ctx* ctx, const vcr_nrc_params* p) {
     nrc_copy_weights_kernel<<<(kNrcWeightCount + 255) / 256, 256>>>(st->w, st->ema, reinterpret_cast<bf16*>(st->wbi));
     VCR_CUDA(ctx, cudaGetLastError());
   }
+  if (st->gw) {
+    VCR_CUDA(ctx, cudaMemset(st->gm, 0, kNrcGridParams * 4));
+    VCR_CUDA(ctx, cudaMemset(st->gv, 0, kNrcGridParams * 4));
+    VCR_CUDA(ctx, cudaMemset(st->ggrad, 0, kNrcGridParams * 4));
+    nrc_grid_init_kernel<<<ctx->sm_count * 8, 256>>>(st->gw, st->gema, p->seed);
+    VCR_CUDA(ctx, cudaGetLastError());
+  }
   VCR_CUDA(ctx, cudaFuncSetAttribute(nrc_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)infer_smem()));
-  VCR_CUDA(ctx, cudaFuncSetAttribute(nrc_train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)train_smem()));
+  VCR_CUDA(ctx, cudaFuncSetAttribute(nrc_train_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)train_smem()));
+  VCR_CUDA(ctx, cudaFuncSetAttribute(nrc_train_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)train_smem()));
   return VCR_OK;
 }
 
@@ -491,10 +603,18 @@ vcr_status nrc_setup(vcr_ctx* ctx, const vcr_nrc_params* p) {
 static vcr_status nrc_grad(vcr_ctx* ctx, const NrcRecord* recs, const uint32_t* d_count, uint32_t capacity,
                            cudaStream_t s, uint32_t first, bool adam) {
   NrcState* st = ctx->nrc;
-  VCR_CUDA(ctx, cudaFuncSetAttribute(nrc_train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)train_smem()));
   const int blocks = st->gpart_blocks;
-  nrc_train_kernel<<<blocks, kTrainThreads, train_smem(), s>>>(nrc_view(ctx), recs, d_count, capacity, first,
-                                                               st->gpart, st->loss);
+  if (st->gw) {
+    VCR_CUDA(ctx, cudaFuncSetAttribute(nrc_train_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)train_smem()));
+    nrc_train_kernel<true><<<blocks, kTrainThreads, train_smem(), s>>>(nrc_view(ctx), recs, d_count, capacity, first,
+                                                                       st->gpart, st->loss);
+  } else {
+    VCR_CUDA(ctx, cudaFuncSetAttribute(nrc_train_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)train_smem()));
+    nrc_train_kernel<false><<<blocks, kTrainThreads, train_smem(), s>>>(nrc_view(ctx), recs, d_count, capacity,
+                                                                        first, st->gpart, st->loss);
+  }
   VCR_CUDA(ctx, cudaGetLastError());
   AdamView a{st->w, reinterpret_cast<bf16*>(st->wb), st->m, st->v, st->ema, reinterpret_cast<bf16*>(st->wbi)};
   AdamStep h{};
@@ -517,6 +637,10 @@ static vcr_status nrc_grad(vcr_ctx* ctx, const NrcRecord* recs, const uint32_t* 
     nrc_grad_reduce_kernel<false><<<grid, block, 0, s>>>(st->gpart, blocks, d_count, capacity, first, st->grad, a, h,
                                                          st->loss);
   VCR_CUDA(ctx, cudaGetLastError());
+  if (adam && st->gw) {
+    nrc_grid_adam_kernel<<<ctx->sm_count * 8, 256, 0, s>>>(st->gw, st->gm, st->gv, st->ggrad, st->gema, h);
+    VCR_CUDA(ctx, cudaGetLastError());
+  }
   return VCR_OK;
 }
 
@@ -547,7 +671,7 @@ vcr_status nrc_infer_queries(vcr_ctx* ctx, cudaStream_t s) {
   NrcState* st = ctx->nrc;
   if (use_tc(st)) {
     const NrcView v = nrc_view(ctx);
-    return nrc_infer_tc_launch(ctx, v.wbi, v.b0, v.inv_ext, v.levels, st->query, st->query_count,
+    return nrc_infer_tc_launch(ctx, v.wbi, v.b0, v.inv_ext, v.levels, v.gtab_i, st->query, st->query_count,
                                st->query_capacity, ctx->d_sum, nullptr, s);
   }
   VCR_CUDA(ctx, cudaFuncSetAttribute(nrc_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)infer_smem()));
@@ -781,7 +905,17 @@ extern "C" VCR_API vcr_status vcr_nrc_info(vcr_ctx* ctx, vcr_nrc_info_t* out) {
   out->last_loss = loss;
   out->train_records = std::min(ntrain, st->train_cap);
   out->queries = std::min(nq, st->query_capacity);
-  out->weights = kNrcWeightCount;
+  out->weights = (uint32_t)nrc_param_count(st);
+  return VCR_OK;
+}
+
+// `count` is the network's weight count, or (grid encoding) the full
+// parameter count with the tables after the weights.
+static vcr_status nrc_check_count(vcr_ctx* ctx, size_t count) {
+  const size_t all = nrc_param_count(ctx->nrc);
+  if (count != (size_t)kNrcWeightCount && count != all)
+    return fail(ctx, VCR_ERR_INVALID, "the cache has %d weights (%zu parameters with the grid tables)",
+                kNrcWeightCount, all);
   return VCR_OK;
 }
 
@@ -790,9 +924,12 @@ extern "C" VCR_API vcr_status vcr_nrc_get_weights(vcr_ctx* ctx, float* host, siz
   if (!ctx || !host) return fail(ctx, VCR_ERR_INVALID, "null argument");
   VCR_CUDA(ctx, cudaSetDevice(ctx->device));
   if (!ctx->nrc) return fail(ctx, VCR_ERR_STATE, "no radiance cache");
-  if (count != (size_t)kNrcWeightCount) return fail(ctx, VCR_ERR_INVALID, "the cache has %d weights", kNrcWeightCount);
+  vcr_status cs = nrc_check_count(ctx, count);
+  if (cs) return cs;
   VCR_CUDA(ctx, cudaEventSynchronize(ctx->work_done));
-  VCR_CUDA(ctx, cudaMemcpy(host, ctx->nrc->w, count * 4, cudaMemcpyDeviceToHost));
+  VCR_CUDA(ctx, cudaMemcpy(host, ctx->nrc->w, kNrcWeightCount * 4, cudaMemcpyDeviceToHost));
+  if (count > (size_t)kNrcWeightCount)
+    VCR_CUDA(ctx, cudaMemcpy(host + kNrcWeightCount, ctx->nrc->gw, kNrcGridParams * 4, cudaMemcpyDeviceToHost));
   return VCR_OK;
 }
 
@@ -800,8 +937,15 @@ extern "C" VCR_API vcr_status vcr_nrc_set_weights(vcr_ctx* ctx, const float* hos
   if (!ctx || !host) return fail(ctx, VCR_ERR_INVALID, "null argument");
   VCR_CUDA(ctx, cudaSetDevice(ctx->device));
   if (!ctx->nrc) return fail(ctx, VCR_ERR_STATE, "no radiance cache");
-  if (count != (size_t)kNrcWeightCount) return fail(ctx, VCR_ERR_INVALID, "the cache has %d weights", kNrcWeightCount);
-  VCR_CUDA(ctx, cudaMemcpy(ctx->nrc->w, host, count * 4, cudaMemcpyHostToDevice));
+  vcr_status cs = nrc_check_count(ctx, count);
+  if (cs) return cs;
+  VCR_CUDA(ctx, cudaDeviceSynchronize());
+  VCR_CUDA(ctx, cudaMemcpy(ctx->nrc->w, host, kNrcWeightCount * 4, cudaMemcpyHostToDevice));
+  if (count > (size_t)kNrcWeightCount) {
+    VCR_CUDA(ctx, cudaMemcpy(ctx->nrc->gw, host + kNrcWeightCount, kNrcGridParams * 4, cudaMemcpyHostToDevice));
+    if (ctx->nrc->gema)
+      VCR_CUDA(ctx, cudaMemcpy(ctx->nrc->gema, ctx->nrc->gw, kNrcGridParams * 4, cudaMemcpyDeviceToDevice));
+  }
   nrc_to_bf16_kernel<<<(kNrcWeightCount + 255) / 256, 256>>>(ctx->nrc->w, reinterpret_cast<bf16*>(ctx->nrc->wb));
   VCR_CUDA(ctx, cudaGetLastError());
   if (ctx->nrc->ema) {
@@ -830,8 +974,8 @@ extern "C" VCR_API vcr_status vcr_nrc_forward(vcr_ctx* ctx, const void* d_record
   VCR_CUDA(ctx, cudaMemcpyAsync(d_n, &n, 4, cudaMemcpyHostToDevice, s));
   if (use_tc(ctx->nrc)) {
     const NrcView v = nrc_view(ctx);
-    vs = nrc_infer_tc_launch(ctx, v.wbi, v.b0, v.inv_ext, v.levels, reinterpret_cast<const NrcRecord*>(d_records),
-                             d_n, n, nullptr, d_out, s);
+    vs = nrc_infer_tc_launch(ctx, v.wbi, v.b0, v.inv_ext, v.levels, v.gtab_i,
+                             reinterpret_cast<const NrcRecord*>(d_records), d_n, n, nullptr, d_out, s);
     if (vs) return vs;
   } else {
     VCR_CUDA(ctx, cudaFuncSetAttribute(nrc_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -872,19 +1016,25 @@ extern "C" VCR_API vcr_status vcr_nrc_gradient(vcr_ctx* ctx, const void* d_recor
   if (!ctx) return fail(nullptr, VCR_ERR_INVALID, "null context");
   VCR_CUDA(ctx, cudaSetDevice(ctx->device));
   if (!ctx->nrc) return fail(ctx, VCR_ERR_STATE, "no radiance cache");
-  if (!d_records || !host_grad || count != (size_t)kNrcWeightCount || n == 0)
-    return fail(ctx, VCR_ERR_INVALID, "bad gradient arguments");
+  if (!d_records || !host_grad || n == 0) return fail(ctx, VCR_ERR_INVALID, "bad gradient arguments");
+  vcr_status cs = nrc_check_count(ctx, count);
+  if (cs) return cs;
   if (!ctx->has_cloud) return fail(ctx, VCR_ERR_STATE, "the encoding needs the cloud box (vcr_set_cloud)");
   vcr_status vs = ensure_scratch(ctx, 4);
   if (vs) return vs;
   uint32_t* d_n = reinterpret_cast<uint32_t*>(ctx->d_scratch);
   VCR_CUDA(ctx, cudaMemcpy(d_n, &n, 4, cudaMemcpyHostToDevice));
-  VCR_CUDA(ctx, cudaMemset(ctx->nrc->grad, 0, kNrcWeightCount * 4));
+  NrcState* st = ctx->nrc;
+  VCR_CUDA(ctx, cudaMemset(st->grad, 0, kNrcWeightCount * 4));
+  if (st->ggrad) VCR_CUDA(ctx, cudaMemset(st->ggrad, 0, kNrcGridParams * 4));
   vs = nrc_grad(ctx, reinterpret_cast<const NrcRecord*>(d_records), d_n, n, 0, 0, false);
   if (vs) return vs;
   VCR_CUDA(ctx, cudaDeviceSynchronize());
-  VCR_CUDA(ctx, cudaMemcpy(host_grad, ctx->nrc->grad, count * 4, cudaMemcpyDeviceToHost));
-  if (out_loss) VCR_CUDA(ctx, cudaMemcpy(out_loss, ctx->nrc->loss + 1, 4, cudaMemcpyDeviceToHost));
-  VCR_CUDA(ctx, cudaMemset(ctx->nrc->grad, 0, kNrcWeightCount * 4));
+  VCR_CUDA(ctx, cudaMemcpy(host_grad, st->grad, kNrcWeightCount * 4, cudaMemcpyDeviceToHost));
+  if (count > (size_t)kNrcWeightCount)
+    VCR_CUDA(ctx, cudaMemcpy(host_grad + kNrcWeightCount, st->ggrad, kNrcGridParams * 4, cudaMemcpyDeviceToHost));
+  if (out_loss) VCR_CUDA(ctx, cudaMemcpy(out_loss, st->loss + 1, 4, cudaMemcpyDeviceToHost));
+  VCR_CUDA(ctx, cudaMemset(st->grad, 0, kNrcWeightCount * 4));
+  if (st->ggrad) VCR_CUDA(ctx, cudaMemset(st->ggrad, 0, kNrcGridParams * 4));
   return VCR_OK;
 }

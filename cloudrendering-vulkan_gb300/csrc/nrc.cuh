@@ -59,6 +59,14 @@ struct NrcState {
   float* ema = nullptr;      // exponential moving average of w (ema_decay > 0)
   void* wbi = nullptr;       // BF16 copy of ema used for inference (ema_decay > 0)
   float* loss = nullptr;     // [2]: the running step's loss sum (zeroed by the reduction), the last step's loss
+  // grid encoding (prm.encoding == VCR_NRC_ENCODING_GRID): the tables
+  // [kNrcGridParams], their Adam moments, gradient accumulator and moving
+  // average (ema_decay > 0)
+  float* gw = nullptr;
+  float* gm = nullptr;
+  float* gv = nullptr;
+  float* ggrad = nullptr;
+  float* gema = nullptr;
   NrcRecord* train = nullptr;  // training records [train_cap]
   uint32_t* train_count = nullptr;
   uint32_t train_cap = 0;      // 2 x train_samples x sets: room for the yield's spread
@@ -162,6 +170,88 @@ __host__ __device__ __forceinline__ void nrc_encode(const NrcRecord& r, f3 b0, f
   nrc_encode_directions(r, o + 32);
 }
 
+// Multiresolution grid encoding, the alternative to the frequency encoding
+// (vcr_nrc_params.encoding = VCR_NRC_ENCODING_GRID): level l has N_l =
+// floor(16 * 64^(l/15)) cells per box axis (16 .. 1024) and a table of
+// kNrcGridTable entries of 2 FP32 features, dense when the level's
+// (N_l + 1)^3 vertices fit (levels 0..4) and indexed by the spatial hash
+// x ^ 2654435761 y ^ 805459861 z of the vertex otherwise; the level's two
+// network inputs (where the frequency encoding has its sin and cos) are the
+// trilinear interpolation of its 8 vertices' features at the box position.
+// The tables are parameters trained with the network.
+constexpr int kNrcGridLog2 = 17;
+constexpr uint32_t kNrcGridTable = 1u << kNrcGridLog2;  // entries per level
+constexpr size_t kNrcGridParams = (size_t)kNrcPosLevels * kNrcGridTable * 2;  // 4,194,304 floats
+constexpr float kNrcGridLrScale = 10.0f;  // the tables' Adam step size relative to the network's
+
+__host__ __device__ __forceinline__ int nrc_grid_res(int l) {
+  switch (l) {
+    case 0: return 16;   case 1: return 21;   case 2: return 27;   case 3: return 36;
+    case 4: return 48;   case 5: return 64;   case 6: return 84;   case 7: return 111;
+    case 8: return 147;  case 9: return 194;  case 10: return 256; case 11: return 337;
+    case 12: return 445; case 13: return 588; case 14: return 776; default: return 1024;
+  }
+}
+
+// Table entry of vertex (x, y, z) of a level with n cells per axis.
+__host__ __device__ __forceinline__ uint32_t nrc_grid_index(int n, uint32_t x, uint32_t y, uint32_t z) {
+  const uint32_t v = (uint32_t)n + 1u;
+  if ((uint64_t)v * v * v <= kNrcGridTable) return x + v * (y + v * z);
+  return (x ^ (y * 2654435761u) ^ (z * 805459861u)) & (kNrcGridTable - 1u);
+}
+
+// The level's cell and trilinear fractions at box coordinates (ux, uy, uz)
+// (clamped to the box).
+struct NrcGridCell {
+  uint32_t x, y, z;
+  float fx, fy, fz;
+};
+__host__ __device__ __forceinline__ NrcGridCell nrc_grid_cell(int n, float ux, float uy, float uz) {
+  NrcGridCell c;
+  const float px = fminf(fmaxf(ux, 0.0f), 1.0f) * (float)n;
+  const float py = fminf(fmaxf(uy, 0.0f), 1.0f) * (float)n;
+  const float pz = fminf(fmaxf(uz, 0.0f), 1.0f) * (float)n;
+  c.x = (uint32_t)((int)px < n - 1 ? (int)px : n - 1);
+  c.y = (uint32_t)((int)py < n - 1 ? (int)py : n - 1);
+  c.z = (uint32_t)((int)pz < n - 1 ? (int)pz : n - 1);
+  c.fx = px - (float)c.x;
+  c.fy = py - (float)c.y;
+  c.fz = pz - (float)c.z;
+  return c;
+}
+
+// Weight of corner k (bit 0: +x, bit 1: +y, bit 2: +z) of the cell.
+__host__ __device__ __forceinline__ float nrc_grid_weight(const NrcGridCell& c, int k) {
+  const float wx = (k & 1) ? c.fx : 1.0f - c.fx;
+  const float wy = (k & 2) ? c.fy : 1.0f - c.fy;
+  const float wz = (k & 4) ? c.fz : 1.0f - c.fz;
+  return (wx * wy) * wz;
+}
+
+// The two features of level l at box coordinates (ux, uy, uz) from the
+// tables `tab` (kNrcPosLevels x kNrcGridTable x 2 floats).
+__host__ __device__ __forceinline__ void nrc_grid_level(const float* tab, int l, float ux, float uy, float uz,
+                                                        float* f0, float* f1) {
+  const int n = nrc_grid_res(l);
+  const NrcGridCell c = nrc_grid_cell(n, ux, uy, uz);
+  const float* t = tab + (size_t)l * kNrcGridTable * 2;
+  float a0 = 0.0f, a1 = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const uint32_t idx = nrc_grid_index(n, c.x + (k & 1), c.y + ((k >> 1) & 1), c.z + (k >> 2));
+    const float w = nrc_grid_weight(c, k);
+#if defined(__CUDA_ARCH__)
+    const float2 v = __ldg(reinterpret_cast<const float2*>(t) + idx);
+#else
+    const float2 v = reinterpret_cast<const float2*>(t)[idx];
+#endif
+    a0 = fmaf(w, v.x, a0);
+    a1 = fmaf(w, v.y, a1);
+  }
+  *f0 = a0;
+  *f1 = a1;
+}
+
 // Layer l weights start at this offset; hidden layers are [in][out] = 64x64
 // row-major, the output layer 64 x 16 (columns 3..15 stay zero).
 __host__ __device__ constexpr int nrc_layer_offset(int l) { return l * kNrcWidth * kNrcWidth; }
@@ -170,7 +260,12 @@ __host__ __device__ constexpr int nrc_layer_cols(int l) { return l < kNrcHidden 
 // nrc_tc.cu: the queries' forward on tcgen05 (128-record tiles, TMEM
 // accumulators): reads the *d_count (<= capacity) records, adds
 // throughput x max(y, 0) to sum[pix] and/or writes y to out.
-vcr_status nrc_infer_tc_launch(vcr_ctx* ctx, const void* wbi, f3 b0, f3 inv_ext, int levels, const NrcRecord* recs,
-                               const uint32_t* d_count, uint32_t capacity, double* sum, float* out, cudaStream_t s);
+// Network weights plus, with the grid encoding, the tables.
+size_t nrc_param_count(const NrcState* st);
+
+// `gtab`: the grid encoding's tables (nullptr: the frequency encoding).
+vcr_status nrc_infer_tc_launch(vcr_ctx* ctx, const void* wbi, f3 b0, f3 inv_ext, int levels, const float* gtab,
+                               const NrcRecord* recs, const uint32_t* d_count, uint32_t capacity, double* sum,
+                               float* out, cudaStream_t s);
 
 }  // namespace vcr

@@ -142,8 +142,10 @@ __device__ __forceinline__ void pick4(const float (&v)[16], int t, float& x0, fl
 // are sin / cos of position level l (k-tiles 0, 1), columns 32.. the view
 // SH, 48.. the sun SH (k-tiles 2, 3), as nrc_encode lays them out.
 // `dirs` holds the 16 level directions (nrc_level_dir) as x, y, z triples.
+// `gtab`: the grid encoding's tables (nullptr: the frequency encoding).
 __device__ __forceinline__ void encode_a(const NrcRecord& r, bool valid, f3 b0, f3 inv_ext, const float* dirs, int t,
-                                         int h, uint32_t (&a)[4][4], int levels = kNrcPosLevels) {
+                                         int h, uint32_t (&a)[4][4], int levels = kNrcPosLevels,
+                                         const float* gtab = nullptr) {
   float s[4] = {0.f, 0.f, 0.f, 0.f}, c[4] = {0.f, 0.f, 0.f, 0.f};
   float v0 = 0.f, v1 = 0.f, v2 = 0.f, v3 = 0.f, w0 = 0.f, w1 = 0.f, w2 = 0.f, w3 = 0.f;
   if (valid) {
@@ -152,7 +154,9 @@ __device__ __forceinline__ void encode_a(const NrcRecord& r, bool valid, f3 b0, 
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int l = 4 * j + t;
-      if (l < levels) nrc_encode_level_dir(l, dirs[3 * l], dirs[3 * l + 1], dirs[3 * l + 2], ux, uy, uz, &s[j], &c[j]);
+      if (l >= levels) continue;
+      if (gtab) nrc_grid_level(gtab, l, ux, uy, uz, &s[j], &c[j]);
+      else nrc_encode_level_dir(l, dirs[3 * l], dirs[3 * l + 1], dirs[3 * l + 2], ux, uy, uz, &s[j], &c[j]);
     }
     float sh[16];
     nrc_sh16(r.vx, r.vy, r.vz, sh);

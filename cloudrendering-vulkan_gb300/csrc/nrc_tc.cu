@@ -139,7 +139,7 @@ __device__ __forceinline__ void stage_weights(const bf16* __restrict__ w, unsign
 
 // The 64 inputs of one record (nrc_encode's order) as 8 chunks of 8 BF16.
 __device__ __forceinline__ void encode_row(const NrcRecord& r, bool valid, f3 b0, f3 inv_ext, const float* dirs,
-                                           unsigned char* a, uint32_t row, int levels) {
+                                           unsigned char* a, uint32_t row, int levels, const float* gtab) {
   float ux = 0.f, uy = 0.f, uz = 0.f;
   if (valid) nrc_box_coords(r, b0, inv_ext, ux, uy, uz);
 #pragma unroll
@@ -149,8 +149,10 @@ __device__ __forceinline__ void encode_row(const NrcRecord& r, bool valid, f3 b0
     for (int j = 0; j < 4; ++j) {
       const int l = 4 * c + j;
       float sn = 0.f, cs = 0.f;
-      if (valid && l < levels)
-        nrc_encode_level_dir(l, dirs[3 * l], dirs[3 * l + 1], dirs[3 * l + 2], ux, uy, uz, &sn, &cs);
+      if (valid && l < levels) {
+        if (gtab) nrc_grid_level(gtab, l, ux, uy, uz, &sn, &cs);
+        else nrc_encode_level_dir(l, dirs[3 * l], dirs[3 * l + 1], dirs[3 * l + 2], ux, uy, uz, &sn, &cs);
+      }
       v[j] = pack_bf16(sn, cs);
     }
     *reinterpret_cast<uint4*>(a + sw128(row, (uint32_t)c)) = make_uint4(v[0], v[1], v[2], v[3]);
@@ -180,7 +182,7 @@ __device__ __forceinline__ void group_sync(uint32_t g) {
 }
 
 __global__ void __launch_bounds__(kTcThreads, 2) nrc_infer_tc_kernel(const bf16* __restrict__ wbi, f3 b0, f3 inv_ext,
-                                                                     int levels,
+                                                                     int levels, const float* __restrict__ gtab,
                                                                   const NrcRecord* __restrict__ recs,
                                                                   const uint32_t* __restrict__ count_ptr,
                                                                   uint32_t capacity, double* __restrict__ sum,
@@ -223,7 +225,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) nrc_infer_tc_kernel(const bf16*
     const bool valid = idx < count;
     NrcRecord r{};
     if (valid) r = recs[idx];
-    encode_row(r, valid, b0, inv_ext, dirs, A, row, levels);
+    encode_row(r, valid, b0, inv_ext, dirs, A, row, levels, gtab);
     float y[3] = {0.f, 0.f, 0.f};
 #pragma unroll 1
     for (int l = 0; l < kNrcLayers; ++l) {
@@ -300,8 +302,9 @@ done:
 }  // namespace
 
 // Queries of one pass on the tensor cores; see nrc.cuh.
-vcr_status nrc_infer_tc_launch(vcr_ctx* ctx, const void* wbi, f3 b0, f3 inv_ext, int levels, const NrcRecord* recs,
-                               const uint32_t* d_count, uint32_t capacity, double* sum, float* out, cudaStream_t s) {
+vcr_status nrc_infer_tc_launch(vcr_ctx* ctx, const void* wbi, f3 b0, f3 inv_ext, int levels, const float* gtab,
+                               const NrcRecord* recs, const uint32_t* d_count, uint32_t capacity, double* sum,
+                               float* out, cudaStream_t s) {
   VCR_CUDA(ctx, cudaFuncSetAttribute(nrc_infer_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem));
   int per_sm = 0;
   VCR_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, nrc_infer_tc_kernel, kTcThreads, kTcSmem));
@@ -311,8 +314,8 @@ vcr_status nrc_infer_tc_launch(vcr_ctx* ctx, const void* wbi, f3 b0, f3 inv_ext,
   const uint32_t need = (tiles + kTcGroups - 1) / kTcGroups;
   if (blocks > need) blocks = need;
   if (blocks == 0) return VCR_OK;
-  nrc_infer_tc_kernel<<<blocks, kTcThreads, kTcSmem, s>>>(reinterpret_cast<const bf16*>(wbi), b0, inv_ext, levels, recs,
-                                                          d_count, capacity, sum, out, ctx->d_error);
+  nrc_infer_tc_kernel<<<blocks, kTcThreads, kTcSmem, s>>>(reinterpret_cast<const bf16*>(wbi), b0, inv_ext, levels,
+                                                          gtab, recs, d_count, capacity, sum, out, ctx->d_error);
   VCR_CUDA(ctx, cudaGetLastError());
   return VCR_OK;
 }

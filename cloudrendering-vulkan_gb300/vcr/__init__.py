@@ -253,9 +253,9 @@ class Context:
     NRC_WEIGHTS = 21504
 
     def nrc_setup(self, train_samples=65536, learning_rate=1e-3, query_capacity=1 << 21, seed=1, ema_decay=0.0,
-                  tail_survival=0.0, query_kernel=0, position_levels=16):
+                  tail_survival=0.0, query_kernel=0, position_levels=16, encoding=_abi.NRC_ENCODING_FREQUENCY):
         p = _abi.NrcParams(train_samples, learning_rate, query_capacity, seed, ema_decay, tail_survival, query_kernel,
-                           16 - position_levels)
+                           16 - position_levels, encoding)
         self._ck(lib().vcr_nrc_setup(self.h, C.byref(p)))
 
     def nrc_free(self):
@@ -282,8 +282,10 @@ class Context:
         self._ck(lib().vcr_nrc_info(self.h, C.byref(i)))
         return {f: getattr(i, f) for f, _ in _abi.NrcInfo._fields_}
 
-    def nrc_get_weights(self) -> np.ndarray:
-        w = np.empty(self.NRC_WEIGHTS, np.float32)
+    def nrc_get_weights(self, tables=False) -> np.ndarray:
+        """The network's weights; with tables=True (grid encoding) followed
+        by the encoding's tables (nrc_info()["weights"] values in all)."""
+        w = np.empty(self.nrc_info()["weights"] if tables else self.NRC_WEIGHTS, np.float32)
         self._ck(lib().vcr_nrc_get_weights(self.h, _ptr(w), w.size))
         return w
 
@@ -297,8 +299,8 @@ class Context:
     def nrc_fit(self, d_records, n, steps, stream=0):
         self._ck(lib().vcr_nrc_fit(self.h, C.c_void_p(d_records), n, steps, C.c_void_p(stream)))
 
-    def nrc_gradient(self, d_records, n):
-        g = np.empty(self.NRC_WEIGHTS, np.float32)
+    def nrc_gradient(self, d_records, n, tables=False):
+        g = np.empty(self.nrc_info()["weights"] if tables else self.NRC_WEIGHTS, np.float32)
         loss = C.c_float()
         self._ck(lib().vcr_nrc_gradient(self.h, C.c_void_p(d_records), n, _ptr(g), g.size, C.byref(loss)))
         return g, loss.value

@@ -24,6 +24,7 @@ BUF_IMAGE_MEAN, BUF_IMAGE_SUM, BUF_PATH_STATS, BUF_PPM_STATS, BUF_SHADOW_VOLUME 
 ORDER_RGBA, ORDER_BGRA = range(2)
 PASS_RECORD_STATS, PASS_NO_ACCUMULATE = 1, 2
 NRC_QUERY_DEFAULT, NRC_QUERY_MMA, NRC_QUERY_TCGEN05 = 0, 1, 2
+NRC_ENCODING_FREQUENCY, NRC_ENCODING_GRID = 0, 1
 PPM_GATHER, PPM_MARCH = 0, 1
 
 F3 = C.c_float * 3
@@ -83,7 +84,7 @@ class BatchInfo(C.Structure):
 class NrcParams(C.Structure):
     _fields_ = [("train_samples", C.c_uint32), ("learning_rate", C.c_float), ("query_capacity", C.c_uint32),
                 ("seed", C.c_uint32), ("ema_decay", C.c_float), ("tail_survival", C.c_float),
-                ("query_kernel", C.c_uint32), ("position_drop", C.c_uint32)]
+                ("query_kernel", C.c_uint32), ("position_drop", C.c_uint32), ("encoding", C.c_uint32)]
 
 
 class NrcInfo(C.Structure):

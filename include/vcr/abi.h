@@ -399,7 +399,21 @@ typedef struct vcr_nrc_params {
                               position encoding whose inputs are held at 0
                               (0: all 16 levels, 16: no position input; for
                               measuring what the encoding contributes) */
+  uint32_t encoding;       /* VCR_NRC_ENCODING_*: how the 32 position inputs
+                              are formed */
 } vcr_nrc_params;
+
+/* Position encodings of the cache (the 16 levels' 2 inputs each):
+ * FREQUENCY (default): sin and cos of 2 pi 2^(l/2) d_l . p along a fixed
+ * direction d_l per level.  GRID: a multiresolution grid, level l with
+ * floor(16 * 64^(l/15)) cells per box axis (16 .. 1024) and a table of
+ * 2^17 entries of 2 trainable features (dense for levels 0..4, spatially
+ * hashed above), trilinearly interpolated; the 4,194,304 table values are
+ * parameters after the network's weights (vcr_nrc_get_weights and the
+ * gradient take either the weight count or the full count, which
+ * vcr_nrc_info reports) and take Adam steps 10x the network's size. */
+#define VCR_NRC_ENCODING_FREQUENCY 0u
+#define VCR_NRC_ENCODING_GRID 1u
 
 #define VCR_NRC_QUERY_DEFAULT 0u  /* the library's choice (the faster measured) */
 #define VCR_NRC_QUERY_MMA 1u      /* warp-level mma.sync, 16-record tiles per warp */
@@ -410,7 +424,7 @@ typedef struct vcr_nrc_info_t {
   float last_loss;        /* relative L2 loss of the last step */
   uint32_t train_records; /* training records of the last step */
   uint32_t queries;       /* cache queries of the last pass */
-  uint32_t weights;       /* parameter count */
+  uint32_t weights;       /* parameter count (network weights, then the grid encoding's tables) */
 } vcr_nrc_info_t;
 
 VCR_API vcr_status vcr_nrc_setup(vcr_ctx* ctx, const vcr_nrc_params* p);

@@ -26,6 +26,9 @@ def _lib():
         L.oracle_nrc_forward.argtypes = [P, P, u32, P, P, P]
         L.oracle_nrc_gradient.restype = C.c_double
         L.oracle_nrc_gradient.argtypes = [P, P, u32, P, P, P]
+        L.oracle_nrc_gradient_tables.restype = C.c_double
+        L.oracle_nrc_gradient_tables.argtypes = [P, P, u32, P, P, P, P]
+        L.oracle_nrc_set_grid.argtypes = [P]
         _bound = True
     return L
 
@@ -50,6 +53,34 @@ def set_levels(levels: int) -> None:
     """Position levels the encoding computes (0..16, default 16), as the
     cache's 16 - position_drop; the inputs of the other levels are 0."""
     _lib().oracle_nrc_set_levels(int(levels))
+
+
+GRID_PARAMS = 16 * (1 << 17) * 2
+
+_grid_keep = None
+
+
+def set_grid(tables) -> None:
+    """The grid encoding's tables (16 x 2^17 x 2 floats, as the cache's
+    parameters after its weights), or None for the frequency encoding."""
+    global _grid_keep
+    if tables is None:
+        _grid_keep = None
+        _lib().oracle_nrc_set_grid(None)
+        return
+    _grid_keep = np.ascontiguousarray(tables, np.float32)
+    assert _grid_keep.size == GRID_PARAMS
+    _lib().oracle_nrc_set_grid(_p(_grid_keep))
+
+
+def gradient_tables(weights: np.ndarray, recs: np.ndarray, cloud):
+    """(weight gradient, table gradient, loss) with the grid encoding set."""
+    b0, inv = _box(cloud)
+    g = np.zeros(weight_count(), np.float64)
+    gt = np.zeros(GRID_PARAMS, np.float64)
+    loss = _lib().oracle_nrc_gradient_tables(_p(np.ascontiguousarray(weights, np.float32)), _p(recs), len(recs),
+                                             _p(b0), _p(inv), _p(g), _p(gt))
+    return g, gt, loss
 
 
 def encode(recs: np.ndarray, cloud) -> np.ndarray:

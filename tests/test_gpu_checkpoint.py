@@ -68,27 +68,40 @@ def test_ppm_statistics_resume(cuda, tmp_path):
     np.testing.assert_allclose(resumed, full, rtol=1e-9, atol=1e-12)
 
 
-def test_radiance_cache_training_resumes(cuda, tmp_path):
+@pytest.mark.parametrize("encoding", [vcr.NRC_ENCODING_FREQUENCY, vcr.NRC_ENCODING_GRID])
+def test_radiance_cache_training_resumes(cuda, tmp_path, encoding):
+    """The cache's weights, Adam state and moving average (and, with the
+    grid encoding, its tables' values, moments and average) survive a
+    checkpoint; a cache with the other encoding refuses it."""
     path = str(tmp_path / "nrc.ckpt")
+    grid = encoding == vcr.NRC_ENCODING_GRID
     with vcr.Context() as ctx:
         _scene(ctx, nrc=True)
-        ctx.nrc_setup(train_samples=8192, learning_rate=3e-3, query_capacity=W * H, seed=4, ema_decay=0.9)
+        ctx.nrc_setup(train_samples=8192, learning_rate=3e-3, query_capacity=W * H, seed=4, ema_decay=0.9,
+                      encoding=encoding)
         for k in range(6):
             ctx.nrc_frame(seed=5, pass_index=k)
             if k == 3:
                 ctx.checkpoint_save(path)
         ctx.synchronize()
-        w_full, info_full = ctx.nrc_get_weights(), ctx.nrc_info()
+        w_full, info_full = ctx.nrc_get_weights(tables=grid), ctx.nrc_info()
     with vcr.Context() as ctx:
         _scene(ctx, nrc=True)
-        ctx.nrc_setup(train_samples=8192, learning_rate=3e-3, query_capacity=W * H, seed=99, ema_decay=0.9)
+        ctx.nrc_setup(train_samples=8192, learning_rate=3e-3, query_capacity=W * H, seed=99, ema_decay=0.9,
+                      encoding=encoding)
         ctx.checkpoint_load(path)
         for k in range(4, 6):
             ctx.nrc_frame(seed=5, pass_index=k)
         ctx.synchronize()
-        w_res, info_res = ctx.nrc_get_weights(), ctx.nrc_info()
+        w_res, info_res = ctx.nrc_get_weights(tables=grid), ctx.nrc_info()
+        other = vcr.NRC_ENCODING_FREQUENCY if grid else vcr.NRC_ENCODING_GRID
+        ctx.nrc_setup(train_samples=8192, learning_rate=3e-3, query_capacity=W * H, seed=99, ema_decay=0.9,
+                      encoding=other)
+        with pytest.raises(vcr.VcrError, match="STATE"):
+            ctx.checkpoint_load(path)
     assert info_res["steps"] == info_full["steps"] == 6
     assert info_res["train_records"] == info_full["train_records"]
+    assert info_res["weights"] == w_res.size
     # gradients are flushed with float atomics: the same up to their order
     np.testing.assert_allclose(w_res, w_full, rtol=0, atol=2e-5)
 

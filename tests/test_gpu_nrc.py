@@ -138,6 +138,71 @@ def test_gradient_matches_oracle(cuda, n):
     assert np.all(out[:, 3:] == 0)
 
 
+def _grid_ctx(ctx, desc, cloud, kernel, rng):
+    """A grid-encoded cache with random tables (large enough that the
+    position inputs matter); returns all its parameters."""
+    _ctx_with_cloud(ctx, desc, cloud)
+    ctx.nrc_setup(train_samples=4096, seed=7, query_kernel=kernel, encoding=vcr.NRC_ENCODING_GRID)
+    p = ctx.nrc_get_weights(tables=True)
+    assert p.size == vcr.Context.NRC_WEIGHTS + onrc.GRID_PARAMS
+    assert np.all(np.abs(p[vcr.Context.NRC_WEIGHTS:]) <= 1e-4)  # initial tables
+    p[vcr.Context.NRC_WEIGHTS:] = rng.uniform(-0.5, 0.5, onrc.GRID_PARAMS)
+    ctx.nrc_set_weights(p)
+    return p
+
+
+@pytest.mark.parametrize("kernel", [vcr.NRC_QUERY_MMA, vcr.NRC_QUERY_TCGEN05])
+def test_grid_encoding_forward_matches_oracle(cuda, kernel):
+    """The grid encoding (16 levels of trilinearly interpolated 2-feature
+    tables, dense then hashed) through both query kernels against the
+    oracle's restatement of it."""
+    import torch
+    desc, cloud = _cloud()
+    rng = np.random.default_rng(8)
+    recs = onrc.random_records(900, cloud, rng)
+    with vcr.Context() as ctx:
+        p = _grid_ctx(ctx, desc, cloud, kernel, rng)
+        dr = _dev_records(recs, cuda)
+        out = torch.zeros(3 * len(recs), dtype=torch.float32, device=cuda)
+        ctx.nrc_forward(dr.data_ptr(), len(recs), out.data_ptr())
+        got = out.cpu().numpy().reshape(-1, 3)
+    w = p[:vcr.Context.NRC_WEIGHTS]
+    try:
+        onrc.set_grid(p[vcr.Context.NRC_WEIGHTS:])
+        ref = onrc.forward(w, recs, cloud)
+    finally:
+        onrc.set_grid(None)
+    freq = onrc.forward(w, recs, cloud)
+    scale = np.abs(ref).mean() + 1e-3
+    assert np.abs(got - ref).max() <= 3e-2 * scale, (np.abs(got - ref).max(), scale)
+    assert np.abs(got - ref).mean() <= 3e-3 * scale
+    assert np.abs(freq - ref).mean() > 10 * np.abs(got - ref).mean()  # the tables are what it read
+
+
+def test_grid_encoding_gradient_matches_oracle(cuda):
+    """The fused training kernel's gradient with the grid encoding: the
+    network's weights and the tables (dX_0 = dY_0 W_0^T spread over each
+    level's 8 vertices by float atomics) against the oracle."""
+    desc, cloud = _cloud()
+    rng = np.random.default_rng(9)
+    recs = onrc.random_records(600, cloud, rng)
+    with vcr.Context() as ctx:
+        p = _grid_ctx(ctx, desc, cloud, vcr.NRC_QUERY_MMA, rng)
+        dr = _dev_records(recs, cuda)
+        g, loss = ctx.nrc_gradient(dr.data_ptr(), len(recs), tables=True)
+    try:
+        onrc.set_grid(p[vcr.Context.NRC_WEIGHTS:])
+        gw, gt, lref = onrc.gradient_tables(p[:vcr.Context.NRC_WEIGHTS], recs, cloud)
+    finally:
+        onrc.set_grid(None)
+    assert abs(loss - lref) <= 1e-2 * abs(lref)
+    for got, ref in ((g[:vcr.Context.NRC_WEIGHTS], gw), (g[vcr.Context.NRC_WEIGHTS:], gt)):
+        cos = float(got @ ref / (np.linalg.norm(got) * np.linalg.norm(ref)))
+        rel = float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
+        assert cos > 0.999 and rel < 3e-2, (cos, rel)
+    assert np.array_equal(np.nonzero(g[vcr.Context.NRC_WEIGHTS:])[0], np.nonzero(gt)[0])
+
+
 def _smooth_targets(recs, cloud):
     b0, b1 = np.array(cloud.bounds_min), np.array(cloud.bounds_max)
     x = (recs["p"] - b0) / (b1 - b0)
@@ -145,14 +210,15 @@ def _smooth_targets(recs, cloud):
     recs["w"] = base[:, None] * np.array([1.0, 0.8, 0.6])
 
 
-def test_fit_converges_on_a_deterministic_target(cuda):
+@pytest.mark.parametrize("encoding", [vcr.NRC_ENCODING_FREQUENCY, vcr.NRC_ENCODING_GRID])
+def test_fit_converges_on_a_deterministic_target(cuda, encoding):
     desc, cloud = _cloud()
     rng = np.random.default_rng(4)
     recs = onrc.random_records(8192, cloud, rng)
     _smooth_targets(recs, cloud)
     with vcr.Context() as ctx:
         _ctx_with_cloud(ctx, desc, cloud)
-        ctx.nrc_setup(train_samples=8192, learning_rate=3e-3, seed=5)
+        ctx.nrc_setup(train_samples=8192, learning_rate=3e-3, seed=5, encoding=encoding)
         dr = _dev_records(recs, cuda)
         _, l0 = ctx.nrc_gradient(dr.data_ptr(), len(recs))
         ctx.nrc_fit(dr.data_ptr(), len(recs), 400)

@@ -76,3 +76,66 @@ def test_position_levels_zero_the_finer_levels(levels):
     np.testing.assert_array_equal(e[:, :2 * k], full[:, :2 * k])
     assert not e[:, 2 * k:32].any()
     np.testing.assert_array_equal(e[:, 32:], full[:, 32:])
+
+
+def test_grid_encoding_interpolates_its_tables():
+    """The grid encoding: a position on a vertex of level 0 (16 cells a
+    side, dense) reads that vertex's two features; halfway between two
+    vertices along x it reads their mean; the frequency inputs are gone."""
+    cloud = _cloud()
+    rng = np.random.default_rng(5)
+    tab = rng.uniform(-1, 1, onrc.GRID_PARAMS).astype(np.float32)
+    recs = onrc.random_records(3, cloud, rng)
+    b0, b1 = np.array(cloud.bounds_min), np.array(cloud.bounds_max)
+    on_vertex = np.array([3, 5, 7]) / 16.0
+    recs["p"][0] = b0 + (b1 - b0) * on_vertex
+    recs["p"][1] = b0 + (b1 - b0) * ((np.array([3, 5, 7]) + np.array([0.5, 0, 0])) / 16.0)
+    try:
+        onrc.set_grid(tab)
+        e = onrc.encode(recs, cloud)
+    finally:
+        onrc.set_grid(None)
+    v = 17
+    i0 = 3 + v * (5 + v * 7)
+    np.testing.assert_allclose(e[0, 0:2], tab[2 * i0:2 * i0 + 2], rtol=1e-6, atol=1e-6)
+    i1 = i0 + 1
+    np.testing.assert_allclose(e[1, 0:2], 0.5 * (tab[2 * i0:2 * i0 + 2] + tab[2 * i1:2 * i1 + 2]), rtol=1e-5,
+                               atol=1e-6)
+    assert np.all(np.abs(e[:, :32]) <= 1.0)
+
+
+def test_grid_table_gradient_equals_finite_differences():
+    """With the grid encoding the tables are parameters: the analytic
+    gradient of the touched table entries (dX_0 spread by trilinear
+    weights) equals central differences of the loss (exact mode)."""
+    cloud = _cloud()
+    rng = np.random.default_rng(6)
+    recs = onrc.random_records(12, cloud, rng)
+    w = ((rng.random(onrc.weight_count()) - 0.5) * 0.4).astype(np.float32)
+    w[5 * 64 * 64:].reshape(64, 16)[:, 3:] = 0
+    tab = rng.uniform(-0.5, 0.5, onrc.GRID_PARAMS).astype(np.float32)
+    onrc.set_exact(True)
+    try:
+        onrc.set_grid(tab)
+        g, gt, loss = onrc.gradient_tables(w, recs, cloud)
+        y0 = onrc.forward(w, recs, cloud)  # the loss's (stop-gradient) denominators
+        t = recs["w"].astype(np.float64)
+
+        def loss_at(table):
+            onrc.set_grid(table)
+            y = onrc.forward(w, recs, cloud)
+            return float(np.sum((y - t) ** 2 / (y0 ** 2 + 0.01)) / (3 * len(recs)))
+
+        touched = np.nonzero(gt)[0]
+        assert touched.size > 12 * 8
+        for i in rng.choice(touched, 16, replace=False):
+            h = 1e-3
+            tp, tm = tab.copy(), tab.copy()
+            tp[i] += h
+            tm[i] -= h
+            step = float(tp[i]) - float(tm[i])
+            fd = (loss_at(tp) - loss_at(tm)) / step
+            assert abs(fd - gt[i]) <= 2e-3 * abs(gt[i]) + 1e-9, (i, fd, gt[i])
+    finally:
+        onrc.set_exact(False)
+        onrc.set_grid(None)
