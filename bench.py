@@ -310,7 +310,10 @@ PLAIN_PASSES_PER_LAUNCH = 25  # the plain tracker's error curve: one launch of 2
 CONV = {"ref_samples": 147456, "ref_spp": 16, "plain_max_passes": 30000, "warm_steps": 6000, "warm_sets": 32, "warm_more": 19, "warm_batch": 16384,
         "pool_sets": 32, "pool_every": 96, "max_frames": 8000, "chunk": 500, "spp": 1, "train_samples": 65536,
         "learning_rate": 1e-3, "ema_decay": 0.99, "nrc_events": 2, "repeats": 3, "position_levels": 16,
-        "ablation_levels": [8, 0], "ablation_grid": True, "frame_group": 8}
+        "ablation_levels": [8, 0], "frame_group": 8,
+        # the grid-encoding leg: its best setting of those tried (8 coarse
+        # levels, Adam 3e-3; 16 levels at 1e-3 did not reach 1 % in 8,000 frames)
+        "ablation_grid": {"position_levels": 8, "learning_rate": 3e-3}}
 
 
 class Reference:
@@ -549,8 +552,9 @@ def convergence(ctx, sc, stream, args, overrides=None):
     grid = None
     if cfg.get("ablation_grid"):
         import vcr
-        r = cached_time_to_1pct(ctx, sc, stream, ref, dict(cfg, encoding=vcr.NRC_ENCODING_GRID))
+        r = cached_time_to_1pct(ctx, sc, stream, ref, dict(cfg, encoding=vcr.NRC_ENCODING_GRID, **cfg["ablation_grid"]))
         grid = {k: r[k] for k in ("frames", "time_s", "frame_ms", "warm_s", "relrmse_last", "frames_run", "loss")}
+        grid["settings"] = cfg["ablation_grid"]
     return {"plain": plain, "nrc": nrc, "position_levels_ablation": ablation, "grid_encoding": grid,
             "speedup": round(plain["time_s"] / nrc["time_s"], 2) if (nrc["time_s"] and plain["time_s"]) else None,
             "reference": {"samples_per_pixel": ref.samples, "spp_per_launch": ref.spp,
