@@ -189,7 +189,7 @@ def run_vcr(args):
     if ws > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    sc = _divided(configs.C5_NRC, args.image_div)  # --image-div: a small case for profiler captures
+    sc = _divided(configs.C5_NRC, args.image_div, args.grid_div)  # a small case for profiler captures
     W, H = sc.width, sc.height
     prec = sc.precision
     stream = torch.cuda.Stream()
@@ -278,7 +278,8 @@ def run_vcr(args):
         "config": {"workload": sc.name, "grid": list(sc.size), "precision": "fp16-bricks", "sigma_t_scale": 32,
                    "image": [W, H], "spp_per_step": 1, "max_events": sc.max_events, "tracker": "dda-wavefront",
                    "tuning": tuning,
-                   "l2": "inputs larger than L2 (1 GiB FP16 grid), no flush",
+                   "l2": f"inputs larger than L2 ({int(np.prod(sc.size)) * 2 / 2**30:.2f} GiB FP16 grid, 16x that in "
+                         "corner blocks), no flush",
                    **({"l2_fetch_bytes": args.l2_fetch} if args.l2_fetch else {}),
                    "parallelism": f"replicas{ws}"},
         "gpu_launches": 1,
@@ -705,15 +706,20 @@ def _timed_passes(stream, fn, steps):
     return a.elapsed_time(b) / steps
 
 
-def _divided(sc, div):
-    """The scene with its image sides divided by div (a small case of the
-    same workload, for profiler captures)."""
+def _divided(sc, div, grid_div=1):
+    """The scene with its image sides divided by div and its grid sides by
+    grid_div (the same cloud at a coarser resolution: the box stays the
+    unit-longest-axis box): a small case of the same workload, for profiler
+    captures that must hold a few GB at most."""
     import dataclasses
 
-    if div <= 1:
-        return sc
-    return dataclasses.replace(sc, name=f"{sc.name}/{div}", width=max(1, sc.width // div),
-                               height=max(1, sc.height // div))
+    if div > 1:
+        sc = dataclasses.replace(sc, name=f"{sc.name}/{div}", width=max(1, sc.width // div),
+                                 height=max(1, sc.height // div))
+    if grid_div > 1:
+        sc = dataclasses.replace(sc, name=f"{sc.name}/grid{grid_div}",
+                                 size=tuple(max(8, n // grid_div) for n in sc.size))
+    return sc
 
 
 def run_sort(args):
@@ -886,8 +892,9 @@ def run_nrc_frames(args):
         prm = sc.params(vcr.TRACKER_DDA)
         prm.nrc_events = CONV["nrc_events"]
         ctx.set_params(prm)
+        enc = vcr.NRC_ENCODING_GRID if args.nrc_encoding == "grid" else vcr.NRC_ENCODING_FREQUENCY
         ctx.nrc_setup(train_samples=CONV["train_samples"], learning_rate=CONV["learning_rate"],
-                      query_capacity=sc.width * sc.height, seed=1, ema_decay=CONV["ema_decay"])
+                      query_capacity=sc.width * sc.height, seed=1, ema_decay=CONV["ema_decay"], encoding=enc)
         for k in range(args.warmup):
             ctx.nrc_train_step(seed=400, pass_index=k, stream=sh)
         ms = []
@@ -899,7 +906,8 @@ def run_nrc_frames(args):
             b.synchronize()
             ms.append(a.elapsed_time(b))
         info = ctx.nrc_info()
-    print(json.dumps({"workload": sc.name + " radiance-cached frames", "frames": args.nrc_frames,
+    print(json.dumps({"workload": sc.name + " radiance-cached frames", "encoding": args.nrc_encoding,
+                      "frames": args.nrc_frames,
                       "frame_ms": round(float(np.mean(ms)), 4), "queries": info["queries"],
                       "train_records": info["train_records"]}), flush=True)
 
@@ -1042,6 +1050,8 @@ def main():
     ap.add_argument("--no-convergence", action="store_true", help="skip the time-to-1 %% comparison")
     ap.add_argument("--nrc-frames", type=int, default=0,
                     help="only time this many radiance-cached frames on the scene (a profiling workload)")
+    ap.add_argument("--nrc-encoding", default="frequency", choices=["frequency", "grid"],
+                    help="the cache's position encoding for --nrc-frames")
     ap.add_argument("--batch", action="store_true",
                     help="only measure the batched 64-view configuration (CUDA graph, autotuned)")
     ap.add_argument("--ppm", action="store_true", help="only measure the photon-mapping configuration")
@@ -1050,6 +1060,8 @@ def main():
     ap.add_argument("--sort", action="store_true", help="only measure the radix sort")
     ap.add_argument("--image-div", type=int, default=1,
                     help="divide the image sides (a small case of the workload for profiler captures)")
+    ap.add_argument("--grid-div", type=int, default=1,
+                    help="divide the grid sides (the same cloud, coarser; with --image-div, a small case)")
     ap.add_argument("--l2-fetch", type=int, default=0,
                     help="set this process's maximum L2 fetch granularity in bytes (32/64/128) before the run: "
                          "how DRAM traffic per lookup depends on the L2's fetch size")
