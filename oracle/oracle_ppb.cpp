@@ -12,8 +12,10 @@
 //   refit     : PPB_CalculateAABB.comp (:64-120), upper bounds fixed
 //   gather    : PPB_PE.comp traverseTree (:408-466) / accumulateRadiance
 //               (:362-404) as the beam x beam 1D estimator
-// Per photon, beam and pixel the float operations follow the CUDA kernels
-// in the same order, so results agree bit for bit.
+// The algorithm is the reference's (the lines cited above; departures are
+// named).  Per photon, beam and pixel its evaluation order is written out
+// explicitly and the CUDA kernels keep the same order, so results agree bit
+// for bit.
 #include <algorithm>
 #include <cmath>
 #include <numeric>

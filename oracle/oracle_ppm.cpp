@@ -13,7 +13,10 @@
 //   march    : the reference's estimate instead of the gather (PPM_PE.comp
 //              main :443-546, samplePhotonMap :304-375) with the global
 //              radius of UpdateRadius (RenderTechniquePPM.cpp:302-312)
-// The float and double operations follow the CUDA kernels in order.
+// The algorithm is the reference's (the lines cited above; where it departs,
+// the departure is named).  Its evaluation order is written out explicitly
+// (every fused multiply-add as fma, sums in a stated order), and the CUDA
+// kernels keep that same order, so the two compare bit for bit.
 #include <algorithm>
 #include <cmath>
 #include <numeric>
