@@ -230,6 +230,19 @@ __device__ __forceinline__ void segment_box(float4 A, float4 B, float4& lo, floa
   hi = make_float4(fmaxf(pa.x + e.x, pb.x + e.x), fmaxf(pa.y + e.y, pb.y + e.y), fmaxf(pa.z + e.z, pb.z + e.z), 0.f);
 }
 
+// The segments in leaf order: leaf i holds segment order[i].
+__global__ void ppb_leaf_order_kernel(const uint32_t* __restrict__ order, const float4* __restrict__ seg_a,
+                                      const float4* __restrict__ seg_b, const uint32_t* __restrict__ seg_beam,
+                                      uint32_t n, float4* __restrict__ leaf_a, float4* __restrict__ leaf_b,
+                                      uint32_t* __restrict__ leaf_beam) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint32_t sid = order[i];
+    leaf_a[i] = seg_a[sid];
+    leaf_b[i] = seg_b[sid];
+    leaf_beam[i] = seg_beam[sid];
+  }
+}
+
 // Leaf boxes, then a bottom-up walk: the second child to arrive at a node
 // (atomic counter) computes its box from both children and moves up.
 __global__ void lbvh_refit_kernel(const float4* __restrict__ seg_a, const float4* __restrict__ seg_b,
@@ -267,7 +280,7 @@ __global__ void lbvh_refit_kernel(const float4* __restrict__ seg_a, const float4
 // gather
 // ---------------------------------------------------------------------------
 struct PpbGatherView {
-  const float4* seg_a;
+  const float4* seg_a;     // leaf order (leaf i: segment order[i])
   const float4* seg_b;
   const uint32_t* seg_beam;
   const float* slots;
@@ -293,11 +306,11 @@ __device__ __forceinline__ bool ray_box(f3 o, f3 inv, float t0, float t1, float4
 }
 
 // Beam x beam (1D) estimate of one segment (accumulateRadiance,
-// PPB_PE.comp:362-404, with the fixes named at the top of the file).
+// PPB_PE.comp:362-404, with the fixes named at the top of the file); A, B:
+// its endpoints (with the radius and the offset from the beam origin).
 __device__ __forceinline__ f3 beam_contribution(const GridView& g, const SceneView& s, const PpbGatherView& v,
-                                                uint32_t sid, f3 o, f3 rd, float t_in, float t_out,
-                                                const float* cam_d, uint32_t& lookups) {
-  float4 A = v.seg_a[sid], B = v.seg_b[sid];
+                                                float4 A, float4 B, uint32_t beam, f3 o, f3 rd, float t_in,
+                                                float t_out, const float* cam_d, uint32_t& lookups) {
   f3 pa = mk(A.x, A.y, A.z), pb = mk(B.x, B.y, B.z);
   float r = A.w;
   f3 ax = pb - pa;
@@ -323,7 +336,7 @@ __device__ __forceinline__ f3 beam_contribution(const GridView& g, const SceneVi
   float rho = density_at(g, s, xc);
   ++lookups;
   float sigma_s = (s.albedo * s.k_sigma) * rho;
-  const float* sl = v.slots + (size_t)v.seg_beam[sid] * kSlotFloats;
+  const float* sl = v.slots + (size_t)beam * kSlotFloats;
   float sbeam = sb + B.w;  // distance from the beam origin
   uint32_t cb = 0, cc = 0;
   float tc = t - t_in;
@@ -392,10 +405,13 @@ __global__ void __launch_bounds__(kGatherThreads) ppb_gather_kernel(GridView g, 
     while (true) {
       const bool mine = (active >> lane) & 1u;
       if (node & kLeafBit) {
+        // the leaf's box and its segment (leaf order) in one round of loads
         const uint32_t lf = node & ~kLeafBit;
         const float4 lo = v.leaf_lo[lf], hi = v.leaf_hi[lf];
+        const float4 A = v.seg_a[lf], B = v.seg_b[lf];
+        const uint32_t beam = v.seg_beam[lf];
         if (mine && ray_box(o, inv, t_in, t_out, lo, hi)) {
-          L = L + beam_contribution(g, s, v, v.order[lf], o, rd, t_in, t_out, cam_d, lookups);
+          L = L + beam_contribution(g, s, v, A, B, beam, o, rd, t_in, t_out, cam_d, lookups);
           ++segs;
         }
       } else {
@@ -431,7 +447,7 @@ __global__ void __launch_bounds__(kGatherThreads) ppb_gather_kernel(GridView g, 
 // ---------------------------------------------------------------------------
 static void ppb_release(PpbState* st) {
   void* ptrs[] = {st->slots, st->nbeams, st->slot_segs, st->slot_off, st->photon_segs, st->photon_off, st->scan_sums,
-                  st->total, st->seg_a, st->seg_b, st->seg_beam, st->codes, st->idx, st->codes_sorted,
+                  st->total, st->seg_a, st->seg_b, st->leaf_a, st->leaf_b, st->leaf_beam, st->seg_beam, st->codes, st->idx, st->codes_sorted,
                   st->idx_sorted, st->left, st->right, st->parent_int, st->parent_leaf, st->flags, st->leaf_lo,
                   st->leaf_hi, st->node_lo, st->node_hi};
   for (void* p : ptrs) cudaFree(p);
@@ -476,6 +492,9 @@ vcr_status ppb_setup(vcr_ctx* ctx, const vcr_ppb_params* p) {
   VCR_ALLOC(st->total, 4);
   VCR_ALLOC(st->seg_a, C * sizeof(float4));
   VCR_ALLOC(st->seg_b, C * sizeof(float4));
+  VCR_ALLOC(st->leaf_a, C * sizeof(float4));
+  VCR_ALLOC(st->leaf_b, C * sizeof(float4));
+  VCR_ALLOC(st->leaf_beam, C * 4);
   VCR_ALLOC(st->seg_beam, C * 4);
   VCR_ALLOC(st->codes, C * 4);
   VCR_ALLOC(st->idx, C * 4);
@@ -548,7 +567,12 @@ vcr_status ppb_pass_launch(vcr_ctx* ctx, const vcr_pass_desc* pass, cudaStream_t
                         st->parent_int, st->parent_leaf, st->flags, st->leaf_lo, st->leaf_hi, st->node_lo,
                         st->node_hi, st_);
   if (vs) return vs;
-  PpbGatherView gv{st->seg_a, st->seg_b, st->seg_beam, st->slots, st->idx_sorted, st->left, st->right,
+  if (n) {
+    ppb_leaf_order_kernel<<<ctx->sm_count * 8, 256, 0, st_>>>(st->idx_sorted, st->seg_a, st->seg_b, st->seg_beam, n,
+                                                              st->leaf_a, st->leaf_b, st->leaf_beam);
+    VCR_CUDA(ctx, cudaGetLastError());
+  }
+  PpbGatherView gv{st->leaf_a, st->leaf_b, st->leaf_beam, st->slots, st->idx_sorted, st->left, st->right,
                    st->leaf_lo, st->leaf_hi, st->node_lo, st->node_hi, (int)n, pass->seed, pass->pass_index};
   // one warp per 8x4 pixel tile
   uint32_t tiles = ((pv.cw + 7u) / 8u) * ((pv.ch + 3u) / 4u);

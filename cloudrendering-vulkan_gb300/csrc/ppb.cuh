@@ -27,6 +27,10 @@ struct PpbState {
   uint32_t *nbeams = nullptr, *slot_segs = nullptr, *slot_off = nullptr, *photon_segs = nullptr,
            *photon_off = nullptr, *scan_sums = nullptr, *total = nullptr;
   float4 *seg_a = nullptr, *seg_b = nullptr;
+  // the segments again in the LBVH's leaf (Morton) order, for the gather:
+  // leaf i's segment is at i, loaded together with the leaf's box
+  float4 *leaf_a = nullptr, *leaf_b = nullptr;
+  uint32_t* leaf_beam = nullptr;
   uint32_t *seg_beam = nullptr, *codes = nullptr, *idx = nullptr, *codes_sorted = nullptr, *idx_sorted = nullptr;
   uint32_t *left = nullptr, *right = nullptr, *parent_int = nullptr, *parent_leaf = nullptr, *flags = nullptr;
   float4 *leaf_lo = nullptr, *leaf_hi = nullptr, *node_lo = nullptr, *node_hi = nullptr;
