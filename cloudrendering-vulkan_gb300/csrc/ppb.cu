@@ -250,7 +250,8 @@ __global__ void lbvh_refit_kernel(const float4* __restrict__ seg_a, const float4
                                   const uint32_t* __restrict__ right, const uint32_t* __restrict__ parent_int,
                                   const uint32_t* __restrict__ parent_leaf, uint32_t* __restrict__ flags,
                                   float4* __restrict__ leaf_lo, float4* __restrict__ leaf_hi,
-                                  float4* __restrict__ node_lo, float4* __restrict__ node_hi) {
+                                  float4* __restrict__ node_lo, float4* __restrict__ node_hi,
+                                  float4* __restrict__ node_pk) {
   int g = (int)(blockIdx.x * blockDim.x + threadIdx.x);
   if (g >= n) return;
   uint32_t sid = order[g];
@@ -271,6 +272,12 @@ __global__ void lbvh_refit_kernel(const float4* __restrict__ seg_a, const float4
     float4 bh = (r & kLeafBit) ? __ldcg(leaf_hi + (r & ~kLeafBit)) : __ldcg(node_hi + r);
     node_lo[node] = make_float4(fminf(al.x, bl.x), fminf(al.y, bl.y), fminf(al.z, bl.z), 0.f);
     node_hi[node] = make_float4(fmaxf(ah.x, bh.x), fmaxf(ah.y, bh.y), fmaxf(ah.z, bh.z), 0.f);
+    if (node_pk) {  // box and children together: one 32-byte sector per node for the gathers
+      node_pk[2 * (size_t)node] =
+          make_float4(fminf(al.x, bl.x), fminf(al.y, bl.y), fminf(al.z, bl.z), __uint_as_float(l));
+      node_pk[2 * (size_t)node + 1] =
+          make_float4(fmaxf(ah.x, bh.x), fmaxf(ah.y, bh.y), fmaxf(ah.z, bh.z), __uint_as_float(r));
+    }
     __threadfence();
     node = parent_int[node];
   }
@@ -291,6 +298,7 @@ struct PpbGatherView {
   const float4* leaf_hi;
   const float4* node_lo;
   const float4* node_hi;
+  const float4* node_pk;  // per internal node: (lo, left bits), (hi, right bits)
   int n;
   uint32_t seed, pass;
 };
@@ -415,10 +423,10 @@ __global__ void __launch_bounds__(kGatherThreads) ppb_gather_kernel(GridView g, 
           ++segs;
         }
       } else {
-        const float4 lo = v.node_lo[node], hi = v.node_hi[node];
+        const float4 lo = v.node_pk[2 * (size_t)node], hi = v.node_pk[2 * (size_t)node + 1];
         const uint32_t hit = __ballot_sync(0xffffffffu, mine && ray_box(o, inv, t_in, t_out, lo, hi));
         if (hit) {
-          const uint32_t l = v.left[node], r = v.right[node];
+          const uint32_t l = __float_as_uint(lo.w), r = __float_as_uint(hi.w);
           if (sp < kGatherStack) {  // depth bounded by 64 (30-bit keys + index bits)
             if (lane == 0) stk[sp] = make_uint2(r, hit);
             ++sp;
@@ -446,10 +454,12 @@ __global__ void __launch_bounds__(kGatherThreads) ppb_gather_kernel(GridView g, 
 // host side
 // ---------------------------------------------------------------------------
 static void ppb_release(PpbState* st) {
-  void* ptrs[] = {st->slots, st->nbeams, st->slot_segs, st->slot_off, st->photon_segs, st->photon_off, st->scan_sums,
-                  st->total, st->seg_a, st->seg_b, st->leaf_a, st->leaf_b, st->leaf_beam, st->seg_beam, st->codes, st->idx, st->codes_sorted,
-                  st->idx_sorted, st->left, st->right, st->parent_int, st->parent_leaf, st->flags, st->leaf_lo,
-                  st->leaf_hi, st->node_lo, st->node_hi};
+  void* ptrs[] = {st->slots,      st->nbeams,      st->slot_segs,   st->slot_off,   st->photon_segs,
+                  st->photon_off, st->scan_sums,   st->total,       st->seg_a,      st->seg_b,
+                  st->leaf_a,     st->leaf_b,      st->leaf_beam,   st->node_pk,    st->seg_beam,
+                  st->codes,      st->idx,         st->codes_sorted, st->idx_sorted, st->left,
+                  st->right,      st->parent_int,  st->parent_leaf, st->flags,      st->leaf_lo,
+                  st->leaf_hi,    st->node_lo,     st->node_hi};
   for (void* p : ptrs) cudaFree(p);
   probe_free(st->gather);
 }
@@ -492,6 +502,7 @@ vcr_status ppb_setup(vcr_ctx* ctx, const vcr_ppb_params* p) {
   VCR_ALLOC(st->total, 4);
   VCR_ALLOC(st->seg_a, C * sizeof(float4));
   VCR_ALLOC(st->seg_b, C * sizeof(float4));
+  VCR_ALLOC(st->node_pk, 2 * C * sizeof(float4));
   VCR_ALLOC(st->leaf_a, C * sizeof(float4));
   VCR_ALLOC(st->leaf_b, C * sizeof(float4));
   VCR_ALLOC(st->leaf_beam, C * 4);
@@ -516,7 +527,7 @@ vcr_status ppb_setup(vcr_ctx* ctx, const vcr_ppb_params* p) {
 vcr_status lbvh_build_refit(vcr_ctx* ctx, const uint32_t* codes, const uint32_t* order, const float4* seg_a,
                             const float4* seg_b, int n, uint32_t* left, uint32_t* right, uint32_t* parent_int,
                             uint32_t* parent_leaf, uint32_t* flags, float4* leaf_lo, float4* leaf_hi,
-                            float4* node_lo, float4* node_hi, cudaStream_t st) {
+                            float4* node_lo, float4* node_hi, cudaStream_t st, float4* node_pk) {
   if (n <= 0) return VCR_OK;
   if (n > 1) {
     lbvh_build_kernel<<<(n - 1 + 255) / 256, 256, 0, st>>>(codes, n, left, right, parent_int, parent_leaf);
@@ -524,7 +535,7 @@ vcr_status lbvh_build_refit(vcr_ctx* ctx, const uint32_t* codes, const uint32_t*
     VCR_CUDA(ctx, cudaMemsetAsync(flags, 0, (size_t)(n - 1) * 4, st));
   }
   lbvh_refit_kernel<<<(n + 255) / 256, 256, 0, st>>>(seg_a, seg_b, order, n, left, right, parent_int, parent_leaf,
-                                                     flags, leaf_lo, leaf_hi, node_lo, node_hi);
+                                                     flags, leaf_lo, leaf_hi, node_lo, node_hi, node_pk);
   VCR_CUDA(ctx, cudaGetLastError());
   return VCR_OK;
 }
@@ -565,7 +576,7 @@ vcr_status ppb_pass_launch(vcr_ctx* ctx, const vcr_pass_desc* pass, cudaStream_t
                                    st->idx_sorted, n, 0, 30, st_));
   vs = lbvh_build_refit(ctx, st->codes_sorted, st->idx_sorted, st->seg_a, st->seg_b, (int)n, st->left, st->right,
                         st->parent_int, st->parent_leaf, st->flags, st->leaf_lo, st->leaf_hi, st->node_lo,
-                        st->node_hi, st_);
+                        st->node_hi, st_, st->node_pk);
   if (vs) return vs;
   if (n) {
     ppb_leaf_order_kernel<<<ctx->sm_count * 8, 256, 0, st_>>>(st->idx_sorted, st->seg_a, st->seg_b, st->seg_beam, n,
@@ -573,7 +584,8 @@ vcr_status ppb_pass_launch(vcr_ctx* ctx, const vcr_pass_desc* pass, cudaStream_t
     VCR_CUDA(ctx, cudaGetLastError());
   }
   PpbGatherView gv{st->leaf_a, st->leaf_b, st->leaf_beam, st->slots, st->idx_sorted, st->left, st->right,
-                   st->leaf_lo, st->leaf_hi, st->node_lo, st->node_hi, (int)n, pass->seed, pass->pass_index};
+                   st->leaf_lo, st->leaf_hi, st->node_lo, st->node_hi, st->node_pk, (int)n, pass->seed,
+                   pass->pass_index};
   // one warp per 8x4 pixel tile
   uint32_t tiles = ((pv.cw + 7u) / 8u) * ((pv.ch + 3u) / 4u);
   uint32_t warps_per_block = kGatherThreads / 32;
@@ -686,7 +698,7 @@ extern "C" VCR_API vcr_status vcr_lbvh_build(vcr_ctx* ctx, const uint32_t* d_sor
   vs = lbvh_build_refit(ctx, d_sorted_codes, d_order, reinterpret_cast<const float4*>(d_seg_a),
                         reinterpret_cast<const float4*>(d_seg_b), (int)n, d_left, d_right, pi, pl, fl,
                         reinterpret_cast<float4*>(d_leaf_lo), reinterpret_cast<float4*>(d_leaf_hi),
-                        reinterpret_cast<float4*>(d_node_lo), reinterpret_cast<float4*>(d_node_hi), st);
+                        reinterpret_cast<float4*>(d_node_lo), reinterpret_cast<float4*>(d_node_hi), st, nullptr);
   if (vs) return vs;
   VCR_CUDA(ctx, cudaEventRecord(ctx->work_done, st));
   return VCR_OK;

@@ -34,6 +34,7 @@ struct PpbState {
   uint32_t *seg_beam = nullptr, *codes = nullptr, *idx = nullptr, *codes_sorted = nullptr, *idx_sorted = nullptr;
   uint32_t *left = nullptr, *right = nullptr, *parent_int = nullptr, *parent_leaf = nullptr, *flags = nullptr;
   float4 *leaf_lo = nullptr, *leaf_hi = nullptr, *node_lo = nullptr, *node_hi = nullptr;
+  float4* node_pk = nullptr;  // internal nodes packed for the gather: (lo, left), (hi, right)
   GatherProbe gather;  // segments the last gather evaluated, its device time
 };
 

@@ -33,7 +33,7 @@ namespace vcr {
 vcr_status lbvh_build_refit(vcr_ctx* ctx, const uint32_t* codes, const uint32_t* order, const float4* seg_a,
                             const float4* seg_b, int n, uint32_t* left, uint32_t* right, uint32_t* parent_int,
                             uint32_t* parent_leaf, uint32_t* flags, float4* leaf_lo, float4* leaf_hi,
-                            float4* node_lo, float4* node_hi, cudaStream_t st);
+                            float4* node_lo, float4* node_hi, cudaStream_t st, float4* node_pk);
 
 // Photon box entry and power: the same sun / constant-sky emission as the
 // beams (see ppb.cu).
@@ -142,16 +142,29 @@ __host__ __device__ __forceinline__ double ppm_cbrt_ratio(double r) {
   return y;
 }
 
+// Photon powers and directions in the tree's leaf order: leaf i holds
+// photon order[i].
+__global__ void ppm_leaf_order_kernel(const uint32_t* __restrict__ order, const float4* __restrict__ pw,
+                                      const float4* __restrict__ dir, uint32_t n, float4* __restrict__ leaf_pw,
+                                      float4* __restrict__ leaf_dir) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint32_t ph = order[i];
+    leaf_pw[i] = pw[ph];
+    leaf_dir[i] = dir[ph];
+  }
+}
+
 struct PpmGatherView {
   const float4* pos;
-  const float4* pw;
-  const float4* dir;
+  const float4* pw;       // leaf order (leaf i: photon order[i])
+  const float4* dir;      // leaf order
   const uint32_t* order;  // sorted leaf -> photon
   const uint32_t* left;
   const uint32_t* right;
   const float4* leaf_lo;
   const float4* node_lo;
   const float4* node_hi;
+  const float4* node_pk;  // per internal node: (lo, left bits), (hi, right bits)
   int n;
   double* stats;  // per pixel: N, R, tau rgb, background rgb
   float alpha;
@@ -205,16 +218,18 @@ __global__ void __launch_bounds__(128, 8) ppm_gather_kernel(GridView g, SceneVie
             float4 q = v.leaf_lo[lf];
             f3 dq = mk(q.x, q.y, q.z) - xm;
             if (dot(dq, dq) <= r2) {
-              uint32_t ph = v.order[lf];
-              float4 w = v.dir[ph], pw = v.pw[ph];
+              float4 w = v.dir[lf], pw = v.pw[lf];
               float f = hg_pdf(s.ph, dot(mk(w.x, w.y, w.z), wo));
               phi = phi + mk(pw.x, pw.y, pw.z) * f;
               ++M;
             }
-          } else if (box_dist2(xm, v.node_lo[node], v.node_hi[node]) <= r2) {
-            if (sp < kGatherStack) stack[sp++] = v.right[node];
-            node = v.left[node];
-            continue;
+          } else {
+            const float4 lo = v.node_pk[2 * (size_t)node], hi = v.node_pk[2 * (size_t)node + 1];
+            if (box_dist2(xm, lo, hi) <= r2) {
+              if (sp < kGatherStack) stack[sp++] = __float_as_uint(hi.w);
+              node = __float_as_uint(lo.w);
+              continue;
+            }
           }
           if (sp == 0) break;
           node = stack[--sp];
@@ -282,15 +297,17 @@ __device__ f3 march_photon_map(const PpmGatherView& v, const SceneView& s, f3 x,
       const float4 q = v.leaf_lo[lf];
       const f3 dq = mk(q.x, q.y, q.z) - x;
       if (dot(dq, dq) <= r2) {
-        const uint32_t ph = v.order[lf];
-        const float4 w = v.dir[ph], pw = v.pw[ph];
+        const float4 w = v.dir[lf], pw = v.pw[lf];
         const float f = hg_pdf(s.ph, dot(wo, mk(w.x, w.y, w.z)));
         phi = phi + mk(f * pw.x, f * pw.y, f * pw.z);
       }
-    } else if (box_dist2(x, v.node_lo[node], v.node_hi[node]) <= r2) {
-      if (sp < kGatherStack) stack[sp++] = v.right[node];
-      node = v.left[node];
-      continue;
+    } else {
+      const float4 lo = v.node_pk[2 * (size_t)node], hi = v.node_pk[2 * (size_t)node + 1];
+      if (box_dist2(x, lo, hi) <= r2) {
+        if (sp < kGatherStack) stack[sp++] = __float_as_uint(hi.w);
+        node = __float_as_uint(lo.w);
+        continue;
+      }
     }
     if (sp == 0) break;
     node = stack[--sp];
@@ -378,7 +395,8 @@ void ppm_free(vcr_ctx* ctx) {
   if (!st) return;
   void* ptrs[] = {st->pos, st->pw, st->dir, st->uid, st->count, st->by_uid, st->uid_sorted, st->codes, st->idx,
                   st->codes_sorted, st->order, st->left, st->right, st->parent_int, st->parent_leaf, st->flags,
-                  st->leaf_lo, st->leaf_hi, st->node_lo, st->node_hi, st->stats, st->iota};
+                  st->leaf_lo, st->leaf_hi, st->node_lo, st->node_hi, st->node_pk, st->leaf_pw, st->leaf_dir,
+                  st->stats, st->iota};
   for (void* p : ptrs) cudaFree(p);
   probe_free(st->gather);
   delete st;
@@ -424,6 +442,9 @@ vcr_status ppm_setup(vcr_ctx* ctx, const vcr_ppm_params* p) {
   VCR_ALLOC(st->leaf_hi, C * 16);
   VCR_ALLOC(st->node_lo, C * 16);
   VCR_ALLOC(st->node_hi, C * 16);
+  VCR_ALLOC(st->node_pk, 2 * C * 16);
+  VCR_ALLOC(st->leaf_pw, C * 16);
+  VCR_ALLOC(st->leaf_dir, C * 16);
   VCR_ALLOC(st->iota, C * 4);
   size_t px = (size_t)ctx->width * ctx->height;
   VCR_ALLOC(st->stats, px * 8 * sizeof(double));
@@ -499,9 +520,15 @@ vcr_status ppm_pass_launch(vcr_ctx* ctx, const vcr_pass_desc* pass, cudaStream_t
                                    st->codes_sorted, st->order, n, 0, 30, cs));
   vs = lbvh_build_refit(ctx, st->codes_sorted, st->order, st->pos, st->pos, (int)n, st->left, st->right,
                         st->parent_int, st->parent_leaf, st->flags, st->leaf_lo, st->leaf_hi, st->node_lo,
-                        st->node_hi, cs);
+                        st->node_hi, cs, st->node_pk);
   if (vs) return vs;
-  PpmGatherView gv{st->pos, st->pw, st->dir, st->order, st->left, st->right, st->leaf_lo, st->node_lo, st->node_hi,
+  if (n) {  // powers and directions in leaf order, read with the leaf's position
+    ppm_leaf_order_kernel<<<ctx->sm_count * 8, 256, 0, cs>>>(st->order, st->pw, st->dir, n, st->leaf_pw,
+                                                             st->leaf_dir);
+    VCR_CUDA(ctx, cudaGetLastError());
+  }
+  PpmGatherView gv{st->pos, st->leaf_pw, st->leaf_dir, st->order, st->left, st->right, st->leaf_lo, st->node_lo,
+                   st->node_hi, st->node_pk,
                    (int)n, st->stats, st->prm.alpha, pass->seed, pass->pass_index};
   uint32_t pixels = pv.cw * pv.ch;
   vcr_status ps = probe_begin(ctx, st->gather, cs);

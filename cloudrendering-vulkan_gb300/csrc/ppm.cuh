@@ -19,6 +19,9 @@ struct PpmState {
            *idx = nullptr, *codes_sorted = nullptr, *order = nullptr, *iota = nullptr;
   uint32_t *left = nullptr, *right = nullptr, *parent_int = nullptr, *parent_leaf = nullptr, *flags = nullptr;
   float4 *leaf_lo = nullptr, *leaf_hi = nullptr, *node_lo = nullptr, *node_hi = nullptr;
+  float4* node_pk = nullptr;   // internal nodes packed for the gather: (lo, left), (hi, right)
+  float4* leaf_pw = nullptr;   // photon powers in leaf order
+  float4* leaf_dir = nullptr;  // photon directions in leaf order
   double* stats = nullptr;  // per pixel: N, R, tau rgb, background rgb
   GatherProbe gather;       // photons the last gather tested, its device time
 };
