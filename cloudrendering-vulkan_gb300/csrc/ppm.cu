@@ -509,9 +509,12 @@ vcr_status ppm_pass_launch(vcr_ctx* ctx, const vcr_pass_desc* pass, cudaStream_t
   uint32_t n = std::min(total, C);
   st->photons_stored = n;
   st->dropped = total - n;
-  // deterministic order: by (photon, event) uid, then stable along the Morton curve
+  // deterministic order: by (photon, event) uid, then stable along the Morton
+  // curve; the uid sort covers only the bits a uid of this photon count uses
+  uint32_t uid_bits = 1;
+  while (uid_bits < 32 && (1ull << uid_bits) <= (uint64_t)P * kPpmMaxEvents + kPpmMaxEvents) ++uid_bits;
   VCR_CUDA(ctx, sort_pairs_enqueue(ctx->sm_count, ctx->d_error, ctx->d_scratch, st->uid, st->iota, st->uid_sorted,
-                                   st->by_uid, n, 0, 32, cs));
+                                   st->by_uid, n, 0, uid_bits, cs));
   if (n) {
     ppm_keys_kernel<<<(n + 255) / 256, 256, 0, cs>>>(s, st->pos, st->by_uid, n, st->codes, st->idx);
     VCR_CUDA(ctx, cudaGetLastError());
