@@ -309,9 +309,9 @@ def run_vcr(args):
 PLAIN_PASSES_PER_LAUNCH = 25  # the plain tracker's error curve: one launch of 25 passes per point
 
 CONV = {"ref_samples": 147456, "ref_spp": 16, "plain_max_passes": 30000, "warm_steps": 6000, "warm_sets": 32, "warm_more": 19, "warm_batch": 16384,
-        "pool_sets": 32, "pool_every": 96, "max_frames": 8000, "chunk": 500, "spp": 1, "train_samples": 65536,
+        "pool_sets": 32, "pool_every": 96, "max_frames": 8000, "chunk": 500, "spp": 2, "train_samples": 65536,
         "learning_rate": 1e-3, "ema_decay": 0.99, "nrc_events": 2, "repeats": 3, "position_levels": 16,
-        "ablation_levels": [8, 0], "frame_group": 8,
+        "ablation_levels": [8, 0], "frame_group": 4,
         # the grid-encoding leg: its best setting of those tried (8 coarse
         # levels, Adam 3e-3; 16 levels at 1e-3 did not reach 1 % in 8,000 frames)
         "ablation_grid": {"position_levels": 8, "learning_rate": 3e-3}}
