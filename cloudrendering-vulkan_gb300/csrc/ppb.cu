@@ -243,8 +243,18 @@ __global__ void ppb_leaf_order_kernel(const uint32_t* __restrict__ order, const 
   }
 }
 
+// Arrival counter of the refit: an atomic add with acquire-release
+// semantics at GPU scope, so the box a thread stored before its arrival is
+// visible to the sibling that arrives second, without separate fences.
+__device__ __forceinline__ uint32_t arrive_acq_rel(uint32_t* p) {
+  uint32_t old;
+  asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(old) : "l"(p) : "memory");
+  return old;
+}
+
 // Leaf boxes, then a bottom-up walk: the second child to arrive at a node
-// (atomic counter) computes its box from both children and moves up.
+// (atomic counter) computes its box from both children and moves up; it
+// holds its own child's box and loads only the sibling's.
 __global__ void lbvh_refit_kernel(const float4* __restrict__ seg_a, const float4* __restrict__ seg_b,
                                   const uint32_t* __restrict__ order, int n, const uint32_t* __restrict__ left,
                                   const uint32_t* __restrict__ right, const uint32_t* __restrict__ parent_int,
@@ -260,25 +270,26 @@ __global__ void lbvh_refit_kernel(const float4* __restrict__ seg_a, const float4
   leaf_lo[g] = lo;
   leaf_hi[g] = hi;
   if (n == 1) return;
-  __threadfence();
+  uint32_t me = (uint32_t)g | kLeafBit;  // the child this thread climbs from, and its box (lo, hi)
   uint32_t node = parent_leaf[g];
   for (int guard = 0; node != 0xFFFFFFFFu && guard < 64; ++guard) {
-    if (atomicAdd(flags + node, 1u) == 0u) return;  // first arrival: the sibling finishes this node
-    __threadfence();
-    uint32_t l = left[node], r = right[node];
-    float4 al = (l & kLeafBit) ? __ldcg(leaf_lo + (l & ~kLeafBit)) : __ldcg(node_lo + l);
-    float4 ah = (l & kLeafBit) ? __ldcg(leaf_hi + (l & ~kLeafBit)) : __ldcg(node_hi + l);
-    float4 bl = (r & kLeafBit) ? __ldcg(leaf_lo + (r & ~kLeafBit)) : __ldcg(node_lo + r);
-    float4 bh = (r & kLeafBit) ? __ldcg(leaf_hi + (r & ~kLeafBit)) : __ldcg(node_hi + r);
-    node_lo[node] = make_float4(fminf(al.x, bl.x), fminf(al.y, bl.y), fminf(al.z, bl.z), 0.f);
-    node_hi[node] = make_float4(fmaxf(ah.x, bh.x), fmaxf(ah.y, bh.y), fmaxf(ah.z, bh.z), 0.f);
+    if (arrive_acq_rel(flags + node) == 0u) return;  // first arrival: the sibling finishes this node
+    const uint32_t l = left[node], r = right[node];
+    const bool mine_left = l == me;
+    const uint32_t sib = mine_left ? r : l;
+    const float4 slo = (sib & kLeafBit) ? __ldcg(leaf_lo + (sib & ~kLeafBit)) : __ldcg(node_lo + sib);
+    const float4 shi = (sib & kLeafBit) ? __ldcg(leaf_hi + (sib & ~kLeafBit)) : __ldcg(node_hi + sib);
+    const float4 al = mine_left ? lo : slo, ah = mine_left ? hi : shi;  // left child's box
+    const float4 bl = mine_left ? slo : lo, bh = mine_left ? shi : hi;  // right child's box
+    lo = make_float4(fminf(al.x, bl.x), fminf(al.y, bl.y), fminf(al.z, bl.z), 0.f);
+    hi = make_float4(fmaxf(ah.x, bh.x), fmaxf(ah.y, bh.y), fmaxf(ah.z, bh.z), 0.f);
+    node_lo[node] = lo;
+    node_hi[node] = hi;
     if (node_pk) {  // box and children together: one 32-byte sector per node for the gathers
-      node_pk[2 * (size_t)node] =
-          make_float4(fminf(al.x, bl.x), fminf(al.y, bl.y), fminf(al.z, bl.z), __uint_as_float(l));
-      node_pk[2 * (size_t)node + 1] =
-          make_float4(fmaxf(ah.x, bh.x), fmaxf(ah.y, bh.y), fmaxf(ah.z, bh.z), __uint_as_float(r));
+      node_pk[2 * (size_t)node] = make_float4(lo.x, lo.y, lo.z, __uint_as_float(l));
+      node_pk[2 * (size_t)node + 1] = make_float4(hi.x, hi.y, hi.z, __uint_as_float(r));
     }
-    __threadfence();
+    me = node;
     node = parent_int[node];
   }
 }
