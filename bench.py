@@ -1017,7 +1017,9 @@ def run_reference(args):
     from vcr import configs
     sc = configs.C5_NRC
     os_ = OracleScene(sc)
-    rows = os_.rows_for(6.0)  # each step: one pass over a ~6 s band of rows
+    # each step: one pass over a band of rows, sized so that all steps take
+    # about a minute (at most 6 s, at least 0.5 s a step)
+    rows = os_.rows_for(min(6.0, max(0.5, 60.0 / max(1, args.steps))))
     for k in range(args.warmup):
         os_.pass_rows(max(1, rows // 4), k + 1)
     done = t = 0.0
