@@ -297,19 +297,17 @@ __global__ void lbvh_refit_kernel(const float4* __restrict__ seg_a, const float4
 // ---------------------------------------------------------------------------
 // gather
 // ---------------------------------------------------------------------------
+// What the gather reads: the segments in the LBVH's leaf order (leaf i
+// holds segment order[i]), the leaf boxes, and the internal nodes packed
+// as (low corner, left child bits) (high corner, right child bits).
 struct PpbGatherView {
-  const float4* seg_a;     // leaf order (leaf i: segment order[i])
+  const float4* seg_a;
   const float4* seg_b;
   const uint32_t* seg_beam;
   const float* slots;
-  const uint32_t* order;
-  const uint32_t* left;
-  const uint32_t* right;
   const float4* leaf_lo;
   const float4* leaf_hi;
-  const float4* node_lo;
-  const float4* node_hi;
-  const float4* node_pk;  // per internal node: (lo, left bits), (hi, right bits)
+  const float4* node_pk;
   int n;
   uint32_t seed, pass;
 };
@@ -594,9 +592,8 @@ vcr_status ppb_pass_launch(vcr_ctx* ctx, const vcr_pass_desc* pass, cudaStream_t
                                                               st->leaf_a, st->leaf_b, st->leaf_beam);
     VCR_CUDA(ctx, cudaGetLastError());
   }
-  PpbGatherView gv{st->leaf_a, st->leaf_b, st->leaf_beam, st->slots, st->idx_sorted, st->left, st->right,
-                   st->leaf_lo, st->leaf_hi, st->node_lo, st->node_hi, st->node_pk, (int)n, pass->seed,
-                   pass->pass_index};
+  PpbGatherView gv{st->leaf_a,  st->leaf_b,  st->leaf_beam, st->slots,      st->leaf_lo,
+                   st->leaf_hi, st->node_pk, (int)n,        pass->seed, pass->pass_index};
   // one warp per 8x4 pixel tile
   uint32_t tiles = ((pv.cw + 7u) / 8u) * ((pv.ch + 3u) / 4u);
   uint32_t warps_per_block = kGatherThreads / 32;

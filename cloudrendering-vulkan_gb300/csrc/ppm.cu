@@ -154,17 +154,15 @@ __global__ void ppm_leaf_order_kernel(const uint32_t* __restrict__ order, const 
   }
 }
 
+// What the gather and the march read: photon powers and directions in the
+// tree's leaf order (leaf i holds photon order[i]), the leaf positions, and
+// the internal nodes packed as (low corner, left child bits) (high corner,
+// right child bits).
 struct PpmGatherView {
-  const float4* pos;
-  const float4* pw;       // leaf order (leaf i: photon order[i])
-  const float4* dir;      // leaf order
-  const uint32_t* order;  // sorted leaf -> photon
-  const uint32_t* left;
-  const uint32_t* right;
+  const float4* pw;
+  const float4* dir;
   const float4* leaf_lo;
-  const float4* node_lo;
-  const float4* node_hi;
-  const float4* node_pk;  // per internal node: (lo, left bits), (hi, right bits)
+  const float4* node_pk;
   int n;
   double* stats;  // per pixel: N, R, tau rgb, background rgb
   float alpha;
@@ -530,9 +528,8 @@ vcr_status ppm_pass_launch(vcr_ctx* ctx, const vcr_pass_desc* pass, cudaStream_t
                                                              st->leaf_dir);
     VCR_CUDA(ctx, cudaGetLastError());
   }
-  PpmGatherView gv{st->pos, st->leaf_pw, st->leaf_dir, st->order, st->left, st->right, st->leaf_lo, st->node_lo,
-                   st->node_hi, st->node_pk,
-                   (int)n, st->stats, st->prm.alpha, pass->seed, pass->pass_index};
+  PpmGatherView gv{st->leaf_pw, st->leaf_dir, st->leaf_lo, st->node_pk, (int)n, st->stats, st->prm.alpha, pass->seed,
+                   pass->pass_index};
   uint32_t pixels = pv.cw * pv.ch;
   vcr_status ps = probe_begin(ctx, st->gather, cs);
   if (ps) return ps;
