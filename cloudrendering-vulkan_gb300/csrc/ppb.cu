@@ -298,8 +298,10 @@ __global__ void lbvh_refit_kernel(const float4* __restrict__ seg_a, const float4
 // gather
 // ---------------------------------------------------------------------------
 // What the gather reads: the segments in the LBVH's leaf order (leaf i
-// holds segment order[i]), the leaf boxes, and the internal nodes packed
-// as (low corner, left child bits) (high corner, right child bits).
+// holds segment order[i]), the leaf boxes, and per internal node its own
+// packed node (low corner, left child bits) (high corner, right child bits)
+// followed by its two children's (a child leaf: its box), so that one round
+// of loads covers two levels of the tree.
 struct PpbGatherView {
   const float4* seg_a;
   const float4* seg_b;
@@ -307,10 +309,36 @@ struct PpbGatherView {
   const float* slots;
   const float4* leaf_lo;
   const float4* leaf_hi;
-  const float4* node_pk;
+  const float4* node2;
   int n;
   uint32_t seed, pass;
 };
+
+// Two levels of the LBVH per internal node b: node2[6b..6b+1] = b's packed
+// node, [6b+2..6b+3] and [6b+4..6b+5] = its left and right child's packed
+// node, or the child leaf's box (its leaf id stays in b's child bits).
+__global__ void lbvh_node2_kernel(const float4* __restrict__ node_pk, const float4* __restrict__ leaf_lo,
+                                  const float4* __restrict__ leaf_hi, uint32_t internal,
+                                  float4* __restrict__ node2) {
+  for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < internal; b += gridDim.x * blockDim.x) {
+    const float4 q0 = node_pk[2 * (size_t)b], q1 = node_pk[2 * (size_t)b + 1];
+    float4* o = node2 + 6 * (size_t)b;
+    o[0] = q0;
+    o[1] = q1;
+    const uint32_t ch[2] = {__float_as_uint(q0.w), __float_as_uint(q1.w)};
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      const uint32_t c = ch[k];
+      if (c & kLeafBit) {
+        o[2 + 2 * k] = leaf_lo[c & ~kLeafBit];
+        o[3 + 2 * k] = leaf_hi[c & ~kLeafBit];
+      } else {
+        o[2 + 2 * k] = node_pk[2 * (size_t)c];
+        o[3 + 2 * k] = node_pk[2 * (size_t)c + 1];
+      }
+    }
+  }
+}
 
 // Ray-box overlap of [t0, t1] with the slab interval.
 __device__ __forceinline__ bool ray_box(f3 o, f3 inv, float t0, float t1, float4 lo, float4 hi) {
@@ -373,13 +401,19 @@ __device__ __forceinline__ f3 beam_contribution(const GridView& g, const SceneVi
 // evaluates exactly the nodes and leaves its own single-ray depth-first walk
 // would, in the same order (so its sum is the same); node data are loaded
 // once for the warp (one broadcast transaction instead of one per lane).
+// A visit of internal node b loads b's and its children's boxes together
+// (node2) and tests both levels: the right child's part goes onto the stack
+// first (its leaf, or its two children with the lanes that hit it), then
+// the left child's (its right child), and the walk continues at the left
+// child's left child (or the left leaf) — the binary walk's order.
 constexpr int kGatherThreads = 128;
+constexpr int kGatherStack2 = 128;  // up to 3 entries a visit of two levels (depth <= 64)
 
 __global__ void __launch_bounds__(kGatherThreads) ppb_gather_kernel(GridView g, SceneView s, CamView cam, PassView pv,
                                                                     PpbGatherView v, double* __restrict__ sum,
                                                                     Counters cnt,
                                                                     unsigned long long* __restrict__ evaluated) {
-  __shared__ uint2 s_stack[kGatherThreads / 32][kGatherStack];
+  __shared__ uint2 s_stack[kGatherThreads / 32][kGatherStack2];
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t tiles_x = (pv.cw + 7u) / 8u;
@@ -432,17 +466,45 @@ __global__ void __launch_bounds__(kGatherThreads) ppb_gather_kernel(GridView g, 
           ++segs;
         }
       } else {
-        const float4 lo = v.node_pk[2 * (size_t)node], hi = v.node_pk[2 * (size_t)node + 1];
-        const uint32_t hit = __ballot_sync(0xffffffffu, mine && ray_box(o, inv, t_in, t_out, lo, hi));
+        const float4* q = v.node2 + 6 * (size_t)node;
+        const float4 q0 = q[0], q1 = q[1], q2 = q[2], q3 = q[3], q4 = q[4], q5 = q[5];
+        const uint32_t hit = __ballot_sync(0xffffffffu, mine && ray_box(o, inv, t_in, t_out, q0, q1));
         if (hit) {
-          const uint32_t l = __float_as_uint(lo.w), r = __float_as_uint(hi.w);
-          if (sp < kGatherStack) {  // depth bounded by 64 (30-bit keys + index bits)
-            if (lane == 0) stk[sp] = make_uint2(r, hit);
-            ++sp;
+          const bool hb = (hit >> lane) & 1u;
+          const uint32_t l = __float_as_uint(q0.w), r = __float_as_uint(q1.w);
+          // at most 3 pushes a visit of two levels: below kGatherStack2 for
+          // depth <= 64 (30-bit keys + index bits); the guard only keeps a
+          // deeper tree in bounds
+          if (r & kLeafBit) {
+            if (sp < kGatherStack2) {
+              if (lane == 0) stk[sp] = make_uint2(r, hit);
+              ++sp;
+            }
+          } else {
+            const uint32_t h1 = __ballot_sync(0xffffffffu, hb && ray_box(o, inv, t_in, t_out, q4, q5));
+            if (h1 && sp + 2 <= kGatherStack2) {
+              if (lane == 0) {
+                stk[sp] = make_uint2(__float_as_uint(q5.w), h1);
+                stk[sp + 1] = make_uint2(__float_as_uint(q4.w), h1);
+              }
+              sp += 2;
+            }
           }
-          node = l;
-          active = hit;
-          continue;
+          if (l & kLeafBit) {
+            node = l;
+            active = hit;
+            continue;
+          }
+          const uint32_t h0 = __ballot_sync(0xffffffffu, hb && ray_box(o, inv, t_in, t_out, q2, q3));
+          if (h0) {
+            if (sp < kGatherStack2) {
+              if (lane == 0) stk[sp] = make_uint2(__float_as_uint(q3.w), h0);
+              ++sp;
+            }
+            node = __float_as_uint(q2.w);
+            active = h0;
+            continue;
+          }
         }
       }
       if (sp == 0) break;
@@ -468,7 +530,7 @@ static void ppb_release(PpbState* st) {
                   st->leaf_a,     st->leaf_b,      st->leaf_beam,   st->node_pk,    st->seg_beam,
                   st->codes,      st->idx,         st->codes_sorted, st->idx_sorted, st->left,
                   st->right,      st->parent_int,  st->parent_leaf, st->flags,      st->leaf_lo,
-                  st->leaf_hi,    st->node_lo,     st->node_hi};
+                  st->leaf_hi,    st->node_lo,     st->node_hi,     st->node2};
   for (void* p : ptrs) cudaFree(p);
   probe_free(st->gather);
 }
@@ -512,6 +574,7 @@ vcr_status ppb_setup(vcr_ctx* ctx, const vcr_ppb_params* p) {
   VCR_ALLOC(st->seg_a, C * sizeof(float4));
   VCR_ALLOC(st->seg_b, C * sizeof(float4));
   VCR_ALLOC(st->node_pk, 2 * C * sizeof(float4));
+  VCR_ALLOC(st->node2, 6 * C * sizeof(float4));
   VCR_ALLOC(st->leaf_a, C * sizeof(float4));
   VCR_ALLOC(st->leaf_b, C * sizeof(float4));
   VCR_ALLOC(st->leaf_beam, C * 4);
@@ -592,8 +655,12 @@ vcr_status ppb_pass_launch(vcr_ctx* ctx, const vcr_pass_desc* pass, cudaStream_t
                                                               st->leaf_a, st->leaf_b, st->leaf_beam);
     VCR_CUDA(ctx, cudaGetLastError());
   }
-  PpbGatherView gv{st->leaf_a,  st->leaf_b,  st->leaf_beam, st->slots,      st->leaf_lo,
-                   st->leaf_hi, st->node_pk, (int)n,        pass->seed, pass->pass_index};
+  if (n > 1) {
+    lbvh_node2_kernel<<<ctx->sm_count * 8, 256, 0, st_>>>(st->node_pk, st->leaf_lo, st->leaf_hi, n - 1, st->node2);
+    VCR_CUDA(ctx, cudaGetLastError());
+  }
+  PpbGatherView gv{st->leaf_a,  st->leaf_b, st->leaf_beam, st->slots,      st->leaf_lo,
+                   st->leaf_hi, st->node2, (int)n,        pass->seed, pass->pass_index};
   // one warp per 8x4 pixel tile
   uint32_t tiles = ((pv.cw + 7u) / 8u) * ((pv.ch + 3u) / 4u);
   uint32_t warps_per_block = kGatherThreads / 32;

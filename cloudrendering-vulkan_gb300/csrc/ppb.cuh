@@ -35,6 +35,7 @@ struct PpbState {
   uint32_t *left = nullptr, *right = nullptr, *parent_int = nullptr, *parent_leaf = nullptr, *flags = nullptr;
   float4 *leaf_lo = nullptr, *leaf_hi = nullptr, *node_lo = nullptr, *node_hi = nullptr;
   float4* node_pk = nullptr;  // internal nodes packed for the gather: (lo, left), (hi, right)
+  float4* node2 = nullptr;    // per internal node: its packed node and its two children's (6 float4)
   GatherProbe gather;  // segments the last gather evaluated, its device time
 };
 
