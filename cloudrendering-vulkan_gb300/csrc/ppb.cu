@@ -596,6 +596,15 @@ vcr_status ppb_setup(vcr_ctx* ctx, const vcr_ppb_params* p) {
   return ensure_scratch(ctx, sort_scratch_bytes(p->capacity));
 }
 
+// node2 (two tree levels per internal node, lbvh_node2_kernel) of a refit tree of n leaves.
+vcr_status lbvh_node2(vcr_ctx* ctx, const float4* node_pk, const float4* leaf_lo, const float4* leaf_hi, int n,
+                      float4* node2, cudaStream_t st) {
+  if (n <= 1) return VCR_OK;
+  lbvh_node2_kernel<<<ctx->sm_count * 8, 256, 0, st>>>(node_pk, leaf_lo, leaf_hi, (uint32_t)(n - 1), node2);
+  VCR_CUDA(ctx, cudaGetLastError());
+  return VCR_OK;
+}
+
 vcr_status lbvh_build_refit(vcr_ctx* ctx, const uint32_t* codes, const uint32_t* order, const float4* seg_a,
                             const float4* seg_b, int n, uint32_t* left, uint32_t* right, uint32_t* parent_int,
                             uint32_t* parent_leaf, uint32_t* flags, float4* leaf_lo, float4* leaf_hi,
@@ -655,10 +664,8 @@ vcr_status ppb_pass_launch(vcr_ctx* ctx, const vcr_pass_desc* pass, cudaStream_t
                                                               st->leaf_a, st->leaf_b, st->leaf_beam);
     VCR_CUDA(ctx, cudaGetLastError());
   }
-  if (n > 1) {
-    lbvh_node2_kernel<<<ctx->sm_count * 8, 256, 0, st_>>>(st->node_pk, st->leaf_lo, st->leaf_hi, n - 1, st->node2);
-    VCR_CUDA(ctx, cudaGetLastError());
-  }
+  vs = lbvh_node2(ctx, st->node_pk, st->leaf_lo, st->leaf_hi, (int)n, st->node2, st_);
+  if (vs) return vs;
   PpbGatherView gv{st->leaf_a,  st->leaf_b, st->leaf_beam, st->slots,      st->leaf_lo,
                    st->leaf_hi, st->node2, (int)n,        pass->seed, pass->pass_index};
   // one warp per 8x4 pixel tile
