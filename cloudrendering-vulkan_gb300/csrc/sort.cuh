@@ -9,11 +9,17 @@
 namespace vcr {
 
 constexpr uint32_t kSortTileKeys = 4096;  // keys per tile (256 threads x 16)
+constexpr int kSortDigitBits = 8;         // bits a digit pass sorts on
+constexpr int kSortRadix = 1 << kSortDigitBits;
+constexpr int kSortMaxPasses = 32 / kSortDigitBits;
 
 constexpr size_t sort_round256(size_t b) { return (b + 255) & ~(size_t)255; }
 constexpr size_t sort_tiles(uint32_t n) { return ((size_t)n + kSortTileKeys - 1) / kSortTileKeys; }
-// hist [8][16] + tile counters [8] + look-back words [8][tiles][16]
-constexpr size_t sort_scratch_header_bytes(uint32_t n) { return (8 * 16 + 8 + 8 * sort_tiles(n) * 16) * 4; }
+// hist [4][256] + tile counters [4] + look-back words [4][tiles][256]
+constexpr size_t sort_scratch_header_bytes(uint32_t n) {
+  return ((size_t)kSortMaxPasses * kSortRadix + kSortMaxPasses + (size_t)kSortMaxPasses * sort_tiles(n) * kSortRadix) *
+         4;
+}
 // header + ping-pong copies of keys and values
 constexpr size_t sort_scratch_bytes(uint32_t n) {
   return sort_round256(sort_scratch_header_bytes(n)) + 2 * sort_round256((size_t)n * 4);

@@ -13,7 +13,7 @@
 //
 // Limits and rules:
 //  - at most VCR_SORT_NOALLOC_MAX_KEYS pairs per call (the array is sized
-//    for that many: about 8.5 MB);
+//    for that many: about 9.4 MB);
 //  - all calls share the array, so calls whose work overlaps on the GPU
 //    race with each other; serialise them (one stream, or events);
 //  - the first call on each device looks up the array's device address

@@ -608,7 +608,9 @@ VCR_API vcr_status vcr_lbvh_build(vcr_ctx* ctx, const uint32_t* d_sorted_codes, 
 /* Photon-beam ordering primitives                                          */
 /* ------------------------------------------------------------------------ */
 /* Stable LSD radix sort of (uint32 key, uint32 value) pairs over key bits
- * [begin_bit, end_bit) in 4-bit digits; device pointers, n <= 2^30 - 1.
+ * [begin_bit, end_bit) (8-bit digit passes: the stable order the
+ * reference's 4-bit passes give, in half the passes); device pointers,
+ * n <= 2^30 - 1.
  * d_vals_in == NULL sorts the indices 0..n-1 as values (a permutation).
  * Keys (and values) may be sorted in place.  Scratch comes from the
  * context (about 8 bytes per key).
@@ -623,7 +625,7 @@ VCR_API vcr_status vcr_radix_sort_pairs(vcr_ctx* ctx, const uint32_t* d_keys_in,
  * loop that must not allocate after start-up, a plug-in handed buffers but
  * no allocator).  No counterpart in the reference.  It takes no context and
  * allocates nothing: its working memory is one fixed device array (about
- * 8.5 MB) inside this library, held by every GPU that loads it until the
+ * 9.4 MB) inside this library, held by every GPU that loads it until the
  * process exits.  At most VCR_SORT_NOALLOC_MAX_KEYS pairs per call (larger
  * n returns VCR_ERR_CAPACITY).  Calls share that array: calls that overlap
  * on the GPU race, so serialise them.  The first call on each device looks
