@@ -49,42 +49,69 @@ __device__ __forceinline__ float ppm_box_entry(const SceneView& s, f3 d, Rng& rn
   return at;
 }
 
-// One thread per photon; deposits at every real collision go to a shared
-// buffer through one atomic per warp and round (order fixed later by uid).
+// Persistent photon tracing: a lane takes the next photon (one atomic per
+// warp on the launch's cursor) whenever its photon has ended, so the lanes
+// of a warp whose photons end early keep working while the warp's longest
+// path runs.  Deposits at every real collision go to a shared buffer
+// through one atomic per warp and round (order fixed later by uid; a
+// photon's path, and so every deposit, is the same whichever lane traces
+// it).
+__device__ __forceinline__ void ppm_start_photon(const SceneView& s, uint32_t p, uint32_t photons, uint32_t seed,
+                                                 uint32_t pass, Rng& rng, f3& o, f3& d, f3& power) {
+  rng = rng_pcg(seed ^ kPpmEmitSalt, p, pass);
+  const float inv = 1.0f / ((float)photons * 0.5f);
+  bool sun = rng_next(rng) < 0.5f;
+  if (sun) {
+    d = s.sun;
+  } else {
+    float z = 1.0f - 2.0f * rng_next(rng);
+    float sn, cs;
+    vsincos2pi(rng_next(rng), &sn, &cs);
+    float rr = sqrtf(fmaxf(0.0f, 1.0f - z * z));
+    d = mk(rr * cs, rr * sn, z);
+  }
+  float at = ppm_box_entry(s, d, rng, o);
+  if (sun) {
+    float f = (s.light * at) * inv;
+    power = mk(f, f, f);
+  } else {
+    power = s.sky * (((4.0f * kPI) * at) * inv);
+  }
+}
+
 __global__ void __launch_bounds__(128) ppm_emit_kernel(GridView g, SceneView s, uint32_t photons, uint32_t seed,
                                                        uint32_t pass, uint32_t cap, float4* __restrict__ pos,
                                                        float4* __restrict__ pw, float4* __restrict__ dir,
                                                        uint32_t* __restrict__ uid, uint32_t* __restrict__ count,
                                                        Counters cnt) {
-  uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t lane = threadIdx.x & 31u;
-  bool alive = p < photons;
-  uint32_t lookups = 0, cells = 0, events = 0;
+  bool alive = false, exhausted = false;
+  uint32_t p = 0, events = 0;
+  uint32_t started = 0, lookups = 0, cells = 0, deposits = 0;
   Rng rng{0u, 0u};
   f3 o = mk(0.f, 0.f, 0.f), d = o, power = o;
-  if (alive) {
-    rng = rng_pcg(seed ^ kPpmEmitSalt, p, pass);
-    const float inv = 1.0f / ((float)photons * 0.5f);
-    bool sun = rng_next(rng) < 0.5f;
-    if (sun) {
-      d = s.sun;
-    } else {
-      float z = 1.0f - 2.0f * rng_next(rng);
-      float sn, cs;
-      vsincos2pi(rng_next(rng), &sn, &cs);
-      float rr = sqrtf(fmaxf(0.0f, 1.0f - z * z));
-      d = mk(rr * cs, rr * sn, z);
+  while (true) {
+    const bool need = !alive && !exhausted;
+    const uint32_t want = __ballot_sync(0xffffffffu, need);
+    if (want) {
+      const uint32_t leader = __ffs(want) - 1;
+      uint32_t base = 0;
+      if (lane == leader) base = (uint32_t)atomicAdd(cnt.c + 4, (unsigned long long)__popc(want));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (need) {
+        const uint32_t id = base + __popc(want & ((1u << lane) - 1u));
+        if (id >= photons) {
+          exhausted = true;
+        } else {
+          p = id;
+          events = 0;
+          ++started;
+          ppm_start_photon(s, p, photons, seed, pass, rng, o, d, power);
+          alive = true;
+        }
+      }
     }
-    float at = ppm_box_entry(s, d, rng, o);
-    if (sun) {
-      float f = (s.light * at) * inv;
-      power = mk(f, f, f);
-    } else {
-      power = s.sky * (((4.0f * kPI) * at) * inv);
-    }
-  }
-  // every lane loops until the whole warp is done (warp-aggregated appends)
-  while (__any_sync(0xffffffffu, alive)) {
+    if (__all_sync(0xffffffffu, !alive && exhausted)) break;
     bool dep = false;
     if (alive) {
       float t;
@@ -95,13 +122,14 @@ __global__ void __launch_bounds__(128) ppm_emit_kernel(GridView g, SceneView s, 
         alive = false;
       }
     }
-    uint32_t m = __ballot_sync(0xffffffffu, dep);
+    const uint32_t m = __ballot_sync(0xffffffffu, dep);
     if (m) {
-      uint32_t leader = __ffs(m) - 1, base = 0;
+      const uint32_t leader = __ffs(m) - 1;
+      uint32_t base = 0;
       if (lane == leader) base = atomicAdd(count, (uint32_t)__popc(m));
       base = __shfl_sync(0xffffffffu, base, leader);
       if (dep) {
-        uint32_t slot = base + __popc(m & ((1u << lane) - 1u));
+        const uint32_t slot = base + __popc(m & ((1u << lane) - 1u));
         if (slot < cap) {
           pos[slot] = make_float4(o.x, o.y, o.z, 0.0f);
           pw[slot] = make_float4(power.x, power.y, power.z, 0.0f);
@@ -109,13 +137,14 @@ __global__ void __launch_bounds__(128) ppm_emit_kernel(GridView g, SceneView s, 
           uid[slot] = p * kPpmMaxEvents + events;
         }
         ++events;
+        ++deposits;
         power = power * s.albedo;
         if ((s.max_events && events >= s.max_events) || events >= kPpmMaxEvents) alive = false;
         else d = hg_sample(s.ph, d, rng, true);
       }
     }
   }
-  flush_counters(cnt, p < photons ? 1ull : 0ull, lookups, events, cells);
+  flush_counters(cnt, started, lookups, deposits, cells);
 }
 
 // Morton key of each photon in uid order (order = photons sorted by uid).
@@ -498,8 +527,13 @@ vcr_status ppm_pass_launch(vcr_ctx* ctx, const vcr_pass_desc* pass, cudaStream_t
   Counters cnt{ctx->d_counters};
   VCR_CUDA(ctx, cudaMemsetAsync(ctx->d_counters, 0, 5 * sizeof(unsigned long long), cs));
   VCR_CUDA(ctx, cudaMemsetAsync(st->count, 0, 4, cs));
-  ppm_emit_kernel<<<(P + 127) / 128, 128, 0, cs>>>(g, s, P, pass->seed, pass->pass_index, C, st->pos, st->pw,
-                                                   st->dir, st->uid, st->count, cnt);
+  {  // persistent: as many CTAs as fit, up to one lane a photon
+    int per_sm = 0;
+    VCR_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ppm_emit_kernel, 128, 0));
+    const uint32_t blocks = std::min<uint32_t>((uint32_t)(ctx->sm_count * std::max(per_sm, 1)), (P + 127) / 128);
+    ppm_emit_kernel<<<blocks, 128, 0, cs>>>(g, s, P, pass->seed, pass->pass_index, C, st->pos, st->pw, st->dir,
+                                            st->uid, st->count, cnt);
+  }
   VCR_CUDA(ctx, cudaGetLastError());
   uint32_t total = 0;
   VCR_CUDA(ctx, cudaMemcpyAsync(&total, st->count, 4, cudaMemcpyDeviceToHost, cs));
