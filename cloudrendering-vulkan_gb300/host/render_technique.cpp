@@ -326,7 +326,7 @@ void TechniqueNRC::FreeResources() {
 
 void TechniqueNRC::RecordPass(void* stream, uint32_t passIndex) {
   Require(allocated_, "TechniqueNRC::AllocateResources first");
-  vcr_pass_desc p = PassDesc(passIndex);
+  vcr_pass_desc p = PassDesc(passIndex, std::max(schedule_.spp, 1u));
   if (schedule_.poolSets == 0) {
     Check(vcr_nrc_frame(Context(), &p, stream), Context());
   } else {

@@ -197,6 +197,7 @@ struct NrcSchedule {
   uint32_t poolSets = 0;
   uint32_t poolEvery = 96;
   uint32_t batch = 0;
+  uint32_t spp = 1;  // camera samples per pixel of each pass (the query capacity must cover width x height x spp)
 };
 
 /* The DDA tracker with the learned radiance cache: paths end in the cache
