@@ -61,7 +61,7 @@ def test_sort_permutation_bit_exact(cuda, n, kind):
 @pytest.mark.parametrize("bits", [(0, 30), (4, 12), (0, 4), (28, 32), (3, 13), (5, 6), (0, 31)])
 def test_sort_bit_ranges_and_payload(cuda, bits):
     """Only the bits [begin, end) decide the order, also when the range is
-    not a multiple of the 4-bit digit (the keys' other bits are random)."""
+    not a multiple of the 8-bit digit (the keys' other bits are random)."""
     import torch
     n = 50001
     rng = np.random.default_rng(bits[0])
@@ -81,9 +81,11 @@ def test_sort_bit_ranges_and_payload(cuda, bits):
     np.testing.assert_array_equal(_from_dev(vo), vals[perm])
 
 
-@pytest.mark.parametrize("bits", [(0, 32), (0, 28)])
+@pytest.mark.parametrize("bits", [(0, 32), (0, 28), (0, 24), (0, 8)])
 def test_sort_in_place(cuda, bits):
-    """Even (8) and odd (7) pass counts in place."""
+    """Even (4) and odd (3, 1) pass counts in place, and a last digit
+    narrower than 8 bits (28 bits); keys above 24 bits also carry bits
+    outside the sorted range."""
     n = 70000
     rng = np.random.default_rng(3)
     keys = rng.integers(0, 1 << 28, n).astype(np.uint32)

@@ -72,22 +72,27 @@ def test_noalloc_sort_matches_context_sort_twice(cuda):
                 np.testing.assert_array_equal(out_v[:n].cpu().numpy().view(np.uint32), perm)
 
 
-def test_noalloc_sort_in_place_and_on_a_stream(cuda):
+@pytest.mark.parametrize("end_bit", [28, 24])
+def test_noalloc_sort_in_place_and_on_a_stream(cuda, end_bit):
+    """In place with an even (4) and an odd (3) pass count: the order is the
+    stable argsort of the keys' bits [0, end_bit)."""
     import torch
 
     n = 300001
     keys, _, _ = _case(torch, cuda, n, 21, False, (0, 32))
+    k0 = keys.cpu().numpy().view(np.uint32).copy()
     vals = torch.arange(n, dtype=torch.int32, device=cuda)
     s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())  # the inputs were written on the default stream
     with torch.cuda.stream(s):
-        st = _noalloc(keys.data_ptr(), vals.data_ptr(), keys.data_ptr(), vals.data_ptr(), n, 0, 28,
+        st = _noalloc(keys.data_ptr(), vals.data_ptr(), keys.data_ptr(), vals.data_ptr(), n, 0, end_bit,
                       stream=s.cuda_stream)
         assert st == _abi.OK, vcr.lib().vcr_last_error(None)
         assert _status(s.cuda_stream) == _abi.OK
     s.synchronize()
-    k = keys.cpu().numpy().view(np.uint32)
-    assert np.all(np.diff((k & np.uint32(0x0FFFFFFF)).astype(np.int64)) >= 0)
-    assert len(np.unique(vals.cpu().numpy())) == n
+    perm = np.argsort(k0 & np.uint32((1 << end_bit) - 1), kind="stable").astype(np.uint32)
+    np.testing.assert_array_equal(vals.cpu().numpy().view(np.uint32), perm)
+    np.testing.assert_array_equal(keys.cpu().numpy().view(np.uint32), k0[perm])
 
 
 def test_noalloc_sort_rejects_sizes_beyond_its_scratch(cuda):
