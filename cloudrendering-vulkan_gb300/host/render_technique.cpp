@@ -184,6 +184,16 @@ std::vector<uint8_t> RenderTechnique::ReadDisplay(float exposure, bool bgra) con
   return out;
 }
 
+void RenderTechnique::WriteExr(const std::string& path, bool half) const {
+  std::vector<float> rgb = ReadMean();
+  Check(vcr_write_exr(path.c_str(), width_, height_, rgb.data(), half ? VCR_EXR_HALF : VCR_EXR_FLOAT), nullptr);
+}
+
+void RenderTechnique::WritePng(const std::string& path, float exposure) const {
+  std::vector<uint8_t> rgba = ReadDisplay(exposure, false);
+  Check(vcr_write_png(path.c_str(), width_, height_, rgba.data()), nullptr);
+}
+
 uint32_t RenderTechnique::PassCount() const {
   uint32_t n = 0;
   Check(vcr_pass_count(Context(), &n), Context());

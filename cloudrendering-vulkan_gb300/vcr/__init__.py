@@ -116,6 +116,17 @@ def write_png(path: str, rgba: np.ndarray) -> None:
         f.write(chunk(b"IEND", b""))
 
 
+def write_exr(path: str, rgb: np.ndarray, half: bool = False) -> None:
+    """HDR image [H, W, 3] (float; the mean image) as an uncompressed
+    OpenEXR file with FLOAT or, with half=True, HALF channels
+    (vcr_write_exr)."""
+    img = np.ascontiguousarray(rgb, np.float32)
+    if img.ndim != 3 or img.shape[2] != 3:
+        raise ValueError("write_exr wants an [H, W, 3] float array")
+    h, w = img.shape[:2]
+    check(lib().vcr_write_exr(path.encode(), w, h, _ptr(img), _abi.EXR_HALF if half else _abi.EXR_FLOAT))
+
+
 class Context:
     """One vcr_ctx: owns the device grid, frame sums and scratch."""
 

@@ -26,6 +26,7 @@ PASS_RECORD_STATS, PASS_NO_ACCUMULATE = 1, 2
 NRC_QUERY_DEFAULT, NRC_QUERY_MMA, NRC_QUERY_TCGEN05 = 0, 1, 2
 NRC_ENCODING_FREQUENCY, NRC_ENCODING_GRID = 0, 1
 PPM_GATHER, PPM_MARCH = 0, 1
+EXR_HALF, EXR_FLOAT = 1, 2
 
 F3 = C.c_float * 3
 
@@ -216,6 +217,8 @@ SIGNATURES = {
     "vcr_grid_read_dense": (_S, [_P, _P, _sz]),
     "vcr_pass_count": (_S, [_P, C.POINTER(_u32)]),
     "vcr_image_rel_rmse": (_S, [_P, _P, _P, _P]),
+    "vcr_write_exr": (_S, [C.c_char_p, _u32, _u32, _P, _u32]),
+    "vcr_write_png": (_S, [C.c_char_p, _u32, _u32, _P]),
 }
 
 _lib = None

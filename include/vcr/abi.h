@@ -763,6 +763,22 @@ VCR_API vcr_status vcr_pass_count(vcr_ctx* ctx, uint32_t* out);
  * No reference counterpart (the reference only displays the image). */
 VCR_API vcr_status vcr_image_rel_rmse(vcr_ctx* ctx, const double* d_ref, double* d_out, void* stream);
 
+/* ------------------------------------------------------------------------ */
+/* Image files (host memory, synchronous, no GPU needed)                    */
+/* ------------------------------------------------------------------------ */
+/* Where the reference shows the result in its window, a headless renderer
+ * writes files.  vcr_write_exr: the HDR image (W*H*3 floats, RGB, rows top
+ * to bottom: what vcr_readback(VCR_BUF_IMAGE_MEAN) returns) as an OpenEXR
+ * 2.0 file — single part, scan lines, no compression, channels B, G, R of
+ * pixel type VCR_EXR_HALF (rounded to nearest, ties to even; past 65504 it
+ * is infinity) or VCR_EXR_FLOAT.  vcr_write_png: W*H*4 bytes of 8-bit RGBA
+ * (vcr_display's VCR_ORDER_RGBA output) as a PNG file with stored
+ * (uncompressed) deflate blocks, so that no compression library is needed. */
+typedef enum vcr_exr_type { VCR_EXR_HALF = 1, VCR_EXR_FLOAT = 2 } vcr_exr_type;
+VCR_API vcr_status vcr_write_exr(const char* path, uint32_t width, uint32_t height, const float* rgb,
+                                 uint32_t type);
+VCR_API vcr_status vcr_write_png(const char* path, uint32_t width, uint32_t height, const uint8_t* rgba);
+
 #ifdef __cplusplus
 }
 #endif

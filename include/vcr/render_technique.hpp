@@ -115,6 +115,11 @@ class VCR_API RenderTechnique {
    * the B8G8R8A8_SRGB swapchain): 8-bit sRGB pixels, width * height * 4
    * bytes, R G B A or (bgra) B G R A, alpha 255. */
   std::vector<uint8_t> ReadDisplay(float exposure = 1.0f, bool bgra = false) const;
+  /* The mean image as an OpenEXR file (FLOAT or, with half, HALF channels;
+   * vcr_write_exr) and the display bytes as a PNG file (vcr_write_png):
+   * the headless stand-in for presenting the frame. */
+  void WriteExr(const std::string& path, bool half = false) const;
+  void WritePng(const std::string& path, float exposure = 1.0f) const;
   uint32_t PassCount() const;
   uint32_t Width() const { return width_; }
   uint32_t Height() const { return height_; }

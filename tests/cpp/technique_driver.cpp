@@ -6,7 +6,8 @@
 //   [vcr_params][vcr_camera][vcr_cloud][vcr_grid_desc][u32 w][u32 h]
 //   [u32 passes][f32 pmRadius][f32 mean image w*h*3]
 // to the output file, so a test can re-render the same structs through
-// the C-ABI and compare.
+// the C-ABI and compare.  The PT mode also writes the frame through
+// WriteExr / WritePng next to it.
 //   technique_driver <pt|ppm|ppb|nrc|nrcpool|misuse> <out> [passes]
 #include <cmath>
 #include <cstdio>
@@ -108,6 +109,12 @@ int main(int argc, char** argv) {
     if (tech->PassCount() != (uint32_t)passes || pc.frameCount != (uint32_t)passes + 1u) {
       std::fprintf(stderr, "pass count %u frameCount %u\n", tech->PassCount(), pc.frameCount);
       return 1;
+    }
+    if (mode == "pt") {  // the frame as files: <out>.exr (FLOAT), <out>.half.exr, <out>.png
+      const std::string base = argv[2];
+      tech->WriteExr(base + ".exr");
+      tech->WriteExr(base + ".half.exr", true);
+      tech->WritePng(base + ".png");
     }
     tech->FreeResources();
 

@@ -6,6 +6,7 @@ import ctypes as C
 import os
 import shutil
 import subprocess
+import zlib
 
 import numpy as np
 import pytest
@@ -37,7 +38,8 @@ def test_cpp_layer_compiles_and_links(tmp_path):
     syms = subprocess.run(["nm", "-D", "--defined-only", os.path.join(PKG, "libvcr.so")], capture_output=True,
                           text=True).stdout
     for name in ("TechniquePT", "TechniquePPM", "TechniquePPB", "TechniqueNRC", "RenderTechnique6Commit",
-                 "Renderer5Apply", "Renderer9LoadCloud", "Renderer12SetTechnique"):
+                 "Renderer5Apply", "Renderer9LoadCloud", "Renderer12SetTechnique", "RenderTechnique8WriteExr",
+                 "RenderTechnique8WritePng"):
         assert name in syms
     assert os.path.exists(_build(tmp_path, RENDERER))
 
@@ -85,8 +87,19 @@ def test_technique_pt_equals_the_c_abi_path(cuda, tmp_path):
             ctx.pt_pass(seed=17, pass_index=k)
         ctx.synchronize()
         ref = ctx.image_mean()
+        shown = ctx.display()
     np.testing.assert_array_equal(d["image"], ref)
     assert (ref > 0.1).any()
+    # RenderTechnique::WriteExr / WritePng: the same frame as files
+    from test_image_files import read_exr
+    _, _, _, exr, _ = read_exr(str(tmp_path / "pt.bin.exr"))
+    np.testing.assert_array_equal(exr, ref)
+    _, _, _, half, _ = read_exr(str(tmp_path / "pt.bin.half.exr"))
+    np.testing.assert_array_equal(half, ref.astype(np.float16).astype(np.float64))
+    png = open(tmp_path / "pt.bin.png", "rb").read()
+    idat = png[png.index(b"IDAT") + 4:png.index(b"IEND") - 8]
+    rows = np.frombuffer(zlib.decompress(idat), np.uint8).reshape(h, 1 + 4 * w)
+    np.testing.assert_array_equal(rows[:, 1:].reshape(h, w, 4), shown)
 
 
 @pytest.mark.gpu
