@@ -54,6 +54,7 @@ def lib():
             "oracle_lsd_sort_pairs": (None, [P, P, u32, u32, u32, P, P]),
             "oracle_morton": (None, [P, u32, P, P, u32, P]),
             "oracle_params_set_phase_g": (C.c_int, [C.POINTER(_abi.Params), f]),
+            "oracle_hg": (None, [C.POINTER(_abi.Params), P, u32, P, _abi.F3, u32, u32, P]),
             "oracle_cloud_from_grid": (C.c_int, [C.POINTER(_abi.GridDesc), f, f, C.POINTER(_abi.Cloud)]),
             "oracle_camera_look": (C.c_int, [C.POINTER(_abi.Camera), _abi.F3, _abi.F3, f, f, C.c_int32,
                                              C.c_int32]),
@@ -85,6 +86,19 @@ def scene_structs(sc, tracker=_abi.TRACKER_DDA):
     p = sc.params_fields(tracker)
     assert L.oracle_params_set_phase_g(C.byref(p), sc.g) == 0
     return desc, cloud, cam, p
+
+
+def hg(g: float, cosines, n_samples: int = 0, incoming=(0.0, 0.0, 1.0), seed: int = 1):
+    """The oracle's HG phase function for parameter g (set as
+    Parameters::SetPhaseG sets it): (pdf at `cosines`, `n_samples`
+    directions scattered from `incoming`)."""
+    p = _abi.Params()
+    assert lib().oracle_params_set_phase_g(C.byref(p), g) == 0
+    c = np.ascontiguousarray(cosines, np.float32)
+    pdf = np.empty(len(c), np.float32)
+    dirs = np.empty((max(n_samples, 1), 3), np.float32)
+    lib().oracle_hg(C.byref(p), _p(c), len(c), _p(pdf), _abi.F3(*incoming), seed, n_samples, _p(dirs))
+    return pdf, dirs[:n_samples]
 
 
 def _p(a: np.ndarray):

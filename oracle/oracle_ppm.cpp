@@ -70,6 +70,34 @@ struct PhotonTree {
   std::vector<F4> leaf_lo, leaf_hi, node_lo, node_hi;
 };
 
+// The radius query of samplePhotonMap (PPM_PE.comp:304-375) over the tree:
+// depth first, left child before right, a subtree entered when its box
+// comes within r of x (box_dist2 <= r2), a photon taken when its own
+// squared distance is <= r2; `take` receives each taken leaf (tree order)
+// in walk order, which fixes the order of the caller's sums.
+template <class Take>
+static void tree_query(const PhotonTree& T, V3 x, float r2, Take&& take) {
+  const int n = (int)T.ph.size();
+  if (n <= 0) return;
+  uint32_t stack[64];
+  int sp = 0;
+  uint32_t node = n == 1 ? kLeafBit : 0u;
+  while (true) {
+    if (node & kLeafBit) {
+      uint32_t lf = node & ~kLeafBit;
+      F4 q = T.leaf_lo[lf];
+      V3 dq = sub(v3(q.x, q.y, q.z), x);
+      if (dot(dq, dq) <= r2) take(lf);
+    } else if (box_dist2(x, T.node_lo[node], T.node_hi[node]) <= r2) {
+      if (sp < 64) stack[sp++] = T.right[node];
+      node = T.left[node];
+      continue;
+    }
+    if (sp == 0) break;
+    node = stack[--sp];
+  }
+}
+
 static void emit(const Scene& s, uint32_t P, uint32_t cap, uint32_t seed, uint32_t pass, PhotonTree& T,
                  int threads) {
   std::vector<std::vector<Photon>> per(P);
@@ -178,28 +206,12 @@ static void gather(const Scene& s, const PhotonTree& T, const vcr_camera& cam, u
           float r = (float)st[1];
           float r2 = r * r;
           V3 wo = neg(rd);
-          uint32_t stack[64];
-          int sp = 0;
-          uint32_t node = n == 1 ? kLeafBit : 0u;
-          while (true) {
-            if (node & kLeafBit) {
-              uint32_t lf = node & ~kLeafBit;
-              F4 q = T.leaf_lo[lf];
-              V3 dq = sub(v3(q.x, q.y, q.z), xm);
-              if (dot(dq, dq) <= r2) {
-                const Photon& ph = T.ph[T.order[lf]];
-                float f = hg_pdf(s, dot(v3(ph.dir.x, ph.dir.y, ph.dir.z), wo));
-                phi = add(phi, scale(v3(ph.pw.x, ph.pw.y, ph.pw.z), f));
-                ++M;
-              }
-            } else if (box_dist2(xm, T.node_lo[node], T.node_hi[node]) <= r2) {
-              if (sp < 64) stack[sp++] = T.right[node];
-              node = T.left[node];
-              continue;
-            }
-            if (sp == 0) break;
-            node = stack[--sp];
-          }
+          tree_query(T, xm, r2, [&](uint32_t lf) {
+            const Photon& ph = T.ph[T.order[lf]];
+            float f = hg_pdf(s, dot(v3(ph.dir.x, ph.dir.y, ph.dir.z), wo));
+            phi = add(phi, scale(v3(ph.pw.x, ph.pw.y, ph.pw.z), f));
+            ++M;
+          });
           if (sigma_t > 0.0f) phi = v3(phi.x / sigma_t, phi.y / sigma_t, phi.z / sigma_t);
           else phi = v3(0, 0, 0);
         }
@@ -249,27 +261,11 @@ static V3 photon_map(const Scene& s, const PhotonTree& T, V3 x, V3 wo, float r, 
   int n = (int)T.ph.size();
   if (scatter == 0.0f || n <= 0) return phi;
   const float r2 = r * r;
-  uint32_t stack[64];
-  int sp = 0;
-  uint32_t node = n == 1 ? kLeafBit : 0u;
-  while (true) {
-    if (node & kLeafBit) {
-      uint32_t lf = node & ~kLeafBit;
-      F4 q = T.leaf_lo[lf];
-      V3 dq = sub(v3(q.x, q.y, q.z), x);
-      if (dot(dq, dq) <= r2) {
-        const Photon& ph = T.ph[T.order[lf]];
-        float f = hg_pdf(s, dot(wo, v3(ph.dir.x, ph.dir.y, ph.dir.z)));
-        phi = add(phi, v3(f * ph.pw.x, f * ph.pw.y, f * ph.pw.z));
-      }
-    } else if (box_dist2(x, T.node_lo[node], T.node_hi[node]) <= r2) {
-      if (sp < 64) stack[sp++] = T.right[node];
-      node = T.left[node];
-      continue;
-    }
-    if (sp == 0) break;
-    node = stack[--sp];
-  }
+  tree_query(T, x, r2, [&](uint32_t lf) {
+    const Photon& ph = T.ph[T.order[lf]];
+    float f = hg_pdf(s, dot(wo, v3(ph.dir.x, ph.dir.y, ph.dir.z)));
+    phi = add(phi, v3(f * ph.pw.x, f * ph.pw.y, f * ph.pw.z));
+  });
   if ((phi.x + phi.y) + phi.z <= 0.0f) return v3(0, 0, 0);
   rng.next();  // the reference's unused six-tap density average draws one number
   const float kPI4_3 = kPI * 4.0f / 3.0f;
@@ -399,6 +395,38 @@ int oracle_ppm_march_pass(void* h, int level, const vcr_cloud* cl, const vcr_cam
   }
   if (radius_out) *radius_out = r;
   return 0;
+}
+
+// The photon tree alone: built over n photon positions (xyz floats) in the
+// box [b0, b1] as a pass builds it (30-bit Morton order, radix tree, refit),
+// then, for each of m query points q with radius r, the photons the
+// gather's walk takes: counts[i] and their input indices in hits (walk
+// order, queries one after another, at most cap entries).  Returns the
+// total number taken.
+uint64_t oracle_ppm_tree_query(const float* pos, uint32_t n, const float b0[3], const float b1[3], const float* q,
+                               const float* r, uint32_t m, uint32_t* counts, uint32_t* hits, uint64_t cap) {
+  Scene s{};
+  s.b0 = v3(b0[0], b0[1], b0[2]);
+  s.b1 = v3(b1[0], b1[1], b1[2]);
+  PhotonTree T;
+  T.ph.resize(n);
+  for (uint32_t i = 0; i < n; ++i) {
+    T.ph[i] = Photon{};
+    T.ph[i].pos = F4{pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], 0.0f};
+    T.ph[i].uid = i;
+  }
+  build(s, T);
+  uint64_t total = 0;
+  for (uint32_t i = 0; i < m; ++i) {
+    uint32_t c = 0;
+    tree_query(T, v3(q[3 * i], q[3 * i + 1], q[3 * i + 2]), r[i] * r[i], [&](uint32_t lf) {
+      if (total < cap) hits[total] = T.order[lf];
+      ++total;
+      ++c;
+    });
+    counts[i] = c;
+  }
+  return total;
 }
 
 }  // extern "C"

@@ -26,8 +26,28 @@ def _lib():
         L.oracle_ppm_march_pass.argtypes = [P, C.c_int, C.POINTER(_abi.Cloud), C.POINTER(_abi.Camera),
                                             C.POINTER(_abi.Params), C.POINTER(_abi.ShadowVolume), P, u32, u32, f, f,
                                             f, f, u32, u32, C.POINTER(_abi.PassDesc), P, P, C.POINTER(f), C.c_int]
+        L.oracle_ppm_tree_query.restype = C.c_uint64
+        L.oracle_ppm_tree_query.argtypes = [P, u32, _abi.F3, _abi.F3, P, P, u32, P, P, C.c_uint64]
         _bound = True
     return L
+
+
+def tree_query(positions, bmin, bmax, queries, radii, cap=None):
+    """Photons within each query's radius, found by the gather's walk over
+    the tree a pass builds on `positions`: (counts per query, input indices
+    of the photons taken, queries one after another in walk order)."""
+    L = _lib()
+    pos = np.ascontiguousarray(positions, np.float32).reshape(-1, 3)
+    q = np.ascontiguousarray(queries, np.float32).reshape(-1, 3)
+    r = np.ascontiguousarray(radii, np.float32).reshape(-1)
+    assert len(r) == len(q)
+    counts = np.zeros(max(len(q), 1), np.uint32)
+    cap = cap if cap is not None else max(1, len(pos) * max(len(q), 1))
+    hits = np.zeros(cap, np.uint32)
+    total = L.oracle_ppm_tree_query(_p(pos), len(pos), _abi.F3(*bmin), _abi.F3(*bmax), _p(q), _p(r), len(q),
+                                    _p(counts), _p(hits), cap)
+    assert total <= cap
+    return counts[:len(q)], hits[:total]
 
 
 def init_stats(width, height, r0):

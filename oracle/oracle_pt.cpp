@@ -569,6 +569,28 @@ void oracle_grid_decoded(void* h, float* out) {
   std::copy(g->tex.begin(), g->tex.end(), out);
 }
 
+// The phase function alone (hg_pdf / hg_sample above, as the tracker calls
+// them): its density at n cosines, and m directions scattered from `in`,
+// sample i drawn from the stream rng_pcg(seed, i, 0).
+void oracle_hg(const vcr_params* p, const float* cosines, uint32_t n, float* pdf, const float in[3], uint32_t seed,
+               uint32_t m, float* dirs) {
+  Scene s{};
+  s.g_ = p->phase_g;
+  s.opg2 = p->phase_one_plus_g2;
+  s.omg2 = p->phase_one_minus_g2;
+  s.o2g = p->phase_one_over_2g;
+  s.iso = p->isotropic != 0;
+  for (uint32_t i = 0; i < n; ++i) pdf[i] = hg_pdf(s, cosines[i]);
+  const V3 d = v3(in[0], in[1], in[2]);
+  for (uint32_t i = 0; i < m; ++i) {
+    Rng rng = rng_pcg(seed, i, 0u);
+    V3 o = hg_sample(s, d, rng, true);
+    dirs[3 * i] = o.x;
+    dirs[3 * i + 1] = o.y;
+    dirs[3 * i + 2] = o.z;
+  }
+}
+
 void oracle_grid_sample(void* h, const vcr_cloud* cl, const float* pos, uint32_t n, float* out) {
   vcr_params p{};
   Scene s = make_scene(static_cast<Grid*>(h), *cl, p, nullptr, 0, nullptr);
