@@ -275,7 +275,8 @@ def run_vcr(args):
         "warmup": args.warmup, "ms_per_step": round(ms_total / args.steps, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 (fp16 texels, fp64 accumulation)",
         "data": "synthetic: seeded 8-octave Perlin fBm cloud generated on the device",
-        "config": {"workload": sc.name, "grid": list(sc.size), "precision": "fp16-bricks", "sigma_t_scale": 32,
+        "config": {"workload": sc.name, "scene_hash": sc.digest(), "grid": list(sc.size), "precision": "fp16-bricks",
+                   "sigma_t_scale": 32,
                    "image": [W, H], "spp_per_step": 1, "max_events": sc.max_events, "tracker": "dda-wavefront",
                    "tuning": tuning,
                    "l2": f"inputs larger than L2 ({int(np.prod(sc.size)) * 2 / 2**30:.2f} GiB FP16 grid, 16x that in "
@@ -1039,8 +1040,8 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32 (fp16 texels decoded, fp64 accumulation)", "data": "synthetic",
-            "config": {"workload": sc.name, "grid": list(sc.size), "image": [sc.width, sc.height],
-                       "tracker": "dda (CPU port)"},
+            "config": {"workload": sc.name, "scene_hash": sc.digest(), "grid": list(sc.size),
+                       "image": [sc.width, sc.height], "tracker": "dda (CPU port)"},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": cpu["cores"], "kind": "port",
                              "sample": cpu["sample"]},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}

@@ -46,6 +46,16 @@ class Scene:
     seed: int = 1
     extra: dict = field(default_factory=dict)
 
+    def digest(self) -> str:
+        """The first 16 hex digits of the SHA-256 of the scene's fields as
+        canonical JSON: the same configuration hashes the same in every
+        output that names it (pure Python; loads no library)."""
+        import hashlib
+        import json
+        from dataclasses import asdict
+        blob = json.dumps(asdict(self), sort_keys=True, separators=(",", ":"))
+        return hashlib.sha256(blob.encode()).hexdigest()[:16]
+
     def grid_desc(self):
         n = max(self.size)
         return grid_desc(self.size, (1.0 / n,) * 3)

@@ -26,3 +26,15 @@ def test_c4_cameras_look_at_the_cloud():
         n = math.sqrt(sum(c * c for c in to_centre))
         assert sum(f * c / n for f, c in zip(fwd, to_centre)) > 0.999
         assert cam.half_width * 2 in (w, w - 1, w + 1)
+
+
+def test_scene_digest_names_the_configuration():
+    import dataclasses
+    digests = {sc.digest() for sc in configs.ALL}
+    assert len(digests) == len(configs.ALL)
+    sc = configs.C5_NRC
+    d = sc.digest()
+    assert len(d) == 16 and int(d, 16) >= 0
+    assert dataclasses.replace(sc).digest() == d
+    assert dataclasses.replace(sc, seed=sc.seed + 1).digest() != d
+    assert dataclasses.replace(sc, g=0.5).digest() != d
