@@ -101,24 +101,48 @@ def measured_peaks():
 
 
 class Clocks:
-    """nvidia-smi sampling during the timed region."""
+    """nvidia-smi sampling of the timed region.  The sampler starts before
+    the region and the constructor waits (at most `ready_s`) for its first
+    row, so that the tool's start-up does not eat a short region; `mark()`
+    at the region's start drops the rows written before it, and `stop()`
+    after the region keeps the rows since the mark (waiting up to 0.25 s for
+    one, when the region was shorter than the sampling interval)."""
 
-    def __init__(self, index: int):
-        fd, self.path = tempfile.mkstemp(prefix="vcr_clocks_", suffix=".csv")
-        os.close(fd)
-        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int, interval_ms: int = 20, ready_s: float = 5.0):
+        fd, self.path = tempfile.mkstemp(prefix="vcr_clocks_", suffix=".csv")
+        os.close(fd)
+        self.skip = 0
         try:
             self.f = open(self.path, "w")
-            self.p = subprocess.Popen(["nvidia-smi", f"--id={index}", f"--query-gpu={q}", "--format=csv,noheader,nounits",
-                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={index}", f"--query-gpu={self.QUERY}",
+                                       "--format=csv,noheader,nounits", "-lms", str(interval_ms)],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
         except Exception:
             self.p = None
+            return
+        t_end = time.time() + ready_s
+        while self.p.poll() is None and time.time() < t_end and self._rows() == 0:
+            time.sleep(0.005)
+
+    def _rows(self) -> int:
+        """Complete rows written so far."""
+        with open(self.path) as r:
+            return r.read().count("\n")
+
+    def mark(self):
+        if self.p:
+            self.skip = self._rows()
 
     def stop(self):
         if not self.p:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        t_end = time.time() + 0.25
+        while self.p.poll() is None and time.time() < t_end and self._rows() <= self.skip:
+            time.sleep(0.005)
         self.p.terminate()
         try:
             self.p.wait(timeout=5)
@@ -127,7 +151,9 @@ class Clocks:
         self.f.close()
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in open(self.path):
+        with open(self.path) as r:
+            rows = r.read().split("\n")[self.skip:]
+        for line in rows:
             parts = [x.strip() for x in line.split(",")]
             if len(parts) < 9:
                 continue
@@ -216,6 +242,7 @@ def run_vcr(args):
         clk = Clocks(local)
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         barrier()
+        clk.mark()
         ev0.record(stream)
         ctx.pt_passes(seed=seed, first=args.warmup, count=args.steps, stream=sh)
         ev1.record(stream)
@@ -593,6 +620,7 @@ def run_batch(args):
         torch.cuda.synchronize()
         clk = Clocks(0)
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        clk.mark()
         a.record(stream)
         ctx.batch_graph_replay(args.steps, stream=sh)
         b.record(stream)
