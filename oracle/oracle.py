@@ -265,6 +265,8 @@ def _ppb_lib():
                                       C.POINTER(_PpbOut), C.c_int]
         L.oracle_lbvh.restype = None
         L.oracle_lbvh.argtypes = [P, P, P, P, u32, P, P, P, P, P, P]
+        L.oracle_ppb_walk.restype = C.c_uint64
+        L.oracle_ppb_walk.argtypes = [P, P, P, P, P, P, u32, P, P, P, u32, P, P, C.c_uint64]
         L._ppb_bound = True
     return L
 
@@ -286,6 +288,37 @@ def lbvh(sorted_codes, order, seg_a, seg_b):
     _ppb_lib().oracle_lbvh(_p(sc), _p(od), _p(a), _p(b), n, _p(left), _p(right), _p(nlo), _p(nhi), _p(llo), _p(lhi))
     k = max(n - 1, 0)
     return dict(left=left[:k], right=right[:k], node_lo=nlo[:k], node_hi=nhi[:k], leaf_lo=llo, leaf_hi=lhi)
+
+
+def ppb_walk(tree, origins, dirs, t01, cap=None):
+    """The beam gather's walk over a tree from `lbvh` for each ray (origin,
+    direction, [t0, t1]): (counts per ray, leaf indices visited, rays one
+    after another in walk order)."""
+    L = _ppb_lib()
+    n = len(tree["leaf_lo"])
+    k = max(n - 1, 1)
+
+    def arr(key, shape, dt):
+        a = np.zeros(shape, dt)
+        v = np.asarray(tree[key], dt)
+        a[:len(v)] = v
+        return a
+
+    left, right = arr("left", k, np.uint32), arr("right", k, np.uint32)
+    nlo, nhi = arr("node_lo", (k, 4), np.float32), arr("node_hi", (k, 4), np.float32)
+    llo = np.ascontiguousarray(tree["leaf_lo"], np.float32).reshape(-1, 4)
+    lhi = np.ascontiguousarray(tree["leaf_hi"], np.float32).reshape(-1, 4)
+    o = np.ascontiguousarray(origins, np.float32).reshape(-1, 3)
+    d = np.ascontiguousarray(dirs, np.float32).reshape(-1, 3)
+    t = np.ascontiguousarray(t01, np.float32).reshape(-1, 2)
+    m = len(o)
+    counts = np.zeros(max(m, 1), np.uint32)
+    cap = cap if cap is not None else max(1, n * max(m, 1))
+    hits = np.zeros(cap, np.uint32)
+    total = L.oracle_ppb_walk(_p(left), _p(right), _p(nlo), _p(nhi), _p(llo), _p(lhi), n, _p(o), _p(d), _p(t), m,
+                              _p(counts), _p(hits), cap)
+    assert total <= cap
+    return counts[:m], hits[:total]
 
 
 def ppb_pass(grid, cloud, cam, params, photons, capacity, r0, alpha, width, height, seed=0, pass_index=0,

@@ -149,6 +149,32 @@ struct Beams {
   std::vector<F4> leaf_lo, leaf_hi, node_lo, node_hi;
 };
 
+// The gather's walk over the beam tree (PPB_PE.comp:408-466 visits every
+// beam whose box the camera ray crosses): depth first, left child before
+// right, a subtree entered when the ray's [t_in, t_out] crosses its box
+// (ray_box), `visit` called with each leaf (tree order) whose own box the
+// ray crosses, in walk order, which fixes the order of the caller's sums.
+template <class Visit>
+static void beam_walk(const Beams& B, V3 o, V3 inv, float t_in, float t_out, Visit&& visit) {
+  const int n = (int)B.n;
+  if (n <= 0) return;
+  uint32_t stack[64];
+  int sp = 0;
+  uint32_t node = n == 1 ? (0u | kLeafBit) : 0u;
+  while (true) {
+    if (node & kLeafBit) {
+      uint32_t lf = node & ~kLeafBit;
+      if (ray_box(o, inv, t_in, t_out, B.leaf_lo[lf], B.leaf_hi[lf])) visit(lf);
+    } else if (ray_box(o, inv, t_in, t_out, B.node_lo[node], B.node_hi[node])) {
+      if (sp < 64) stack[sp++] = B.right[node];
+      node = B.left[node];
+      continue;
+    }
+    if (sp == 0) break;
+    node = stack[--sp];
+  }
+}
+
 static V3 beam_contribution(const Scene& s, const Beams& B, uint32_t sid, V3 o, V3 rd, float t_in, float t_out,
                             const float* cam_d, Counts& c) {
   F4 A = B.seg_a[sid], Bq = B.seg_b[sid];
@@ -343,22 +369,9 @@ static void gather(const Scene& s, const Beams& B, const vcr_camera& cam, uint32
         L = scale(sky(s, rd), (float)cexit * (1.0f / kBeamDists));
         if (n > 0) {
           V3 inv = v3(1.0f / rd.x, 1.0f / rd.y, 1.0f / rd.z);
-          uint32_t stack[64];
-          int sp = 0;
-          uint32_t node = n == 1 ? (0u | kLeafBit) : 0u;
-          while (true) {
-            if (node & kLeafBit) {
-              uint32_t lf = node & ~kLeafBit;
-              if (ray_box(o, inv, t_in, t_out, B.leaf_lo[lf], B.leaf_hi[lf]))
-                L = add(L, beam_contribution(s, B, B.order[lf], o, rd, t_in, t_out, cam_d, c));
-            } else if (ray_box(o, inv, t_in, t_out, B.node_lo[node], B.node_hi[node])) {
-              if (sp < 64) stack[sp++] = B.right[node];
-              node = B.left[node];
-              continue;
-            }
-            if (sp == 0) break;
-            node = stack[--sp];
-          }
+          beam_walk(B, o, inv, t_in, t_out, [&](uint32_t lf) {
+            L = add(L, beam_contribution(s, B, B.order[lf], o, rd, t_in, t_out, cam_d, c));
+          });
         }
       }
       double* out = sum + 3 * (size_t)pix;
@@ -430,6 +443,38 @@ int oracle_ppb_pass(void* h, int level, const vcr_cloud* cl, const vcr_camera* c
     }
   }
   return 0;
+}
+
+// The gather's walk alone over a given tree (left / right children, node
+// and leaf boxes as float4, n leaves): for each of m rays (origin,
+// direction, [t0, t1]) the leaves it visits, counts[i] and the leaf indices
+// in hits (walk order, rays one after another, at most cap entries).
+// Returns the total.
+uint64_t oracle_ppb_walk(const uint32_t* left, const uint32_t* right, const float* node_lo, const float* node_hi,
+                         const float* leaf_lo, const float* leaf_hi, uint32_t n, const float* ro, const float* rdir,
+                         const float* t01, uint32_t m, uint32_t* counts, uint32_t* hits, uint64_t cap) {
+  Beams B;
+  B.n = n;
+  const size_t ni = n > 1 ? n - 1 : 0;
+  B.left.assign(left, left + ni);
+  B.right.assign(right, right + ni);
+  B.node_lo.assign(reinterpret_cast<const F4*>(node_lo), reinterpret_cast<const F4*>(node_lo) + ni);
+  B.node_hi.assign(reinterpret_cast<const F4*>(node_hi), reinterpret_cast<const F4*>(node_hi) + ni);
+  B.leaf_lo.assign(reinterpret_cast<const F4*>(leaf_lo), reinterpret_cast<const F4*>(leaf_lo) + n);
+  B.leaf_hi.assign(reinterpret_cast<const F4*>(leaf_hi), reinterpret_cast<const F4*>(leaf_hi) + n);
+  uint64_t total = 0;
+  for (uint32_t i = 0; i < m; ++i) {
+    const V3 o = v3(ro[3 * i], ro[3 * i + 1], ro[3 * i + 2]), d = v3(rdir[3 * i], rdir[3 * i + 1], rdir[3 * i + 2]);
+    const V3 inv = v3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
+    uint32_t c = 0;
+    beam_walk(B, o, inv, t01[2 * i], t01[2 * i + 1], [&](uint32_t lf) {
+      if (total < cap) hits[total] = lf;
+      ++total;
+      ++c;
+    });
+    counts[i] = c;
+  }
+  return total;
 }
 
 // LBVH + refit over given sorted keys / segments (for the primitive test).
