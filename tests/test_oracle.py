@@ -54,20 +54,31 @@ def test_fbm_oracle_equals_product_host_generator():
 
 
 def test_grid_majorant_bounds_every_trilinear_sample():
+    """Every pyramid level: no trilinear sample inside a cell exceeds the
+    cell's majorant, also right at and next to the cell faces (where the
+    footprint reaches into the neighbouring bricks)."""
     size = (20, 17, 12)
     dense = orc.fbm_fill(size, seed=3, octaves=4)
     for prec in (0, 1, 2):
         g = orc.Grid(dense, prec)
-        maj = g.majorants()
         cloud = vcr.cloud_from_grid(vcr.grid_desc(size, (1 / 20,) * 3), 1.0, 8.0)
         b0 = np.array(cloud.bounds_min, np.float32)
         b1 = np.array(cloud.bounds_max, np.float32)
-        pts = (b0 + (b1 - b0) * np.random.default_rng(prec).random((20000, 3))).astype(np.float32)
+        rng = np.random.default_rng(prec)
+        pts = (b0 + (b1 - b0) * rng.random((20000, 3))).astype(np.float32)
+        brick = (b1 - b0) / np.array(size) * 8
+        faces = np.round((pts[:6000] - b0) / brick) * brick + b0  # on brick faces (all levels' faces are among them)
+        faces += rng.choice([-1e-6, 0.0, 1e-6], faces.shape) * (b1 - b0)
+        pts = np.concatenate([pts, np.clip(faces, b0, b1).astype(np.float32)])
         vals = g.sample(cloud, pts)
-        cells = np.minimum(((pts - b0) / ((b1 - b0) / np.array(size) * 8)).astype(int), np.array(g.nb) - 1)
-        lin = cells[:, 0] + g.nb[0] * (cells[:, 1] + g.nb[1] * cells[:, 2])
-        assert np.all(vals <= maj[lin]), prec
-        assert g.max_density() == maj.max()
+        for level in range(4):
+            maj = g.majorants(level)
+            dims = np.array(g.level_dims(level))
+            cells = np.minimum(np.floor((pts - b0) / (brick * (1 << level))).astype(int), dims - 1)
+            cells = np.maximum(cells, 0)
+            lin = cells[:, 0] + dims[0] * (cells[:, 1] + dims[1] * cells[:, 2])
+            assert np.all(vals <= maj[lin]), (prec, level)
+            assert g.max_density() == maj.max(), (prec, level)
 
 
 def _small_scene(tracker, size=(32, 32, 32), ds=8.0):
