@@ -139,3 +139,41 @@ def test_grid_table_gradient_equals_finite_differences():
     finally:
         onrc.set_exact(False)
         onrc.set_grid(None)
+
+
+def _bf16(x):
+    """float64 -> float32 -> BF16 (round to nearest, ties to even) -> float64."""
+    u = np.asarray(x, np.float64).astype(np.float32).view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) >> 16
+    return (u.astype(np.uint32) << 16).view(np.float32).astype(np.float64)
+
+
+@pytest.mark.parametrize("exact", [True, False])
+def test_forward_is_the_documented_network(exact):
+    """64 encoded inputs -> five 64-wide ReLU layers -> 3 outputs; weights
+    stored row-major by input (layer l at l * 64 * 64; the output layer 64 x
+    16, its first 3 columns used); weights and activations rounded to BF16
+    (not in the exact mode); sums in float64 over the inputs in order.
+    Restated here in numpy: the same numbers, bit for bit."""
+    cloud = _cloud()
+    rng = np.random.default_rng(11)
+    recs = onrc.random_records(40, cloud, rng)
+    w = ((rng.random(onrc.weight_count()) - 0.5) * 0.5).astype(np.float32)
+    rnd = (lambda v: np.asarray(v, np.float64)) if exact else _bf16
+    onrc.set_exact(exact)
+    try:
+        got = onrc.forward(w, recs, cloud)
+        x = rnd(onrc.encode(recs, cloud).astype(np.float64))
+    finally:
+        onrc.set_exact(False)
+    wb = rnd(w.astype(np.float64))
+    h = x
+    for layer in range(6):
+        cols = 64 if layer < 5 else 16
+        m = wb[layer * 64 * 64: layer * 64 * 64 + 64 * cols].reshape(64, cols)
+        z = np.zeros((len(h), cols))
+        for i in range(64):  # the oracle's summation order
+            z = z + h[:, i:i + 1] * m[i]
+        h = rnd(np.maximum(z, 0.0)) if layer < 5 else z
+    np.testing.assert_array_equal(got, h[:, :3])
+    assert np.abs(got).max() > 0
