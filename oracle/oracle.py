@@ -55,6 +55,15 @@ def lib():
             "oracle_morton": (None, [P, u32, P, P, u32, P]),
             "oracle_params_set_phase_g": (C.c_int, [C.POINTER(_abi.Params), f]),
             "oracle_hg": (None, [C.POINTER(_abi.Params), P, u32, P, _abi.F3, u32, u32, P]),
+            "oracle_sky_gradient": (None, [P, P]),
+            "oracle_slab": (C.c_int, [P, P, P, P, C.POINTER(f), C.POINTER(f)]),
+            "oracle_onb": (None, [P, P, P]),
+            "oracle_camera_ray": (None, [C.POINTER(_abi.Camera), C.c_int, C.c_int, P, P]),
+            "oracle_xorshift_init": (u32, [u32]),
+            "oracle_xorshift_numbers": (u32, [u32, u32, P]),
+            "oracle_hg_sample_xorshift": (None, [C.POINTER(_abi.Params), P, C.POINTER(u32), P]),
+            "oracle_find_scatter_global": (C.c_int, [P, C.POINTER(_abi.Cloud), P, P, C.POINTER(u32)]),
+            "oracle_sv_lookup": (f, [P, C.POINTER(_abi.Cloud), C.POINTER(_abi.ShadowVolume), P, P]),
             "oracle_cloud_from_grid": (C.c_int, [C.POINTER(_abi.GridDesc), f, f, C.POINTER(_abi.Cloud)]),
             "oracle_camera_look": (C.c_int, [C.POINTER(_abi.Camera), _abi.F3, _abi.F3, f, f, C.c_int32,
                                              C.c_int32]),

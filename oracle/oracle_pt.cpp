@@ -569,6 +569,78 @@ void oracle_grid_decoded(void* h, float* out) {
   std::copy(g->tex.begin(), g->tex.end(), out);
 }
 
+// ---- single functions, for checks against the reference's shader code run
+// on the CPU (oracle/ref_shaders.cpp) ----------------------------------------
+void oracle_sky_gradient(const float dir[3], float out[3]) {
+  V3 c = sky_gradient(v3(dir[0], dir[1], dir[2]));
+  out[0] = c.x; out[1] = c.y; out[2] = c.z;
+}
+
+int oracle_slab(const float b0[3], const float b1[3], const float pos[3], const float dir[3], float* tmin,
+                float* tmax) {
+  return slab(v3(pos[0], pos[1], pos[2]), v3(dir[0], dir[1], dir[2]), v3(b0[0], b0[1], b0[2]), v3(b1[0], b1[1], b1[2]),
+              *tmin, *tmax) ? 1 : 0;
+}
+
+void oracle_onb(const float n[3], float xp[3], float yp[3]) {
+  V3 a, b;
+  onb(v3(n[0], n[1], n[2]), a, b);
+  xp[0] = a.x; xp[1] = a.y; xp[2] = a.z;
+  yp[0] = b.x; yp[1] = b.y; yp[2] = b.z;
+}
+
+void oracle_camera_ray(const vcr_camera* cam, int x, int y, float pos[3], float dir[3]) {
+  V3 p, d;
+  camera_ray(*cam, x, y, p, d);
+  pos[0] = p.x; pos[1] = p.y; pos[2] = p.z;
+  dir[0] = d.x; dir[1] = d.y; dir[2] = d.z;
+}
+
+// The reference-parity RNG: the state after initializeRandom(seed), and n
+// numbers from a state (returning the state after them).
+uint32_t oracle_xorshift_init(uint32_t seed) { return rng_xorshift(seed).s; }
+uint32_t oracle_xorshift_numbers(uint32_t state, uint32_t n, float* out) {
+  Rng r{state, true};
+  for (uint32_t i = 0; i < n; ++i) out[i] = r.next();
+  return r.s;
+}
+
+// One scattering direction as the reference-parity path draws it (no
+// renormalisation) from the xorshift state *state.
+void oracle_hg_sample_xorshift(const vcr_params* p, const float in[3], uint32_t* state, float out[3]) {
+  Scene s{};
+  s.g_ = p->phase_g;
+  s.opg2 = p->phase_one_plus_g2;
+  s.omg2 = p->phase_one_minus_g2;
+  s.o2g = p->phase_one_over_2g;
+  s.iso = p->isotropic != 0;
+  Rng rng{*state, true};
+  V3 o = hg_sample(s, v3(in[0], in[1], in[2]), rng, false);
+  out[0] = o.x; out[1] = o.y; out[2] = o.z;
+  *state = rng.s;
+}
+
+// find_scatter_global from (pos, dir) with the xorshift state *state.
+int oracle_find_scatter_global(void* h, const vcr_cloud* cl, float pos[3], const float dir[3], uint32_t* state) {
+  vcr_params p{};
+  Scene s = make_scene(static_cast<Grid*>(h), *cl, p, nullptr, 0, nullptr);
+  const float sigma_bar = (s.max_ext * s.ds) / s.bs;
+  Rng rng{*state, true};
+  Counts c;
+  V3 q = v3(pos[0], pos[1], pos[2]);
+  const bool hit = find_scatter_global(s, sigma_bar, q, v3(dir[0], dir[1], dir[2]), rng, c);
+  pos[0] = q.x; pos[1] = q.y; pos[2] = q.z;
+  *state = rng.s;
+  return hit ? 1 : 0;
+}
+
+float oracle_sv_lookup(void* h, const vcr_cloud* cl, const vcr_shadow_volume* sv, const float* sv_tex,
+                       const float pos[3]) {
+  vcr_params p{};
+  Scene s = make_scene(static_cast<Grid*>(h), *cl, p, sv, 0, sv_tex);
+  return sv_lookup(s, v3(pos[0], pos[1], pos[2]));
+}
+
 // The phase function alone (hg_pdf / hg_sample above, as the tracker calls
 // them): its density at n cosines, and m directions scattered from `in`,
 // sample i drawn from the stream rng_pcg(seed, i, 0).
