@@ -87,7 +87,3 @@ def sv_build(scene: Scene, threads: int = 0) -> np.ndarray:
     out = np.zeros((n, n, n), np.float32)
     lib().ref_sv_build(_p(out), threads or os.cpu_count() or 1)
     return out
-
-
-def _f3(v):
-    return np.ascontiguousarray(v, np.float32).reshape(3)

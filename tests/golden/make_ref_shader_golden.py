@@ -10,7 +10,6 @@ the inputs, shared with the test.
 """
 from __future__ import annotations
 
-import ctypes as C
 import os
 import sys
 

@@ -4,7 +4,6 @@ the timed region starts, keeps only the rows written from the region's
 start, and reads the throttle reasons."""
 import os
 import sys
-import textwrap
 import time
 
 FAKE = """\
